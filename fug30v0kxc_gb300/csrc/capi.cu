@@ -1,0 +1,771 @@
+// capi.cu -- the extern "C" boundary of include/vec.h.
+//
+// The context owns every device array (the module globals of
+// src/arrays.f90:14-74), the spectral tables (src/fft.F90:60-80, 171-221)
+// and the stencil scales (src/dbydz.F90:355-362).  Entry points accept host
+// or device pointers; host buffers are staged through context scratch.
+#include <ctype.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+
+struct vec_ctx {
+    Engine E;
+};
+
+// ---- error string ------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+void vec_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char *vec_last_error(void) { return g_err; }
+
+// ---- profiling ---------------------------------------------------------------------
+void Engine::prof_begin(const char *name)
+{
+    launches++;
+    if (!prof_on) return;
+    int rec = -1;
+    for (size_t i = 0; i < prof.size(); i++)
+        if (prof[i].name == name) { rec = (int)i; break; }
+    if (rec < 0) {
+        ProfRec r;
+        r.name = name;
+        prof.push_back(r);
+        rec = (int)prof.size() - 1;
+    }
+    cudaEvent_t a, b;
+    if (ev_pool.size() >= 2) {
+        a = ev_pool.back(); ev_pool.pop_back();
+        b = ev_pool.back(); ev_pool.pop_back();
+    } else {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    cudaEventRecord(a, stream);
+    prof_cur = rec;
+    prof_a = a;
+    Pending pd;
+    pd.rec = rec; pd.a = a; pd.b = b;
+    pending.push_back(pd);
+}
+
+void Engine::prof_end()
+{
+    if (!prof_on || pending.empty()) return;
+    cudaEventRecord(pending.back().b, stream);
+}
+
+int Engine::prof_flush()
+{
+    if (pending.empty()) return VEC_OK;
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    for (auto &pd : pending) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, pd.a, pd.b);
+        prof[pd.rec].launches += 1;
+        prof[pd.rec].ms += ms;
+        ev_pool.push_back(pd.a);
+        ev_pool.push_back(pd.b);
+    }
+    pending.clear();
+    return VEC_OK;
+}
+
+// ---- parameters ---------------------------------------------------------------
+static double ck_from_ra(double ra, double theta, double cm, double sigma, double gamma)
+{
+    // src/initial.F90:194-196
+    return sqrt((((cm + 1.0) * theta * theta) / (sigma * ra * gamma)) * (cm + 1.0 - (cm * gamma))
+                * pow(1.0 + (0.5 * theta), (2.0 * cm) - 1.0));
+}
+
+extern "C" int vec_params_default(vec_params *p)
+{
+    if (!p) return VEC_ERR_ARG;
+    memset(p, 0, sizeof(*p));
+    // bin/INPUT
+    p->gamma = 1.4; p->sigma = 1.0; p->theta = 10.0; p->cm = 1.0;
+    p->tayl = 0.0; p->psi = 1.570796327; p->zeta = 0.2; p->xmax = 4.0; p->ymax = 4.0; p->sf = 0.2;
+    p->rayl = 1.0e5; p->chand = 2500.0;
+    p->ck = ck_from_ra(p->rayl, p->theta, p->cm, p->sigma, p->gamma);
+    p->f = p->chand * (p->zeta * p->sigma * p->ck * p->ck);
+    p->nx = 30; p->ny = 30; p->nz = 60;
+    p->nframe = 0; p->ntotal = 50000; p->ndu06 = 5000; p->ndu16 = 10000; p->ndurestart = 10000;
+    // src/main.F90:108-116
+    p->dalias = 1; p->kinematic = 0; p->radbc = 0; p->constflux = 0; p->perfect = 0; p->dynamo = 0;
+    // extensions (reference behaviour)
+    p->eta_contrast = 1.0; p->noise_amp = 0.1; p->kappa_uniform = 0; p->seed_base = 1996;
+    p->precision = VEC_PREC_FP64; p->diag_cadence = 1;
+    return VEC_OK;
+}
+
+// next line of the file, first whitespace-separated token parsed as a number
+static int read_value(FILE *fp, double *v)
+{
+    char line[512];
+    if (!fgets(line, sizeof line, fp)) return -1;
+    char *s = line;
+    while (*s && isspace((unsigned char)*s)) s++;
+    // Fortran list-directed input accepts d exponents
+    for (char *c = s; *c && !isspace((unsigned char)*c); c++)
+        if (*c == 'd' || *c == 'D') *c = 'e';
+    char *end = NULL;
+    *v = strtod(s, &end);
+    return end == s ? -1 : 0;
+}
+
+extern "C" int vec_params_read_input(const char *path, vec_params *p)
+{
+    if (!path || !p) return VEC_ERR_ARG;
+    vec_params_default(p);
+    FILE *fp = fopen(path, "r");
+    if (!fp) { vec_set_error("cannot open %s", path); return VEC_ERR_INPUT; }
+    char line[512];
+    double flag, v[20];
+    int ok = fgets(line, sizeof line, fp) && fgets(line, sizeof line, fp) && read_value(fp, &flag) == 0
+             && fgets(line, sizeof line, fp) && fgets(line, sizeof line, fp);
+    for (int i = 0; ok && i < 20; i++) ok = read_value(fp, &v[i]) == 0;
+    fclose(fp);
+    if (!ok) { vec_set_error("malformed INPUT file %s", path); return VEC_ERR_INPUT; }
+    // src/initial.F90:149-171
+    p->gamma = v[0]; p->sigma = v[1]; p->theta = v[2]; p->ck = v[3]; p->cm = v[4]; p->f = v[5];
+    p->tayl = v[6]; p->psi = v[7]; p->zeta = v[8]; p->xmax = v[9]; p->ymax = v[10]; p->sf = v[11];
+    p->nframe = (int)v[12]; p->ntotal = (int)v[13]; p->ndu06 = (int)v[14]; p->ndu16 = (int)v[15];
+    p->ndurestart = (int)v[16]; p->nx = (int)v[17]; p->ny = (int)v[18]; p->nz = (int)v[19];
+    if ((int)flag == 1) {   // :174-185
+        p->chand = p->f / (p->zeta * p->sigma * p->ck * p->ck);
+        p->rayl = (((p->cm + 1.0) * p->theta * p->theta) / (p->sigma * p->ck * p->ck * p->gamma))
+                  * (p->cm + 1.0 - (p->cm * p->gamma)) * pow(1.0 + (0.5 * p->theta), (2.0 * p->cm) - 1.0);
+    } else if ((int)flag == 2) {   // :186-199
+        p->rayl = p->ck;
+        p->chand = p->f;
+        p->ck = ck_from_ra(p->rayl, p->theta, p->cm, p->sigma, p->gamma);
+        p->f = p->chand * (p->zeta * p->sigma * p->ck * p->ck);
+    } else {
+        vec_set_error("unknown input flag %d", (int)flag);
+        return VEC_ERR_INPUT;
+    }
+    if (p->nframe < 0 || p->nframe > 2) { vec_set_error("unknown nframe %d", p->nframe); return VEC_ERR_INPUT; }
+    return VEC_OK;
+}
+
+// ---- context -------------------------------------------------------------------
+static void set_consts(Engine &E)
+{
+    const vec_params &p = E.p;
+    Consts &c = E.k;
+    memset(&c, 0, sizeof(c));
+    // src/constants.f90:62-107
+    c.dx = p.xmax / (double)E.nx;
+    c.dy = p.ymax / (double)E.ny;
+    c.dz = 1.0 / (double)(E.nz - 1);
+    c.dd = c.dx < c.dy ? c.dx : c.dy;
+    c.xn = 1.0 / (double)(E.nx * E.ny);
+    c.xzn = c.dx * c.dy * c.dz;
+    c.taylt = p.tayl / pow(1.0 + p.theta / 2.0, 2.0 * p.cm);
+    c.cpsi = cos(p.psi);
+    c.spsi = sin(p.psi);
+    c.cor = p.ck * p.sigma * sqrt(c.taylt);
+    c.gck = p.gamma * p.ck;
+    c.sck = p.sigma * p.ck;
+    c.zck = p.zeta * p.ck;
+    c.scko3 = c.sck / 3.0;
+    c.sckg = p.sigma * p.ck * (p.gamma - 1.0);
+    c.fzckg = p.f * p.zeta * p.ck * (p.gamma - 1.0);
+    c.thmplus1 = p.theta * (p.cm + 1.0);
+    c.fo2 = p.f / 2.0;
+    c.g1 = sqrt(p.gamma);
+    c.gm1 = p.gamma - 1.0;
+    c.nusstmp = p.theta * (p.cm + 1.0) * (1.0 - (1.0 / p.gamma));
+    c.dtvisc0x = 0.1 * 0.75 * c.dd * c.dd / p.sigma / p.ck;
+    c.dtvisc0z = 0.2 * c.dz * c.dz / p.sigma / p.ck * (1.0 + p.theta / 7.0);
+    c.dtdiff0x = 0.1 * c.dd * c.dd / p.gamma / p.ck;
+    c.dtdiff0z = 0.2 * c.dz * c.dz / p.gamma / p.ck * (1.0 + p.theta / 7.0);
+    // src/dbydz.F90:360-361
+    c.ho12 = (double)(E.nz - 1) / 12.0;
+    c.sc1 = (double)((E.nz - 1) * (E.nz - 1)) / 12.0;
+    c.f = p.f; c.gamma = p.gamma; c.theta = p.theta; c.sf = p.sf;
+    c.var_eta = p.eta_contrast != 1.0;
+    c.icutoffx = (E.nx / 2) / 3;
+    c.icutoffy = (E.ny / 2) / 3;
+}
+
+static int dev_alloc(void **p, size_t bytes)
+{
+    if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) {
+        cudaGetLastError();
+        vec_set_error("cudaMalloc of %zu bytes failed", bytes);
+        return VEC_ERR_ALLOC;
+    }
+    return cudaMemset(*p, 0, bytes ? bytes : 16) == cudaSuccess ? VEC_OK : VEC_ERR_CUDA;
+}
+
+#define ALLOC(ptr, bytes)                                              \
+    do {                                                               \
+        int s_ = dev_alloc((void **)&(ptr), (bytes));                  \
+        if (s_) { vec_destroy(c); return s_; }                         \
+    } while (0)
+
+static int upload(double *d, const std::vector<double> &h)
+{
+    CUDA_TRY(cudaMemcpy(d, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    return VEC_OK;
+}
+
+extern "C" int vec_create(const vec_params *p, vec_ctx **out)
+{
+    if (!p || !out) return VEC_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 4 || p->nx % 2) { vec_set_error("nx must be even and >= 4"); return VEC_ERR_NX; }
+    if (p->ny < 4 || p->ny % 2) { vec_set_error("ny must be even and >= 4"); return VEC_ERR_NY; }
+    if (p->nz < 6) { vec_set_error("nz must be >= 6"); return VEC_ERR_NZ; }
+    if (p->precision != VEC_PREC_FP64 && p->precision != VEC_PREC_SPLIT) return VEC_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        vec_set_error("no CUDA device");
+        return VEC_ERR_CUDA;
+    }
+    static bool configured = false;
+    if (!configured) {
+        int st = line_kernels_configure();
+        if (st) return st;
+        configured = true;
+    }
+    vec_ctx *c = new vec_ctx();
+    Engine &E = c->E;
+    E.p = *p;
+    E.nx = p->nx; E.ny = p->ny; E.nz = p->nz;
+    E.np = (size_t)E.nx * E.ny;
+    E.n = E.np * E.nz;
+    E.split = p->precision == VEC_PREC_SPLIT;
+    set_consts(E);
+    int st;
+    if ((st = line_plan_make(E.nx, E.ny, 8, &E.plx)) || (st = line_plan_make(E.ny, E.nx, 8, &E.ply))) {
+        vec_set_error("line lengths nx=%d ny=%d are not supported (2^a 3^b 5^c <= 2048)", E.nx, E.ny);
+        delete c;
+        return st;
+    }
+    if (cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return VEC_ERR_CUDA;
+    }
+    const size_t n = E.n, nz = E.nz;
+    // wavenumbers, src/fft.F90:171-221
+    std::vector<double> akx1(E.nx, 0.0), akx2(E.nx, 0.0), aky1(E.ny, 0.0), aky2(E.ny, 0.0);
+    {
+        double cx = 8.0 * atan(1.0) / p->xmax, cy = 8.0 * atan(1.0) / p->ymax;
+        for (int i = 1; i <= E.nx / 2 - 1; i++) {
+            akx1[i] = (double)i * cx; akx1[E.nx - i] = (double)i * cx;
+            akx2[i] = -(double)i * (double)i * cx * cx; akx2[E.nx - i] = -(double)i * (double)i * cx * cx;
+        }
+        akx2[E.nx / 2] = -(double)(E.nx / 2) * (double)(E.nx / 2) * cx * cx;
+        for (int i = 1; i <= E.ny / 2 - 1; i++) {
+            aky1[i] = (double)i * cy; aky1[E.ny - i] = (double)i * cy;
+            aky2[i] = -(double)i * (double)i * cy * cy; aky2[E.ny - i] = -(double)i * (double)i * cy * cy;
+        }
+        aky2[E.ny / 2] = -(double)(E.ny / 2) * (double)(E.ny / 2) * cy * cy;
+    }
+    if ((st = line_tables_make<double>(E.nx, akx1.data(), akx2.data(), E.k.icutoffx, &E.tx64)) ||
+        (st = line_tables_make<double>(E.ny, aky1.data(), aky2.data(), E.k.icutoffy, &E.ty64)) ||
+        (st = line_tables_make<float>(E.nx, akx1.data(), akx2.data(), E.k.icutoffx, &E.tx32)) ||
+        (st = line_tables_make<float>(E.ny, aky1.data(), aky2.data(), E.k.icutoffy, &E.ty32))) {
+        vec_destroy(c);
+        return st;
+    }
+    ALLOC(E.akx1, sizeof(double) * E.nx); ALLOC(E.akx2, sizeof(double) * E.nx);
+    ALLOC(E.aky1, sizeof(double) * E.ny); ALLOC(E.aky2, sizeof(double) * E.ny);
+    if (upload(E.akx1, akx1) || upload(E.akx2, akx2) || upload(E.aky1, aky1) || upload(E.aky2, aky2)) {
+        vec_destroy(c);
+        return VEC_ERR_CUDA;
+    }
+    // kappa(z): src/trans_params.f90:36-62; eta(z): the extension
+    std::vector<double> kap(nz), dkap(nz), eta(nz), deta(nz);
+    double emax = 0.0;
+    for (int k = 0; k < E.nz; k++) {
+        double z = (double)k * E.k.dz;
+        if (p->kappa_uniform) { kap[k] = 1.0; dkap[k] = 0.0; }
+        else {
+            double constB = 10.0 * (z - 5.0e-1);
+            kap[k] = 5.0e-1 * (tanh(constB) + 1);
+            dkap[k] = 5.0e-1 * 10.0 * pow(cosh(constB), -2.0);
+        }
+        eta[k] = E.k.zck * (1.0 + (p->eta_contrast - 1.0) * z);
+        deta[k] = E.k.zck * (p->eta_contrast - 1.0);
+        emax = eta[k] > emax ? eta[k] : emax;
+    }
+    E.k.eta_max = emax;
+    ALLOC(E.kappa, sizeof(double) * nz); ALLOC(E.dkappa, sizeof(double) * nz);
+    ALLOC(E.eta, sizeof(double) * nz); ALLOC(E.deta, sizeof(double) * nz);
+    if (upload(E.kappa, kap) || upload(E.dkappa, dkap) || upload(E.eta, eta) || upload(E.deta, deta)) {
+        vec_destroy(c);
+        return VEC_ERR_CUDA;
+    }
+    // state
+    double **st64[] = { &E.r, &E.t, &E.u, &E.v, &E.w, &E.bx, &E.by, &E.bz, &E.jsq, &E.pol, &E.tor };
+    for (auto pp : st64) ALLOC(*pp, sizeof(double) * n);
+    const size_t esz = E.split ? sizeof(float) : sizeof(double);
+    for (int f = 0; f < 7; f++)
+        for (int s = 0; s < 3; s++) ALLOC(E.hist[f][s], esz * n);
+    ALLOC(E.bxbar, sizeof(double) * nz); ALLOC(E.bybar, sizeof(double) * nz);
+    for (int s = 0; s < 3; s++) { ALLOC(E.bxbardot[s], sizeof(double) * nz); ALLOC(E.bybardot[s], sizeof(double) * nz); }
+    ALLOC(E.w1d, sizeof(double) * 8 * nz);
+    for (int i = 0; i < W_COUNT; i++) ALLOC(E.wk[i], esz * n);
+    for (int i = 0; i < 3; i++) ALLOC(E.s64[i], sizeof(double) * n);
+    E.red_blocks = 152 * 4;
+    ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 24 + 64));
+    ALLOC(E.ds, sizeof(DevScalars));
+    if (cudaMallocHost(&E.hs, sizeof(DevScalars)) != cudaSuccess) { vec_destroy(c); return VEC_ERR_ALLOC; }
+    memset(E.hs, 0, sizeof(DevScalars));
+    E.hs->first = 1;
+    E.hs->denmn = 0x7fefffffffffffffull;
+    CUDA_TRY(cudaMemcpy(E.ds, E.hs, sizeof(DevScalars), cudaMemcpyHostToDevice));
+    if (E.split && (st = split_setup(&E))) { vec_destroy(c); return st; }
+    CUDA_TRY(cudaDeviceSynchronize());
+    *out = c;
+    return VEC_OK;
+}
+
+extern "C" int vec_destroy(vec_ctx *c)
+{
+    if (!c) return VEC_OK;
+    Engine &E = c->E;
+    if (E.stream) cudaStreamSynchronize(E.stream);
+    void *ptrs[] = { E.r, E.t, E.u, E.v, E.w, E.bx, E.by, E.bz, E.jsq, E.pol, E.tor, E.bxbar, E.bybar,
+                     E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds,
+                     E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
+                     E.rho0, E.t0, E.hres };
+    for (void *q : ptrs) if (q) cudaFree(q);
+    for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hist[f][s]) cudaFree(E.hist[f][s]);
+    for (int s = 0; s < 3; s++) { if (E.bxbardot[s]) cudaFree(E.bxbardot[s]); if (E.bybardot[s]) cudaFree(E.bybardot[s]); }
+    for (int i = 0; i < W_COUNT; i++) if (E.wk[i]) cudaFree(E.wk[i]);
+    for (int i = 0; i < 6; i++) if (E.s64[i]) cudaFree(E.s64[i]);
+    if (E.tx64.tw) line_tables_free(&E.tx64);
+    if (E.ty64.tw) line_tables_free(&E.ty64);
+    if (E.tx32.tw) line_tables_free(&E.tx32);
+    if (E.ty32.tw) line_tables_free(&E.ty32);
+    if (E.hs) cudaFreeHost(E.hs);
+    for (auto &pd : E.pending) { cudaEventDestroy(pd.a); cudaEventDestroy(pd.b); }
+    for (auto ev : E.ev_pool) cudaEventDestroy(ev);
+    if (E.stream) cudaStreamDestroy(E.stream);
+    delete c;
+    return VEC_OK;
+}
+
+extern "C" void *vec_stream(vec_ctx *c) { return c ? (void *)c->E.stream : nullptr; }
+
+extern "C" int vec_sync(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    CUDA_TRY(cudaStreamSynchronize(c->E.stream));
+    return VEC_OK;
+}
+
+// ---- host/device staging ---------------------------------------------------------
+static bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// copy count doubles from src (host or device) into device dst
+static int stage_in(Engine &E, double *dst, const double *src, size_t count)
+{
+    CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * count,
+                             is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, E.stream));
+    return VEC_OK;
+}
+static int stage_out(Engine &E, double *dst, const double *src, size_t count)
+{
+    CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * count,
+                             is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    return VEC_OK;
+}
+
+// ---- state I/O ------------------------------------------------------------------
+static int hist_index(int field, int *f, int *s)
+{
+    if (field < VEC_F_RDOT || field >= VEC_F_COUNT) return -1;
+    *f = (field - VEC_F_RDOT) / 3;
+    *s = (field - VEC_F_RDOT) % 3;
+    return 0;
+}
+
+static double *state_ptr(Engine &E, int field)
+{
+    switch (field) {
+    case VEC_F_R: return E.r; case VEC_F_T: return E.t; case VEC_F_U: return E.u;
+    case VEC_F_V: return E.v; case VEC_F_W: return E.w; case VEC_F_BX: return E.bx;
+    case VEC_F_BY: return E.by; case VEC_F_BZ: return E.bz; case VEC_F_JSQ: return E.jsq;
+    case VEC_F_POL: return E.pol; case VEC_F_TOR: return E.tor;
+    }
+    return nullptr;
+}
+
+__global__ void k_f2d(const float *a, double *b, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (double)a[i];
+}
+__global__ void k_d2f(const double *a, float *b, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+extern "C" int vec_set_field(vec_ctx *c, int field, const double *src)
+{
+    if (!c || !src) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    double *d = state_ptr(E, field);
+    if (d) {
+        int st = stage_in(E, d, src, E.n);
+        if (st) return st;
+        if (E.split) return split_refresh(&E);
+        CUDA_TRY(cudaStreamSynchronize(E.stream));
+        return VEC_OK;
+    }
+    int f, s;
+    if (hist_index(field, &f, &s)) return VEC_ERR_ARG;
+    if (!E.split) return stage_in(E, (double *)E.hist[f][s], src, E.n) ? VEC_ERR_CUDA : vec_sync(c);
+    int st = stage_in(E, E.s64[0], src, E.n);
+    if (st) return st;
+    k_d2f<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>(E.s64[0], (float *)E.hist[f][s], E.n);
+    return vec_sync(c);
+}
+
+extern "C" int vec_get_field(vec_ctx *c, int field, double *dst)
+{
+    if (!c || !dst) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    double *d = state_ptr(E, field);
+    if (d) return stage_out(E, dst, d, E.n);
+    int f, s;
+    if (hist_index(field, &f, &s)) return VEC_ERR_ARG;
+    if (!E.split) return stage_out(E, dst, (const double *)E.hist[f][s], E.n);
+    k_f2d<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>((const float *)E.hist[f][s], E.s64[0], E.n);
+    return stage_out(E, dst, E.s64[0], E.n);
+}
+
+static double *mean_ptr(Engine &E, int m)
+{
+    switch (m) {
+    case VEC_M_BXBAR: return E.bxbar; case VEC_M_BYBAR: return E.bybar;
+    case VEC_M_KAPPA: return E.kappa; case VEC_M_DKAPPA: return E.dkappa;
+    case VEC_M_ETA: return E.eta; case VEC_M_DETA: return E.deta;
+    }
+    if (m >= VEC_M_BXBARDOT && m < VEC_M_BXBARDOT + 3) return E.bxbardot[m - VEC_M_BXBARDOT];
+    if (m >= VEC_M_BYBARDOT && m < VEC_M_BYBARDOT + 3) return E.bybardot[m - VEC_M_BYBARDOT];
+    return nullptr;
+}
+
+extern "C" int vec_set_mean(vec_ctx *c, int m, const double *src)
+{
+    if (!c || !src) return VEC_ERR_ARG;
+    double *d = mean_ptr(c->E, m);
+    if (!d) return VEC_ERR_ARG;
+    int st = stage_in(c->E, d, src, c->E.nz);
+    return st ? st : vec_sync(c);
+}
+
+extern "C" int vec_get_mean(vec_ctx *c, int m, double *dst)
+{
+    if (!c || !dst) return VEC_ERR_ARG;
+    double *d = mean_ptr(c->E, m);
+    if (!d) return VEC_ERR_ARG;
+    return stage_out(c->E, dst, d, c->E.nz);
+}
+
+extern "C" int vec_set_bzbar(vec_ctx *c, double b) { if (!c) return VEC_ERR_ARG; c->E.bzbar = b; return VEC_OK; }
+extern "C" int vec_get_bzbar(vec_ctx *c, double *b) { if (!c || !b) return VEC_ERR_ARG; *b = c->E.bzbar; return VEC_OK; }
+
+extern "C" int vec_get_scalars(vec_ctx *c, vec_scalars *s)
+{
+    if (!c || !s) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    CUDA_TRY(cudaMemcpyAsync(E.hs, E.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    s->dt = E.hs->dt; s->dt1 = E.hs->dt1; s->dt2 = E.hs->dt2; s->ttime = E.hs->ttime;
+    s->iter = E.iter; s->nit = E.nit; s->first = E.hs->first; s->second = E.hs->second;
+    return VEC_OK;
+}
+
+extern "C" int vec_set_scalars(vec_ctx *c, const vec_scalars *s)
+{
+    if (!c || !s) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    CUDA_TRY(cudaMemcpyAsync(E.hs, E.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    E.hs->dt = s->dt; E.hs->dt1 = s->dt1; E.hs->dt2 = s->dt2; E.hs->ttime = s->ttime;
+    E.hs->first = s->first; E.hs->second = s->second;
+    E.iter = s->iter; E.nit = s->nit;
+    CUDA_TRY(cudaMemcpyAsync(E.ds, E.hs, sizeof(DevScalars), cudaMemcpyHostToDevice, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    return VEC_OK;
+}
+
+// ---- set-up ---------------------------------------------------------------------
+extern "C" int vec_static(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_static(&c->E);
+    if (st) return st;
+    if (c->E.split) return split_refresh(&c->E);
+    return VEC_OK;
+}
+
+extern "C" int vec_calcdt(vec_ctx *c, double *dt)
+{
+    if (!c) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    int st = phys_calcdt(&E);
+    if (st) return st;
+    CUDA_TRY(cudaMemcpyAsync(E.hs, E.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    if (dt) *dt = E.hs->dt;
+    return VEC_OK;
+}
+
+extern "C" int vec_mag_init(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_mag_init(&c->E);
+    if (st) return st;
+    if (c->E.split && (st = split_refresh(&c->E))) return st;
+    return vec_sync(c);
+}
+
+// ---- per-operator entry points (always FP64) --------------------------------------
+static int line_op(vec_ctx *c, int dir, const double *fin, double *f1, int op1, double *f2, int op2)
+{
+    if (!c || !fin || !f1 || (op2 != OP_NONE && !f2)) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    int st;
+    if ((st = stage_in(E, E.s64[0], fin, E.n))) return st;
+    LineJob<double> j = ljob<double>(E.s64[0], E.s64[1], op1, op2 != OP_NONE ? E.s64[2] : nullptr, op2);
+    if ((st = launch_lines<double>(&E, dir, &j, 1))) return st;
+    if ((st = stage_out(E, f1, E.s64[1], E.n))) return st;
+    if (op2 != OP_NONE && (st = stage_out(E, f2, E.s64[2], E.n))) return st;
+    return VEC_OK;
+}
+
+extern "C" int vec_d1bydx(vec_ctx *c, const double *fin, double *fout) { return line_op(c, 0, fin, fout, OP_D1, nullptr, OP_NONE); }
+extern "C" int vec_d1bydy(vec_ctx *c, const double *fin, double *fout) { return line_op(c, 1, fin, fout, OP_D1, nullptr, OP_NONE); }
+extern "C" int vec_d2bydx(vec_ctx *c, const double *fin, double *a, double *b) { return line_op(c, 0, fin, a, OP_D1, b, OP_D2); }
+extern "C" int vec_d2bydy(vec_ctx *c, const double *fin, double *a, double *b) { return line_op(c, 1, fin, a, OP_D1, b, OP_D2); }
+
+extern "C" int vec_dealias(vec_ctx *c, double *z)
+{
+    if (!c || !z) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    int st;
+    if ((st = stage_in(E, E.s64[0], z, E.n))) return st;
+    LineJob<double> j = ljob<double>(E.s64[0], E.s64[0], OP_DEALIAS);
+    if ((st = launch_lines<double>(&E, 0, &j, 1)) || (st = launch_lines<double>(&E, 1, &j, 1))) return st;
+    return stage_out(E, z, E.s64[0], E.n);
+}
+
+extern "C" int vec_forwardfft(vec_ctx *c, const double *fin, double *fout)
+{
+    if (!c || !fin || !fout) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    int st;
+    if ((st = stage_in(E, E.s64[0], fin, E.n))) return st;
+    LineJob<double> jx = ljob<double>(E.s64[0], E.s64[1], OP_FWD);
+    LineJob<double> jy = ljob<double>(E.s64[1], E.s64[1], OP_FWD);
+    if ((st = launch_lines<double>(&E, 0, &jx, 1)) || (st = launch_lines<double>(&E, 1, &jy, 1))) return st;
+    return stage_out(E, fout, E.s64[1], E.n);
+}
+
+extern "C" int vec_inversefft(vec_ctx *c, const double *fin, double *fout)
+{
+    if (!c || !fin || !fout) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    int st;
+    if ((st = stage_in(E, E.s64[0], fin, E.n))) return st;
+    LineJob<double> jx = ljob<double>(E.s64[0], E.s64[1], OP_INV);
+    LineJob<double> jy = ljob<double>(E.s64[1], E.s64[1], OP_INV);
+    if ((st = launch_lines<double>(&E, 0, &jx, 1)) || (st = launch_lines<double>(&E, 1, &jy, 1))) return st;
+    return stage_out(E, fout, E.s64[1], E.n);
+}
+
+static int zop(vec_ctx *c, const double *fin, double *fout, int flag, int kind, int oned)
+{
+    if (!c || !fin || !fout) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    const size_t cnt = oned ? (size_t)E.nz : E.n;
+    int np = oned ? 1 : (int)E.np;
+    int st;
+    if ((st = stage_in(E, E.s64[0], fin, cnt))) return st;
+    if (kind == 0) st = op_d1z(&E, E.s64[0], E.s64[1], flag, np, E.nz);
+    else if (kind == 1) st = op_d1upz(&E, E.s64[0], E.s64[1], flag);
+    else st = op_d2z(&E, E.s64[0], E.s64[1], flag, np, E.nz);
+    if (st) return st;
+    return stage_out(E, fout, E.s64[1], cnt);
+}
+
+extern "C" int vec_d1bydz(vec_ctx *c, const double *fin, double *fout, int dflag) { return zop(c, fin, fout, dflag, 0, 0); }
+extern "C" int vec_d1upbydz(vec_ctx *c, const double *fin, double *fout, int dflag) { return zop(c, fin, fout, dflag, 1, 0); }
+extern "C" int vec_d2bydz(vec_ctx *c, const double *fin, double *fout, int dflag) { return zop(c, fin, fout, dflag, 2, 0); }
+extern "C" int vec_d1bydz1d(vec_ctx *c, const double *fin, double *fout, int dflag) { return zop(c, fin, fout, dflag, 0, 1); }
+extern "C" int vec_d2bydz1d(vec_ctx *c, const double *fin, double *fout, int dflag) { return zop(c, fin, fout, dflag, 2, 1); }
+
+// ---- physics entry points -----------------------------------------------------------
+static int finish(vec_ctx *c, int st)
+{
+    if (st) return st;
+    return vec_sync(c);
+}
+
+static int mag_on(const Engine &E) { return E.p.f != 0.0 || E.p.kinematic; }
+
+extern "C" int vec_hydro_deriv(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    return finish(c, c->E.split ? split_hydro(&c->E) : phys_hydro64(&c->E));
+}
+extern "C" int vec_mag_deriv(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    return finish(c, c->E.split ? split_mag(&c->E) : phys_mag64(&c->E));
+}
+extern "C" int vec_bandj(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    return finish(c, c->E.split ? split_bandj(&c->E) : phys_bandj64(&c->E));
+}
+extern "C" int vec_magdealias(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_magdealias(&c->E);
+    if (!st && c->E.split) st = split_refresh(&c->E);
+    return finish(c, st);
+}
+extern "C" int vec_boundary(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_boundary(&c->E);
+    if (!st && c->E.split) st = split_refresh(&c->E);
+    return finish(c, st);
+}
+extern "C" int vec_mag_boundary(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_mag_boundary(&c->E);
+    if (!st && c->E.split) st = split_refresh(&c->E);
+    return finish(c, st);
+}
+extern "C" int vec_ab3_update(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    return finish(c, c->E.split ? split_ab3(&c->E, 0) : phys_ab3(&c->E, 0));
+}
+extern "C" int vec_diag(vec_ctx *c, vec_diag_out *out)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = phys_diag(&c->E, out);
+    if (c->E.split) {
+        int s2 = split_refresh(&c->E);
+        if (!st) st = s2;
+    }
+    return st;
+}
+
+// one iteration of src/main.F90:340-747 (printing and snapshots excluded)
+static int one_step(Engine &E)
+{
+    int st;
+    const int mag = mag_on(E);
+    E.nit += 1;
+    E.iter += 1;
+    if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
+    if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
+    else st = phys_zero_mag_rhs(&E);
+    if (st) return st;
+    const int mdeal = E.p.dalias && mag;
+    if ((st = E.split ? split_ab3(&E, mdeal) : phys_ab3(&E, mdeal))) return st;
+    const bool dealias_now = E.p.dalias && (E.nit % 10 == 0);
+    if (dealias_now && (st = phys_dealias_state(&E))) return st;
+    if (mag && (st = E.split ? split_bandj(&E) : phys_bandj64(&E))) return st;
+    if ((st = phys_boundary(&E))) return st;
+    if (mag && (st = phys_mag_boundary(&E))) return st;
+    const bool diag_now = E.p.diag_cadence && E.p.ndu06 > 0 && (E.nit % E.p.ndu06 == 0);
+    if (diag_now) {
+        st = phys_diag(&E, nullptr);
+        if (st) return st;
+    }
+    if (E.nit % 10 == 0 && (st = phys_calcdt(&E))) return st;
+    if (E.split && (st = split_refresh(&E))) return st;
+    return VEC_OK;
+}
+
+extern "C" int vec_step(vec_ctx *c, int nsteps)
+{
+    if (!c || nsteps < 0) return VEC_ERR_ARG;
+    for (int s = 0; s < nsteps; s++) {
+        int st = one_step(c->E);
+        if (st) { c->E.prof_flush(); return st; }
+    }
+    if (c->E.prof_on) return c->E.prof_flush();
+    return VEC_OK;
+}
+
+extern "C" int vec_last_diag(vec_ctx *c, vec_diag_out *out)
+{
+    if (!c || !out) return VEC_ERR_ARG;
+    *out = c->E.last_diag;
+    return c->E.have_diag ? VEC_OK : VEC_ERR_ARG;
+}
+
+// ---- instrumentation ------------------------------------------------------------------
+extern "C" int vec_profile(vec_ctx *c, int on)
+{
+    if (!c) return VEC_ERR_ARG;
+    c->E.prof_flush();
+    c->E.prof_on = on != 0;
+    return VEC_OK;
+}
+extern "C" int vec_profile_count(vec_ctx *c)
+{
+    if (!c) return 0;
+    c->E.prof_flush();
+    return (int)c->E.prof.size();
+}
+extern "C" int vec_profile_get(vec_ctx *c, int i, char *name, int *launches, double *ms)
+{
+    if (!c || i < 0 || i >= (int)c->E.prof.size()) return VEC_ERR_ARG;
+    c->E.prof_flush();
+    const ProfRec &r = c->E.prof[i];
+    if (name) { strncpy(name, r.name.c_str(), 63); name[63] = 0; }
+    if (launches) *launches = r.launches;
+    if (ms) *ms = r.ms;
+    return VEC_OK;
+}
+extern "C" int vec_profile_reset(vec_ctx *c)
+{
+    if (!c) return VEC_ERR_ARG;
+    c->E.prof_flush();
+    c->E.prof.clear();
+    return VEC_OK;
+}
+extern "C" long long vec_launch_count(vec_ctx *c) { return c ? c->E.launches : 0; }

@@ -1,0 +1,91 @@
+// common.cuh -- shared types of the GB300 VarElecCond library (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/vec.h"
+
+// complex type per real precision
+template <typename R> struct CT;
+template <> struct CT<double> { using T = double2; };
+template <> struct CT<float> { using T = float2; };
+
+// ---- line-transform (horizontal FFT) plan -------------------------------
+#define LP_MAXST 16
+struct LinePlan {
+    int n;                  // line length (nx or ny)
+    int nst;                // number of Stockham stages
+    int radix[LP_MAXST];    // radix of each stage (2,3,4,5,8)
+    int P;                  // complex sequences (= pairs of real lines) per CTA
+    int lines;              // real lines per plane (ny for x lines, nx for y lines)
+    int tiles;              // CTAs per plane = ceil(lines / (2P))
+    int threads;            // block size
+    size_t smem;            // dynamic shared memory bytes for the precision in use
+};
+
+// operations of one line job
+enum LineOp {
+    OP_NONE = 0,
+    OP_D1 = 1,       // first derivative (+ik), DC and Nyquist dropped: src/fft.F90:292-302
+    OP_D2 = 2,       // second derivative (-k^2), Nyquist kept: src/fft.F90:442-454
+    OP_DEALIAS = 3,  // 2/3-rule truncation: src/fft.F90:618-626
+    OP_FWD = 4,      // real -> halfcomplex, unnormalised (rfftw forward)
+    OP_INV = 5,      // halfcomplex -> real, divided by n (rfftw backward / n)
+};
+
+template <typename R>
+struct LineJob {
+    const R *in;
+    R *out1, *out2;
+    R alpha1, alpha2;   // outputs are alpha * result (+ old value when acc)
+    int op1, op2;
+    int acc1, acc2;
+    const double *addk; // OP_INV only: out1 += addk[plane] + addc
+    double addc;
+};
+
+#define MAX_JOBS 16
+
+// spectral tables of one direction (device pointers)
+template <typename R>
+struct LineTables {
+    typename CT<R>::T *tw;  // exp(-2 pi i e / n), e = 0..n-1
+    R *m1;                  // d1 multiplier (imaginary part, sign and 1/n folded in)
+    R *m2;                  // d2 multiplier (k2 / n, DC zeroed)
+    R *mda;                 // dealias mask (1/n or 0)
+};
+
+// ---- per-context derived constants: src/constants.f90:56-109 -----------
+struct Consts {
+    double dx, dy, dz, dd, xn, xzn, taylt, cpsi, spsi, cor;
+    double gck, sck, zck, scko3, sckg, fzckg, thmplus1, fo2, g1, gm1, nusstmp;
+    double dtvisc0x, dtvisc0z, dtdiff0x, dtdiff0z;
+    double ho12, sc1;
+    double f, gamma, theta, sf;
+    double eta_max;
+    int var_eta;            // eta_contrast != 1
+    int icutoffx, icutoffy;
+};
+
+// time-loop scalars living on the device (src/main.F90:84-103)
+struct DevScalars {
+    double dt, dt1, dt2, ttime;
+    double c0, c1, c2;
+    int first, second;
+    // reductions
+    unsigned long long velmxx, velmxz, denmn;  // ordered bit patterns of non-negative doubles
+    double res[64];                            // diagnostics results
+};
+
+// ---- error helper --------------------------------------------------------
+void vec_set_error(const char *fmt, ...);
+
+#define CUDA_TRY(x)                                                                   \
+    do {                                                                              \
+        cudaError_t e_ = (x);                                                         \
+        if (e_ != cudaSuccess) {                                                      \
+            vec_set_error("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); \
+            return VEC_ERR_CUDA;                                                      \
+        }                                                                             \
+    } while (0)

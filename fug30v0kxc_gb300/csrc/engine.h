@@ -1,0 +1,139 @@
+// engine.h -- the device-resident context behind the C-ABI (internal).
+//
+// All module-global arrays of src/arrays.f90:14-74 live here, in HBM, for
+// the whole run.  Fields are (nx,ny,nz) with x fastest.  In the FP64 form
+// every array is double; in the split form the bulk work arrays, RHS
+// histories and the FP32 mirrors of the state are float while the state
+// itself, the 1-D backgrounds and the diagnostics stay double.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+// work-array slots (FP64 form: double; split form: float)
+enum WorkSlot {
+    // horizontal derivatives of r,t,u,v,w (hydro_deriv)
+    W_RX, W_TX, W_TXX, W_UX, W_UXX, W_VX, W_VXX, W_WX, W_WXX,
+    W_RY, W_TY, W_TYY, W_UY, W_UYY, W_VY, W_VYY, W_WY, W_WYY,
+    // second-level inputs / accumulators
+    W_P1, W_P2, W_Q, W_G, W_H, W_P3, W_P4,
+    W_RACC, W_UACC, W_VACC, W_WACC,
+    // magnetic work (reference: ex, ey, ez, wk1..wk4)
+    W_EX, W_EY, W_EZ, W_M1, W_M2, W_M3, W_M4, W_M5, W_M6,
+    W_COUNT
+};
+
+struct ProfRec {
+    std::string name;
+    int launches = 0;
+    double ms = 0.0;
+};
+
+struct Engine {
+    vec_params p;
+    Consts k;
+    int nx, ny, nz;
+    size_t np, n;
+    int split;                  // VEC_PREC_SPLIT
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+
+    LinePlan plx, ply;          // precision of the bulk path
+    LinePlan plx64, ply64;      // FP64 plans (per-operator entry points)
+    LineTables<double> tx64, ty64;
+    LineTables<float> tx32, ty32;
+
+    // FP64 state (src/arrays.f90)
+    double *r = nullptr, *t = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
+    double *bx = nullptr, *by = nullptr, *bz = nullptr, *jsq = nullptr, *pol = nullptr, *tor = nullptr;
+    // RHS histories [field][slot]: r,t,u,v,w,pol,tor; slot 2 = newest
+    void *hist[7][3] = {};
+    // 1-D
+    double *bxbar = nullptr, *bybar = nullptr, *bxbardot[3] = {}, *bybardot[3] = {};
+    double *kappa = nullptr, *dkappa = nullptr, *eta = nullptr, *deta = nullptr;
+    double *akx1 = nullptr, *akx2 = nullptr, *aky1 = nullptr, *aky2 = nullptr;
+    double *w1d = nullptr;      // 1-D scratch (8 nz)
+    double bzbar = 0.0;
+    // work arrays (bulk precision)
+    void *wk[W_COUNT] = {};
+    // FP64 scratch for per-operator entry points and diagnostics
+    double *s64[6] = {};
+    // split form: FP32 mirrors of the state and FP64 backgrounds
+    float *r32 = nullptr, *t32 = nullptr, *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;
+    float *bx32 = nullptr, *by32 = nullptr, *bz32 = nullptr, *jsq32 = nullptr;
+    float *pol32 = nullptr, *tor32 = nullptr;
+    double *rho0 = nullptr, *t0 = nullptr, *hres = nullptr;   // background profiles, residual
+    // reductions scratch
+    double *red = nullptr;      // per-block partials
+    int red_blocks = 0;
+    DevScalars *ds = nullptr;   // device scalars
+    DevScalars *hs = nullptr;   // pinned host mirror
+    // host counters
+    int nit = 0, iter = 0;
+    vec_diag_out last_diag;
+    int have_diag = 0;
+
+    // profiling
+    bool prof_on = false;
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> ev_pool;
+    struct Pending { int rec; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    int prof_cur = -1;
+    cudaEvent_t prof_a = nullptr;
+
+    template <typename R> const LineTables<R> &tables(int dir) const;
+    template <typename R> R *W(int slot) const { return reinterpret_cast<R *>(wk[slot]); }
+
+    void prof_begin(const char *name);
+    void prof_end();
+    int prof_flush();
+};
+
+template <> inline const LineTables<double> &Engine::tables<double>(int dir) const { return dir == 0 ? tx64 : ty64; }
+template <> inline const LineTables<float> &Engine::tables<float>(int dir) const { return dir == 0 ? tx32 : ty32; }
+
+// lines.cu
+int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl);
+template <typename R> int line_tables_make(int n, const double *k1, const double *k2, int icut, LineTables<R> *tb);
+template <typename R> void line_tables_free(LineTables<R> *tb);
+template <typename R> int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
+int line_kernels_configure();
+
+template <typename R>
+inline LineJob<R> ljob(const R *in, R *out1, int op1, R *out2 = nullptr, int op2 = OP_NONE,
+                       int acc1 = 0, int acc2 = 0, R a1 = (R)1, R a2 = (R)1)
+{
+    LineJob<R> j;
+    j.in = in; j.out1 = out1; j.out2 = out2; j.op1 = op1; j.op2 = op2;
+    j.acc1 = acc1; j.acc2 = acc2; j.alpha1 = a1; j.alpha2 = a2;
+    j.addk = nullptr; j.addc = 0.0;
+    return j;
+}
+
+// physics.cu (FP64 form)
+int op_d1z(Engine *E, const double *in, double *out, int flag, int np, int nz);
+int op_d1upz(Engine *E, const double *in, double *out, int flag);
+int op_d2z(Engine *E, const double *in, double *out, int flag, int np, int nz);
+int phys_hydro64(Engine *E);
+int phys_mag64(Engine *E);
+int phys_zero_mag_rhs(Engine *E);
+int phys_bandj64(Engine *E);
+int phys_magdealias(Engine *E);
+int phys_boundary(Engine *E);
+int phys_mag_boundary(Engine *E);
+int phys_ab3(Engine *E, int magdealias);
+int phys_dealias_state(Engine *E);
+int phys_calcdt(Engine *E);
+int phys_diag(Engine *E, vec_diag_out *out);
+int phys_mag_init(Engine *E);
+int phys_static(Engine *E);
+int phys_step_prologue(Engine *E);
+// split form (split.cu)
+int split_setup(Engine *E);
+int split_hydro(Engine *E);
+int split_mag(Engine *E);
+int split_bandj(Engine *E);
+int split_refresh(Engine *E);
+int split_ab3(Engine *E, int magdealias);

@@ -1,0 +1,1137 @@
+// physics.cu -- the FP64 (plain drop-in) right-hand sides, update, boundary
+// conditions and reductions of the VarElecCond time step, for sm_103a.
+//
+// hydro_deriv (src/hydro_deriv.f90:5-505) is regrouped by data dependence
+// into four passes instead of the reference's 37 operator calls and 11
+// pointwise loops:
+//   1. one x-line launch and one y-line launch produce the 18 horizontal
+//      derivatives of r,t,u,v,w (one forward FFT per field and direction,
+//      d1 and d2 from it);
+//   2. a pointwise kernel evaluates every z derivative of the state on the
+//      fly, completes the energy equation and accumulates the momentum and
+//      continuity terms that need no second-level derivative, and forms the
+//      second-level inputs (viscous grad-div, Maxwell stresses);
+//   3. x- and y-line launches differentiate those inputs straight into the
+//      momentum accumulators (accumulate epilogue);
+//   4. a pointwise kernel adds their z derivatives, applies the boundary
+//      override of d(rho)/dz (:455-470) and divides by rho (:487-497).
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "common.cuh"
+#include "engine.h"
+#include "zstencil.cuh"
+
+#define TPB 256
+static inline unsigned nblk(size_t n, int tpb = TPB)
+{
+    size_t b = (n + tpb - 1) / tpb;
+    return (unsigned)(b > 0x7fffffff ? 0x7fffffff : b);
+}
+
+#define KLAUNCH(E, name, kern, grid, block, ...)                 \
+    do {                                                         \
+        (E)->prof_begin(name);                                   \
+        kern<<<(grid), (block), 0, (E)->stream>>>(__VA_ARGS__);  \
+        (E)->prof_end();                                         \
+        CUDA_TRY(cudaGetLastError());                            \
+    } while (0)
+
+// ============================================================================
+// z-derivative operators (per-operator entry points)
+// ============================================================================
+template <typename R>
+__global__ void k_d1z(const R *in, R *out, int fl, size_t np, int nz, R h)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    size_t q = idx - (size_t)k * np;
+    out[idx] = zd1(in + q, np, k, nz, fl, h);
+}
+template <typename R>
+__global__ void k_d1upz(const R *in, const R *w, R *out, int fl, size_t np, int nz, R h)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    size_t q = idx - (size_t)k * np;
+    out[idx] = zd1up(in + q, np, k, nz, fl, h, w[idx]);
+}
+template <typename R>
+__global__ void k_d2z(const R *in, R *out, int fl, size_t np, int nz, R s)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    size_t q = idx - (size_t)k * np;
+    out[idx] = zd2(in + q, np, k, nz, fl, s);
+}
+
+int op_d1z(Engine *E, const double *in, double *out, int flag, int np, int nz)
+{
+    if (!(flag == 0 || flag == 1 || flag == 2 || flag == 5)) return VEC_ERR_FLAG;
+    KLAUNCH(E, "d1bydz_f64", k_d1z<double>, nblk((size_t)np * nz), TPB, in, out, flag, (size_t)np, nz, E->k.ho12);
+    return VEC_OK;
+}
+int op_d1upz(Engine *E, const double *in, double *out, int flag)
+{
+    if (!(flag == 0 || flag == 1 || flag == 2 || flag == 5)) return VEC_ERR_FLAG;
+    KLAUNCH(E, "d1upbydz_f64", k_d1upz<double>, nblk(E->n), TPB, in, E->w, out, flag, E->np, E->nz, E->k.ho12);
+    return VEC_OK;
+}
+int op_d2z(Engine *E, const double *in, double *out, int flag, int np, int nz)
+{
+    if (!(flag == 0 || flag == 3)) return VEC_ERR_FLAG;
+    KLAUNCH(E, "d2bydz_f64", k_d2z<double>, nblk((size_t)np * nz), TPB, in, out, flag, (size_t)np, nz, E->k.sc1);
+    return VEC_OK;
+}
+
+// ============================================================================
+// hydro_deriv
+// ============================================================================
+struct HydroArgs {
+    const double *r, *t, *u, *v, *w, *bx, *by, *bz, *jsq;
+    const double *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
+    const double *ry, *ty, *tyy, *uy, *uyy, *vy, *vyy, *wy, *wyy;
+    const double *kappa, *dkappa, *eta;
+    double *racc, *tdot, *uacc, *vacc, *wacc;
+    double *p1, *p2, *q, *g, *hh, *p3, *p4;
+    double gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, zck, ho12, sc1;
+    int var_eta;
+    size_t np;
+    int nz;
+};
+
+// pass 2: src/hydro_deriv.f90:45-53, 82-110, 139-168, 201-219, 245-261,
+// 287-309, 360-367, 390-398, 421-432 (every term without a second-level
+// derivative); the energy equation is complete here.
+__global__ void k_hydro_pass2(HydroArgs a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.np * a.nz) return;
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const double h = a.ho12, s = a.sc1;
+
+    const double rr = a.r[idx], tt = a.t[idx], u0 = a.u[idx], v0 = a.v[idx], w0 = a.w[idx];
+    const double bx = a.bx[idx], by = a.by[idx], bz = a.bz[idx];
+    const double rx = a.rx[idx], ry = a.ry[idx];
+    const double tx = a.tx[idx], txx = a.txx[idx], ty = a.ty[idx], tyy = a.tyy[idx];
+    const double ux = a.ux[idx], uxx = a.uxx[idx], uy = a.uy[idx], uyy = a.uyy[idx];
+    const double vx = a.vx[idx], vxx = a.vxx[idx], vy = a.vy[idx], vyy = a.vyy[idx];
+    const double wx = a.wx[idx], wxx = a.wxx[idx], wy = a.wy[idx], wyy = a.wyy[idx];
+
+    // z derivatives (flags: src/hydro_deriv.f90:66-68, 124-125, 233, 275, 349-350)
+    const double tzu = zd1up(a.t + q, np, k, nz, 5, h, w0);
+    const double tz = zd1(a.t + q, np, k, nz, 5, h);
+    const double tzz = zd2(a.t + q, np, k, nz, 0, s);
+    const double wzu = zd1up(a.w + q, np, k, nz, 1, h, w0);
+    const double wz = zd1(a.w + q, np, k, nz, 1, h);
+    const double uzu = zd1up(a.u + q, np, k, nz, 2, h, w0);
+    const double vzu = zd1up(a.v + q, np, k, nz, 2, h, w0);
+    const double uzz = zd2(a.u + q, np, k, nz, 3, s);
+    const double vzz = zd2(a.v + q, np, k, nz, 3, s);
+
+    const double third = 1.0 / 3.0;
+    const double ohm = a.var_eta ? a.eta[k] / a.zck : 1.0;
+    const double divu = ux + vy + wz;
+
+    // continuity: :48, :149 (the w d(rho)/dz term is added in pass 4)
+    a.racc[idx] = -u0 * rx - v0 * ry - rr * divu;
+
+    // energy (rho * dT/dt): :88-102, :150-151, :216, :258, :300, then / rho
+    double td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
+                + a.gck * a.kappa[k] * (txx + tyy + tzz)
+                + a.gck * a.dkappa[k] * tzu
+                + a.fzckg * ohm * a.jsq[idx];
+    td = td - a.gm1 * tt * divu * rr + 2 * a.sckg * (ux * ux + vy * vy + wz * wz - third * divu * divu);
+    td = td + a.sckg * (uy + vx) * (uy + vx);
+    td = td + a.sckg * (wx + uzu) * (wx + uzu);
+    td = td + a.sckg * (wy + vzu) * (wy + vzu);
+    a.tdot[idx] = td * (1.0 / rr);
+
+    // momentum: :103-105, :159-161, :213-214, :253-254, :292-306, :363-364, :393-395, :424-426
+    double ud = -tt * rx - rr * tx;
+    ud = ud - rr * u0 * ux - rr * v0 * uy - rr * w0 * uzu;
+    ud = ud - rr * a.cor * (w0 * a.cpsi + v0 * a.spsi);
+    ud = ud + a.sck * uzz + a.sck * uxx + a.sck * uyy;
+    double vd = -tt * ry - rr * ty;
+    vd = vd - rr * v0 * vy - rr * u0 * vx - rr * w0 * vzu;
+    vd = vd - rr * a.cor * (-u0 * a.spsi);
+    vd = vd + a.sck * vzz + a.sck * vxx + a.sck * vyy;
+    double wd = -rr * tz;
+    wd = wd - rr * w0 * wzu + a.thmplus1 * rr - rr * u0 * wx - rr * v0 * wy;
+    wd = wd - rr * a.cor * (-u0 * a.cpsi);
+    wd = wd + a.sck * wxx + a.sck * wyy;
+    a.uacc[idx] = ud;
+    a.vacc[idx] = vd;
+    a.wacc[idx] = wd;
+
+    // second-level inputs: :152-165, :215, :255-257, :297-299
+    const double temp1 = a.fo2 * bx * bx, temp2 = a.fo2 * by * by, temp3 = a.fo2 * bz * bz;
+    const double dv = a.scko3 * divu;
+    a.p1[idx] = dv + temp1 - temp2 - temp3;
+    a.p2[idx] = dv + temp2 - temp1 - temp3;
+    a.p3[idx] = a.scko3 * ux + a.scko3 * vy + temp3 - temp1 - temp2;
+    a.p4[idx] = 4.0 * a.scko3 * wz;
+    a.q[idx] = a.f * by * bx;
+    a.g[idx] = a.f * bz * bx;
+    a.hh[idx] = a.f * bz * by;
+}
+
+struct Hydro4Args {
+    const double *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
+    double *rdot, *udot, *vdot, *wdot;
+    double ho12;
+    size_t np;
+    int nz;
+};
+
+// pass 4: :183-184, :272, :321 (z derivatives of second-level inputs),
+// :443-497 (d(rho)/dz with the boundary override, division by rho)
+__global__ void k_hydro_pass4(Hydro4Args a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.np * a.nz) return;
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const double h = a.ho12;
+    const double w0 = a.w[idx], tt = a.t[idx], rr = a.r[idx];
+    double wd = a.wacc[idx] + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
+    double ud = a.uacc[idx] + zd1(a.g + q, np, k, nz, 5, h);
+    double vd = a.vacc[idx] + zd1(a.hh + q, np, k, nz, 5, h);
+    double rzu, rz;
+    if (k == 0 || k == nz - 1) {
+        rzu = wd / tt;
+        rz = wd / tt;
+    } else {
+        rzu = zd1up(a.r + q, np, k, nz, 0, h, w0);
+        rz = zd1(a.r + q, np, k, nz, 0, h);
+    }
+    a.rdot[idx] = a.racc[idx] - w0 * rzu;
+    wd = wd - tt * rz;
+    const double ri = 1.0 / rr;
+    a.udot[idx] = ud * ri;
+    a.vdot[idx] = vd * ri;
+    a.wdot[idx] = wd * ri;
+}
+
+int phys_hydro64(Engine *E)
+{
+    double *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
+    int st;
+    // pass 1: horizontal derivatives (:33-34, :64-65, :122-123, :190-191,
+    // :232, :274, :378-380, :409-411)
+    LineJob<double> jx[5] = {
+        ljob<double>(E->r, W[W_RX], OP_D1),
+        ljob<double>(E->t, W[W_TX], OP_D1, W[W_TXX], OP_D2),
+        ljob<double>(E->u, W[W_UX], OP_D1, W[W_UXX], OP_D2),
+        ljob<double>(E->v, W[W_VX], OP_D1, W[W_VXX], OP_D2),
+        ljob<double>(E->w, W[W_WX], OP_D1, W[W_WXX], OP_D2),
+    };
+    if ((st = launch_lines<double>(E, 0, jx, 5))) return st;
+    LineJob<double> jy[5] = {
+        ljob<double>(E->r, W[W_RY], OP_D1),
+        ljob<double>(E->t, W[W_TY], OP_D1, W[W_TYY], OP_D2),
+        ljob<double>(E->u, W[W_UY], OP_D1, W[W_UYY], OP_D2),
+        ljob<double>(E->v, W[W_VY], OP_D1, W[W_VYY], OP_D2),
+        ljob<double>(E->w, W[W_WY], OP_D1, W[W_WYY], OP_D2),
+    };
+    if ((st = launch_lines<double>(E, 1, jy, 5))) return st;
+
+    HydroArgs a;
+    a.r = E->r; a.t = E->t; a.u = E->u; a.v = E->v; a.w = E->w;
+    a.bx = E->bx; a.by = E->by; a.bz = E->bz; a.jsq = E->jsq;
+    a.rx = W[W_RX]; a.tx = W[W_TX]; a.txx = W[W_TXX]; a.ux = W[W_UX]; a.uxx = W[W_UXX];
+    a.vx = W[W_VX]; a.vxx = W[W_VXX]; a.wx = W[W_WX]; a.wxx = W[W_WXX];
+    a.ry = W[W_RY]; a.ty = W[W_TY]; a.tyy = W[W_TYY]; a.uy = W[W_UY]; a.uyy = W[W_UYY];
+    a.vy = W[W_VY]; a.vyy = W[W_VYY]; a.wy = W[W_WY]; a.wyy = W[W_WYY];
+    a.kappa = E->kappa; a.dkappa = E->dkappa; a.eta = E->eta;
+    a.racc = W[W_RACC]; a.tdot = (double *)E->hist[1][2];
+    a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
+    a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H];
+    a.p3 = W[W_P3]; a.p4 = W[W_P4];
+    const Consts &c = E->k;
+    a.gck = c.gck; a.fzckg = c.fzckg; a.gm1 = c.gm1; a.sckg = c.sckg; a.fo2 = c.fo2;
+    a.scko3 = c.scko3; a.f = c.f; a.thmplus1 = c.thmplus1; a.cor = c.cor; a.cpsi = c.cpsi;
+    a.spsi = c.spsi; a.sck = c.sck; a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1;
+    a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
+    KLAUNCH(E, "hydro_pass2_f64", k_hydro_pass2, nblk(E->n), TPB, a);
+
+    // pass 3: d/dx, d/dy of the second-level inputs into the accumulators
+    // (:181-182, :230-231, :273, :320)
+    LineJob<double> kx[3] = {
+        ljob<double>(W[W_P1], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<double>(W[W_Q], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<double>(W[W_G], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+    };
+    if ((st = launch_lines<double>(E, 0, kx, 3))) return st;
+    LineJob<double> ky[3] = {
+        ljob<double>(W[W_P2], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<double>(W[W_Q], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<double>(W[W_H], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+    };
+    if ((st = launch_lines<double>(E, 1, ky, 3))) return st;
+
+    Hydro4Args b;
+    b.r = E->r; b.t = E->t; b.w = E->w; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
+    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC];
+    b.rdot = (double *)E->hist[0][2]; b.udot = (double *)E->hist[2][2];
+    b.vdot = (double *)E->hist[3][2]; b.wdot = (double *)E->hist[4][2];
+    b.ho12 = c.ho12; b.np = E->np; b.nz = E->nz;
+    KLAUNCH(E, "hydro_pass4_f64", k_hydro_pass4, nblk(E->n), TPB, b);
+    return VEC_OK;
+}
+
+// ============================================================================
+// mag_deriv: src/magnetic.f90:285-487 (+ eta(z) extension)
+// ============================================================================
+__global__ void k_emf(const double *u, const double *v, const double *w, const double *bx,
+                      const double *by, const double *bz, double *e1, double *e2, double *e3, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // :311-313
+    e1[i] = v[i] * bz[i] - w[i] * by[i];
+    e2[i] = w[i] * bx[i] - u[i] * bz[i];
+    e3[i] = u[i] * by[i] - v[i] * bx[i];
+}
+
+// mean-field RHS (:328-352) on one CTA; ex, ey are the 2-D spectra of the EMF
+__global__ void k_mean_rhs(const double *ex, const double *ey, const double *bxbar, const double *bybar,
+                           const double *eta, const double *deta, double *bxd, double *byd,
+                           double *scratch, size_t np, int nz, double xn, double zck, double ho12,
+                           double sc1, int var_eta)
+{
+    double *e1 = scratch, *e2 = scratch + nz;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        e1[k] = xn * ex[(size_t)k * np];
+        e2[k] = xn * ey[(size_t)k * np];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        double dey = zd1(e2, 1, k, nz, 5, ho12);   // :337
+        double dex = zd1(e1, 1, k, nz, 5, ho12);   // :338
+        double d2x = zd2(bxbar, 1, k, nz, 3, sc1); // :343
+        double d2y = zd2(bybar, 1, k, nz, 3, sc1); // :344
+        if (!var_eta) {
+            bxd[k] = zck * d2x - dey;              // :350
+            byd[k] = zck * d2y + dex;              // :351
+        } else {
+            double gx = zd1(bxbar, 1, k, nz, 5, ho12), gy = zd1(bybar, 1, k, nz, 5, ho12);
+            bxd[k] = eta[k] * d2x - dey + deta[k] * gx;
+            byd[k] = eta[k] * d2y + dex + deta[k] * gy;
+        }
+    }
+}
+
+// wk1 = dEx/dx + dEy/dy in spectral space (:362-407)
+__global__ void k_mag_div(const double *ex, const double *ey, double *w1, int nx, int ny, int nz,
+                          const double *akx1, const double *aky1)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t np = (size_t)nx * ny;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    size_t q = idx - (size_t)k * np;
+    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    const double *px = ex + (size_t)k * np, *py = ey + (size_t)k * np;
+    w1[idx] = sdx(px, i, j, nx, akx1) + sdy(py, i, j, nx, ny, aky1);
+}
+
+struct MagArgs {
+    const double *ex, *ey, *ez, *w1, *pol, *tor, *eta, *deta;
+    const double *akx1, *aky1, *akx2, *aky2;
+    double *poldot, *tordot;
+    double zck, ho12, sc1;
+    int var_eta, nx, ny, nz;
+};
+
+// :400-479 -- wk2 = dEx/dy - dEy/dx, wk3 = d/dz(wk1), inverse horizontal
+// Laplacian, d2/dz2 of pol and tor, and the final poldot / tordot.
+__global__ void k_mag_final(MagArgs a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+    const double *px = a.ex + (size_t)k * np, *py = a.ey + (size_t)k * np;
+    double w2 = sdy(px, i, j, a.nx, a.ny, a.aky1) - sdx(py, i, j, a.nx, a.akx1);
+    double w3 = zd1(a.w1 + q, np, k, a.nz, 5, a.ho12);
+    const double kk = a.akx2[i] + a.aky2[j];
+    if (i == 0 && j == 0) { w2 = 0.0; w3 = 0.0; }
+    else { w2 = w2 / kk; w3 = w3 / kk; }
+    const double d2p = zd2(a.pol + q, np, k, a.nz, 3, a.sc1);
+    const double d2t = zd2(a.tor + q, np, k, a.nz, 3, a.sc1);
+    if (!a.var_eta) {
+        a.poldot[idx] = a.zck * a.pol[idx] * kk + a.zck * d2p + w2;
+        a.tordot[idx] = a.zck * a.tor[idx] * kk + a.zck * d2t - w3 + a.ez[idx];
+    } else {
+        const double e = a.eta[k];
+        const double dt = zd1(a.tor + q, np, k, a.nz, 5, a.ho12);
+        a.poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
+        a.tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + a.deta[k] * dt;
+    }
+}
+
+int phys_mag64(Engine *E)
+{
+    double *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
+    int st;
+    KLAUNCH(E, "emf_f64", k_emf, nblk(E->n), TPB, E->u, E->v, E->w, E->bx, E->by, E->bz, W[W_M1], W[W_M2], W[W_M3], E->n);
+    // forwardfft x3 (:321-323): x pass then y pass in place
+    LineJob<double> fx[3] = { ljob<double>(W[W_M1], W[W_EX], OP_FWD), ljob<double>(W[W_M2], W[W_EY], OP_FWD),
+                              ljob<double>(W[W_M3], W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<double>(E, 0, fx, 3))) return st;
+    LineJob<double> fy[3] = { ljob<double>(W[W_EX], W[W_EX], OP_FWD), ljob<double>(W[W_EY], W[W_EY], OP_FWD),
+                              ljob<double>(W[W_EZ], W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
+    const Consts &c = E->k;
+    KLAUNCH(E, "mean_rhs", k_mean_rhs, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
+            E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
+    KLAUNCH(E, "mag_div_f64", k_mag_div, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
+    MagArgs a;
+    a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol; a.tor = E->tor;
+    a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.poldot = (double *)E->hist[5][2]; a.tordot = (double *)E->hist[6][2];
+    a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
+    KLAUNCH(E, "mag_final_f64", k_mag_final, nblk(E->n), TPB, a);
+    return VEC_OK;
+}
+
+int phys_zero_mag_rhs(Engine *E)
+{
+    size_t esz = E->split ? sizeof(float) : sizeof(double);
+    CUDA_TRY(cudaMemsetAsync(E->hist[5][2], 0, esz * E->n, E->stream));
+    CUDA_TRY(cudaMemsetAsync(E->hist[6][2], 0, esz * E->n, E->stream));
+    CUDA_TRY(cudaMemsetAsync(E->bxbardot[2], 0, sizeof(double) * E->nz, E->stream));
+    CUDA_TRY(cudaMemsetAsync(E->bybardot[2], 0, sizeof(double) * E->nz, E->stream));
+    return VEC_OK;
+}
+
+// ============================================================================
+// bandj: src/magnetic.f90:492-664
+// ============================================================================
+struct BandjArgs {
+    const double *dzs, *pol, *tor, *akx1, *aky1, *akx2, *aky2;
+    double *bxh, *byh, *bzh, *dybz, *dxbz, *jzh;
+    int nx, ny, nz;
+};
+
+// :525-570 and :584-617 in spectral space
+__global__ void k_bandj_spec(BandjArgs a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+    const size_t pb = (size_t)k * np;
+    const double *s = a.dzs + pb, *tp = a.tor + pb, *pp = a.pol + pb;
+    a.bxh[idx] = sdx(s, i, j, a.nx, a.akx1) + sdy(tp, i, j, a.nx, a.ny, a.aky1);
+    a.byh[idx] = sdy(s, i, j, a.nx, a.ny, a.aky1) - sdx(tp, i, j, a.nx, a.akx1);
+    a.bzh[idx] = -1.0 * a.pol[idx] * (a.akx2[i] + a.aky2[j]);
+    a.jzh[idx] = -1.0 * a.tor[idx] * (a.akx2[i] + a.aky2[j]);
+    // d/dy and d/dx of ez = -pol*(akx2+aky2), evaluated at the mirrored index
+    double dy = 0.0, dx = 0.0;
+    if (!(j == 0 || 2 * j == a.ny)) {
+        int jm = a.ny - j;
+        double ezm = -1.0 * pp[(size_t)jm * a.nx + i] * (a.akx2[i] + a.aky2[jm]);
+        dy = ezm * a.aky1[j];
+        if (2 * j < a.ny) dy = -dy;
+    }
+    if (!(i == 0 || 2 * i == a.nx)) {
+        int im = a.nx - i;
+        double ezm = -1.0 * pp[(size_t)j * a.nx + im] * (a.akx2[im] + a.aky2[j]);
+        dx = ezm * a.akx1[i];
+        if (2 * i < a.nx) dx = -dx;
+    }
+    a.dybz[idx] = dy;
+    a.dxbz[idx] = dx;
+}
+
+// :630-645: jsq from Jz, dBz/dy, dBz/dx and the z derivatives of Bx, By
+__global__ void k_jsq(const double *jz, const double *dybz, const double *dxbz, const double *bx,
+                      const double *by, double *jsq, size_t np, int nz, double h)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    double wk1 = zd1(by + q, np, k, nz, 5, h);
+    double wk2 = zd1(bx + q, np, k, nz, 5, h);
+    double ez = jz[idx], ex = dybz[idx], ey = dxbz[idx];
+    jsq[idx] = ez * ez + ((ex - wk1) * (ex - wk1)) + ((wk2 - ey) * (wk2 - ey));
+}
+
+int phys_bandj64(Engine *E)
+{
+    double *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
+    int st;
+    if ((st = op_d1z(E, E->pol, W[W_M1], 5, (int)E->np, E->nz))) return st;   // :519
+    BandjArgs a;
+    a.dzs = W[W_M1]; a.pol = E->pol; a.tor = E->tor; a.akx1 = E->akx1; a.aky1 = E->aky1;
+    a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
+    KLAUNCH(E, "bandj_spec_f64", k_bandj_spec, nblk(E->n), TPB, a);
+    // six inverse 2-D transforms (:575-577, :623-625): x pass in place, then y
+    LineJob<double> ix[6] = { ljob<double>(W[W_EX], W[W_EX], OP_INV), ljob<double>(W[W_EY], W[W_EY], OP_INV),
+                              ljob<double>(W[W_EZ], W[W_EZ], OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
+                              ljob<double>(W[W_M3], W[W_M3], OP_INV), ljob<double>(W[W_M4], W[W_M4], OP_INV) };
+    if ((st = launch_lines<double>(E, 0, ix, 6))) return st;
+    LineJob<double> iy[6] = { ljob<double>(W[W_EX], E->bx, OP_INV), ljob<double>(W[W_EY], E->by, OP_INV),
+                              ljob<double>(W[W_EZ], E->bz, OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
+                              ljob<double>(W[W_M3], W[W_M3], OP_INV), ljob<double>(W[W_M4], W[W_M4], OP_INV) };
+    iy[0].addk = E->bxbar;       // :587-589
+    iy[1].addk = E->bybar;
+    iy[2].addc = E->bzbar;
+    if ((st = launch_lines<double>(E, 1, iy, 6))) return st;
+    KLAUNCH(E, "jsq_f64", k_jsq, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
+    return VEC_OK;
+}
+
+// ============================================================================
+// magdealias (src/magnetic.f90:666-717) and spectral truncation
+// ============================================================================
+template <typename R>
+__device__ __forceinline__ bool truncated(int i, int j, int nx, int ny, int cx, int cy)
+{
+    return (i >= nx / 2 - cx && i <= nx / 2 + cx) || (j >= ny / 2 - cy && j <= ny / 2 + cy);
+}
+
+template <typename R>
+__global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, int cy)
+{
+    size_t np = (size_t)nx * ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    size_t q = idx % np;
+    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    if (truncated<R>(i, j, nx, ny, cx, cy)) {
+        a[idx] = (R)0;
+        if (b) b[idx] = (R)0;
+    }
+}
+
+int phys_magdealias(Engine *E)
+{
+    KLAUNCH(E, "magdealias_f64", k_truncate<double>, nblk(E->n), TPB, E->pol, E->tor, E->nx, E->ny, E->nz,
+            E->k.icutoffx, E->k.icutoffy);
+    return VEC_OK;
+}
+
+// ============================================================================
+// boundary conditions: src/dbydz.F90:3686-4197 and :4205-4791
+// ============================================================================
+__global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
+                           double dz, int radbc, int constflux)
+{
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const double elf = 1.0 / 11.0;
+#define P(f, kk) f[(size_t)(kk) * np + q]
+    P(w, 0) = 0.0;
+    P(u, 0) = elf * (18.0 * P(u, 1) - 9.0 * P(u, 2) + 2.0 * P(u, 3));
+    P(v, 0) = elf * (18.0 * P(v, 1) - 9.0 * P(v, 2) + 2.0 * P(v, 3));
+    P(w, nz - 1) = 0.0;
+    P(u, nz - 1) = elf * (18.0 * P(u, nz - 2) - 9.0 * P(u, nz - 3) + 2.0 * P(u, nz - 4));
+    P(v, nz - 1) = elf * (18.0 * P(v, nz - 2) - 9.0 * P(v, nz - 3) + 2.0 * P(v, nz - 4));
+    if (radbc) {   // :4036-4055, Newton iterations on the radiative condition
+        double t1old = P(t, 0);
+        for (int it = 0; it < 10; it++) {
+            double ft1 = 6.0 * theta * dz * t1old * t1old * t1old * t1old + 11.0 * t1old - 18.0 * P(t, 1)
+                         + 9.0 * P(t, 2) - 2.0 * P(t, 3);
+            double dft1 = 24.0 * theta * dz * t1old * t1old * t1old + 11.0;
+            t1old = t1old - (ft1 / dft1);
+        }
+        P(t, 0) = t1old;
+    } else {
+        P(t, 0) = 1.0;
+    }
+    if (constflux)
+        P(t, nz - 1) = elf * (18.0 * P(t, nz - 2) - 9.0 * P(t, nz - 3) + 2.0 * P(t, nz - 4) + 6.0 * theta * dz);
+    else
+        P(t, nz - 1) = 1.0 + theta;
+#undef P
+}
+
+int phys_boundary(Engine *E)
+{
+    KLAUNCH(E, "boundary_f64", k_boundary, nblk(E->np), TPB, E->u, E->v, E->w, E->t, E->np, E->nz, E->p.theta,
+            E->k.dz, E->p.radbc, E->p.constflux);
+    return VEC_OK;
+}
+
+__global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect)
+{
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const double elf = 1.0 / 11.0;
+    if (q == 0) {
+        if (perfect) {
+            bxb[0] = elf * (18.0 * bxb[1] - 9.0 * bxb[2] + 2.0 * bxb[3]);
+            byb[0] = elf * (18.0 * byb[1] - 9.0 * byb[2] + 2.0 * byb[3]);
+            bxb[nz - 1] = elf * (18.0 * bxb[nz - 2] - 9.0 * bxb[nz - 3] + 2.0 * bxb[nz - 4]);
+            byb[nz - 1] = elf * (18.0 * byb[nz - 2] - 9.0 * byb[nz - 3] + 2.0 * byb[nz - 4]);
+        } else {
+            bxb[0] = 0.0; byb[0] = 0.0; bxb[nz - 1] = 0.0; byb[nz - 1] = 0.0;
+        }
+    }
+    if (q >= np) return;
+#define P(f, kk) f[(size_t)(kk) * np + q]
+    if (perfect) {   // :4407-4560
+        P(pol, 0) = 0.0;
+        P(tor, 0) = elf * (18.0 * P(tor, 1) - 9.0 * P(tor, 2) + 2.0 * P(tor, 3));
+        P(pol, nz - 1) = 0.0;
+        P(tor, nz - 1) = elf * (18.0 * P(tor, nz - 2) - 9.0 * P(tor, nz - 3) + 2.0 * P(tor, nz - 4));
+    } else {         // :4663-4780
+        P(tor, 0) = 0.0;
+        P(pol, 0) = elf * (18.0 * P(pol, 1) - 9.0 * P(pol, 2) + 2.0 * P(pol, 3));
+        P(tor, nz - 1) = 0.0;
+        P(pol, nz - 1) = elf * (18.0 * P(pol, nz - 2) - 9.0 * P(pol, nz - 3) + 2.0 * P(pol, nz - 4));
+    }
+#undef P
+}
+
+int phys_mag_boundary(Engine *E)
+{
+    KLAUNCH(E, "mag_boundary_f64", k_mag_boundary, nblk(E->np), TPB, E->pol, E->tor, E->bxbar, E->bybar,
+            E->np, E->nz, E->p.perfect);
+    return VEC_OK;
+}
+
+// ============================================================================
+// AB3: src/main.F90:381-489
+// ============================================================================
+// coefficients (:381-403), dt1/dt2 (:488-489), ttime (:345) and the 1-D mean
+// update (:469-476) on one CTA
+__global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const double *bxd0, const double *bxd1,
+                           const double *bxd2, const double *byd0, const double *byd1, const double *byd2, int nz,
+                           int do_means)
+{
+    __shared__ double cc[3];
+    if (threadIdx.x == 0) {
+        double dt = ds->dt, c0, c1, c2;
+        ds->ttime = ds->ttime + dt;
+        if (ds->first) {
+            ds->first = 0; ds->second = 1;
+            ds->dt1 = 0.0; ds->dt2 = 0.0;
+            c0 = dt; c1 = 0.0; c2 = 0.0;
+        } else if (ds->second) {
+            ds->first = 0; ds->second = 0;
+            ds->dt2 = 0.0;
+            c0 = dt * (1.0 + 0.5 * (dt / ds->dt1));
+            c1 = -0.5 * dt * (dt / ds->dt1);
+            c2 = 0.0;
+        } else {
+            double dt1 = ds->dt1, dt2 = ds->dt2;
+            c0 = dt + (((dt * dt) / (dt1 * dt2)) * ((dt / 3.0) + 0.5 * (dt1 + dt2)));
+            c1 = ((dt * dt) / (dt1 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt2);
+            c2 = -((dt * dt) / (dt2 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt1);
+        }
+        ds->c0 = c0; ds->c1 = c1; ds->c2 = c2;
+        ds->dt2 = dt + ds->dt1;
+        ds->dt1 = dt;
+        cc[0] = c0; cc[1] = c1; cc[2] = c2;
+    }
+    __syncthreads();
+    if (!do_means) return;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        bxbar[k] = bxbar[k] + cc[0] * bxd2[k] + cc[1] * bxd1[k] + cc[2] * bxd0[k];
+        bybar[k] = bybar[k] + cc[0] * byd2[k] + cc[1] * byd1[k] + cc[2] * byd0[k];
+    }
+}
+
+struct Ab3Args {
+    double *x[7];
+    const double *h0[7], *h1[7], *h2[7];
+    double *r0, *r1;             // rdot slots 1 and 2 (zeroed at floored points)
+    const DevScalars *ds;
+    int nx, ny, nz, cx, cy, magdealias;
+};
+
+// :413-462 with the history shift done by pointer rotation on the host and
+// magdealias (:503-509) applied to the new pol/tor
+__global__ void k_ab3_update(Ab3Args a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const double c0 = a.ds->c0, c1 = a.ds->c1, c2 = a.ds->c2;
+#pragma unroll
+    for (int f = 0; f < 5; f++)
+        a.x[f][idx] = a.x[f][idx] + c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx];
+    // order of the reference: u,v,w,r,t then pol,tor; density floor after all
+    if (a.x[3][idx] < 0.05) {
+        a.x[3][idx] = 0.05;
+        a.r0[idx] = 0.0;
+        a.r1[idx] = 0.0;
+    }
+    bool trunc = false;
+    if (a.magdealias) {
+        size_t q = idx % np;
+        int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+        trunc = truncated<double>(i, j, a.nx, a.ny, a.cx, a.cy);
+    }
+#pragma unroll
+    for (int f = 5; f < 7; f++) {
+        double xn = a.x[f][idx] + c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx];
+        a.x[f][idx] = trunc ? 0.0 : xn;
+    }
+}
+
+static void rotate_hist(Engine *E)
+{
+    for (int f = 0; f < 7; f++) {
+        void *old0 = E->hist[f][0];
+        E->hist[f][0] = E->hist[f][1];
+        E->hist[f][1] = E->hist[f][2];
+        E->hist[f][2] = old0;
+    }
+    double *bx0 = E->bxbardot[0], *by0 = E->bybardot[0];
+    E->bxbardot[0] = E->bxbardot[1]; E->bxbardot[1] = E->bxbardot[2]; E->bxbardot[2] = bx0;
+    E->bybardot[0] = E->bybardot[1]; E->bybardot[1] = E->bybardot[2]; E->bybardot[2] = by0;
+}
+
+int phys_ab3(Engine *E, int magdealias)
+{
+    KLAUNCH(E, "ab3_coef", k_ab3_coef, 1, 256, E->ds, E->bxbar, E->bybar, E->bxbardot[0], E->bxbardot[1],
+            E->bxbardot[2], E->bybardot[0], E->bybardot[1], E->bybardot[2], E->nz, 1);
+    Ab3Args a;
+    // order of the reference's loop body: u, v, w, r, t, pol, tor
+    double *xs[7] = { E->u, E->v, E->w, E->r, E->t, E->pol, E->tor };
+    const int hmap[7] = { 2, 3, 4, 0, 1, 5, 6 };
+    for (int f = 0; f < 7; f++) {
+        a.x[f] = xs[f];
+        a.h0[f] = (const double *)E->hist[hmap[f]][0];
+        a.h1[f] = (const double *)E->hist[hmap[f]][1];
+        a.h2[f] = (const double *)E->hist[hmap[f]][2];
+    }
+    a.r0 = (double *)E->hist[0][1];   // become slots 1 and 2 after rotation
+    a.r1 = (double *)E->hist[0][2];
+    a.ds = E->ds;
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
+    a.magdealias = magdealias;
+    KLAUNCH(E, "ab3_update_f64", k_ab3_update, nblk(E->n), TPB, a);
+    rotate_hist(E);
+    return VEC_OK;
+}
+
+// dealias(r,t,u,v,w): src/main.F90:495-502 -> src/fft.F90:586-682
+int phys_dealias_state(Engine *E)
+{
+    double *f[5] = { E->r, E->t, E->u, E->v, E->w };
+    LineJob<double> j[5];
+    int st;
+    for (int i = 0; i < 5; i++) j[i] = ljob<double>(f[i], f[i], OP_DEALIAS);
+    if ((st = launch_lines<double>(E, 0, j, 5))) return st;
+    if ((st = launch_lines<double>(E, 1, j, 5))) return st;
+    return VEC_OK;
+}
+
+// ============================================================================
+// calcdt: src/utils.F90:144-244
+// ============================================================================
+__device__ __forceinline__ unsigned long long obits(double x) { return (unsigned long long)__double_as_longlong(x); }
+
+template <typename R>
+__global__ void k_calcdt_red(const R *u, const R *v, const R *w, const R *r, const R *t, const R *bx, const R *by,
+                             const R *bz, size_t n, double g1, double f, DevScalars *ds)
+{
+    double mxx = 0.0, mxz = 0.0, mn = 1.0e300;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double u0 = u[i], v0 = v[i], w0 = w[i], r0 = r[i], t0 = t[i];
+        double bz0 = bz[i], bx0 = bx[i], by0 = by[i];
+        double bsq0 = bx0 * bx0 + by0 * by0 + bz0 * bz0;
+        double xx = sqrt(u0 * u0 + v0 * v0) + g1 * sqrt(t0) + sqrt((bsq0 * f) / r0);
+        double xz = sqrt(w0 * w0) + g1 * sqrt(t0) + sqrt((bsq0 * f) / r0);
+        mn = fmin(mn, r0);
+        mxx = fmax(mxx, xx);
+        mxz = fmax(mxz, xz);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxz = fmax(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&ds->velmxx, obits(mxx));
+        atomicMax(&ds->velmxz, obits(mxz));
+        atomicMin(&ds->denmn, obits(mn));
+    }
+}
+
+__global__ void k_calcdt_fin(DevScalars *ds, double dd, double dz, double dtvisc0x, double dtvisc0z,
+                             double dtdiff0x, double dtdiff0z, double sf, int var_eta, double eta_max)
+{
+    double velmxx = __longlong_as_double((long long)ds->velmxx);
+    double velmxz = __longlong_as_double((long long)ds->velmxz);
+    double denmn = __longlong_as_double((long long)ds->denmn);
+    double m = 0.16 * dd / velmxx;
+    m = fmin(m, 0.3 * dz / velmxz);
+    m = fmin(m, dtvisc0x * denmn);
+    m = fmin(m, dtvisc0z * denmn);
+    m = fmin(m, dtdiff0x * denmn);
+    m = fmin(m, dtdiff0z * denmn);
+    if (var_eta) {   // extension: explicit magnetic diffusion limits for eta(z)
+        m = fmin(m, 0.1 * dd * dd / eta_max);
+        m = fmin(m, 0.2 * dz * dz / eta_max);
+    }
+    ds->dt = sf * m;
+    ds->res[60] = velmxx; ds->res[61] = velmxz; ds->res[62] = denmn;
+    ds->velmxx = 0ull; ds->velmxz = 0ull; ds->denmn = 0x7fefffffffffffffull;
+}
+
+int phys_calcdt(Engine *E)
+{
+    unsigned blocks = (unsigned)(152 * 8);
+    size_t nb = nblk(E->n);
+    if (nb < blocks) blocks = (unsigned)nb;
+    KLAUNCH(E, "calcdt_red_f64", k_calcdt_red<double>, blocks, TPB, E->u, E->v, E->w, E->r, E->t, E->bx, E->by, E->bz,
+            E->n, E->k.g1, E->k.f, E->ds);
+    const Consts &c = E->k;
+    KLAUNCH(E, "calcdt_fin", k_calcdt_fin, 1, 1, E->ds, c.dd, c.dz, c.dtvisc0x, c.dtvisc0z, c.dtdiff0x, c.dtdiff0z,
+            c.sf, c.var_eta, c.eta_max);
+    return VEC_OK;
+}
+
+// ============================================================================
+// diagnostics: GlobalAverages (src/utils.F90:22-139), nusselt
+// (src/dbydz.F90:4877-4921), checkdivb (src/utils.F90:249-318), sminmax
+// ============================================================================
+// per-plane sums: rav, urav, vrav, keav, bsqav (one CTA per plane, fixed order)
+__global__ void k_plane_sums(const double *r, const double *u, const double *v, const double *w,
+                             const double *bx, const double *by, const double *bz, size_t np, double *out)
+{
+    const int k = blockIdx.x;
+    const size_t base = (size_t)k * np;
+    double s[5] = { 0, 0, 0, 0, 0 };
+    for (size_t i = threadIdx.x; i < np; i += blockDim.x) {
+        size_t q = base + i;
+        double uu = u[q], vv = v[q], rr = r[q], ww = w[q];
+        s[0] += rr;
+        s[1] += rr * uu;
+        s[2] += rr * vv;
+        s[3] += 0.5 * rr * (uu * uu + vv * vv + ww * ww);
+        s[4] += bx[q] * bx[q] + by[q] * by[q] + bz[q] * bz[q];
+    }
+    __shared__ double sh[5][256];
+    for (int m = 0; m < 5; m++) sh[m][threadIdx.x] = s[m];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int m = 0; m < 5; m++) sh[m][threadIdx.x] += sh[m][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < 5) out[(size_t)k * 8 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_sub_mean(double *u, double *v, size_t n, const DevScalars *ds)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u[i] = u[i] - ds->res[0];
+    v[i] = v[i] - ds->res[1];
+}
+
+__global__ void k_globalavg_fin(const double *ps, int nz, double xzn, DevScalars *ds)
+{
+    double urbar = 0, vrbar = 0, rbar = 0, me = 0, ke = 0;
+    for (int k = 0; k < nz; k++) {
+        const double *p = ps + (size_t)k * 8;
+        if (k == 0 || k == nz - 1) {
+            urbar += 0.5 * p[1]; vrbar += 0.5 * p[2]; rbar += 0.5 * p[0];
+            me += 0.25 * p[4]; ke += 0.5 * p[3];
+        } else {
+            urbar += p[1]; vrbar += p[2]; rbar += p[0]; me += 0.5 * p[4]; ke += p[3];
+        }
+    }
+    ds->res[0] = urbar / rbar;
+    ds->res[1] = vrbar / rbar;
+    ds->res[2] = ke * xzn;
+    ds->res[3] = me * xzn;
+}
+
+// block partial min/max of 11 quantities + divB, and the Nusselt plane sum
+#define NMM 12
+__global__ void k_minmax(const double *r, const double *t, const double *u, const double *v, const double *w,
+                         const double *bx, const double *by, const double *bz, const double *dxbx,
+                         const double *dyby, size_t np, int nz, double ho12, double *out)
+{
+    double mn[NMM], mx[NMM];
+    for (int m = 0; m < NMM; m++) { mn[m] = 1.0e300; mx[m] = -1.0e300; }
+    const size_t n = np * nz;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int k = (int)(i / np);
+        size_t q = i - (size_t)k * np;
+        double vals[NMM];
+        double uu = u[i], vv = v[i], ww = w[i];
+        vals[0] = r[i]; vals[1] = t[i]; vals[2] = uu; vals[3] = vv; vals[4] = ww;
+        vals[5] = bx[i]; vals[6] = by[i]; vals[7] = bz[i];
+        vals[8] = (uu * uu + vv * vv + ww * ww) / t[i];
+        vals[9] = (bx[i] * bx[i] + by[i] * by[i] + bz[i] * bz[i]) / r[i];
+        vals[10] = (uu * uu + vv * vv + ww * ww);
+        vals[11] = dxbx[i] + dyby[i] + zd1(bz + q, np, k, nz, 5, ho12);
+        for (int m = 0; m < NMM; m++) { mn[m] = fmin(mn[m], vals[m]); mx[m] = fmax(mx[m], vals[m]); }
+    }
+    for (int m = 0; m < NMM; m++)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[m] = fmin(mn[m], __shfl_xor_sync(0xffffffffu, mn[m], o));
+            mx[m] = fmax(mx[m], __shfl_xor_sync(0xffffffffu, mx[m], o));
+        }
+    __shared__ double sh[2 * NMM][8];
+    int wid = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int m = 0; m < NMM; m++) { sh[m][wid] = mn[m]; sh[NMM + m][wid] = mx[m]; }
+    __syncthreads();
+    if (threadIdx.x < NMM) {
+        int m = threadIdx.x;
+        double a = 1.0e300, b = -1.0e300;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) { a = fmin(a, sh[m][q]); b = fmax(b, sh[NMM + m][q]); }
+        out[(size_t)blockIdx.x * 2 * NMM + m] = a;
+        out[(size_t)blockIdx.x * 2 * NMM + NMM + m] = b;
+    }
+}
+
+__global__ void k_nusselt_sum(const double *t, size_t np, int nz, double dz, double *out)
+{
+    double s = 0.0;
+    for (size_t i = threadIdx.x; i < np; i += blockDim.x)
+        s += ((1.0 / (6.0 * dz)) * (11.0 * t[(size_t)(nz - 1) * np + i] - 18.0 * t[(size_t)(nz - 2) * np + i]
+                                     + 9.0 * t[(size_t)(nz - 3) * np + i] - 2.0 * t[(size_t)(nz - 4) * np + i]));
+    __shared__ double sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+int phys_diag(Engine *E, vec_diag_out *out)
+{
+    const Consts &c = E->k;
+    double *ps = E->red;                       // nz*8 plane sums
+    KLAUNCH(E, "plane_sums", k_plane_sums, E->nz, 256, E->r, E->u, E->v, E->w, E->bx, E->by, E->bz, E->np, ps);
+    KLAUNCH(E, "globalavg_fin", k_globalavg_fin, 1, 1, ps, E->nz, c.xzn, E->ds);
+    KLAUNCH(E, "sub_mean", k_sub_mean, nblk(E->n), TPB, E->u, E->v, E->n, E->ds);
+    double *nus = E->red + (size_t)E->nz * 8;
+    KLAUNCH(E, "nusselt_sum", k_nusselt_sum, 1, 256, E->t, E->np, E->nz, c.dz, nus);
+    // checkdivb: d1bydx(bx), d1bydy(by) (src/utils.F90:263-265)
+    int st;
+    LineJob<double> jx = ljob<double>(E->bx, E->s64[0], OP_D1);
+    LineJob<double> jy = ljob<double>(E->by, E->s64[1], OP_D1);
+    if ((st = launch_lines<double>(E, 0, &jx, 1))) return st;
+    if ((st = launch_lines<double>(E, 1, &jy, 1))) return st;
+    double *mm = nus + 8;
+    int blocks = E->red_blocks;
+    KLAUNCH(E, "minmax", k_minmax, blocks, 256, E->r, E->t, E->u, E->v, E->w, E->bx, E->by, E->bz, E->s64[0],
+            E->s64[1], E->np, E->nz, c.ho12, mm);
+    CUDA_TRY(cudaMemcpyAsync(E->hs, E->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E->stream));
+    std::vector<double> h((size_t)blocks * 2 * NMM + 8);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), nus, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, E->stream));
+    CUDA_TRY(cudaStreamSynchronize(E->stream));
+    vec_diag_out d;
+    memset(&d, 0, sizeof(d));
+    d.ubar = E->hs->res[0];
+    d.vbar = E->hs->res[1];
+    d.kenergy = E->hs->res[2];
+    d.menergy = E->p.kinematic ? E->hs->res[3] : E->p.f * E->hs->res[3];
+    double tzbar = h[0] * c.xn;
+    d.nusselt = (tzbar - c.nusstmp) / (c.theta - c.nusstmp);
+    double mn[NMM], mx[NMM];
+    for (int m = 0; m < NMM; m++) { mn[m] = 1.0e300; mx[m] = -1.0e300; }
+    for (int b = 0; b < blocks; b++)
+        for (int m = 0; m < NMM; m++) {
+            mn[m] = fmin(mn[m], h[8 + (size_t)b * 2 * NMM + m]);
+            mx[m] = fmax(mx[m], h[8 + (size_t)b * 2 * NMM + NMM + m]);
+        }
+    d.rmin = mn[0]; d.rmax = mx[0]; d.tmin = mn[1]; d.tmax = mx[1]; d.umin = mn[2]; d.umax = mx[2];
+    d.vmin = mn[3]; d.vmax = mx[3]; d.wmin = mn[4]; d.wmax = mx[4]; d.bxmin = mn[5]; d.bxmax = mx[5];
+    d.bymin = mn[6]; d.bymax = mx[6]; d.bzmin = mn[7]; d.bzmax = mx[7];
+    double fa = E->p.kinematic ? 1.0 : E->p.f;
+    d.machmin = sqrt(mn[8] / E->p.gamma); d.machmax = sqrt(mx[8] / E->p.gamma);
+    d.alfvenmin = sqrt(fa * mn[9]); d.alfvenmax = sqrt(fa * mx[9]);
+    d.rmsmin = sqrt(mn[10]); d.rmsmax = sqrt(mx[10]);
+    // checkdivb starts its minimum at 1.0 (src/utils.F90:275-276)
+    d.divbmax = fmax(-1.0e30, mx[11]);
+    d.divbmin = fmin(1.0, mn[11]);
+    if (out) *out = d;
+    E->last_diag = d;
+    E->have_diag = 1;
+    double divbtest = fmax(fabs(d.divbmax), fabs(d.divbmin));
+    if (divbtest > 0.01) return VEC_ERR_DIVB;
+    return VEC_OK;
+}
+
+// ============================================================================
+// initial state: src/initial.F90:25-86 with RANSET (src/ranset.f90:1-29)
+// ============================================================================
+// RAN0 keeps s = idum XOR MASK as a pure Park-Miller sequence
+// s_{m+1} = 16807 s_m mod (2^31-1) and returns AM*s_{m+1}, so the n-th draw
+// of a layer is AM * 16807^(n+1) s_0 mod (2^31-1): each point jumps ahead on
+// its own.
+__device__ __forceinline__ unsigned long long mulmod31(unsigned long long a, unsigned long long b)
+{
+    return (a * b) % 2147483647ull;
+}
+
+__global__ void k_static(double *r, double *t, double *u, double *v, double *w, double *bx, double *by,
+                         double *bz, const double *t0k, const double *r0k, size_t np, int nz, double amp,
+                         int seed_base, int perfect)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const unsigned MASK = 123459876u;
+    unsigned s0 = (unsigned)(seed_base + 64 * (k + 1)) ^ MASK;
+    // 16807^(q+1) mod M
+    unsigned long long e = (unsigned long long)q + 1ull, base = 16807ull, pw = 1ull;
+    while (e) {
+        if (e & 1ull) pw = mulmod31(pw, base);
+        base = mulmod31(base, base);
+        e >>= 1;
+    }
+    unsigned long long s = mulmod31(pw, (unsigned long long)s0);
+    const double AM = 1.0 / 2147483647.0;
+    double ran = __dmul_rn(AM, (double)s);
+    double noise = __dmul_rn(__dmul_rn(2.0, __dsub_rn(ran, 0.5)), amp);
+    u[idx] = 0.0; v[idx] = 0.0; w[idx] = 0.0;
+    r[idx] = r0k[k];
+    t[idx] = __dadd_rn(noise, t0k[k]);
+    if (perfect) { bx[idx] = 1.0; by[idx] = 0.0; bz[idx] = 0.0; }
+    else { bx[idx] = 0.0; by[idx] = 0.0; bz[idx] = 1.0; }
+}
+
+int phys_static(Engine *E)
+{
+    std::vector<double> t0(E->nz), r0(E->nz);
+    for (int k = 0; k < E->nz; k++) {
+        double z = (double)k * E->k.dz;
+        t0[k] = 1.0 + z * E->p.theta;
+        r0[k] = pow(t0[k], E->p.cm);
+    }
+    double *d = E->w1d;   // 8 nz scratch
+    CUDA_TRY(cudaMemcpyAsync(d, t0.data(), sizeof(double) * E->nz, cudaMemcpyHostToDevice, E->stream));
+    CUDA_TRY(cudaMemcpyAsync(d + E->nz, r0.data(), sizeof(double) * E->nz, cudaMemcpyHostToDevice, E->stream));
+    KLAUNCH(E, "static_ic", k_static, nblk(E->n), TPB, E->r, E->t, E->u, E->v, E->w, E->bx, E->by, E->bz, d,
+            d + E->nz, E->np, E->nz, E->p.noise_amp, E->p.seed_base, E->p.perfect);
+    CUDA_TRY(cudaStreamSynchronize(E->stream));
+    return VEC_OK;
+}
+
+// ============================================================================
+// mag_init: src/magnetic.f90:5-279
+// ============================================================================
+__global__ void k_dynamo_seed(double *bx, double *by, double *bz, int nx, int ny, size_t n, int perfect)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    size_t np = (size_t)nx * ny;
+    size_t q = idx % np;
+    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    const double seedfield = 0.003;
+    const double tpx = 8.0 * atan(1.0) / (nx * 1.0), tpy = 8.0 * atan(1.0) / (ny * 1.0);
+    if (perfect) {
+        bx[idx] = seedfield * cos(tpy * (j + 1));
+        by[idx] = seedfield * cos(tpx * (i + 1));
+        bz[idx] = 0.0;
+    } else {
+        bx[idx] = 0.0;
+        by[idx] = 0.0;
+        bz[idx] = seedfield * cos(tpx * (i + 1)) * cos(tpy * (j + 1));
+    }
+}
+
+struct MagInitArgs {
+    const double *ex, *ey, *ez, *akx1, *aky1, *akx2, *aky2;
+    double *pol, *tor, *w1, *w2, *w3;
+    int nx, ny, nz;
+};
+
+// :123-233: pol, tor from the truncated spectra; Jz, dBz/dy, dBz/dx spectra
+__global__ void k_mag_init_spec(MagInitArgs a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+    const double *pey = a.ey + (size_t)k * np, *pex = a.ex + (size_t)k * np, *pez = a.ez + (size_t)k * np;
+    const double kk = a.akx2[i] + a.aky2[j];
+    double pol, tor;
+    if (i == 0 && j == 0) { pol = 0.0; tor = 0.0; }
+    else {
+        pol = -1.0 * a.ez[idx] / kk;
+        double jz = sdx(pey, i, j, a.nx, a.akx1) - sdy(pex, i, j, a.nx, a.ny, a.aky1);
+        tor = -1.0 * jz / kk;
+    }
+    a.pol[idx] = pol;
+    a.tor[idx] = tor;
+    a.w3[idx] = -1.0 * tor * kk;
+    a.w1[idx] = sdy(pez, i, j, a.nx, a.ny, a.aky1);
+    a.w2[idx] = sdx(pez, i, j, a.nx, a.akx1);
+}
+
+__global__ void k_mag_init_means(const double *ex, const double *ey, const double *ez, double *bxbar,
+                                 double *bybar, double *bzbar_out, size_t np, int nz, double xn)
+{
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        bxbar[k] = ex[(size_t)k * np] * xn;
+        bybar[k] = ey[(size_t)k * np] * xn;
+    }
+    if (threadIdx.x == 0) bzbar_out[0] = ez[0] * xn;
+}
+
+int phys_mag_init(Engine *E)
+{
+    double *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
+    int st;
+    if (E->p.dynamo)
+        KLAUNCH(E, "dynamo_seed", k_dynamo_seed, nblk(E->n), TPB, E->bx, E->by, E->bz, E->nx, E->ny, E->n, E->p.perfect);
+    LineJob<double> fx[3] = { ljob<double>(E->bx, W[W_EX], OP_FWD), ljob<double>(E->by, W[W_EY], OP_FWD),
+                              ljob<double>(E->bz, W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<double>(E, 0, fx, 3))) return st;
+    LineJob<double> fy[3] = { ljob<double>(W[W_EX], W[W_EX], OP_FWD), ljob<double>(W[W_EY], W[W_EY], OP_FWD),
+                              ljob<double>(W[W_EZ], W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
+    for (int f = 0; f < 3; f++)     // :70-103
+        KLAUNCH(E, "truncate_f64", k_truncate<double>, nblk(E->n), TPB, W[W_EX + f], (double *)nullptr, E->nx, E->ny,
+                E->nz, E->k.icutoffx, E->k.icutoffy);
+    KLAUNCH(E, "mag_init_means", k_mag_init_means, 1, 256, W[W_EX], W[W_EY], W[W_EZ], E->bxbar, E->bybar,
+            E->w1d + 7 * E->nz, E->np, E->nz, E->k.xn);
+    double bzb = 0.0;
+    CUDA_TRY(cudaMemcpyAsync(&bzb, E->w1d + 7 * E->nz, sizeof(double), cudaMemcpyDeviceToHost, E->stream));
+    CUDA_TRY(cudaStreamSynchronize(E->stream));
+    E->bzbar = bzb;
+    MagInitArgs a;
+    a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2;
+    a.aky2 = E->aky2; a.pol = E->pol; a.tor = E->tor; a.w1 = W[W_M1]; a.w2 = W[W_M2]; a.w3 = W[W_M3];
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
+    KLAUNCH(E, "mag_init_spec", k_mag_init_spec, nblk(E->n), TPB, a);
+    LineJob<double> ix[3] = { ljob<double>(W[W_M1], W[W_M1], OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
+                              ljob<double>(W[W_M3], W[W_M3], OP_INV) };
+    if ((st = launch_lines<double>(E, 0, ix, 3))) return st;
+    if ((st = launch_lines<double>(E, 1, ix, 3))) return st;
+    // jsq (:246-261): ex = inv(dBz/dy), ey = inv(dBz/dx), ez = inv(Jz)
+    KLAUNCH(E, "jsq_f64", k_jsq, nblk(E->n), TPB, W[W_M3], W[W_M1], W[W_M2], E->bx, E->by, E->jsq, E->np, E->nz,
+            E->k.ho12);
+    return phys_mag_boundary(E);
+}

@@ -1,0 +1,94 @@
+// zstencil.cuh -- the 4th-order z finite differences of src/dbydz.F90,
+// evaluated for one (i,j) column at plane k (0-based; k=0 is the top).
+// f points at plane 0 of the column; planes are np elements apart.
+// Row formulas (serial branches src/dbydz.F90:1685-1751, 2353-2424,
+// 3007-3083):
+//   d1:   k=0 topdz(flag) :927, k=1 topdz_low :1053, interior :371,
+//         k=nz-2 lastdz_up :776, k=nz-1 lastdz(flag) :626
+//   d1up: as d1 but k=2 dup_up :532, 3..nz-4 dupinterior :485,
+//         k=nz-3 dup_low :579, sign test on w at the same point
+//   d2:   k=0 d2topdz(flag) :1368, k=1 d2topdz_low :1462, d2interior :428,
+//         k=nz-2 d2lastdz_up :1271, k=nz-1 d2lastdz(flag) :1180
+#pragma once
+
+template <typename R>
+__device__ __forceinline__ R zld(const R *f, size_t np, int k) { return f[(size_t)k * np]; }
+
+template <typename R>
+__device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R h)
+{
+#define F(kk) zld(f, np, kk)
+    if (k == 0) {
+        if (fl == 1) return h * ((R)14 * F(0) + (R)36 * F(1) - (R)18 * F(2) + (R)4 * F(3));
+        if (fl == 5) return h * ((R)-22 * F(0) + (R)36 * F(1) - (R)18 * F(2) + (R)4 * F(3));
+        return (R)0;
+    }
+    if (k == 1) return h * ((R)-4 * F(0) - (R)6 * F(1) + (R)12 * F(2) - (R)2 * F(3));
+    if (k == nz - 2) return h * ((R)4 * F(nz - 1) + (R)6 * F(nz - 2) - (R)12 * F(nz - 3) + (R)2 * F(nz - 4));
+    if (k == nz - 1) {
+        if (fl == 1) return h * ((R)-14 * F(nz - 1) - (R)36 * F(nz - 2) + (R)18 * F(nz - 3) - (R)4 * F(nz - 4));
+        if (fl == 5) return h * ((R)22 * F(nz - 1) - (R)36 * F(nz - 2) + (R)18 * F(nz - 3) - (R)4 * F(nz - 4));
+        return (R)0;
+    }
+    return h * (F(k - 2) - (R)8 * F(k - 1) + (R)8 * F(k + 1) - F(k + 2));
+#undef F
+}
+
+template <typename R>
+__device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl, R h, R wv)
+{
+#define F(kk) zld(f, np, kk)
+    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k == 2) {
+        if (wv >= (R)0) return h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3));
+        return h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1));
+    }
+    if (k == nz - 3) {
+        if (wv >= (R)0)
+            return h * (-F(nz - 6) + (R)6 * F(nz - 5) - (R)18 * F(nz - 4) + (R)10 * F(nz - 3) + (R)3 * F(nz - 2));
+        return h * ((R)-2 * F(nz - 1) + (R)12 * F(nz - 2) - (R)6 * F(nz - 3) - (R)4 * F(nz - 4));
+    }
+    if (wv >= (R)0)
+        return h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1));
+    return h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1));
+#undef F
+}
+
+template <typename R>
+__device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, int fl, R s)
+{
+#define F(kk) zld(f, np, kk)
+    if (k == 0) {
+        if (fl == 3)
+            return s * ((R)45 * F(0) - (R)154 * F(1) + (R)214 * F(2) - (R)156 * F(3) + (R)61 * F(4) - (R)10 * F(5));
+        return (R)0;
+    }
+    if (k == 1)
+        return s * ((R)10 * F(0) - (R)15 * F(1) - (R)4 * F(2) + (R)14 * F(3) - (R)6 * F(4) + F(5));
+    if (k == nz - 2)
+        return s * ((R)10 * F(nz - 1) - (R)15 * F(nz - 2) - (R)4 * F(nz - 3) + (R)14 * F(nz - 4) - (R)6 * F(nz - 5) + F(nz - 6));
+    if (k == nz - 1) {
+        if (fl == 3)
+            return s * ((R)45 * F(nz - 1) - (R)154 * F(nz - 2) + (R)214 * F(nz - 3) - (R)156 * F(nz - 4) + (R)61 * F(nz - 5) - (R)10 * F(nz - 6));
+        return (R)0;
+    }
+    return s * (-F(k - 2) + (R)16 * F(k - 1) - (R)30 * F(k) + (R)16 * F(k + 1) - F(k + 2));
+#undef F
+}
+
+// spectral d/dx of a 2-D halfcomplex plane at (i,j): index shuffle of
+// src/fft.F90:292-302 (the reference's "+ik" on the x halfcomplex index).
+template <typename R>
+__device__ __forceinline__ R sdx(const R *plane, int i, int j, int nx, const double *akx1)
+{
+    if (i == 0 || 2 * i == nx) return (R)0;
+    R v = plane[(size_t)j * nx + (nx - i)] * (R)akx1[i];
+    return 2 * i < nx ? -v : v;
+}
+template <typename R>
+__device__ __forceinline__ R sdy(const R *plane, int i, int j, int nx, int ny, const double *aky1)
+{
+    if (j == 0 || 2 * j == ny) return (R)0;
+    R v = plane[(size_t)(ny - j) * nx + i] * (R)aky1[j];
+    return 2 * j < ny ? -v : v;
+}

@@ -1,0 +1,86 @@
+"""ctypes binding of libvec_gpu.so (the C-ABI of include/vec.h).
+
+There is no CPU fallback: if the CUDA library is missing, loading fails
+with an error naming the file.
+"""
+import ctypes as C
+import os
+
+from .params import VecDiag, VecParams, VecScalars
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libvec_gpu.so")
+
+# exported symbols of include/vec.h with their ctypes signatures
+_vp = C.c_void_p
+_dp = C.c_void_p   # double* (host numpy data pointer or device pointer)
+SIGNATURES = {
+    "vec_params_default": (C.c_int, [C.POINTER(VecParams)]),
+    "vec_params_read_input": (C.c_int, [C.c_char_p, C.POINTER(VecParams)]),
+    "vec_create": (C.c_int, [C.POINTER(VecParams), C.POINTER(_vp)]),
+    "vec_destroy": (C.c_int, [_vp]),
+    "vec_last_error": (C.c_char_p, []),
+    "vec_stream": (_vp, [_vp]),
+    "vec_sync": (C.c_int, [_vp]),
+    "vec_set_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "vec_get_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "vec_set_mean": (C.c_int, [_vp, C.c_int, _dp]),
+    "vec_get_mean": (C.c_int, [_vp, C.c_int, _dp]),
+    "vec_set_bzbar": (C.c_int, [_vp, C.c_double]),
+    "vec_get_bzbar": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "vec_get_scalars": (C.c_int, [_vp, C.POINTER(VecScalars)]),
+    "vec_set_scalars": (C.c_int, [_vp, C.POINTER(VecScalars)]),
+    "vec_static": (C.c_int, [_vp]),
+    "vec_mag_init": (C.c_int, [_vp]),
+    "vec_calcdt": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "vec_d1bydx": (C.c_int, [_vp, _dp, _dp]),
+    "vec_d1bydy": (C.c_int, [_vp, _dp, _dp]),
+    "vec_d2bydx": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "vec_d2bydy": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "vec_dealias": (C.c_int, [_vp, _dp]),
+    "vec_forwardfft": (C.c_int, [_vp, _dp, _dp]),
+    "vec_inversefft": (C.c_int, [_vp, _dp, _dp]),
+    "vec_d1bydz": (C.c_int, [_vp, _dp, _dp, C.c_int]),
+    "vec_d1upbydz": (C.c_int, [_vp, _dp, _dp, C.c_int]),
+    "vec_d2bydz": (C.c_int, [_vp, _dp, _dp, C.c_int]),
+    "vec_d1bydz1d": (C.c_int, [_vp, _dp, _dp, C.c_int]),
+    "vec_d2bydz1d": (C.c_int, [_vp, _dp, _dp, C.c_int]),
+    "vec_hydro_deriv": (C.c_int, [_vp]),
+    "vec_mag_deriv": (C.c_int, [_vp]),
+    "vec_bandj": (C.c_int, [_vp]),
+    "vec_magdealias": (C.c_int, [_vp]),
+    "vec_boundary": (C.c_int, [_vp]),
+    "vec_mag_boundary": (C.c_int, [_vp]),
+    "vec_ab3_update": (C.c_int, [_vp]),
+    "vec_diag": (C.c_int, [_vp, C.POINTER(VecDiag)]),
+    "vec_step": (C.c_int, [_vp, C.c_int]),
+    "vec_last_diag": (C.c_int, [_vp, C.POINTER(VecDiag)]),
+    "vec_profile": (C.c_int, [_vp, C.c_int]),
+    "vec_profile_count": (C.c_int, [_vp]),
+    "vec_profile_get": (C.c_int, [_vp, C.c_int, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "vec_profile_reset": (C.c_int, [_vp]),
+    "vec_launch_count": (C.c_longlong, [_vp]),
+}
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def load():
+    """Load libvec_gpu.so (loading needs no GPU; calls that compute do)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(
+                f"CUDA library {LIB_PATH} is missing: run `python -m fug30v0kxc_gb300.build` "
+                "(or __graft_entry__.build()) first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib

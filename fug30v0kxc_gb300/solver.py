@@ -1,0 +1,226 @@
+"""Python mirror of the reference's operator interface, backed by the GPU.
+
+The names follow the reference's module procedures (src/fft.F90,
+src/dbydz.F90, src/hydro_deriv.f90, src/magnetic.f90, src/utils.F90,
+src/main.F90); arrays are numpy (nz, ny, nx) views of the Fortran
+(nx, ny, nz) layout.  Every call goes through the C-ABI of include/vec.h
+into the sm_103a kernels; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _L
+from .params import (FIELD_NAMES, MEAN_NAMES, STATE_FIELDS, STATUS, VecDiag, VecParams,
+                     VecScalars)
+
+
+class VecError(RuntimeError):
+    def __init__(self, where, status):
+        msg = _L.load().vec_last_error().decode(errors="replace")
+        super().__init__(f"{where}: status {status} ({STATUS.get(status, '?')}) {msg}")
+        self.status = status
+
+
+def _ptr(a):
+    """data pointer of a numpy array, or an int device pointer (torch tensors)."""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return int(a)
+
+
+class P3D:
+    """One device-resident VarElecCond context (src/arrays.f90 in HBM)."""
+
+    def __init__(self, params: VecParams):
+        self.L = _L.load()
+        self.p = params.copy()
+        h = C.c_void_p()
+        st = self.L.vec_create(C.byref(self.p), C.byref(h))
+        if st != 0:
+            raise VecError("vec_create", st)
+        self.h = h
+        self.shape = (self.p.nz, self.p.ny, self.p.nx)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.vec_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st, where):
+        if st != 0:
+            raise VecError(where, st)
+
+    # -- state ----------------------------------------------------------------
+    def get(self, name):
+        out = np.empty(self.shape, dtype=np.float64)
+        self._chk(self.L.vec_get_field(self.h, FIELD_NAMES[name], out.ctypes.data), name)
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.shape)
+        self._chk(self.L.vec_set_field(self.h, FIELD_NAMES[name], a.ctypes.data), name)
+
+    def get_mean(self, name):
+        out = np.empty(self.p.nz, dtype=np.float64)
+        self._chk(self.L.vec_get_mean(self.h, MEAN_NAMES[name], out.ctypes.data), name)
+        return out
+
+    def set_mean(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._chk(self.L.vec_set_mean(self.h, MEAN_NAMES[name], a.ctypes.data), name)
+
+    @property
+    def bzbar(self):
+        v = C.c_double()
+        self.L.vec_get_bzbar(self.h, C.byref(v))
+        return v.value
+
+    @bzbar.setter
+    def bzbar(self, v):
+        self.L.vec_set_bzbar(self.h, float(v))
+
+    def scalars(self):
+        s = VecScalars()
+        self._chk(self.L.vec_get_scalars(self.h, C.byref(s)), "scalars")
+        return s
+
+    def set_scalars(self, s):
+        self._chk(self.L.vec_set_scalars(self.h, C.byref(s)), "set_scalars")
+
+    def state(self):
+        d = {n: self.get(n) for n in STATE_FIELDS}
+        d["bxbar"] = self.get_mean("bxbar")
+        d["bybar"] = self.get_mean("bybar")
+        return d
+
+    def load_state(self, d, bzbar=None):
+        for n in STATE_FIELDS:
+            if n in d:
+                self.set(n, d[n])
+        for n in ("bxbar", "bybar"):
+            if n in d:
+                self.set_mean(n, d[n])
+        if bzbar is not None:
+            self.bzbar = bzbar
+
+    # -- src/fft.F90 ---------------------------------------------------------------
+    def _o1(self, fn, fin, name):
+        fin = np.ascontiguousarray(fin, dtype=np.float64).reshape(self.shape)
+        out = np.empty_like(fin)
+        self._chk(fn(self.h, fin.ctypes.data, out.ctypes.data), name)
+        return out
+
+    def d1bydx(self, f): return self._o1(self.L.vec_d1bydx, f, "d1bydx")
+    def d1bydy(self, f): return self._o1(self.L.vec_d1bydy, f, "d1bydy")
+    def forwardfft(self, f): return self._o1(self.L.vec_forwardfft, f, "forwardfft")
+    def inversefft(self, f): return self._o1(self.L.vec_inversefft, f, "inversefft")
+
+    def d2bydx(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.shape)
+        a, b = np.empty_like(f), np.empty_like(f)
+        self._chk(self.L.vec_d2bydx(self.h, f.ctypes.data, a.ctypes.data, b.ctypes.data), "d2bydx")
+        return a, b
+
+    def d2bydy(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.shape)
+        a, b = np.empty_like(f), np.empty_like(f)
+        self._chk(self.L.vec_d2bydy(self.h, f.ctypes.data, a.ctypes.data, b.ctypes.data), "d2bydy")
+        return a, b
+
+    def dealias(self, f):
+        z = np.array(f, dtype=np.float64).reshape(self.shape)
+        self._chk(self.L.vec_dealias(self.h, z.ctypes.data), "dealias")
+        return z
+
+    # -- src/dbydz.F90 ---------------------------------------------------------------
+    def _oz(self, fn, f, flag, shape, name):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(shape)
+        out = np.empty_like(f)
+        self._chk(fn(self.h, f.ctypes.data, out.ctypes.data, flag), name)
+        return out
+
+    def d1bydz(self, f, flag): return self._oz(self.L.vec_d1bydz, f, flag, self.shape, "d1bydz")
+    def d1upbydz(self, f, flag): return self._oz(self.L.vec_d1upbydz, f, flag, self.shape, "d1upbydz")
+    def d2bydz(self, f, flag): return self._oz(self.L.vec_d2bydz, f, flag, self.shape, "d2bydz")
+    def d1bydz1d(self, f, flag): return self._oz(self.L.vec_d1bydz1d, f, flag, (self.p.nz,), "d1bydz1D")
+    def d2bydz1d(self, f, flag): return self._oz(self.L.vec_d2bydz1d, f, flag, (self.p.nz,), "d2bydz1D")
+
+    # -- physics -------------------------------------------------------------------------
+    def static(self): self._chk(self.L.vec_static(self.h), "static")
+    def mag_init(self): self._chk(self.L.vec_mag_init(self.h), "mag_init")
+    def hydro_deriv(self): self._chk(self.L.vec_hydro_deriv(self.h), "hydro_deriv")
+    def mag_deriv(self): self._chk(self.L.vec_mag_deriv(self.h), "mag_deriv")
+    def bandj(self): self._chk(self.L.vec_bandj(self.h), "bandj")
+    def magdealias(self): self._chk(self.L.vec_magdealias(self.h), "magdealias")
+    def boundary(self): self._chk(self.L.vec_boundary(self.h), "boundary")
+    def mag_boundary(self): self._chk(self.L.vec_mag_boundary(self.h), "mag_boundary")
+    def ab3_update(self): self._chk(self.L.vec_ab3_update(self.h), "ab3_update")
+
+    def calcdt(self):
+        dt = C.c_double()
+        self._chk(self.L.vec_calcdt(self.h, C.byref(dt)), "calcdt")
+        return dt.value
+
+    def diag(self):
+        d = VecDiag()
+        st = self.L.vec_diag(self.h, C.byref(d))
+        return st, d.as_dict()
+
+    def last_diag(self):
+        d = VecDiag()
+        self.L.vec_last_diag(self.h, C.byref(d))
+        return d.as_dict()
+
+    def step(self, n=1):
+        """n iterations of the time loop (src/main.F90:340-747); returns the status."""
+        return self.L.vec_step(self.h, n)
+
+    def start(self):
+        """static IC, calcdt, mag_init (src/main.F90:275-333, nframe=0)."""
+        self.static()
+        self.calcdt()
+        if self.p.f != 0.0 or self.p.kinematic:
+            self.mag_init()
+
+    # -- instrumentation -----------------------------------------------------------------
+    def stream(self):
+        return self.L.vec_stream(self.h)
+
+    def sync(self):
+        self._chk(self.L.vec_sync(self.h), "sync")
+
+    def profile(self, on=True):
+        self._chk(self.L.vec_profile(self.h, 1 if on else 0), "profile")
+
+    def profile_reset(self):
+        self.L.vec_profile_reset(self.h)
+
+    def profile_records(self):
+        out = []
+        name = C.create_string_buffer(64)
+        for i in range(self.L.vec_profile_count(self.h)):
+            n, ms = C.c_int(), C.c_double()
+            self.L.vec_profile_get(self.h, i, name, C.byref(n), C.byref(ms))
+            out.append((name.value.decode(), n.value, ms.value))
+        return out
+
+    def launch_count(self):
+        return self.L.vec_launch_count(self.h)
+
+
+def read_input(path):
+    """Parse a reference INPUT file (src/initial.F90:94-201) via the C-ABI."""
+    p = VecParams()
+    st = _L.load().vec_params_read_input(path.encode(), C.byref(p))
+    if st != 0:
+        raise VecError("vec_params_read_input", st)
+    return p

@@ -1,0 +1,206 @@
+/*
+ * vec.h -- C-ABI of the GB300 (sm_103a) VarElecCond time-step library.
+ *
+ * The reference (VarElecCond "p3d", Fortran 90) keeps all of its state in
+ * module globals (src/arrays.f90:14-74) and exposes argument-light module
+ * procedures.  This header replaces those procedures with plain C entry
+ * points over an opaque context that owns every device array.
+ *
+ * Conventions
+ *   - Fields are (nx,ny,nz) arrays of double, x fastest, exactly the
+ *     Fortran column-major layout of src/arrays.f90:14-74: element
+ *     (i,j,k) (1-based) lives at offset (i-1) + nx*((j-1) + ny*(k-1)).
+ *     Plane k=1 is the top of the layer (z=0), k=nz the bottom (z=1),
+ *     src/main.F90:5-9.
+ *   - pol/tor are stored in the reference's 2-D halfcomplex x halfcomplex
+ *     order (src/magnetic.f90:123-136, src/fft.F90:687-735).
+ *   - Array pointers handed to an entry point may be host or device
+ *     pointers: the library asks the CUDA runtime which one it got.  Host
+ *     buffers are read/written only during the call; no pointer is kept.
+ *   - Every entry point returns an int status: VEC_OK (0) or a negative
+ *     code below.  Nothing aborts, traps or exits inside the library.
+ *   - One context per host thread; calls on a context are stream-ordered
+ *     on the context's own stream and are not re-entrant.
+ */
+#ifndef VEC_H
+#define VEC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (negative, mirroring the reference's iret/abort codes) */
+#define VEC_OK              0
+#define VEC_ERR_NX         -1   /* odd nx: src/fft.F90:112-115 (also nx<4)  */
+#define VEC_ERR_NY         -2   /* odd ny: src/fft.F90:116-119 (also ny<4)  */
+#define VEC_ERR_NZ         -4   /* nz<6: src/main.F90:216-219, dbydz :355-358 */
+#define VEC_ERR_ALLOC      -5   /* allocation failure: src/fft.F90:150-157  */
+#define VEC_ERR_FLAG       -7   /* unknown dflag: src/dbydz.F90:704-707      */
+#define VEC_ERR_INPUT      -8   /* unreadable / inconsistent INPUT file      */
+#define VEC_ERR_DIVB      -12   /* |div B| > 0.01: src/main.F90:583-590      */
+#define VEC_ERR_NAN       -20   /* non-finite value in the state             */
+#define VEC_ERR_CUDA      -30   /* CUDA runtime error                        */
+#define VEC_ERR_ARG       -31   /* null pointer / bad field id / bad value   */
+#define VEC_ERR_SIZE      -32   /* size outside what the kernels support     */
+
+/* ---- precision forms */
+#define VEC_PREC_FP64       0   /* plain FP64 drop-in                        */
+#define VEC_PREC_SPLIT      1   /* FP32 bulk, FP64 background/state/diagnostics */
+
+/* ---- parameters: the INPUT file (src/initial.F90:142-172), the control
+ *      flags hard-coded in src/main.F90:108-116, and the extensions. */
+typedef struct vec_params {
+    /* physical parameters, src/params.f90:9-28 (after the Ra/Q -> ck/F
+     * conversion of src/initial.F90:174-201) */
+    double gamma, sigma, theta, ck, cm, f, tayl, psi, zeta, xmax, ymax, sf;
+    double rayl, chand;
+    /* extensions with no reference counterpart (1.0 / 0 reproduce it) */
+    double eta_contrast;   /* eta(z) = zeta*ck*(1 + (eta_contrast-1)*z)     */
+    double noise_amp;      /* static IC noise amplitude (reference: 0.1)     */
+    /* grid and run control */
+    int32_t nx, ny, nz;
+    int32_t nframe, ntotal, ndu06, ndu16, ndurestart;
+    /* control flags, src/main.F90:108-116 (reference defaults in brackets) */
+    int32_t dalias;        /* [1] dealias r,t,u,v,w every 10 steps           */
+    int32_t kinematic;     /* [0]                                           */
+    int32_t radbc;         /* [0] radiative upper temperature BC            */
+    int32_t constflux;     /* [0] fixed-flux lower temperature BC           */
+    int32_t perfect;       /* [0] perfectly conducting magnetic BC          */
+    int32_t dynamo;        /* [0] seed field inserted by mag_init           */
+    /* extensions */
+    int32_t kappa_uniform; /* [0] 0: tanh kappa(z) of trans_params.f90:36-62 */
+    int32_t seed_base;     /* [1996] RANSET seed base, src/ranset.f90:7      */
+    int32_t precision;     /* VEC_PREC_FP64 or VEC_PREC_SPLIT               */
+    int32_t diag_cadence;  /* [1] run GlobalAverages/nusselt/checkdivb every ndu06 */
+} vec_params;
+
+/* scalars of the time loop, src/main.F90:84-103 */
+typedef struct vec_scalars {
+    double dt, dt1, dt2, ttime;
+    int32_t iter, nit, first, second;
+} vec_scalars;
+
+/* diagnostics printed every ndu06 steps, src/main.F90:552-647 */
+typedef struct vec_diag_out {
+    double ubar, vbar, kenergy, menergy, nusselt;
+    double divbmax, divbmin;
+    double rmin, rmax, tmin, tmax, umin, umax, vmin, vmax, wmin, wmax;
+    double bxmin, bxmax, bymin, bymax, bzmin, bzmax;
+    double machmin, machmax, alfvenmin, alfvenmax, rmsmin, rmsmax;
+} vec_diag_out;
+
+/* field ids for vec_get_field / vec_set_field (src/arrays.f90:14-74) */
+enum vec_field {
+    VEC_F_R = 0, VEC_F_T, VEC_F_U, VEC_F_V, VEC_F_W,
+    VEC_F_BX, VEC_F_BY, VEC_F_BZ, VEC_F_JSQ, VEC_F_POL, VEC_F_TOR,
+    /* RHS histories: slot s (1..3 in the reference) = base + (s-1) */
+    VEC_F_RDOT = 16, VEC_F_TDOT = 19, VEC_F_UDOT = 22, VEC_F_VDOT = 25,
+    VEC_F_WDOT = 28, VEC_F_POLDOT = 31, VEC_F_TORDOT = 34,
+    VEC_F_COUNT = 37
+};
+/* 1-D mean-field ids for vec_get_mean / vec_set_mean */
+enum vec_mean {
+    VEC_M_BXBAR = 0, VEC_M_BYBAR,
+    VEC_M_BXBARDOT = 2,  /* +0..2 = slots 1..3 */
+    VEC_M_BYBARDOT = 5,
+    VEC_M_KAPPA = 8, VEC_M_DKAPPA, VEC_M_ETA, VEC_M_DETA,
+    VEC_M_COUNT = 12
+};
+
+typedef struct vec_ctx vec_ctx;
+
+/* ---- parameters and context ------------------------------------------ */
+/* Reference defaults: bin/INPUT values and the flags of src/main.F90:108-116. */
+int vec_params_default(vec_params *p);
+/* Reads an INPUT file (src/initial.F90:94-201, flag 1 = CK/F, 2 = Ra/Q). */
+int vec_params_read_input(const char *path, vec_params *p);
+/* Derived constants are set as in src/constants.f90:56-109, wavenumbers as
+ * in init_fft (src/fft.F90:88-223), stencil scales as in init_dbydz
+ * (src/dbydz.F90:355-362); all arrays of src/arrays.f90:81-300 are
+ * allocated on the current CUDA device. */
+int vec_create(const vec_params *p, vec_ctx **ctx);
+int vec_destroy(vec_ctx *ctx);
+const char *vec_last_error(void);
+/* the context's CUDA stream (a cudaStream_t) */
+void *vec_stream(vec_ctx *ctx);
+int vec_sync(vec_ctx *ctx);
+
+/* ---- state I/O --------------------------------------------------------- */
+int vec_set_field(vec_ctx *ctx, int field, const double *src);
+int vec_get_field(vec_ctx *ctx, int field, double *dst);
+int vec_set_mean(vec_ctx *ctx, int mean, const double *src);  /* nz values */
+int vec_get_mean(vec_ctx *ctx, int mean, double *dst);
+int vec_set_bzbar(vec_ctx *ctx, double bzbar);
+int vec_get_bzbar(vec_ctx *ctx, double *bzbar);
+int vec_get_scalars(vec_ctx *ctx, vec_scalars *s);
+int vec_set_scalars(vec_ctx *ctx, const vec_scalars *s);
+
+/* ---- set-up ------------------------------------------------------------ */
+/* static polytrope + seeded noise, src/initial.F90:25-86 with RANSET
+ * (src/ranset.f90:1-29), then ini_trans_params (src/main.F90:276-280) */
+int vec_static(vec_ctx *ctx);
+/* B (real space) -> pol, tor, means, jsq; src/magnetic.f90:5-279 */
+int vec_mag_init(vec_ctx *ctx);
+/* CFL + diffusive time step, src/utils.F90:144-244; also stored as ctx dt */
+int vec_calcdt(vec_ctx *ctx, double *dt);
+
+/* ---- horizontal spectral operators, src/fft.F90:255-799 ---------------- */
+int vec_d1bydx(vec_ctx *ctx, const double *fin, double *fout);
+int vec_d1bydy(vec_ctx *ctx, const double *fin, double *fout);
+int vec_d2bydx(vec_ctx *ctx, const double *fin, double *f1out, double *f2out);
+int vec_d2bydy(vec_ctx *ctx, const double *fin, double *f1out, double *f2out);
+int vec_dealias(vec_ctx *ctx, double *z);
+int vec_forwardfft(vec_ctx *ctx, const double *fin, double *fout);
+int vec_inversefft(vec_ctx *ctx, const double *fin, double *fout);
+
+/* ---- vertical finite differences, src/dbydz.F90:1588-3673 -------------- */
+int vec_d1bydz(vec_ctx *ctx, const double *fin, double *fout, int dflag);
+/* the upwind sign test reads the context's w, as the reference reads the
+ * module-global w (src/dbydz.F90:511,559,606) */
+int vec_d1upbydz(vec_ctx *ctx, const double *fin, double *fout, int dflag);
+int vec_d2bydz(vec_ctx *ctx, const double *fin, double *fout, int dflag);
+int vec_d1bydz1d(vec_ctx *ctx, const double *fin, double *fout, int dflag);
+int vec_d2bydz1d(vec_ctx *ctx, const double *fin, double *fout, int dflag);
+
+/* ---- physics on the context's state ------------------------------------ */
+int vec_hydro_deriv(vec_ctx *ctx);   /* src/hydro_deriv.f90:5-505 -> slot 3 */
+int vec_mag_deriv(vec_ctx *ctx);     /* src/magnetic.f90:285-487 -> slot 3  */
+int vec_bandj(vec_ctx *ctx);         /* src/magnetic.f90:492-664            */
+int vec_magdealias(vec_ctx *ctx);    /* src/magnetic.f90:666-717            */
+int vec_boundary(vec_ctx *ctx);      /* src/dbydz.F90:3686-4197             */
+int vec_mag_boundary(vec_ctx *ctx);  /* src/dbydz.F90:4205-4791             */
+/* AB3 coefficients + update + density floor + history shift + dt1/dt2,
+ * src/main.F90:381-489 (uses and advances the context's scalars) */
+int vec_ab3_update(vec_ctx *ctx);
+/* GlobalAverages (which removes the mean horizontal momentum from u,v),
+ * nusselt, checkdivb, sminmax: src/utils.F90:22-371, src/dbydz.F90:4796-4925,
+ * src/main.F90:552-647.  Returns VEC_ERR_DIVB when |div B| > 0.01. */
+int vec_diag(vec_ctx *ctx, vec_diag_out *out);
+
+/* ---- the time loop ----------------------------------------------------- */
+/* nsteps iterations of src/main.F90:340-747 (no printing, no snapshots):
+ * diagnostics every ndu06 steps, calcdt every 10, dealias every 10.
+ * Returns VEC_ERR_DIVB / VEC_ERR_NAN if a check fails. */
+int vec_step(vec_ctx *ctx, int nsteps);
+/* last diagnostics computed inside vec_step (valid after an ndu06 step) */
+int vec_last_diag(vec_ctx *ctx, vec_diag_out *out);
+
+/* ---- instrumentation --------------------------------------------------- */
+/* When on, every kernel launch of the context is bracketed by CUDA events
+ * on the context stream and its duration is accumulated per kernel name. */
+int vec_profile(vec_ctx *ctx, int on);
+/* number of distinct kernels recorded */
+int vec_profile_count(vec_ctx *ctx);
+/* i-th record: name (<= 63 chars), launches, total milliseconds */
+int vec_profile_get(vec_ctx *ctx, int i, char *name, int *launches, double *ms);
+int vec_profile_reset(vec_ctx *ctx);
+/* kernels launched by this context since creation */
+long long vec_launch_count(vec_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VEC_H */

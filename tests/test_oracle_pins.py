@@ -1,0 +1,182 @@
+"""Pins of the CPU oracle (the parity checker) against independent truths.
+
+* FFTW-2 rfftw semantics (src/fft.F90:125-136): checked against numpy's
+  FFT, an independent implementation of the same DFT.
+* The reference's own derivative test, src/test_dbydxy.F90:118-332:
+  analytic cos/sin fields for every wavenumber 0..n/2, d1bydx/d2bydx/
+  dealias and the y variants; the reference's stated outcome (:4-5) is
+  ~0 error except for the top third of modes, which dealias removes.
+* z stencils (src/dbydz.F90:366-1558): interior rows exact for quartics,
+  boundary rows exact for cubics, with the documented flag semantics.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from fug30v0kxc_gb300.params import default_params
+
+
+@pytest.mark.parametrize("n", [4, 6, 8, 30, 60, 64, 96, 192, 256, 250])
+def test_r2hc_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n)
+    h = O.r2hc(x)
+    X = np.fft.fft(x)
+    ref = np.zeros(n)
+    ref[: n // 2 + 1] = X[: n // 2 + 1].real
+    for k in range(1, (n + 1) // 2):
+        ref[n - k] = X[k].imag
+    assert np.abs(h - ref).max() < 1e-13 * max(1.0, np.abs(ref).max())
+    # unnormalised backward transform: hc2r(r2hc(x)) = n x
+    assert np.abs(O.hc2r(h) / n - x).max() < 1e-14 * n
+
+
+def _oracle(nx, ny, nz):
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    return O.Oracle(p), p
+
+
+@pytest.mark.parametrize("direction", ["x", "y"])
+@pytest.mark.parametrize("func", ["cos", "sin"])
+def test_dbydxy_kat(direction, func):
+    nx, ny, nz = 30, 24, 6
+    o, p = _oracle(nx, ny, nz)
+    n = nx if direction == "x" else ny
+    L = p.xmax if direction == "x" else p.ymax
+    d = L / n
+    s = np.arange(n) * d
+    icut = (n // 2) // 3
+    k3 = np.arange(1, nz + 1)[:, None, None].astype(float)
+    for iw in range(0, n // 2 + 1):
+        om = iw * 2 * np.pi / L
+        if func == "cos":
+            g, g1, g2 = np.cos(om * s), -om * np.sin(om * s), -om * om * np.cos(om * s)
+        else:
+            g, g1, g2 = np.sin(om * s), om * np.cos(om * s), -om * om * np.sin(om * s)
+        if direction == "x":
+            f = k3 * g[None, None, :] * np.ones((nz, ny, nx))
+            e1, e2 = k3 * g1[None, None, :], k3 * g2[None, None, :]
+            d1 = o.d1bydx(f)
+            a, b = o.d2bydx(f)
+        else:
+            f = k3 * g[None, :, None] * np.ones((nz, ny, nx))
+            e1, e2 = k3 * g1[None, :, None], k3 * g2[None, :, None]
+            d1 = o.d1bydy(f)
+            a, b = o.d2bydy(f)
+        dz = o.dealias(f)
+        scale = nz * max(1.0, om * om)
+        if iw < n // 2:
+            assert np.abs(d1 - e1).max() < 1e-12 * scale, iw
+            assert np.abs(a - e1).max() < 1e-12 * scale, iw
+            assert np.abs(b - e2).max() < 1e-11 * scale, iw
+        else:
+            # Nyquist: d1 drops it (:292-302), d2 keeps it (:442-454)
+            assert np.abs(d1).max() < 1e-12 * scale
+            assert np.abs(b - e2).max() < 1e-11 * scale
+        if iw < n // 2 - icut:
+            assert np.abs(dz - f).max() < 1e-12 * nz, iw
+        else:
+            assert np.abs(dz).max() < 1e-12 * nz, iw
+
+
+def test_forward_inverse_2d_roundtrip():
+    o, p = _oracle(30, 20, 6)
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal((6, 20, 30))
+    F = o.forwardfft(f)
+    # 2-D halfcomplex x halfcomplex = rfftw along x then along y
+    ref = np.apply_along_axis(O.r2hc, 2, f)
+    ref = np.apply_along_axis(O.r2hc, 1, ref)
+    assert np.abs(F - ref).max() < 1e-12 * np.abs(ref).max()
+    assert np.abs(o.inversefft(F) - f).max() < 1e-13
+
+
+def _poly(nz, deg, rng):
+    z = np.arange(nz) / (nz - 1)
+    c = rng.standard_normal(deg + 1)
+    f = sum(c[i] * z ** i for i in range(deg + 1))
+    f1 = sum(i * c[i] * z ** (i - 1) for i in range(1, deg + 1))
+    f2 = sum(i * (i - 1) * c[i] * z ** (i - 2) for i in range(2, deg + 1))
+    return f, f1, f2
+
+
+def test_z_stencils_polynomial_exactness():
+    nz = 17
+    o, p = _oracle(4, 4, nz)
+    rng = np.random.default_rng(3)
+    # interior rows: 4th order -> exact for quartics (d1 interior is exact
+    # to degree 4, d2 interior to degree 5)
+    f, f1, f2 = _poly(nz, 4, rng)
+    F = np.broadcast_to(f[:, None, None], (nz, 4, 4)).copy()
+    d1 = o.d1bydz(F, 5)[:, 0, 0]
+    d2 = o.d2bydz(F, 3)[:, 0, 0]
+    assert np.abs(d1[2:-2] - f1[2:-2]).max() < 1e-10
+    assert np.abs(d2[2:-2] - f2[2:-2]).max() < 1e-8
+    # boundary rows: third order -> exact for cubics (flag 5 one-sided)
+    f, f1, f2 = _poly(nz, 3, rng)
+    F = np.broadcast_to(f[:, None, None], (nz, 4, 4)).copy()
+    d1 = o.d1bydz(F, 5)[:, 0, 0]
+    assert np.abs(d1 - f1).max() < 1e-10
+    d2 = o.d2bydz(F, 3)[:, 0, 0]
+    assert np.abs(d2 - f2).max() < 1e-8
+    # flag semantics: 0/2 zero the outer rows, flag 0 zeroes d2 at the walls
+    assert np.all(o.d1bydz(F, 0)[[0, -1]] == 0.0)
+    assert np.all(o.d1bydz(F, 2)[[0, -1]] == 0.0)
+    assert np.all(o.d2bydz(F, 0)[[0, -1]] == 0.0)
+    # flag 1 ("conserves mass"): top row = ho12*(14f1+36f2-18f3+4f4)
+    h = (nz - 1) / 12.0
+    top = o.d1bydz(F, 1)[0, 0, 0]
+    assert abs(top - h * (14 * f[0] + 36 * f[1] - 18 * f[2] + 4 * f[3])) < 1e-12 * abs(top) + 1e-12
+    # 1-D twins are the same stencils
+    assert np.allclose(o.d1bydz1d(f, 5), d1, rtol=0, atol=1e-12)
+
+
+def test_upwind_follows_sign_of_w():
+    nz = 12
+    o, p = _oracle(4, 4, nz)
+    rng = np.random.default_rng(4)
+    f = rng.standard_normal((nz, 4, 4))
+    h = (nz - 1) / 12.0
+    for wsign in (1.0, -1.0):
+        o.set("w", np.full((nz, 4, 4), wsign))
+        d = o.d1upbydz(f, 5)
+        k = 6
+        F = f[:, 0, 0]
+        if wsign > 0:
+            ref = h * (-F[k - 3] + 6 * F[k - 2] - 18 * F[k - 1] + 10 * F[k] + 3 * F[k + 1])
+        else:
+            ref = h * (F[k + 3] - 6 * F[k + 2] + 18 * F[k + 1] - 10 * F[k] - 3 * F[k - 1])
+        assert abs(d[k, 0, 0] - ref) < 1e-12
+
+
+def test_bad_flag_and_sizes():
+    o, p = _oracle(8, 8, 8)
+    f = np.zeros((8, 8, 8))
+    with pytest.raises(O.OracleError):
+        o.d1bydz(f, 3)
+    with pytest.raises(O.OracleError):
+        o.d2bydz(f, 5)
+    for nx, ny, nz in ((7, 8, 8), (8, 9, 8), (8, 8, 5)):
+        p2 = default_params()
+        p2.nx, p2.ny, p2.nz = nx, ny, nz
+        with pytest.raises(O.OracleError):
+            O.Oracle(p2)
+
+
+def test_ran0_sequence():
+    """RANSET/ran0 (src/ranset.f90): first draws of layer 1, seed 1996+64."""
+    p = default_params()
+    p.nx, p.ny, p.nz = 4, 4, 6
+    p.noise_amp = 0.5
+    o = O.Oracle(p)
+    o.static()
+    t = o.get("t")
+    # Park-Miller with the XOR mask: s0 = seed ^ MASK, s_{n+1} = 16807 s_n mod (2^31-1)
+    M, A, MASK = 2147483647, 16807, 123459876
+    s = (1996 + 64 * 1) ^ MASK
+    vals = []
+    for _ in range(16):
+        s = (A * s) % M
+        vals.append(2.0 * (s * (1.0 / M) - 0.5) * 0.5)
+    assert np.array_equal(t[0].ravel(), np.array(vals) + 1.0)
