@@ -1,0 +1,339 @@
+"""Benchmark: grid-point-steps/s of the VarElecCond time step on one GB300.
+
+Workload: 256 x 256 x 129, Ra 1e5, Q 100, m=1, theta 9 (density contrast
+10), gamma 1.4, zeta 0.2, fixed-flux bottom, vertical seed field, eta(z)
+contrast 20, seeded +-1e-3 temperature noise (synthetic state), SF 0.3.
+One step = one iteration of the time loop (src/main.F90:340-747): RHS,
+AB3 update, dealias every 10 steps, bandj, boundary conditions, calcdt
+every 10 steps.  The state (>1 GB) is far larger than L2, so no explicit
+L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  Under torchrun every rank runs an independent
+replica (the path does not shard: replicas only); rank 0 prints.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ = 256, 256, 129
+WORKLOAD = "VarElecCond 256x256x129 Ra1e5 Q100 eta-contrast-20"
+METRIC = "grid-point-steps/s at 256^2x129"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_params(precision):
+    from fug30v0kxc_gb300.params import config1
+    p = config1(precision=precision)
+    p.ndu06 = 1000000          # diagnostics printing cadence of bin/INPUT is 5000 steps
+    return p
+
+
+def time_gpu(args, precision):
+    """Device-resident timed region: W warmup steps, K timed steps."""
+    import torch
+    from fug30v0kxc_gb300.solver import P3D
+    g = P3D(make_params(precision))
+    g.start()
+    stream = torch.cuda.ExternalStream(g.stream())
+    st = g.step(args.warmup)
+    assert st == 0, f"warmup step failed: {st}"
+    g.sync()
+    g.profile(True)
+    g.profile_reset()
+    launches0 = g.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    ev0.record(stream)
+    st = g.step(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    assert st == 0, f"timed step failed: {st}"
+    ms = ev0.elapsed_time(ev1)
+    launches = g.launch_count() - launches0
+    prof = g.profile_records()
+    g.profile(False)
+    ms = reduce_max(ms)
+    return g, ms, launches, prof, clocks
+
+
+def time_e2e(g, args):
+    """Through the C-ABI with host buffers: upload the state from pinned host
+    memory, K calls of vec_step(1) each reading the step's scalars back, then
+    download the state; every copy is inside the timed region."""
+    import numpy as np
+    import torch
+    from fug30v0kxc_gb300.params import FIELD_NAMES, VecScalars
+    names = ("r", "t", "u", "v", "w", "bx", "by", "bz", "pol", "tor")
+    host = {}
+    for n in names:
+        a = torch.empty(g.shape, dtype=torch.float64, pin_memory=True).numpy()
+        a[...] = g.get(n)
+        host[n] = a
+    sc = VecScalars()
+    L = g.L
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for n in names:
+        assert L.vec_set_field(g.h, FIELD_NAMES[n], host[n].ctypes.data) == 0
+    for _ in range(args.steps):
+        assert L.vec_step(g.h, 1) == 0
+        assert L.vec_get_scalars(g.h, C.byref(sc)) == 0
+    for n in names:
+        assert L.vec_get_field(g.h, FIELD_NAMES[n], host[n].ctypes.data) == 0
+    dt = time.perf_counter() - t0
+    dt = reduce_max(dt * 1e3) / 1e3
+    nbytes = sum(host[n].nbytes for n in names)
+    return dt, nbytes, C.sizeof(VecScalars)
+
+
+def cpu_baseline(nsteps, precision_note=""):
+    """The oracle (plain C restatement, OpenMP over planes) on the host cores."""
+    from oracle import oracle as O
+    threads = O.nthreads(os.cpu_count() or 1)
+    o = O.Oracle(make_params(0))
+    o.start()
+    o.step(1)
+    t0 = time.perf_counter()
+    assert o.step(nsteps) == 0
+    dt = time.perf_counter() - t0
+    return NX * NY * NZ * nsteps / dt, threads, dt
+
+
+_dist = {"on": False}
+
+
+def barrier():
+    if _dist["on"]:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x):
+    if not _dist["on"]:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dominant_roofline(prof, hbm_peak, peak_kind):
+    """Dominant kernel = largest share of the timed region's device time.
+    achieved = its algorithmic bytes per launch (every field it must read or
+    write, once; recorded per launch by the library) / its mean launch time
+    measured with CUDA events on the library stream."""
+    total = sum(r[2] for r in prof) or 1.0
+    name, launches, ms, nbytes = max(prof, key=lambda r: r[2])
+    avg_ms = ms / launches
+    per_launch = nbytes / launches
+    achieved = per_launch / (avg_ms * 1e-3) / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+            "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+            "traffic": TRAFFIC.get(name), "share": round(ms / total, 4),
+            "avg_launch_ms": round(avg_ms, 4), "launches": launches,
+            "alg_bytes_per_launch": per_launch}
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from the ncu capture
+# summarised under profiles/ (None until captured for the kernel)
+TRAFFIC = {}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path.  The Fortran reference
+    cannot be built here (no Fortran compiler, MPI, FFTW 2 or netCDF), so
+    this times the oracle port of its serial path on all host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    threads = O.nthreads(os.cpu_count() or 1)
+    o = O.Oracle(make_params(0))
+    o.start()
+    assert o.step(args.warmup) == 0
+    t0 = time.perf_counter()
+    assert o.step(args.steps) == 0
+    dt = time.perf_counter() - t0
+    v = NX * NY * NZ * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "grid-point-steps/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded static polytrope + noise)",
+            "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "nz": NZ, "precision": "fp64",
+                       "l2": "state >1 GB, larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"{args.steps} steps of the full 256x256x129 workload after "
+                                       f"{args.warmup} warm-up steps (reference Fortran unbuildable: "
+                                       "oracle port of its serial path)"},
+            "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend="nccl" if args.impl == "ours" else "gloo")
+        _dist["on"] = True
+    if args.impl == "reference":
+        run_reference(args)
+        if _dist["on"]:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
+    precision = VEC_PREC_FP64 if args.precision == "fp64" else VEC_PREC_SPLIT
+    hbm, pk = peaks()
+
+    g, ms, launches, prof, clocks = time_gpu(args, precision)
+    npts = NX * NY * NZ
+    value = npts * args.steps * ws / (ms * 1e-3)
+    e2e_s, e2e_bytes, sc_bytes = time_e2e(g, args)
+    e2e_value = npts * args.steps * ws / e2e_s
+    roof = dominant_roofline(prof, hbm, pk)
+    alg_step = 280 if precision == VEC_PREC_FP64 else 196
+    total_ms = sum(r[2] for r in prof) or 1.0
+    kernels = sorted(({"kernel": n, "launches": l, "ms": round(m, 3), "share": round(m / total_ms, 4),
+                       "gbs": round(b / (m * 1e-3) / 1e9, 1) if m > 0 else None}
+                      for n, l, m, b in prof), key=lambda d: -d["ms"])
+    line = {
+        "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == VEC_PREC_FP64 else "f32/f64",
+        "data": "synthetic (seeded static polytrope + uniform +-1e-3 T noise)",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "nz": NZ,
+                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "l2": "no flush: resident state >1 GB, larger than L2"},
+        "roofline": roof,
+        "step_roofline": {"alg_bytes_per_gps": alg_step,
+                          "achieved_gbs": round(value / ws * alg_step / 1e9, 1),
+                          "frac": round(value / ws * alg_step / 1e9 / hbm, 4)},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "grid-point-steps/s",
+                "h2d_bytes_per_step": e2e_bytes / args.steps,
+                "d2h_bytes_per_step": e2e_bytes / args.steps + sc_bytes},
+        "gpu_launches": launches,
+        "kernels": kernels[:12],
+    }
+    if rank == 0 and not args.no_cpu:
+        v, cores, dt = cpu_baseline(args.cpu_steps)
+        line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+                                "sample": f"{args.cpu_steps} steps of the full 256x256x129 workload "
+                                          f"({dt:.1f} s) by the oracle port, OpenMP over planes"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if _dist["on"]:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -35,7 +35,7 @@ void vec_set_error(const char *fmt, ...)
 extern "C" const char *vec_last_error(void) { return g_err; }
 
 // ---- profiling ---------------------------------------------------------------------
-void Engine::prof_begin(const char *name)
+void Engine::prof_begin(const char *name, double bytes)
 {
     launches++;
     if (!prof_on) return;
@@ -60,7 +60,7 @@ void Engine::prof_begin(const char *name)
     prof_cur = rec;
     prof_a = a;
     Pending pd;
-    pd.rec = rec; pd.a = a; pd.b = b;
+    pd.rec = rec; pd.a = a; pd.b = b; pd.bytes = bytes;
     pending.push_back(pd);
 }
 
@@ -79,6 +79,7 @@ int Engine::prof_flush()
         cudaEventElapsedTime(&ms, pd.a, pd.b);
         prof[pd.rec].launches += 1;
         prof[pd.rec].ms += ms;
+        prof[pd.rec].bytes += pd.bytes;
         ev_pool.push_back(pd.a);
         ev_pool.push_back(pd.b);
     }
@@ -751,7 +752,7 @@ extern "C" int vec_profile_count(vec_ctx *c)
     c->E.prof_flush();
     return (int)c->E.prof.size();
 }
-extern "C" int vec_profile_get(vec_ctx *c, int i, char *name, int *launches, double *ms)
+extern "C" int vec_profile_get(vec_ctx *c, int i, char *name, int *launches, double *ms, double *bytes)
 {
     if (!c || i < 0 || i >= (int)c->E.prof.size()) return VEC_ERR_ARG;
     c->E.prof_flush();
@@ -759,6 +760,7 @@ extern "C" int vec_profile_get(vec_ctx *c, int i, char *name, int *launches, dou
     if (name) { strncpy(name, r.name.c_str(), 63); name[63] = 0; }
     if (launches) *launches = r.launches;
     if (ms) *ms = r.ms;
+    if (bytes) *bytes = r.bytes;
     return VEC_OK;
 }
 extern "C" int vec_profile_reset(vec_ctx *c)

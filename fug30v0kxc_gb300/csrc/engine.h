@@ -28,6 +28,7 @@ struct ProfRec {
     std::string name;
     int launches = 0;
     double ms = 0.0;
+    double bytes = 0.0;     // algorithmic bytes (fields read + written once)
 };
 
 struct Engine {
@@ -78,7 +79,7 @@ struct Engine {
     bool prof_on = false;
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> ev_pool;
-    struct Pending { int rec; cudaEvent_t a, b; };
+    struct Pending { int rec; cudaEvent_t a, b; double bytes; };
     std::vector<Pending> pending;
     int prof_cur = -1;
     cudaEvent_t prof_a = nullptr;
@@ -86,7 +87,7 @@ struct Engine {
     template <typename R> const LineTables<R> &tables(int dir) const;
     template <typename R> R *W(int slot) const { return reinterpret_cast<R *>(wk[slot]); }
 
-    void prof_begin(const char *name);
+    void prof_begin(const char *name, double bytes = 0.0);
     void prof_end();
     int prof_flush();
 };

@@ -417,7 +417,13 @@ int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
         size_t smem = (size_t)(2 * pl.P * (pl.n + 1) + pl.n) * sizeof(typename CT<R>::T);
         const char *name = dir == 0 ? (sizeof(R) == 8 ? "line_x_f64" : "line_x_f32")
                                     : (sizeof(R) == 8 ? "line_y_f64" : "line_y_f32");
-        E->prof_begin(name);
+        double fields = 0.0;
+        for (int j = 0; j < nj; j++) {
+            const LineJob<R> &q = pk.j[j];
+            fields += 1.0 + 1.0 + (q.acc1 ? 1.0 : 0.0);
+            if (q.op2 != OP_NONE) fields += 1.0 + (q.acc2 ? 1.0 : 0.0);
+        }
+        E->prof_begin(name, fields * (double)E->n * sizeof(R));
         if (dir == 0)
             line_kernel<R, 0><<<grid, pl.threads, smem, E->stream>>>(pk, pl, tb, E->nx, E->ny, E->nz);
         else

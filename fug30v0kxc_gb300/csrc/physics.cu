@@ -30,13 +30,16 @@ static inline unsigned nblk(size_t n, int tpb = TPB)
     return (unsigned)(b > 0x7fffffff ? 0x7fffffff : b);
 }
 
-#define KLAUNCH(E, name, kern, grid, block, ...)                 \
+#define KLAUNCHB(E, name, bytes, kern, grid, block, ...)         \
     do {                                                         \
-        (E)->prof_begin(name);                                   \
+        (E)->prof_begin(name, (double)(bytes));                  \
         kern<<<(grid), (block), 0, (E)->stream>>>(__VA_ARGS__);  \
         (E)->prof_end();                                         \
         CUDA_TRY(cudaGetLastError());                            \
     } while (0)
+#define KLAUNCH(E, name, kern, grid, block, ...) KLAUNCHB(E, name, 0, kern, grid, block, __VA_ARGS__)
+// algorithmic bytes of a pointwise kernel touching nf full fields of esz bytes
+#define FB(E, nf, esz) ((double)(nf) * (double)(E)->n * (double)(esz))
 
 // ============================================================================
 // z-derivative operators (per-operator entry points)
@@ -72,7 +75,7 @@ __global__ void k_d2z(const R *in, R *out, int fl, size_t np, int nz, R s)
 int op_d1z(Engine *E, const double *in, double *out, int flag, int np, int nz)
 {
     if (!(flag == 0 || flag == 1 || flag == 2 || flag == 5)) return VEC_ERR_FLAG;
-    KLAUNCH(E, "d1bydz_f64", k_d1z<double>, nblk((size_t)np * nz), TPB, in, out, flag, (size_t)np, nz, E->k.ho12);
+    KLAUNCHB(E, "d1bydz_f64", 2.0 * np * nz * 8, k_d1z<double>, nblk((size_t)np * nz), TPB, in, out, flag, (size_t)np, nz, E->k.ho12);
     return VEC_OK;
 }
 int op_d1upz(Engine *E, const double *in, double *out, int flag)
@@ -263,7 +266,7 @@ int phys_hydro64(Engine *E)
     a.scko3 = c.scko3; a.f = c.f; a.thmplus1 = c.thmplus1; a.cor = c.cor; a.cpsi = c.cpsi;
     a.spsi = c.spsi; a.sck = c.sck; a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
-    KLAUNCH(E, "hydro_pass2_f64", k_hydro_pass2, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "hydro_pass2_f64", FB(E, 39, 8), k_hydro_pass2, nblk(E->n), TPB, a);
 
     // pass 3: d/dx, d/dy of the second-level inputs into the accumulators
     // (:181-182, :230-231, :273, :320)
@@ -286,7 +289,7 @@ int phys_hydro64(Engine *E)
     b.rdot = (double *)E->hist[0][2]; b.udot = (double *)E->hist[2][2];
     b.vdot = (double *)E->hist[3][2]; b.wdot = (double *)E->hist[4][2];
     b.ho12 = c.ho12; b.np = E->np; b.nz = E->nz;
-    KLAUNCH(E, "hydro_pass4_f64", k_hydro_pass4, nblk(E->n), TPB, b);
+    KLAUNCHB(E, "hydro_pass4_f64", FB(E, 15, 8), k_hydro_pass4, nblk(E->n), TPB, b);
     return VEC_OK;
 }
 
@@ -388,7 +391,7 @@ int phys_mag64(Engine *E)
     double *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
     int st;
-    KLAUNCH(E, "emf_f64", k_emf, nblk(E->n), TPB, E->u, E->v, E->w, E->bx, E->by, E->bz, W[W_M1], W[W_M2], W[W_M3], E->n);
+    KLAUNCHB(E, "emf_f64", FB(E, 9, 8), k_emf, nblk(E->n), TPB, E->u, E->v, E->w, E->bx, E->by, E->bz, W[W_M1], W[W_M2], W[W_M3], E->n);
     // forwardfft x3 (:321-323): x pass then y pass in place
     LineJob<double> fx[3] = { ljob<double>(W[W_M1], W[W_EX], OP_FWD), ljob<double>(W[W_M2], W[W_EY], OP_FWD),
                               ljob<double>(W[W_M3], W[W_EZ], OP_FWD) };
@@ -399,14 +402,14 @@ int phys_mag64(Engine *E)
     const Consts &c = E->k;
     KLAUNCH(E, "mean_rhs", k_mean_rhs, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
             E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
-    KLAUNCH(E, "mag_div_f64", k_mag_div, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
+    KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
     MagArgs a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol; a.tor = E->tor;
     a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
     a.poldot = (double *)E->hist[5][2]; a.tordot = (double *)E->hist[6][2];
     a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCH(E, "mag_final_f64", k_mag_final, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final, nblk(E->n), TPB, a);
     return VEC_OK;
 }
 
@@ -487,7 +490,7 @@ int phys_bandj64(Engine *E)
     a.akx2 = E->akx2; a.aky2 = E->aky2;
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCH(E, "bandj_spec_f64", k_bandj_spec, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "bandj_spec_f64", FB(E, 9, 8), k_bandj_spec, nblk(E->n), TPB, a);
     // six inverse 2-D transforms (:575-577, :623-625): x pass in place, then y
     LineJob<double> ix[6] = { ljob<double>(W[W_EX], W[W_EX], OP_INV), ljob<double>(W[W_EY], W[W_EY], OP_INV),
                               ljob<double>(W[W_EZ], W[W_EZ], OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
@@ -500,7 +503,7 @@ int phys_bandj64(Engine *E)
     iy[1].addk = E->bybar;
     iy[2].addc = E->bzbar;
     if ((st = launch_lines<double>(E, 1, iy, 6))) return st;
-    KLAUNCH(E, "jsq_f64", k_jsq, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
+    KLAUNCHB(E, "jsq_f64", FB(E, 6, 8), k_jsq, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
     return VEC_OK;
 }
 
@@ -725,7 +728,7 @@ int phys_ab3(Engine *E, int magdealias)
     a.ds = E->ds;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
-    KLAUNCH(E, "ab3_update_f64", k_ab3_update, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "ab3_update_f64", FB(E, 35, 8), k_ab3_update, nblk(E->n), TPB, a);
     rotate_hist(E);
     return VEC_OK;
 }
@@ -800,7 +803,7 @@ int phys_calcdt(Engine *E)
     unsigned blocks = (unsigned)(152 * 8);
     size_t nb = nblk(E->n);
     if (nb < blocks) blocks = (unsigned)nb;
-    KLAUNCH(E, "calcdt_red_f64", k_calcdt_red<double>, blocks, TPB, E->u, E->v, E->w, E->r, E->t, E->bx, E->by, E->bz,
+    KLAUNCHB(E, "calcdt_red_f64", FB(E, 8, 8), k_calcdt_red<double>, blocks, TPB, E->u, E->v, E->w, E->r, E->t, E->bx, E->by, E->bz,
             E->n, E->k.g1, E->k.f, E->ds);
     const Consts &c = E->k;
     KLAUNCH(E, "calcdt_fin", k_calcdt_fin, 1, 1, E->ds, c.dd, c.dz, c.dtvisc0x, c.dtvisc0z, c.dtdiff0x, c.dtdiff0z,

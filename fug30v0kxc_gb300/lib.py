@@ -57,7 +57,8 @@ SIGNATURES = {
     "vec_last_diag": (C.c_int, [_vp, C.POINTER(VecDiag)]),
     "vec_profile": (C.c_int, [_vp, C.c_int]),
     "vec_profile_count": (C.c_int, [_vp]),
-    "vec_profile_get": (C.c_int, [_vp, C.c_int, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "vec_profile_get": (C.c_int, [_vp, C.c_int, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]),
     "vec_profile_reset": (C.c_int, [_vp]),
     "vec_launch_count": (C.c_longlong, [_vp]),
 }

@@ -208,9 +208,9 @@ class P3D:
         out = []
         name = C.create_string_buffer(64)
         for i in range(self.L.vec_profile_count(self.h)):
-            n, ms = C.c_int(), C.c_double()
-            self.L.vec_profile_get(self.h, i, name, C.byref(n), C.byref(ms))
-            out.append((name.value.decode(), n.value, ms.value))
+            n, ms, by = C.c_int(), C.c_double(), C.c_double()
+            self.L.vec_profile_get(self.h, i, name, C.byref(n), C.byref(ms), C.byref(by))
+            out.append((name.value.decode(), n.value, ms.value, by.value))
         return out
 
     def launch_count(self):

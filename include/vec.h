@@ -194,8 +194,9 @@ int vec_last_diag(vec_ctx *ctx, vec_diag_out *out);
 int vec_profile(vec_ctx *ctx, int on);
 /* number of distinct kernels recorded */
 int vec_profile_count(vec_ctx *ctx);
-/* i-th record: name (<= 63 chars), launches, total milliseconds */
-int vec_profile_get(vec_ctx *ctx, int i, char *name, int *launches, double *ms);
+/* i-th record: name (<= 63 chars), launches, total milliseconds and total
+ * algorithmic bytes (every field the kernel must read or write, once) */
+int vec_profile_get(vec_ctx *ctx, int i, char *name, int *launches, double *ms, double *bytes);
 int vec_profile_reset(vec_ctx *ctx);
 /* kernels launched by this context since creation */
 long long vec_launch_count(vec_ctx *ctx);
