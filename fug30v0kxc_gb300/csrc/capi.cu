@@ -334,7 +334,9 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     if (cudaMallocHost(&E.hs, sizeof(DevScalars)) != cudaSuccess) { vec_destroy(c); return VEC_ERR_ALLOC; }
     memset(E.hs, 0, sizeof(DevScalars));
     E.hs->first = 1;
-    E.hs->denmn = 0x7fefffffffffffffull;
+    E.hs->velmxx = OKEY_NEG_HUGE;
+    E.hs->velmxz = OKEY_NEG_HUGE;
+    E.hs->denmn = OKEY_POS_HUGE;
     CUDA_TRY(cudaMemcpy(E.ds, E.hs, sizeof(DevScalars), cudaMemcpyHostToDevice));
     if (E.split && (st = split_setup(&E))) { vec_destroy(c); return st; }
     CUDA_TRY(cudaDeviceSynchronize());

@@ -68,13 +68,17 @@ struct Consts {
     int icutoffx, icutoffy;
 };
 
+// order-preserving keys (see okey in physics.cu) of -DBL_MAX and +DBL_MAX
+#define OKEY_NEG_HUGE 0x0010000000000000ull
+#define OKEY_POS_HUGE 0xffefffffffffffffull
+
 // time-loop scalars living on the device (src/main.F90:84-103)
 struct DevScalars {
     double dt, dt1, dt2, ttime;
     double c0, c1, c2;
     int first, second;
     // reductions
-    unsigned long long velmxx, velmxz, denmn;  // ordered bit patterns of non-negative doubles
+    unsigned long long velmxx, velmxz, denmn;  // order-preserving keys of the reductions
     double res[64];                            // diagnostics results
 };
 

@@ -748,13 +748,25 @@ int phys_dealias_state(Engine *E)
 // ============================================================================
 // calcdt: src/utils.F90:144-244
 // ============================================================================
-__device__ __forceinline__ unsigned long long obits(double x) { return (unsigned long long)__double_as_longlong(x); }
+// order-preserving map of a double onto an unsigned 64-bit key (all
+// non-NaN values, negatives included), so that atomicMax/atomicMin on the
+// keys give the max/min of the doubles
+__device__ __forceinline__ unsigned long long okey(double x)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double okey_dec(unsigned long long e)
+{
+    unsigned long long u = (e >> 63) ? (e & 0x7fffffffffffffffull) : ~e;
+    return __longlong_as_double((long long)u);
+}
 
 template <typename R>
 __global__ void k_calcdt_red(const R *u, const R *v, const R *w, const R *r, const R *t, const R *bx, const R *by,
                              const R *bz, size_t n, double g1, double f, DevScalars *ds)
 {
-    double mxx = 0.0, mxz = 0.0, mn = 1.0e300;
+    double mxx = -1.0e-50, mxz = -1.0e-50, mn = 1.0e300;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double u0 = u[i], v0 = v[i], w0 = w[i], r0 = r[i], t0 = t[i];
         double bz0 = bz[i], bx0 = bx[i], by0 = by[i];
@@ -771,18 +783,18 @@ __global__ void k_calcdt_red(const R *u, const R *v, const R *w, const R *r, con
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     }
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(&ds->velmxx, obits(mxx));
-        atomicMax(&ds->velmxz, obits(mxz));
-        atomicMin(&ds->denmn, obits(mn));
+        atomicMax(&ds->velmxx, okey(mxx));
+        atomicMax(&ds->velmxz, okey(mxz));
+        atomicMin(&ds->denmn, okey(mn));
     }
 }
 
 __global__ void k_calcdt_fin(DevScalars *ds, double dd, double dz, double dtvisc0x, double dtvisc0z,
                              double dtdiff0x, double dtdiff0z, double sf, int var_eta, double eta_max)
 {
-    double velmxx = __longlong_as_double((long long)ds->velmxx);
-    double velmxz = __longlong_as_double((long long)ds->velmxz);
-    double denmn = __longlong_as_double((long long)ds->denmn);
+    double velmxx = okey_dec(ds->velmxx);
+    double velmxz = okey_dec(ds->velmxz);
+    double denmn = okey_dec(ds->denmn);
     double m = 0.16 * dd / velmxx;
     m = fmin(m, 0.3 * dz / velmxz);
     m = fmin(m, dtvisc0x * denmn);
@@ -795,7 +807,7 @@ __global__ void k_calcdt_fin(DevScalars *ds, double dd, double dz, double dtvisc
     }
     ds->dt = sf * m;
     ds->res[60] = velmxx; ds->res[61] = velmxz; ds->res[62] = denmn;
-    ds->velmxx = 0ull; ds->velmxz = 0ull; ds->denmn = 0x7fefffffffffffffull;
+    ds->velmxx = OKEY_NEG_HUGE; ds->velmxz = OKEY_NEG_HUGE; ds->denmn = OKEY_POS_HUGE;
 }
 
 int phys_calcdt(Engine *E)
