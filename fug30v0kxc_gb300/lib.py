@@ -61,6 +61,7 @@ SIGNATURES = {
                                   C.POINTER(C.c_double)]),
     "vec_profile_reset": (C.c_int, [_vp]),
     "vec_launch_count": (C.c_longlong, [_vp]),
+    "vec_calcdt_noalloc": (C.c_int, [C.POINTER(VecParams)] + [_dp] * 9 + [_vp]),
 }
 
 _lib = None

@@ -188,6 +188,22 @@ int vec_step(vec_ctx *ctx, int nsteps);
 /* last diagnostics computed inside vec_step (valid after an ndu06 step) */
 int vec_last_diag(vec_ctx *ctx, vec_diag_out *out);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+/* No counterpart in the reference.  calcdt (src/utils.F90:144-244) for
+ * callers that cannot allocate device memory: programs whose device memory
+ * is all handed out by their own arena or pool, and which therefore cannot
+ * create a vec_ctx (vec_create allocates).  The caller passes device
+ * pointers to the eight fields (nx*ny*nz doubles each, sizes taken from p)
+ * and dt_out (device or host).  No memory is allocated: the reduction's
+ * scratch is a fixed 1.5 MiB __device__ array inside the library, held by
+ * every GPU that loads it until the process exits.  The first call on a
+ * device looks up that array's address, so make the first call before any
+ * stream capture.  Grids above 2^27 points return VEC_ERR_SIZE.  All calls
+ * on a device share the scratch: calls that overlap on the GPU race. */
+int vec_calcdt_noalloc(const vec_params *p, const double *u, const double *v, const double *w,
+                       const double *r, const double *t, const double *bx, const double *by,
+                       const double *bz, double *dt_out, void *stream);
+
 /* ---- instrumentation --------------------------------------------------- */
 /* When on, every kernel launch of the context is bracketed by CUDA events
  * on the context stream and its duration is accumulated per kernel name. */
