@@ -104,6 +104,7 @@ def dist_env():
 def make_params(precision):
     from fug30v0kxc_gb300.params import config1
     p = config1(precision=precision)
+    p.nx, p.ny, p.nz = NX, NY, NZ
     p.ndu06 = 1000000          # diagnostics printing cadence of bin/INPUT is 5000 steps
     return p
 
@@ -257,17 +258,45 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure(args, precision, ws, hbm, pk, with_e2e):
+    g, ms, launches, prof, clocks = time_gpu(args, precision)
+    npts = NX * NY * NZ
+    value = npts * args.steps * ws / (ms * 1e-3)
+    res = {"value": value, "ms_per_step": ms / args.steps, "launches": launches, "clocks": clocks,
+           "roofline": dominant_roofline(prof, hbm, pk)}
+    alg_step = 280 if precision == 0 else 196
+    res["step_roofline"] = {"alg_bytes_per_gps": alg_step,
+                            "achieved_gbs": round(value / ws * alg_step / 1e9, 1),
+                            "frac": round(value / ws * alg_step / 1e9 / hbm, 4)}
+    total_ms = sum(r[2] for r in prof) or 1.0
+    res["kernels"] = sorted(({"kernel": n, "launches": l, "ms": round(m, 3), "share": round(m / total_ms, 4),
+                              "gbs": round(b / (m * 1e-3) / 1e9, 1) if m > 0 else None}
+                             for n, l, m, b in prof), key=lambda d: -d["ms"])[:12]
+    if with_e2e:
+        e2e_s, e2e_bytes, sc_bytes = time_e2e(g, args)
+        res["e2e"] = {"value": npts * args.steps * ws / e2e_s, "unit": "grid-point-steps/s",
+                      "h2d_bytes_per_step": e2e_bytes / args.steps,
+                      "d2h_bytes_per_step": e2e_bytes / args.steps + sc_bytes}
+    g.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "split"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--grid", default=None, help="NX,NY,NZ (smaller cases for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.grid:
+        global NX, NY, NZ, WORKLOAD
+        NX, NY, NZ = (int(x) for x in args.grid.split(","))
+        WORKLOAD = f"VarElecCond {NX}x{NY}x{NZ} Ra1e5 Q100 eta-contrast-20"
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -288,45 +317,37 @@ def main():
     import torch
     torch.cuda.set_device(local)
     from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
-    precision = VEC_PREC_FP64 if args.precision == "fp64" else VEC_PREC_SPLIT
     hbm, pk = peaks()
-
-    g, ms, launches, prof, clocks = time_gpu(args, precision)
-    npts = NX * NY * NZ
-    value = npts * args.steps * ws / (ms * 1e-3)
-    e2e_s, e2e_bytes, sc_bytes = time_e2e(g, args)
-    e2e_value = npts * args.steps * ws / e2e_s
-    roof = dominant_roofline(prof, hbm, pk)
-    alg_step = 280 if precision == VEC_PREC_FP64 else 196
-    total_ms = sum(r[2] for r in prof) or 1.0
-    kernels = sorted(({"kernel": n, "launches": l, "ms": round(m, 3), "share": round(m / total_ms, 4),
-                       "gbs": round(b / (m * 1e-3) / 1e9, 1) if m > 0 else None}
-                      for n, l, m, b in prof), key=lambda d: -d["ms"])
+    head_prec = VEC_PREC_FP64 if args.precision == "fp64" else VEC_PREC_SPLIT
+    head = measure(args, head_prec, ws, hbm, pk, with_e2e=True)
     line = {
-        "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "metric": METRIC, "value": head["value"], "unit": "grid-point-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if precision == VEC_PREC_FP64 else "f32/f64",
+        "dtype": "f64" if head_prec == VEC_PREC_FP64 else "f32/f64",
         "data": "synthetic (seeded static polytrope + uniform +-1e-3 T noise)",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "nz": NZ,
-                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "precision": "fp64" if head_prec == VEC_PREC_FP64 else "split (FP32 bulk, FP64 state)",
+                   "parallelism": f"replicas{ws}",
                    "l2": "no flush: resident state >1 GB, larger than L2"},
-        "roofline": roof,
-        "step_roofline": {"alg_bytes_per_gps": alg_step,
-                          "achieved_gbs": round(value / ws * alg_step / 1e9, 1),
-                          "frac": round(value / ws * alg_step / 1e9 / hbm, 4)},
-        "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": "grid-point-steps/s",
-                "h2d_bytes_per_step": e2e_bytes / args.steps,
-                "d2h_bytes_per_step": e2e_bytes / args.steps + sc_bytes},
-        "gpu_launches": launches,
-        "kernels": kernels[:12],
+        "roofline": head["roofline"],
+        "step_roofline": head["step_roofline"],
+        "clocks": head["clocks"],
+        "e2e": head["e2e"],
+        "gpu_launches": head["launches"],
+        "kernels": head["kernels"],
     }
+    if args.precision == "both":
+        f64 = measure(args, VEC_PREC_FP64, ws, hbm, pk, with_e2e=False)
+        line["fp64"] = {"value": f64["value"], "ms_per_step": f64["ms_per_step"],
+                        "roofline": f64["roofline"], "step_roofline": f64["step_roofline"],
+                        "clocks": f64["clocks"], "gpu_launches": f64["launches"]}
+        line["split_over_fp64"] = head["value"] / f64["value"]
     if rank == 0 and not args.no_cpu:
         v, cores, dt = cpu_baseline(args.cpu_steps)
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
                                 "sample": f"{args.cpu_steps} steps of the full 256x256x129 workload "
-                                          f"({dt:.1f} s) by the oracle port, OpenMP over planes"}
+                                          f"({dt:.1f} s) by the oracle port, FP64, OpenMP over planes"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if _dist["on"]:

@@ -326,7 +326,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     ALLOC(E.bxbar, sizeof(double) * nz); ALLOC(E.bybar, sizeof(double) * nz);
     for (int s = 0; s < 3; s++) { ALLOC(E.bxbardot[s], sizeof(double) * nz); ALLOC(E.bybardot[s], sizeof(double) * nz); }
     ALLOC(E.w1d, sizeof(double) * 8 * nz);
-    for (int i = 0; i < W_COUNT; i++) ALLOC(E.wk[i], esz * n);
+    ALLOC(E.wblock, esz * n * W_COUNT);
+    for (int i = 0; i < W_COUNT; i++) E.wk[i] = (char *)E.wblock + esz * n * (size_t)i;
     for (int i = 0; i < 3; i++) ALLOC(E.s64[i], sizeof(double) * n);
     E.red_blocks = 152 * 4;
     ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 24 + 64));
@@ -356,7 +357,7 @@ extern "C" int vec_destroy(vec_ctx *c)
     for (void *q : ptrs) if (q) cudaFree(q);
     for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hist[f][s]) cudaFree(E.hist[f][s]);
     for (int s = 0; s < 3; s++) { if (E.bxbardot[s]) cudaFree(E.bxbardot[s]); if (E.bybardot[s]) cudaFree(E.bybardot[s]); }
-    for (int i = 0; i < W_COUNT; i++) if (E.wk[i]) cudaFree(E.wk[i]);
+    if (E.wblock) cudaFree(E.wblock);
     for (int i = 0; i < 6; i++) if (E.s64[i]) cudaFree(E.s64[i]);
     if (E.tx64.tw) line_tables_free(&E.tx64);
     if (E.ty64.tw) line_tables_free(&E.ty64);
@@ -442,9 +443,10 @@ extern "C" int vec_set_field(vec_ctx *c, int field, const double *src)
     Engine &E = c->E;
     double *d = state_ptr(E, field);
     if (d) {
-        int st = stage_in(E, d, src, E.n);
-        if (st) return st;
-        if (E.split) return split_refresh(&E);
+        int st;
+        if (E.split && (st = split_sync_b64(&E))) return st;
+        if ((st = stage_in(E, d, src, E.n))) return st;
+        if (E.split && (st = split_refresh(&E))) return st;
         CUDA_TRY(cudaStreamSynchronize(E.stream));
         return VEC_OK;
     }
@@ -462,7 +464,11 @@ extern "C" int vec_get_field(vec_ctx *c, int field, double *dst)
     if (!c || !dst) return VEC_ERR_ARG;
     Engine &E = c->E;
     double *d = state_ptr(E, field);
-    if (d) return stage_out(E, dst, d, E.n);
+    if (d) {
+        int st;
+        if (E.split && (st = split_sync_b64(&E))) return st;
+        return stage_out(E, dst, d, E.n);
+    }
     int f, s;
     if (hist_index(field, &f, &s)) return VEC_ERR_ARG;
     if (!E.split) return stage_out(E, dst, (const double *)E.hist[f][s], E.n);
@@ -499,7 +505,15 @@ extern "C" int vec_get_mean(vec_ctx *c, int m, double *dst)
     return stage_out(c->E, dst, d, c->E.nz);
 }
 
-extern "C" int vec_set_bzbar(vec_ctx *c, double b) { if (!c) return VEC_ERR_ARG; c->E.bzbar = b; return VEC_OK; }
+extern "C" int vec_set_bzbar(vec_ctx *c, double b)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st;
+    if (c->E.split && (st = split_sync_b64(&c->E))) return st;
+    c->E.bzbar = b;
+    if (c->E.split && (st = split_refresh(&c->E))) return st;
+    return vec_sync(c);
+}
 extern "C" int vec_get_bzbar(vec_ctx *c, double *b) { if (!c || !b) return VEC_ERR_ARG; *b = c->E.bzbar; return VEC_OK; }
 
 extern "C" int vec_get_scalars(vec_ctx *c, vec_scalars *s)
@@ -531,6 +545,7 @@ extern "C" int vec_set_scalars(vec_ctx *c, const vec_scalars *s)
 extern "C" int vec_static(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
+    c->E.b32_auth = 0;
     int st = phys_static(&c->E);
     if (st) return st;
     if (c->E.split) return split_refresh(&c->E);
@@ -541,7 +556,7 @@ extern "C" int vec_calcdt(vec_ctx *c, double *dt)
 {
     if (!c) return VEC_ERR_ARG;
     Engine &E = c->E;
-    int st = phys_calcdt(&E);
+    int st = E.split ? split_calcdt(&E) : phys_calcdt(&E);
     if (st) return st;
     CUDA_TRY(cudaMemcpyAsync(E.hs, E.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E.stream));
     CUDA_TRY(cudaStreamSynchronize(E.stream));
@@ -552,7 +567,9 @@ extern "C" int vec_calcdt(vec_ctx *c, double *dt)
 extern "C" int vec_mag_init(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
-    int st = phys_mag_init(&c->E);
+    int st;
+    if (c->E.split && (st = split_sync_b64(&c->E))) return st;
+    st = phys_mag_init(&c->E);
     if (st) return st;
     if (c->E.split && (st = split_refresh(&c->E))) return st;
     return vec_sync(c);
@@ -664,34 +681,50 @@ extern "C" int vec_magdealias(vec_ctx *c)
     if (!st && c->E.split) st = split_refresh(&c->E);
     return finish(c, st);
 }
+static int boundary_step(Engine &E)
+{
+    int st = phys_boundary(&E);
+    if (!st && E.split) st = split_refresh_planes(&E, 1 | 2);
+    return st;
+}
+static int mag_boundary_step(Engine &E)
+{
+    int st = phys_mag_boundary(&E);
+    if (!st && E.split) st = split_refresh_planes(&E, 8);
+    return st;
+}
 extern "C" int vec_boundary(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
-    int st = phys_boundary(&c->E);
-    if (!st && c->E.split) st = split_refresh(&c->E);
-    return finish(c, st);
+    return finish(c, boundary_step(c->E));
 }
 extern "C" int vec_mag_boundary(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
-    int st = phys_mag_boundary(&c->E);
-    if (!st && c->E.split) st = split_refresh(&c->E);
-    return finish(c, st);
+    return finish(c, mag_boundary_step(c->E));
 }
 extern "C" int vec_ab3_update(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
     return finish(c, c->E.split ? split_ab3(&c->E, 0) : phys_ab3(&c->E, 0));
 }
-extern "C" int vec_diag(vec_ctx *c, vec_diag_out *out)
+static int diag_step(Engine &E, vec_diag_out *out)
 {
-    if (!c) return VEC_ERR_ARG;
-    int st = phys_diag(&c->E, out);
-    if (c->E.split) {
-        int s2 = split_refresh(&c->E);
+    int st;
+    if (E.split && (st = split_sync_b64(&E))) return st;
+    st = phys_diag(&E, out);
+    if (E.split) {
+        int s2 = split_refresh_uv(&E);   // GlobalAverages changed u and v
         if (!st) st = s2;
     }
     return st;
+}
+extern "C" int vec_diag(vec_ctx *c, vec_diag_out *out)
+{
+    if (!c) return VEC_ERR_ARG;
+    int st = diag_step(c->E, out);
+    int s2 = vec_sync(c);
+    return st ? st : s2;
 }
 
 // one iteration of src/main.F90:340-747 (printing and snapshots excluded)
@@ -708,17 +741,13 @@ static int one_step(Engine &E)
     const int mdeal = E.p.dalias && mag;
     if ((st = E.split ? split_ab3(&E, mdeal) : phys_ab3(&E, mdeal))) return st;
     const bool dealias_now = E.p.dalias && (E.nit % 10 == 0);
-    if (dealias_now && (st = phys_dealias_state(&E))) return st;
+    if (dealias_now && (st = E.split ? split_dealias(&E) : phys_dealias_state(&E))) return st;
     if (mag && (st = E.split ? split_bandj(&E) : phys_bandj64(&E))) return st;
-    if ((st = phys_boundary(&E))) return st;
-    if (mag && (st = phys_mag_boundary(&E))) return st;
+    if ((st = boundary_step(E))) return st;
+    if (mag && (st = mag_boundary_step(E))) return st;
     const bool diag_now = E.p.diag_cadence && E.p.ndu06 > 0 && (E.nit % E.p.ndu06 == 0);
-    if (diag_now) {
-        st = phys_diag(&E, nullptr);
-        if (st) return st;
-    }
-    if (E.nit % 10 == 0 && (st = phys_calcdt(&E))) return st;
-    if (E.split && (st = split_refresh(&E))) return st;
+    if (diag_now && (st = diag_step(E, nullptr))) return st;
+    if (E.nit % 10 == 0 && (st = E.split ? split_calcdt(&E) : phys_calcdt(&E))) return st;
     return VEC_OK;
 }
 

@@ -56,15 +56,17 @@ struct Engine {
     double *akx1 = nullptr, *akx2 = nullptr, *aky1 = nullptr, *aky2 = nullptr;
     double *w1d = nullptr;      // 1-D scratch (8 nz)
     double bzbar = 0.0;
-    // work arrays (bulk precision)
+    // work arrays (bulk precision), carved from one contiguous block
     void *wk[W_COUNT] = {};
+    void *wblock = nullptr;
     // FP64 scratch for per-operator entry points and diagnostics
     double *s64[6] = {};
     // split form: FP32 mirrors of the state and FP64 backgrounds
     float *r32 = nullptr, *t32 = nullptr, *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;
     float *bx32 = nullptr, *by32 = nullptr, *bz32 = nullptr, *jsq32 = nullptr;
     float *pol32 = nullptr, *tor32 = nullptr;
-    double *rho0 = nullptr, *t0 = nullptr, *hres = nullptr;   // background profiles, residual
+    double *rho0 = nullptr, *t0 = nullptr, *hres = nullptr;   // 1-D FP64 background block (split.cu)
+    int b32_auth = 0;           // split form: the FP32 B/jsq are newer than the FP64 ones
     // reductions scratch
     double *red = nullptr;      // per-block partials
     int red_blocks = 0;
@@ -86,6 +88,9 @@ struct Engine {
 
     template <typename R> const LineTables<R> &tables(int dir) const;
     template <typename R> R *W(int slot) const { return reinterpret_cast<R *>(wk[slot]); }
+    // FP64 work array i (i < W_COUNT/2 in the split form, whose block holds
+    // W_COUNT float arrays = W_COUNT/2 double arrays)
+    double *W64(int i) const { return split ? reinterpret_cast<double *>(wblock) + (size_t)i * n : (double *)wk[i]; }
 
     void prof_begin(const char *name, double bytes = 0.0);
     void prof_end();
@@ -125,6 +130,8 @@ int phys_magdealias(Engine *E);
 int phys_boundary(Engine *E);
 int phys_mag_boundary(Engine *E);
 int phys_ab3(Engine *E, int magdealias);
+int phys_ab3_coef(Engine *E);
+void phys_rotate_hist(Engine *E);
 int phys_dealias_state(Engine *E);
 int phys_calcdt(Engine *E);
 int phys_diag(Engine *E, vec_diag_out *out);
@@ -137,4 +144,9 @@ int split_hydro(Engine *E);
 int split_mag(Engine *E);
 int split_bandj(Engine *E);
 int split_refresh(Engine *E);
+int split_refresh_planes(Engine *E, int mask);
+int split_refresh_uv(Engine *E);
+int split_sync_b64(Engine *E);
 int split_ab3(Engine *E, int magdealias);
+int split_dealias(Engine *E);
+int split_calcdt(Engine *E);

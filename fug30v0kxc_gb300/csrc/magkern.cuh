@@ -1,0 +1,181 @@
+// magkern.cuh -- induction and B/J kernels shared by the FP64 and the split
+// forms (R = double or float).  src/magnetic.f90:285-717.
+#pragma once
+#include "zstencil.cuh"
+
+// E = u x B (:308-316); bzoff is added to bz (the split form stores bz
+// minus its constant mean bzbar)
+template <typename R>
+static __global__ void k_emf(const R *u, const R *v, const R *w, const R *bx, const R *by, const R *bz, R *e1,
+                             R *e2, R *e3, size_t n, R bzoff)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const R bzv = bz[i] + bzoff;
+    e1[i] = v[i] * bzv - w[i] * by[i];
+    e2[i] = w[i] * bx[i] - u[i] * bzv;
+    e3[i] = u[i] * by[i] - v[i] * bx[i];
+}
+
+// mean-field RHS (:328-352) on one CTA; ex, ey are the 2-D spectra of the EMF
+template <typename R>
+static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar, const double *bybar,
+                                  const double *eta, const double *deta, double *bxd, double *byd,
+                                  double *scratch, size_t np, int nz, double xn, double zck, double ho12,
+                                  double sc1, int var_eta)
+{
+    double *e1 = scratch, *e2 = scratch + nz;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        e1[k] = xn * (double)ex[(size_t)k * np];
+        e2[k] = xn * (double)ey[(size_t)k * np];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        double dey = zd1(e2, 1, k, nz, 5, ho12);   // :337
+        double dex = zd1(e1, 1, k, nz, 5, ho12);   // :338
+        double d2x = zd2(bxbar, 1, k, nz, 3, sc1); // :343
+        double d2y = zd2(bybar, 1, k, nz, 3, sc1); // :344
+        if (!var_eta) {
+            bxd[k] = zck * d2x - dey;              // :350
+            byd[k] = zck * d2y + dex;              // :351
+        } else {
+            // extension: eta(z) d2b/dz2 + eta'(z) db/dz
+            double gx = zd1(bxbar, 1, k, nz, 5, ho12), gy = zd1(bybar, 1, k, nz, 5, ho12);
+            bxd[k] = eta[k] * d2x - dey + deta[k] * gx;
+            byd[k] = eta[k] * d2y + dex + deta[k] * gy;
+        }
+    }
+}
+
+// wk1 = dEx/dx + dEy/dy in spectral space (:362-407)
+template <typename R>
+static __global__ void k_mag_div(const R *ex, const R *ey, R *w1, int nx, int ny, int nz, const double *akx1,
+                                 const double *aky1)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t np = (size_t)nx * ny;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    size_t q = idx - (size_t)k * np;
+    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    const R *px = ex + (size_t)k * np, *py = ey + (size_t)k * np;
+    w1[idx] = sdx(px, i, j, nx, akx1) + sdy(py, i, j, nx, ny, aky1);
+}
+
+template <typename R>
+struct MagArgs {
+    const R *ex, *ey, *ez, *w1, *pol, *tor;
+    const double *eta, *deta, *akx1, *aky1, *akx2, *aky2;
+    R *poldot, *tordot;
+    double zck, ho12, sc1;
+    int var_eta, nx, ny, nz;
+};
+
+// :400-479 -- wk2 = dEx/dy - dEy/dx, wk3 = d/dz(wk1), inverse horizontal
+// Laplacian, d2/dz2 of pol and tor, and the final poldot / tordot.
+template <typename R>
+static __global__ void k_mag_final(MagArgs<R> a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+    const R *px = a.ex + (size_t)k * np, *py = a.ey + (size_t)k * np;
+    R w2 = sdy(px, i, j, a.nx, a.ny, a.aky1) - sdx(py, i, j, a.nx, a.akx1);
+    R w3 = zd1(a.w1 + q, np, k, a.nz, 5, (R)a.ho12);
+    const R kk = (R)(a.akx2[i] + a.aky2[j]);
+    if (i == 0 && j == 0) { w2 = (R)0; w3 = (R)0; }
+    else { w2 = w2 / kk; w3 = w3 / kk; }
+    const R d2p = zd2(a.pol + q, np, k, a.nz, 3, (R)a.sc1);
+    const R d2t = zd2(a.tor + q, np, k, a.nz, 3, (R)a.sc1);
+    if (!a.var_eta) {
+        const R zck = (R)a.zck;
+        a.poldot[idx] = zck * a.pol[idx] * kk + zck * d2p + w2;
+        a.tordot[idx] = zck * a.tor[idx] * kk + zck * d2t - w3 + a.ez[idx];
+    } else {
+        // extension: eta(z) replaces zeta*ck, tordot gains eta'(z) d(tor)/dz
+        const R e = (R)a.eta[k];
+        const R dt = zd1(a.tor + q, np, k, a.nz, 5, (R)a.ho12);
+        a.poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
+        a.tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + (R)a.deta[k] * dt;
+    }
+}
+
+template <typename R>
+struct BandjArgs {
+    const R *dzs, *pol, *tor;
+    const double *akx1, *aky1, *akx2, *aky2;
+    R *bxh, *byh, *bzh, *dybz, *dxbz, *jzh;
+    int nx, ny, nz;
+};
+
+// bandj in spectral space, src/magnetic.f90:525-570 and :584-617
+template <typename R>
+static __global__ void k_bandj_spec(BandjArgs<R> a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+    const size_t pb = (size_t)k * np;
+    const R *s = a.dzs + pb, *tp = a.tor + pb, *pp = a.pol + pb;
+    a.bxh[idx] = sdx(s, i, j, a.nx, a.akx1) + sdy(tp, i, j, a.nx, a.ny, a.aky1);
+    a.byh[idx] = sdy(s, i, j, a.nx, a.ny, a.aky1) - sdx(tp, i, j, a.nx, a.akx1);
+    a.bzh[idx] = (R)-1 * a.pol[idx] * (R)(a.akx2[i] + a.aky2[j]);
+    a.jzh[idx] = (R)-1 * a.tor[idx] * (R)(a.akx2[i] + a.aky2[j]);
+    // d/dy and d/dx of ez = -pol*(akx2+aky2), evaluated at the mirrored index
+    R dy = (R)0, dx = (R)0;
+    if (!(j == 0 || 2 * j == a.ny)) {
+        int jm = a.ny - j;
+        R ezm = (R)-1 * pp[(size_t)jm * a.nx + i] * (R)(a.akx2[i] + a.aky2[jm]);
+        dy = ezm * (R)a.aky1[j];
+        if (2 * j < a.ny) dy = -dy;
+    }
+    if (!(i == 0 || 2 * i == a.nx)) {
+        int im = a.nx - i;
+        R ezm = (R)-1 * pp[(size_t)j * a.nx + im] * (R)(a.akx2[im] + a.aky2[j]);
+        dx = ezm * (R)a.akx1[i];
+        if (2 * i < a.nx) dx = -dx;
+    }
+    a.dybz[idx] = dy;
+    a.dxbz[idx] = dx;
+}
+
+// :630-645: jsq from Jz, dBz/dy, dBz/dx and the z derivatives of Bx, By
+template <typename R>
+static __global__ void k_jsq(const R *jz, const R *dybz, const R *dxbz, const R *bx, const R *by, R *jsq,
+                             size_t np, int nz, R h)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    R wk1 = zd1(by + q, np, k, nz, 5, h);
+    R wk2 = zd1(bx + q, np, k, nz, 5, h);
+    R ez = jz[idx], ex = dybz[idx], ey = dxbz[idx];
+    jsq[idx] = ez * ez + ((ex - wk1) * (ex - wk1)) + ((wk2 - ey) * (wk2 - ey));
+}
+
+// spectral truncation of the 2/3 rule, src/magnetic.f90:666-717
+__host__ __device__ __forceinline__ bool truncated(int i, int j, int nx, int ny, int cx, int cy)
+{
+    return (i >= nx / 2 - cx && i <= nx / 2 + cx) || (j >= ny / 2 - cy && j <= ny / 2 + cy);
+}
+
+template <typename R>
+static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, int cy)
+{
+    size_t np = (size_t)nx * ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    size_t q = idx % np;
+    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    if (truncated(i, j, nx, ny, cx, cy)) {
+        a[idx] = (R)0;
+        if (b) b[idx] = (R)0;
+    }
+}

@@ -22,6 +22,7 @@
 #include "common.cuh"
 #include "engine.h"
 #include "zstencil.cuh"
+#include "magkern.cuh"
 
 #define TPB 256
 static inline unsigned nblk(size_t n, int tpb = TPB)
@@ -296,102 +297,12 @@ int phys_hydro64(Engine *E)
 // ============================================================================
 // mag_deriv: src/magnetic.f90:285-487 (+ eta(z) extension)
 // ============================================================================
-__global__ void k_emf(const double *u, const double *v, const double *w, const double *bx,
-                      const double *by, const double *bz, double *e1, double *e2, double *e3, size_t n)
-{
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    // :311-313
-    e1[i] = v[i] * bz[i] - w[i] * by[i];
-    e2[i] = w[i] * bx[i] - u[i] * bz[i];
-    e3[i] = u[i] * by[i] - v[i] * bx[i];
-}
-
-// mean-field RHS (:328-352) on one CTA; ex, ey are the 2-D spectra of the EMF
-__global__ void k_mean_rhs(const double *ex, const double *ey, const double *bxbar, const double *bybar,
-                           const double *eta, const double *deta, double *bxd, double *byd,
-                           double *scratch, size_t np, int nz, double xn, double zck, double ho12,
-                           double sc1, int var_eta)
-{
-    double *e1 = scratch, *e2 = scratch + nz;
-    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        e1[k] = xn * ex[(size_t)k * np];
-        e2[k] = xn * ey[(size_t)k * np];
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        double dey = zd1(e2, 1, k, nz, 5, ho12);   // :337
-        double dex = zd1(e1, 1, k, nz, 5, ho12);   // :338
-        double d2x = zd2(bxbar, 1, k, nz, 3, sc1); // :343
-        double d2y = zd2(bybar, 1, k, nz, 3, sc1); // :344
-        if (!var_eta) {
-            bxd[k] = zck * d2x - dey;              // :350
-            byd[k] = zck * d2y + dex;              // :351
-        } else {
-            double gx = zd1(bxbar, 1, k, nz, 5, ho12), gy = zd1(bybar, 1, k, nz, 5, ho12);
-            bxd[k] = eta[k] * d2x - dey + deta[k] * gx;
-            byd[k] = eta[k] * d2y + dex + deta[k] * gy;
-        }
-    }
-}
-
-// wk1 = dEx/dx + dEy/dy in spectral space (:362-407)
-__global__ void k_mag_div(const double *ex, const double *ey, double *w1, int nx, int ny, int nz,
-                          const double *akx1, const double *aky1)
-{
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t np = (size_t)nx * ny;
-    if (idx >= np * nz) return;
-    int k = (int)(idx / np);
-    size_t q = idx - (size_t)k * np;
-    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
-    const double *px = ex + (size_t)k * np, *py = ey + (size_t)k * np;
-    w1[idx] = sdx(px, i, j, nx, akx1) + sdy(py, i, j, nx, ny, aky1);
-}
-
-struct MagArgs {
-    const double *ex, *ey, *ez, *w1, *pol, *tor, *eta, *deta;
-    const double *akx1, *aky1, *akx2, *aky2;
-    double *poldot, *tordot;
-    double zck, ho12, sc1;
-    int var_eta, nx, ny, nz;
-};
-
-// :400-479 -- wk2 = dEx/dy - dEy/dx, wk3 = d/dz(wk1), inverse horizontal
-// Laplacian, d2/dz2 of pol and tor, and the final poldot / tordot.
-__global__ void k_mag_final(MagArgs a)
-{
-    const size_t np = (size_t)a.nx * a.ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * a.nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
-    const double *px = a.ex + (size_t)k * np, *py = a.ey + (size_t)k * np;
-    double w2 = sdy(px, i, j, a.nx, a.ny, a.aky1) - sdx(py, i, j, a.nx, a.akx1);
-    double w3 = zd1(a.w1 + q, np, k, a.nz, 5, a.ho12);
-    const double kk = a.akx2[i] + a.aky2[j];
-    if (i == 0 && j == 0) { w2 = 0.0; w3 = 0.0; }
-    else { w2 = w2 / kk; w3 = w3 / kk; }
-    const double d2p = zd2(a.pol + q, np, k, a.nz, 3, a.sc1);
-    const double d2t = zd2(a.tor + q, np, k, a.nz, 3, a.sc1);
-    if (!a.var_eta) {
-        a.poldot[idx] = a.zck * a.pol[idx] * kk + a.zck * d2p + w2;
-        a.tordot[idx] = a.zck * a.tor[idx] * kk + a.zck * d2t - w3 + a.ez[idx];
-    } else {
-        const double e = a.eta[k];
-        const double dt = zd1(a.tor + q, np, k, a.nz, 5, a.ho12);
-        a.poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
-        a.tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + a.deta[k] * dt;
-    }
-}
-
 int phys_mag64(Engine *E)
 {
     double *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
     int st;
-    KLAUNCHB(E, "emf_f64", FB(E, 9, 8), k_emf, nblk(E->n), TPB, E->u, E->v, E->w, E->bx, E->by, E->bz, W[W_M1], W[W_M2], W[W_M3], E->n);
+    KLAUNCHB(E, "emf_f64", FB(E, 9, 8), k_emf<double>, nblk(E->n), TPB, E->u, E->v, E->w, E->bx, E->by, E->bz, W[W_M1], W[W_M2], W[W_M3], E->n, 0.0);
     // forwardfft x3 (:321-323): x pass then y pass in place
     LineJob<double> fx[3] = { ljob<double>(W[W_M1], W[W_EX], OP_FWD), ljob<double>(W[W_M2], W[W_EY], OP_FWD),
                               ljob<double>(W[W_M3], W[W_EZ], OP_FWD) };
@@ -400,16 +311,16 @@ int phys_mag64(Engine *E)
                               ljob<double>(W[W_EZ], W[W_EZ], OP_FWD) };
     if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
     const Consts &c = E->k;
-    KLAUNCH(E, "mean_rhs", k_mean_rhs, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
+    KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
             E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
-    KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
-    MagArgs a;
+    KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
+    MagArgs<double> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol; a.tor = E->tor;
     a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
     a.poldot = (double *)E->hist[5][2]; a.tordot = (double *)E->hist[6][2];
     a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final<double>, nblk(E->n), TPB, a);
     return VEC_OK;
 }
 
@@ -426,71 +337,18 @@ int phys_zero_mag_rhs(Engine *E)
 // ============================================================================
 // bandj: src/magnetic.f90:492-664
 // ============================================================================
-struct BandjArgs {
-    const double *dzs, *pol, *tor, *akx1, *aky1, *akx2, *aky2;
-    double *bxh, *byh, *bzh, *dybz, *dxbz, *jzh;
-    int nx, ny, nz;
-};
-
-// :525-570 and :584-617 in spectral space
-__global__ void k_bandj_spec(BandjArgs a)
-{
-    const size_t np = (size_t)a.nx * a.ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * a.nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
-    const size_t pb = (size_t)k * np;
-    const double *s = a.dzs + pb, *tp = a.tor + pb, *pp = a.pol + pb;
-    a.bxh[idx] = sdx(s, i, j, a.nx, a.akx1) + sdy(tp, i, j, a.nx, a.ny, a.aky1);
-    a.byh[idx] = sdy(s, i, j, a.nx, a.ny, a.aky1) - sdx(tp, i, j, a.nx, a.akx1);
-    a.bzh[idx] = -1.0 * a.pol[idx] * (a.akx2[i] + a.aky2[j]);
-    a.jzh[idx] = -1.0 * a.tor[idx] * (a.akx2[i] + a.aky2[j]);
-    // d/dy and d/dx of ez = -pol*(akx2+aky2), evaluated at the mirrored index
-    double dy = 0.0, dx = 0.0;
-    if (!(j == 0 || 2 * j == a.ny)) {
-        int jm = a.ny - j;
-        double ezm = -1.0 * pp[(size_t)jm * a.nx + i] * (a.akx2[i] + a.aky2[jm]);
-        dy = ezm * a.aky1[j];
-        if (2 * j < a.ny) dy = -dy;
-    }
-    if (!(i == 0 || 2 * i == a.nx)) {
-        int im = a.nx - i;
-        double ezm = -1.0 * pp[(size_t)j * a.nx + im] * (a.akx2[im] + a.aky2[j]);
-        dx = ezm * a.akx1[i];
-        if (2 * i < a.nx) dx = -dx;
-    }
-    a.dybz[idx] = dy;
-    a.dxbz[idx] = dx;
-}
-
-// :630-645: jsq from Jz, dBz/dy, dBz/dx and the z derivatives of Bx, By
-__global__ void k_jsq(const double *jz, const double *dybz, const double *dxbz, const double *bx,
-                      const double *by, double *jsq, size_t np, int nz, double h)
-{
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    double wk1 = zd1(by + q, np, k, nz, 5, h);
-    double wk2 = zd1(bx + q, np, k, nz, 5, h);
-    double ez = jz[idx], ex = dybz[idx], ey = dxbz[idx];
-    jsq[idx] = ez * ez + ((ex - wk1) * (ex - wk1)) + ((wk2 - ey) * (wk2 - ey));
-}
-
 int phys_bandj64(Engine *E)
 {
     double *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
     int st;
     if ((st = op_d1z(E, E->pol, W[W_M1], 5, (int)E->np, E->nz))) return st;   // :519
-    BandjArgs a;
+    BandjArgs<double> a;
     a.dzs = W[W_M1]; a.pol = E->pol; a.tor = E->tor; a.akx1 = E->akx1; a.aky1 = E->aky1;
     a.akx2 = E->akx2; a.aky2 = E->aky2;
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "bandj_spec_f64", FB(E, 9, 8), k_bandj_spec, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "bandj_spec_f64", FB(E, 9, 8), k_bandj_spec<double>, nblk(E->n), TPB, a);
     // six inverse 2-D transforms (:575-577, :623-625): x pass in place, then y
     LineJob<double> ix[6] = { ljob<double>(W[W_EX], W[W_EX], OP_INV), ljob<double>(W[W_EY], W[W_EY], OP_INV),
                               ljob<double>(W[W_EZ], W[W_EZ], OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
@@ -503,33 +361,13 @@ int phys_bandj64(Engine *E)
     iy[1].addk = E->bybar;
     iy[2].addc = E->bzbar;
     if ((st = launch_lines<double>(E, 1, iy, 6))) return st;
-    KLAUNCHB(E, "jsq_f64", FB(E, 6, 8), k_jsq, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
+    KLAUNCHB(E, "jsq_f64", FB(E, 6, 8), k_jsq<double>, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
     return VEC_OK;
 }
 
 // ============================================================================
 // magdealias (src/magnetic.f90:666-717) and spectral truncation
 // ============================================================================
-template <typename R>
-__device__ __forceinline__ bool truncated(int i, int j, int nx, int ny, int cx, int cy)
-{
-    return (i >= nx / 2 - cx && i <= nx / 2 + cx) || (j >= ny / 2 - cy && j <= ny / 2 + cy);
-}
-
-template <typename R>
-__global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, int cy)
-{
-    size_t np = (size_t)nx * ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * nz) return;
-    size_t q = idx % np;
-    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
-    if (truncated<R>(i, j, nx, ny, cx, cy)) {
-        a[idx] = (R)0;
-        if (b) b[idx] = (R)0;
-    }
-}
-
 int phys_magdealias(Engine *E)
 {
     KLAUNCH(E, "magdealias_f64", k_truncate<double>, nblk(E->n), TPB, E->pol, E->tor, E->nx, E->ny, E->nz,
@@ -687,7 +525,7 @@ __global__ void k_ab3_update(Ab3Args a)
     if (a.magdealias) {
         size_t q = idx % np;
         int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
-        trunc = truncated<double>(i, j, a.nx, a.ny, a.cx, a.cy);
+        trunc = truncated(i, j, a.nx, a.ny, a.cx, a.cy);
     }
 #pragma unroll
     for (int f = 5; f < 7; f++) {
@@ -696,7 +534,7 @@ __global__ void k_ab3_update(Ab3Args a)
     }
 }
 
-static void rotate_hist(Engine *E)
+void phys_rotate_hist(Engine *E)
 {
     for (int f = 0; f < 7; f++) {
         void *old0 = E->hist[f][0];
@@ -709,10 +547,17 @@ static void rotate_hist(Engine *E)
     E->bybardot[0] = E->bybardot[1]; E->bybardot[1] = E->bybardot[2]; E->bybardot[2] = by0;
 }
 
-int phys_ab3(Engine *E, int magdealias)
+int phys_ab3_coef(Engine *E)
 {
     KLAUNCH(E, "ab3_coef", k_ab3_coef, 1, 256, E->ds, E->bxbar, E->bybar, E->bxbardot[0], E->bxbardot[1],
             E->bxbardot[2], E->bybardot[0], E->bybardot[1], E->bybardot[2], E->nz, 1);
+    return VEC_OK;
+}
+
+int phys_ab3(Engine *E, int magdealias)
+{
+    int st = phys_ab3_coef(E);
+    if (st) return st;
     Ab3Args a;
     // order of the reference's loop body: u, v, w, r, t, pol, tor
     double *xs[7] = { E->u, E->v, E->w, E->r, E->t, E->pol, E->tor };
@@ -729,7 +574,7 @@ int phys_ab3(Engine *E, int magdealias)
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
     KLAUNCHB(E, "ab3_update_f64", FB(E, 35, 8), k_ab3_update, nblk(E->n), TPB, a);
-    rotate_hist(E);
+    phys_rotate_hist(E);
     return VEC_OK;
 }
 
@@ -1116,8 +961,11 @@ __global__ void k_mag_init_means(const double *ex, const double *ey, const doubl
 
 int phys_mag_init(Engine *E)
 {
+    // six FP64 work arrays (valid in both forms, see Engine::W64)
     double *W[W_COUNT];
-    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<double>(i);
+    for (int i = 0; i < W_COUNT; i++) W[i] = nullptr;
+    W[W_EX] = E->W64(0); W[W_EY] = E->W64(1); W[W_EZ] = E->W64(2);
+    W[W_M1] = E->W64(3); W[W_M2] = E->W64(4); W[W_M3] = E->W64(5);
     int st;
     if (E->p.dynamo)
         KLAUNCH(E, "dynamo_seed", k_dynamo_seed, nblk(E->n), TPB, E->bx, E->by, E->bz, E->nx, E->ny, E->n, E->p.perfect);
@@ -1146,7 +994,7 @@ int phys_mag_init(Engine *E)
     if ((st = launch_lines<double>(E, 0, ix, 3))) return st;
     if ((st = launch_lines<double>(E, 1, ix, 3))) return st;
     // jsq (:246-261): ex = inv(dBz/dy), ey = inv(dBz/dx), ez = inv(Jz)
-    KLAUNCH(E, "jsq_f64", k_jsq, nblk(E->n), TPB, W[W_M3], W[W_M1], W[W_M2], E->bx, E->by, E->jsq, E->np, E->nz,
+    KLAUNCH(E, "jsq_f64", k_jsq<double>, nblk(E->n), TPB, W[W_M3], W[W_M1], W[W_M2], E->bx, E->by, E->jsq, E->np, E->nz,
             E->k.ho12);
     return phys_mag_boundary(E);
 }

@@ -1,10 +1,594 @@
-// split.cu -- FP32-bulk / FP64-background form (filled in below).
+// split.cu -- the FP32-bulk / FP64-background form of the time step.
+//
+// FP64 is kept for: the state and its AB3 accumulation (r,t,u,v,w,pol,tor),
+// the horizontally uniform polytropic background rho0(z) = T0(z)^m,
+// T0(z) = 1 + theta z, the residual of the discrete pressure-gradient-minus-
+// gravity balance of that background, the mean fields and the diagnostics.
+// Everything else -- the FFTs, z stencils, nonlinear products and the RHS
+// histories -- runs in FP32 on perturbation mirrors of the state:
+//     r32 = r - rho0(z),  t32 = t - T0(z),  bz32 = bz - bzbar,
+// so that no FP32 operation ever has to resolve the O(1e-3) dynamics on top
+// of the O(10) background.
+//
+// The split is exact in exact arithmetic: every z stencil is linear, so
+// D(rho0 + r') = D(rho0) + D(r'), and the background parts D(rho0), D(T0)
+// are applied once on the host in FP64 with the same stencils and flags the
+// reference uses (src/hydro_deriv.f90:66-68, 184, 443-444).  In the
+// vertical momentum equation the large terms
+//     -rho dT/dz + theta(m+1) rho - T d(rho)/dz
+// become  [-rho0 T0' + theta(m+1) rho0 - T0 rho0'](z)   (FP64, 1-D)
+//       + [-rho0 T'z - r' T0' - r' T'z + theta(m+1) r' - T0 r'z - T' rho0' - T' r'z]
+// and the magnetic pressure uses bz^2 - bzbar^2 = bz'(2 bzbar + bz'), whose
+// horizontal and vertical derivatives equal those of bz^2 (the difference is
+// a constant; the spectral derivative drops the mean and every z stencil
+// annihilates constants).
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
 #include "common.cuh"
 #include "engine.h"
+#include "magkern.cuh"
+#include "zstencil.cuh"
 
-int split_setup(Engine *E) { (void)E; vec_set_error("split form not built"); return VEC_ERR_ARG; }
-int split_hydro(Engine *E) { (void)E; return VEC_ERR_ARG; }
-int split_mag(Engine *E) { (void)E; return VEC_ERR_ARG; }
-int split_bandj(Engine *E) { (void)E; return VEC_ERR_ARG; }
-int split_refresh(Engine *E) { (void)E; return VEC_ERR_ARG; }
-int split_ab3(Engine *E, int m) { (void)E; (void)m; return VEC_ERR_ARG; }
+#define TPB 256
+static inline unsigned nblk(size_t n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+#define KLAUNCHB(E, name, bytes, kern, grid, block, ...)         \
+    do {                                                         \
+        (E)->prof_begin(name, (double)(bytes));                  \
+        kern<<<(grid), (block), 0, (E)->stream>>>(__VA_ARGS__);  \
+        (E)->prof_end();                                         \
+        CUDA_TRY(cudaGetLastError());                            \
+    } while (0)
+#define FB(E, nf, esz) ((double)(nf) * (double)(E)->n * (double)(esz))
+
+// 1-D FP64 background profiles and their discrete derivatives
+enum Bg {
+    BG_RHO0, BG_T0, BG_T0Z5, BG_T0ZU_P, BG_T0ZU_M, BG_T0ZZ0, BG_RHO0Z0, BG_RHO0ZU_P, BG_RHO0ZU_M,
+    BG_A, BG_B, BG_COUNT
+};
+
+static int falloc(float **p, size_t n)
+{
+    if (cudaMalloc((void **)p, sizeof(float) * (n ? n : 1)) != cudaSuccess) {
+        cudaGetLastError();
+        vec_set_error("cudaMalloc of %zu floats failed", n);
+        return VEC_ERR_ALLOC;
+    }
+    return cudaMemset(*p, 0, sizeof(float) * n) == cudaSuccess ? VEC_OK : VEC_ERR_CUDA;
+}
+
+int split_setup(Engine *E)
+{
+    const size_t n = E->n;
+    const int nz = E->nz;
+    float **m[] = { &E->r32, &E->t32, &E->u32, &E->v32, &E->w32, &E->bx32, &E->by32, &E->bz32, &E->jsq32,
+                    &E->pol32, &E->tor32 };
+    for (auto pp : m) {
+        int st = falloc(pp, n);
+        if (st) return st;
+    }
+    std::vector<double> bg((size_t)BG_COUNT * nz, 0.0);
+    double *rho0 = &bg[(size_t)BG_RHO0 * nz], *t0 = &bg[(size_t)BG_T0 * nz];
+    for (int k = 0; k < nz; k++) {
+        double z = (double)k * E->k.dz;
+        t0[k] = 1.0 + z * E->p.theta;
+        rho0[k] = pow(t0[k], E->p.cm);
+    }
+    const double h = E->k.ho12, s = E->k.sc1;
+    for (int k = 0; k < nz; k++) {
+        bg[(size_t)BG_T0Z5 * nz + k] = zd1(t0, 1, k, nz, 5, h);
+        bg[(size_t)BG_T0ZU_P * nz + k] = zd1up(t0, 1, k, nz, 5, h, 1.0);
+        bg[(size_t)BG_T0ZU_M * nz + k] = zd1up(t0, 1, k, nz, 5, h, -1.0);
+        bg[(size_t)BG_T0ZZ0 * nz + k] = zd2(t0, 1, k, nz, 0, s);
+        bg[(size_t)BG_RHO0Z0 * nz + k] = zd1(rho0, 1, k, nz, 0, h);
+        bg[(size_t)BG_RHO0ZU_P * nz + k] = zd1up(rho0, 1, k, nz, 0, h, 1.0);
+        bg[(size_t)BG_RHO0ZU_M * nz + k] = zd1up(rho0, 1, k, nz, 0, h, -1.0);
+    }
+    for (int k = 0; k < nz; k++) {
+        // -rho0 dT0/dz + theta(m+1) rho0  (the rho*tz and gravity terms)
+        bg[(size_t)BG_A * nz + k] = -rho0[k] * bg[(size_t)BG_T0Z5 * nz + k] + E->k.thmplus1 * rho0[k];
+        // -T0 d(rho0)/dz  (the t*rz term, interior rows)
+        bg[(size_t)BG_B * nz + k] = -t0[k] * bg[(size_t)BG_RHO0Z0 * nz + k];
+    }
+    if (cudaMalloc((void **)&E->hres, sizeof(double) * bg.size()) != cudaSuccess) {
+        cudaGetLastError();
+        return VEC_ERR_ALLOC;
+    }
+    CUDA_TRY(cudaMemcpy(E->hres, bg.data(), sizeof(double) * bg.size(), cudaMemcpyHostToDevice));
+    E->b32_auth = 0;
+    return VEC_OK;
+}
+
+// ---- mirrors ---------------------------------------------------------------
+struct MirrorArgs {
+    const double *r, *t, *u, *v, *w, *pol, *tor, *bx, *by, *bz, *jsq, *bg;
+    float *r32, *t32, *u32, *v32, *w32, *pol32, *tor32, *bx32, *by32, *bz32, *jsq32;
+    double bzbar;
+    size_t np;
+    int nz, k0, k1, mask;   // planes [k0,k1); mask: 1 state, 2 uv only, 4 B, 8 pol/tor only
+};
+
+__global__ void k_mirror(MirrorArgs a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x + (size_t)a.k0 * a.np;
+    if (idx >= (size_t)a.k1 * a.np) return;
+    const int k = (int)(idx / a.np);
+    if (a.mask & 1) {
+        a.r32[idx] = (float)(a.r[idx] - a.bg[BG_RHO0 * a.nz + k]);
+        a.t32[idx] = (float)(a.t[idx] - a.bg[BG_T0 * a.nz + k]);
+        a.w32[idx] = (float)a.w[idx];
+    }
+    if (a.mask & 3) {
+        a.u32[idx] = (float)a.u[idx];
+        a.v32[idx] = (float)a.v[idx];
+    }
+    if (a.mask & 9) {
+        a.pol32[idx] = (float)a.pol[idx];
+        a.tor32[idx] = (float)a.tor[idx];
+    }
+    if (a.mask & 4) {
+        a.bx32[idx] = (float)a.bx[idx];
+        a.by32[idx] = (float)a.by[idx];
+        a.bz32[idx] = (float)(a.bz[idx] - a.bzbar);
+        a.jsq32[idx] = (float)a.jsq[idx];
+    }
+}
+
+static int mirror(Engine *E, int mask, int k0, int k1)
+{
+    MirrorArgs a;
+    a.r = E->r; a.t = E->t; a.u = E->u; a.v = E->v; a.w = E->w; a.pol = E->pol; a.tor = E->tor;
+    a.bx = E->bx; a.by = E->by; a.bz = E->bz; a.jsq = E->jsq; a.bg = E->hres;
+    a.r32 = E->r32; a.t32 = E->t32; a.u32 = E->u32; a.v32 = E->v32; a.w32 = E->w32;
+    a.pol32 = E->pol32; a.tor32 = E->tor32; a.bx32 = E->bx32; a.by32 = E->by32; a.bz32 = E->bz32;
+    a.jsq32 = E->jsq32; a.bzbar = E->bzbar; a.np = E->np; a.nz = E->nz; a.k0 = k0; a.k1 = k1; a.mask = mask;
+    KLAUNCHB(E, "mirror", 0, k_mirror, nblk((size_t)(k1 - k0) * E->np), TPB, a);
+    return VEC_OK;
+}
+
+__global__ void k_b64(const float *bx32, const float *by32, const float *bz32, const float *jsq32, double *bx,
+                      double *by, double *bz, double *jsq, double bzbar, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bx[i] = (double)bx32[i];
+    by[i] = (double)by32[i];
+    bz[i] = bzbar + (double)bz32[i];
+    jsq[i] = (double)jsq32[i];
+}
+
+// FP64 B and jsq from the FP32 ones when the FP32 copy is the newer one
+int split_sync_b64(Engine *E)
+{
+    if (!E->b32_auth) return VEC_OK;
+    KLAUNCHB(E, "b_to_f64", FB(E, 4, 12), k_b64, nblk(E->n), TPB, E->bx32, E->by32, E->bz32, E->jsq32, E->bx,
+             E->by, E->bz, E->jsq, E->bzbar, E->n);
+    E->b32_auth = 0;
+    return VEC_OK;
+}
+
+// all FP32 mirrors from the FP64 state (after the state was set from outside)
+int split_refresh(Engine *E)
+{
+    int st = split_sync_b64(E);
+    if (st) return st;
+    return mirror(E, 1 | 4 | 8, 0, E->nz);
+}
+
+int split_refresh_planes(Engine *E, int mask)
+{
+    int st = mirror(E, mask, 0, 1);
+    if (st) return st;
+    return mirror(E, mask, E->nz - 1, E->nz);
+}
+
+int split_refresh_uv(Engine *E) { return mirror(E, 2, 0, E->nz); }
+
+// ---- hydro_deriv ------------------------------------------------------------
+struct SplitHydroArgs {
+    const float *r, *t, *u, *v, *w, *bx, *by, *bz, *jsq;
+    const float *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
+    const float *ry, *ty, *tyy, *uy, *uyy, *vy, *vyy, *wy, *wyy;
+    const double *kappa, *dkappa, *eta, *bg;
+    float *racc, *tdot, *uacc, *vacc, *wacc;
+    float *p1, *p2, *q, *g, *hh, *p3, *p4;
+    float gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, ho12, sc1, bzbar;
+    double zck;
+    int var_eta;
+    size_t np;
+    int nz;
+};
+
+// the FP32 counterpart of k_hydro_pass2 (src/hydro_deriv.f90 terms without
+// a second-level derivative) on perturbation mirrors
+__global__ void k_split_pass2(SplitHydroArgs a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.np * a.nz) return;
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const float h = a.ho12, s = a.sc1;
+    const double *bg = a.bg;
+
+    const float rho0 = (float)bg[BG_RHO0 * nz + k], t0 = (float)bg[BG_T0 * nz + k];
+    const float rp = a.r[idx], tp = a.t[idx], u0 = a.u[idx], v0 = a.v[idx], w0 = a.w[idx];
+    const float rr = rho0 + rp, tt = t0 + tp;
+    const float bx = a.bx[idx], by = a.by[idx], bzp = a.bz[idx], bz = a.bzbar + bzp;
+    const float rx = a.rx[idx], ry = a.ry[idx];
+    const float tx = a.tx[idx], txx = a.txx[idx], ty = a.ty[idx], tyy = a.tyy[idx];
+    const float ux = a.ux[idx], uxx = a.uxx[idx], uy = a.uy[idx], uyy = a.uyy[idx];
+    const float vx = a.vx[idx], vxx = a.vxx[idx], vy = a.vy[idx], vyy = a.vyy[idx];
+    const float wx = a.wx[idx], wxx = a.wxx[idx], wy = a.wy[idx], wyy = a.wyy[idx];
+
+    const bool wpos = w0 >= 0.0f;
+    const float tzu = zd1up(a.t + q, np, k, nz, 5, h, w0) + (float)bg[(wpos ? BG_T0ZU_P : BG_T0ZU_M) * nz + k];
+    const float tzp = zd1(a.t + q, np, k, nz, 5, h);
+    const float tzz = zd2(a.t + q, np, k, nz, 0, s) + (float)bg[BG_T0ZZ0 * nz + k];
+    const float wzu = zd1up(a.w + q, np, k, nz, 1, h, w0);
+    const float wz = zd1(a.w + q, np, k, nz, 1, h);
+    const float uzu = zd1up(a.u + q, np, k, nz, 2, h, w0);
+    const float vzu = zd1up(a.v + q, np, k, nz, 2, h, w0);
+    const float uzz = zd2(a.u + q, np, k, nz, 3, s);
+    const float vzz = zd2(a.v + q, np, k, nz, 3, s);
+
+    const float third = 1.0f / 3.0f;
+    const float ohm = a.var_eta ? (float)(a.eta[k] / a.zck) : 1.0f;
+    const float divu = ux + vy + wz;
+
+    a.racc[idx] = -u0 * rx - v0 * ry - rr * divu;
+
+    float td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
+               + a.gck * (float)a.kappa[k] * (txx + tyy + tzz)
+               + a.gck * (float)a.dkappa[k] * tzu
+               + a.fzckg * ohm * a.jsq[idx];
+    td = td - a.gm1 * tt * divu * rr + 2.0f * a.sckg * (ux * ux + vy * vy + wz * wz - third * divu * divu);
+    td = td + a.sckg * (uy + vx) * (uy + vx);
+    td = td + a.sckg * (wx + uzu) * (wx + uzu);
+    td = td + a.sckg * (wy + vzu) * (wy + vzu);
+    a.tdot[idx] = td / rr;
+
+    float ud = -tt * rx - rr * tx;
+    ud = ud - rr * u0 * ux - rr * v0 * uy - rr * w0 * uzu;
+    ud = ud - rr * a.cor * (w0 * a.cpsi + v0 * a.spsi);
+    ud = ud + a.sck * (uzz + uxx + uyy);
+    float vd = -tt * ry - rr * ty;
+    vd = vd - rr * v0 * vy - rr * u0 * vx - rr * w0 * vzu;
+    vd = vd - rr * a.cor * (-u0 * a.spsi);
+    vd = vd + a.sck * (vzz + vxx + vyy);
+    // -rho dT/dz + theta(m+1) rho minus its FP64 background part
+    const float t0z = (float)bg[BG_T0Z5 * nz + k];
+    float wd = -rho0 * tzp - rp * t0z - rp * tzp + a.thmplus1 * rp;
+    wd = wd - rr * w0 * wzu - rr * u0 * wx - rr * v0 * wy;
+    wd = wd - rr * a.cor * (-u0 * a.cpsi);
+    wd = wd + a.sck * (wxx + wyy);
+    a.uacc[idx] = ud;
+    a.vacc[idx] = vd;
+    a.wacc[idx] = wd;
+
+    const float b2z = bzp * (2.0f * a.bzbar + bzp);          // bz^2 - bzbar^2
+    const float temp1 = a.fo2 * bx * bx, temp2 = a.fo2 * by * by, temp3 = a.fo2 * b2z;
+    const float dv = a.scko3 * divu;
+    a.p1[idx] = dv + temp1 - temp2 - temp3;
+    a.p2[idx] = dv + temp2 - temp1 - temp3;
+    a.p3[idx] = a.scko3 * ux + a.scko3 * vy + temp3 - temp1 - temp2;
+    a.p4[idx] = 4.0f * a.scko3 * wz;
+    a.q[idx] = a.f * by * bx;
+    a.g[idx] = a.f * bz * bx;
+    a.hh[idx] = a.f * bz * by;
+}
+
+struct SplitHydro4Args {
+    const float *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
+    const double *bg;
+    float *rdot, *udot, *vdot, *wdot;
+    float ho12;
+    size_t np;
+    int nz;
+};
+
+__global__ void k_split_pass4(SplitHydro4Args a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.np * a.nz) return;
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const int k = (int)(idx / np);
+    const size_t q = idx - (size_t)k * np;
+    const float h = a.ho12;
+    const double *bg = a.bg;
+    const float rho0 = (float)bg[BG_RHO0 * nz + k], t0 = (float)bg[BG_T0 * nz + k];
+    const float rp = a.r[idx], tp = a.t[idx], w0 = a.w[idx];
+    const float rr = rho0 + rp, tt = t0 + tp;
+    float wd = a.wacc[idx] + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
+    const float ud = a.uacc[idx] + zd1(a.g + q, np, k, nz, 5, h);
+    const float vd = a.vacc[idx] + zd1(a.hh + q, np, k, nz, 5, h);
+    float rdot, wfin;
+    if (k == 0 || k == nz - 1) {
+        // src/hydro_deriv.f90:455-470: d(rho)/dz chosen so that dw/dt = 0
+        const double wdn = (double)wd + bg[BG_A * nz + k];
+        const double rz = wdn / (double)tt;
+        rdot = a.racc[idx] - w0 * (float)rz;
+        wfin = (float)(wdn - (double)tt * rz);
+    } else {
+        const bool wpos = w0 >= 0.0f;
+        const float rzu = zd1up(a.r + q, np, k, nz, 0, h, w0) + (float)bg[(wpos ? BG_RHO0ZU_P : BG_RHO0ZU_M) * nz + k];
+        const float rzp = zd1(a.r + q, np, k, nz, 0, h);
+        rdot = a.racc[idx] - w0 * rzu;
+        wfin = wd + (float)(bg[BG_A * nz + k] + bg[BG_B * nz + k]) - t0 * rzp
+               - tp * (float)bg[BG_RHO0Z0 * nz + k] - tp * rzp;
+    }
+    const float ri = 1.0f / rr;
+    a.rdot[idx] = rdot;
+    a.udot[idx] = ud * ri;
+    a.vdot[idx] = vd * ri;
+    a.wdot[idx] = wfin * ri;
+}
+
+int split_hydro(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    int st;
+    LineJob<float> jx[5] = {
+        ljob<float>(E->r32, W[W_RX], OP_D1),
+        ljob<float>(E->t32, W[W_TX], OP_D1, W[W_TXX], OP_D2),
+        ljob<float>(E->u32, W[W_UX], OP_D1, W[W_UXX], OP_D2),
+        ljob<float>(E->v32, W[W_VX], OP_D1, W[W_VXX], OP_D2),
+        ljob<float>(E->w32, W[W_WX], OP_D1, W[W_WXX], OP_D2),
+    };
+    if ((st = launch_lines<float>(E, 0, jx, 5))) return st;
+    LineJob<float> jy[5] = {
+        ljob<float>(E->r32, W[W_RY], OP_D1),
+        ljob<float>(E->t32, W[W_TY], OP_D1, W[W_TYY], OP_D2),
+        ljob<float>(E->u32, W[W_UY], OP_D1, W[W_UYY], OP_D2),
+        ljob<float>(E->v32, W[W_VY], OP_D1, W[W_VYY], OP_D2),
+        ljob<float>(E->w32, W[W_WY], OP_D1, W[W_WYY], OP_D2),
+    };
+    if ((st = launch_lines<float>(E, 1, jy, 5))) return st;
+
+    const Consts &c = E->k;
+    SplitHydroArgs a;
+    a.r = E->r32; a.t = E->t32; a.u = E->u32; a.v = E->v32; a.w = E->w32;
+    a.bx = E->bx32; a.by = E->by32; a.bz = E->bz32; a.jsq = E->jsq32;
+    a.rx = W[W_RX]; a.tx = W[W_TX]; a.txx = W[W_TXX]; a.ux = W[W_UX]; a.uxx = W[W_UXX];
+    a.vx = W[W_VX]; a.vxx = W[W_VXX]; a.wx = W[W_WX]; a.wxx = W[W_WXX];
+    a.ry = W[W_RY]; a.ty = W[W_TY]; a.tyy = W[W_TYY]; a.uy = W[W_UY]; a.uyy = W[W_UYY];
+    a.vy = W[W_VY]; a.vyy = W[W_VYY]; a.wy = W[W_WY]; a.wyy = W[W_WYY];
+    a.kappa = E->kappa; a.dkappa = E->dkappa; a.eta = E->eta; a.bg = E->hres;
+    a.racc = W[W_RACC]; a.tdot = (float *)E->hist[1][2];
+    a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
+    a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H]; a.p3 = W[W_P3]; a.p4 = W[W_P4];
+    a.gck = (float)c.gck; a.fzckg = (float)c.fzckg; a.gm1 = (float)c.gm1; a.sckg = (float)c.sckg;
+    a.fo2 = (float)c.fo2; a.scko3 = (float)c.scko3; a.f = (float)c.f; a.thmplus1 = (float)c.thmplus1;
+    a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
+    a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar; a.zck = c.zck;
+    a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
+    KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, nblk(E->n), TPB, a);
+
+    LineJob<float> kx[3] = {
+        ljob<float>(W[W_P1], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_Q], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_G], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+    };
+    if ((st = launch_lines<float>(E, 0, kx, 3))) return st;
+    LineJob<float> ky[3] = {
+        ljob<float>(W[W_P2], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_Q], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_H], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+    };
+    if ((st = launch_lines<float>(E, 1, ky, 3))) return st;
+
+    SplitHydro4Args b;
+    b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
+    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres;
+    b.rdot = (float *)E->hist[0][2]; b.udot = (float *)E->hist[2][2];
+    b.vdot = (float *)E->hist[3][2]; b.wdot = (float *)E->hist[4][2];
+    b.ho12 = (float)c.ho12; b.np = E->np; b.nz = E->nz;
+    KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4, nblk(E->n), TPB, b);
+    return VEC_OK;
+}
+
+// ---- mag_deriv ---------------------------------------------------------------
+int split_mag(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    int st;
+    KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf<float>, nblk(E->n), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
+             E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n, (float)E->bzbar);
+    LineJob<float> fx[3] = { ljob<float>(W[W_M1], W[W_EX], OP_FWD), ljob<float>(W[W_M2], W[W_EY], OP_FWD),
+                             ljob<float>(W[W_M3], W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<float>(E, 0, fx, 3))) return st;
+    LineJob<float> fy[3] = { ljob<float>(W[W_EX], W[W_EX], OP_FWD), ljob<float>(W[W_EY], W[W_EY], OP_FWD),
+                             ljob<float>(W[W_EZ], W[W_EZ], OP_FWD) };
+    if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
+    const Consts &c = E->k;
+    KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
+             E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
+    KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx,
+             E->ny, E->nz, E->akx1, E->aky1);
+    MagArgs<float> a;
+    a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol32; a.tor = E->tor32;
+    a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.poldot = (float *)E->hist[5][2]; a.tordot = (float *)E->hist[6][2];
+    a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
+    KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, nblk(E->n), TPB, a);
+    return VEC_OK;
+}
+
+// ---- bandj --------------------------------------------------------------------
+__global__ void k_d1z_f(const float *in, float *out, int fl, size_t np, int nz, float h)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * nz) return;
+    int k = (int)(idx / np);
+    out[idx] = zd1(in + (idx - (size_t)k * np), np, k, nz, fl, h);
+}
+
+int split_bandj(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    int st;
+    KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, nblk(E->n), TPB, E->pol32, W[W_M1], 5, E->np, E->nz,
+             (float)E->k.ho12);
+    BandjArgs<float> a;
+    a.dzs = W[W_M1]; a.pol = E->pol32; a.tor = E->tor32; a.akx1 = E->akx1; a.aky1 = E->aky1;
+    a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
+    KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, nblk(E->n), TPB, a);
+    LineJob<float> ix[6] = { ljob<float>(W[W_EX], W[W_EX], OP_INV), ljob<float>(W[W_EY], W[W_EY], OP_INV),
+                             ljob<float>(W[W_EZ], W[W_EZ], OP_INV), ljob<float>(W[W_M2], W[W_M2], OP_INV),
+                             ljob<float>(W[W_M3], W[W_M3], OP_INV), ljob<float>(W[W_M4], W[W_M4], OP_INV) };
+    if ((st = launch_lines<float>(E, 0, ix, 6))) return st;
+    // bz32 keeps bz - bzbar: no constant added
+    LineJob<float> iy[6] = { ljob<float>(W[W_EX], E->bx32, OP_INV), ljob<float>(W[W_EY], E->by32, OP_INV),
+                             ljob<float>(W[W_EZ], E->bz32, OP_INV), ljob<float>(W[W_M2], W[W_M2], OP_INV),
+                             ljob<float>(W[W_M3], W[W_M3], OP_INV), ljob<float>(W[W_M4], W[W_M4], OP_INV) };
+    iy[0].addk = E->bxbar;
+    iy[1].addk = E->bybar;
+    if ((st = launch_lines<float>(E, 1, iy, 6))) return st;
+    KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq<float>, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx32,
+             E->by32, E->jsq32, E->np, E->nz, (float)E->k.ho12);
+    E->b32_auth = 1;
+    return VEC_OK;
+}
+
+// ---- AB3 update in FP64 with FP32 histories ------------------------------------------
+struct SplitAb3Args {
+    double *x[7];
+    const float *h0[7], *h1[7], *h2[7];
+    float *m[7];           // mirrors, same order
+    float *r0, *r1;        // rdot slots zeroed at floored points
+    const double *bg;
+    const DevScalars *ds;
+    int nx, ny, nz, cx, cy, magdealias;
+};
+
+// src/main.F90:413-462 with FP64 accumulation; order u,v,w,r,t,pol,tor
+__global__ void k_split_ab3(SplitAb3Args a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np * a.nz) return;
+    const int k = (int)(idx / np);
+    const double c0 = a.ds->c0, c1 = a.ds->c1, c2 = a.ds->c2;
+    double xs[7];
+#pragma unroll
+    for (int f = 0; f < 5; f++)
+        xs[f] = a.x[f][idx] + c0 * (double)a.h2[f][idx] + c1 * (double)a.h1[f][idx] + c2 * (double)a.h0[f][idx];
+    if (xs[3] < 0.05) {
+        xs[3] = 0.05;
+        a.r0[idx] = 0.0f;
+        a.r1[idx] = 0.0f;
+    }
+    bool trunc = false;
+    if (a.magdealias) {
+        size_t q = idx - (size_t)k * np;
+        int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
+        trunc = truncated(i, j, a.nx, a.ny, a.cx, a.cy);
+    }
+#pragma unroll
+    for (int f = 5; f < 7; f++) {
+        double v = a.x[f][idx] + c0 * (double)a.h2[f][idx] + c1 * (double)a.h1[f][idx] + c2 * (double)a.h0[f][idx];
+        xs[f] = trunc ? 0.0 : v;
+    }
+#pragma unroll
+    for (int f = 0; f < 7; f++) a.x[f][idx] = xs[f];
+    a.m[0][idx] = (float)xs[0];
+    a.m[1][idx] = (float)xs[1];
+    a.m[2][idx] = (float)xs[2];
+    a.m[3][idx] = (float)(xs[3] - a.bg[BG_RHO0 * a.nz + k]);
+    a.m[4][idx] = (float)(xs[4] - a.bg[BG_T0 * a.nz + k]);
+    a.m[5][idx] = (float)xs[5];
+    a.m[6][idx] = (float)xs[6];
+}
+
+int split_ab3(Engine *E, int magdealias)
+{
+    int st = phys_ab3_coef(E);
+    if (st) return st;
+    SplitAb3Args a;
+    double *xs[7] = { E->u, E->v, E->w, E->r, E->t, E->pol, E->tor };
+    float *ms[7] = { E->u32, E->v32, E->w32, E->r32, E->t32, E->pol32, E->tor32 };
+    const int hmap[7] = { 2, 3, 4, 0, 1, 5, 6 };
+    for (int f = 0; f < 7; f++) {
+        a.x[f] = xs[f];
+        a.m[f] = ms[f];
+        a.h0[f] = (const float *)E->hist[hmap[f]][0];
+        a.h1[f] = (const float *)E->hist[hmap[f]][1];
+        a.h2[f] = (const float *)E->hist[hmap[f]][2];
+    }
+    a.r0 = (float *)E->hist[0][1];
+    a.r1 = (float *)E->hist[0][2];
+    a.bg = E->hres;
+    a.ds = E->ds;
+    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
+    a.magdealias = magdealias;
+    // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B
+    KLAUNCHB(E, "ab3_update_split", (double)E->n * (14 * 8 + 21 * 4 + 7 * 4), k_split_ab3, nblk(E->n), TPB, a);
+    phys_rotate_hist(E);
+    return VEC_OK;
+}
+
+// ---- dealias of r,t,u,v,w (every 10 steps) -----------------------------------------
+// The background is horizontally uniform, so the 2/3 truncation only touches
+// the perturbation: x64 -= x32 - D(x32), then the mirror is refreshed.
+struct DealiasArgs {
+    double *x[5];
+    float *m[5];
+    const float *d[5];
+    const double *bg;
+    size_t np;
+    int nz;
+};
+
+__global__ void k_split_dealias_apply(DealiasArgs a)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.np * a.nz) return;
+    const int k = (int)(idx / a.np);
+#pragma unroll
+    for (int f = 0; f < 5; f++) {
+        double xn = a.x[f][idx] - ((double)a.m[f][idx] - (double)a.d[f][idx]);
+        a.x[f][idx] = xn;
+        double b = f == 0 ? a.bg[BG_RHO0 * a.nz + k] : f == 1 ? a.bg[BG_T0 * a.nz + k] : 0.0;
+        a.m[f][idx] = (float)(xn - b);
+    }
+}
+
+int split_dealias(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    float *ms[5] = { E->r32, E->t32, E->u32, E->v32, E->w32 };
+    double *xs[5] = { E->r, E->t, E->u, E->v, E->w };
+    float *tmp[5] = { W[W_RX], W[W_TX], W[W_UX], W[W_VX], W[W_WX] };
+    LineJob<float> jx[5], jy[5];
+    for (int i = 0; i < 5; i++) {
+        jx[i] = ljob<float>(ms[i], tmp[i], OP_DEALIAS);
+        jy[i] = ljob<float>(tmp[i], tmp[i], OP_DEALIAS);
+    }
+    int st;
+    if ((st = launch_lines<float>(E, 0, jx, 5)) || (st = launch_lines<float>(E, 1, jy, 5))) return st;
+    DealiasArgs a;
+    for (int i = 0; i < 5; i++) { a.x[i] = xs[i]; a.m[i] = ms[i]; a.d[i] = tmp[i]; }
+    a.bg = E->hres; a.np = E->np; a.nz = E->nz;
+    KLAUNCHB(E, "dealias_apply_split", FB(E, 5, 24), k_split_dealias_apply, nblk(E->n), TPB, a);
+    return VEC_OK;
+}
+
+// ---- calcdt on the FP64 state with the FP32 field ---------------------------------------
+int split_calcdt(Engine *E)
+{
+    int st = split_sync_b64(E);
+    if (st) return st;
+    return phys_calcdt(E);
+}

@@ -12,10 +12,10 @@
 #pragma once
 
 template <typename R>
-__device__ __forceinline__ R zld(const R *f, size_t np, int k) { return f[(size_t)k * np]; }
+__host__ __device__ __forceinline__ R zld(const R *f, size_t np, int k) { return f[(size_t)k * np]; }
 
 template <typename R>
-__device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R h)
+__host__ __device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R h)
 {
 #define F(kk) zld(f, np, kk)
     if (k == 0) {
@@ -35,7 +35,7 @@ __device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R
 }
 
 template <typename R>
-__device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl, R h, R wv)
+__host__ __device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl, R h, R wv)
 {
 #define F(kk) zld(f, np, kk)
     if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
@@ -55,7 +55,7 @@ __device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl,
 }
 
 template <typename R>
-__device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, int fl, R s)
+__host__ __device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, int fl, R s)
 {
 #define F(kk) zld(f, np, kk)
     if (k == 0) {
