@@ -242,11 +242,13 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         vec_set_error("no CUDA device");
         return VEC_ERR_CUDA;
     }
-    static bool configured = false;
-    if (!configured) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static bool configured[64] = {};
+    if (dev >= 0 && dev < 64 && !configured[dev]) {
         int st = line_kernels_configure();
         if (st) return st;
-        configured = true;
+        configured[dev] = true;
     }
     vec_ctx *c = new vec_ctx();
     Engine &E = c->E;
@@ -255,6 +257,11 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     E.np = (size_t)E.nx * E.ny;
     E.n = E.np * E.nz;
     E.split = p->precision == VEC_PREC_SPLIT;
+    cudaDeviceGetAttribute(&E.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    {
+        const char *g = getenv("VEC_GENERIC_LINES");
+        E.generic_lines = g && g[0] == '1';
+    }
     set_consts(E);
     int st;
     if ((st = line_plan_make(E.nx, E.ny, 8, &E.plx)) || (st = line_plan_make(E.ny, E.nx, 8, &E.ply))) {
@@ -332,6 +339,7 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     E.red_blocks = 152 * 4;
     ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 24 + 64));
     ALLOC(E.ds, sizeof(DevScalars));
+    ALLOC(E.dev_err, sizeof(int) * 4);
     if (cudaMallocHost(&E.hs, sizeof(DevScalars)) != cudaSuccess) { vec_destroy(c); return VEC_ERR_ALLOC; }
     memset(E.hs, 0, sizeof(DevScalars));
     E.hs->first = 1;
@@ -351,7 +359,7 @@ extern "C" int vec_destroy(vec_ctx *c)
     Engine &E = c->E;
     if (E.stream) cudaStreamSynchronize(E.stream);
     void *ptrs[] = { E.r, E.t, E.u, E.v, E.w, E.bx, E.by, E.bz, E.jsq, E.pol, E.tor, E.bxbar, E.bybar,
-                     E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds,
+                     E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds, E.dev_err,
                      E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
                      E.rho0, E.t0, E.hres };
     for (void *q : ptrs) if (q) cudaFree(q);
@@ -377,6 +385,12 @@ extern "C" int vec_sync(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;
     CUDA_TRY(cudaStreamSynchronize(c->E.stream));
+    int err = 0;
+    CUDA_TRY(cudaMemcpy(&err, c->E.dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        vec_set_error("a bounded device wait ran out (TMA tile load did not complete)");
+        return VEC_ERR_CUDA;
+    }
     return VEC_OK;
 }
 

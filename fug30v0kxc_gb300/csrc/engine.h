@@ -39,6 +39,9 @@ struct Engine {
     int split;                  // VEC_PREC_SPLIT
     cudaStream_t stream = nullptr;
     long long launches = 0;
+    int num_sms = 152;
+    int *dev_err = nullptr;     // set by kernels whose bounded waits ran out
+    int generic_lines = 0;      // force the generic line kernel (VEC_GENERIC_LINES=1)
 
     LinePlan plx, ply;          // precision of the bulk path
     LinePlan plx64, ply64;      // FP64 plans (per-operator entry points)
@@ -106,6 +109,8 @@ template <typename R> int line_tables_make(int n, const double *k1, const double
 template <typename R> void line_tables_free(LineTables<R> *tb);
 template <typename R> int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
 int line_kernels_configure();
+int line_ct_configure();
+template <typename R> int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
 
 template <typename R>
 inline LineJob<R> ljob(const R *in, R *out1, int op1, R *out2 = nullptr, int op2 = OP_NONE,

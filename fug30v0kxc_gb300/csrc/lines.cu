@@ -406,6 +406,11 @@ template <typename R>
 int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
 {
     if (njobs <= 0) return VEC_OK;
+    if (!E->generic_lines) {
+        int h = launch_lines_ct<R>(E, dir, jobs, njobs);
+        if (h == 1) return VEC_OK;
+        if (h < 0) return h;
+    }
     const LinePlan &pl = dir == 0 ? E->plx : E->ply;
     const LineTables<R> &tb = E->tables<R>(dir);
     for (int j0 = 0; j0 < njobs; j0 += MAX_JOBS) {
@@ -436,6 +441,8 @@ int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
 
 int line_kernels_configure()
 {
+    int st = line_ct_configure();
+    if (st) return st;
     CUDA_TRY(cudaFuncSetAttribute(line_kernel<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(line_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(line_kernel<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

@@ -1,0 +1,442 @@
+// lines_ct.cu -- horizontal spectral operators (src/fft.F90) for power-of-two
+// line lengths n = N1*N2 (64..1024), the hot path of the time step.
+//
+// Per tile a CTA owns 2S real lines of one z-plane (S complex sequences
+// z = a + ib).  The tile is brought into shared memory by TMA bulk copies
+// (cp.async.bulk + mbarrier): one copy for 2S contiguous x rows, or one
+// 2S-wide copy per row for y columns.  CTAs are persistent over tiles and the
+// next tile is prefetched into the second buffer while the current one is
+// transformed.
+//
+// Each length-n FFT is a two-level four-step decomposition held in
+// registers: n = N1*N2, m = N2*m1 + m2, k = k1 + N1*k2.  Thread m2 does an
+// N1-point DFT over m1 (itself a four-step of radix-2/4/8 kernels), applies
+// the twiddle W_n^(m2 k1) and hands its results to thread k1 through one
+// padded, bank-conflict-free shared-memory exchange; thread k1 then does the
+// N2-point DFT over m2 and holds X[k1 + N1 k2] for all k2.  The spectral
+// operator (+ik, -k^2, 2/3 truncation, all Hermitian-symmetric multipliers)
+// is applied in registers and the inverse runs the same two levels in the
+// opposite order, so each transform costs one exchange.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "common.cuh"
+#include "engine.h"
+
+template <typename R> struct JobPackCT { LineJob<R> j[MAX_JOBS]; };
+
+// W_32^q = exp(-2 pi i q/32), q = 0..31 (the in-register radix kernels)
+__constant__ float2 c_tw32f[32];
+__constant__ double2 c_tw32d[32];
+
+template <typename C> __device__ __forceinline__ C tw32(int q);
+template <> __device__ __forceinline__ float2 tw32<float2>(int q) { return c_tw32f[q]; }
+template <> __device__ __forceinline__ double2 tw32<double2>(int q) { return c_tw32d[q]; }
+
+template <typename C>
+__device__ __forceinline__ C cmul_(C a, C b) { C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
+template <typename C>
+__device__ __forceinline__ C cadd_(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C csub_(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <bool INV, typename C>
+__device__ __forceinline__ C rot_(C a) { C r; if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; } return r; }
+
+// multiply by W_N^e (e compile-time after unrolling); conjugate for INV
+template <int N, bool INV, typename C>
+__device__ __forceinline__ C twc(C a, int e)
+{
+    const int q = (e * (32 / N)) & 31;
+    if (q == 0) return a;
+    if (q == 8) return rot_<INV>(a);                           // -i (fwd)
+    if (q == 16) { C r; r.x = -a.x; r.y = -a.y; return r; }
+    if (q == 24) return rot_<!INV>(a);                         // +i (fwd)
+    C w = tw32<C>(q);
+    if (INV) w.y = -w.y;
+    return cmul_(a, w);
+}
+
+// in-register natural-order DFT of N points
+template <int N, bool INV> struct RDft;
+template <bool INV> struct RDft<1, INV> { template <typename C> static __device__ __forceinline__ void run(C *) {} };
+template <bool INV> struct RDft<2, INV> {
+    template <typename C> static __device__ __forceinline__ void run(C *v) { C a = v[0], b = v[1]; v[0] = cadd_(a, b); v[1] = csub_(a, b); }
+};
+template <bool INV> struct RDft<4, INV> {
+    template <typename C> static __device__ __forceinline__ void run(C *v) {
+        C a0 = cadd_(v[0], v[2]), a1 = csub_(v[0], v[2]);
+        C b0 = cadd_(v[1], v[3]), b1 = rot_<INV>(csub_(v[1], v[3]));
+        v[0] = cadd_(a0, b0); v[1] = cadd_(a1, b1); v[2] = csub_(a0, b0); v[3] = csub_(a1, b1);
+    }
+};
+// four-step in registers: N = A*B, m = B*m1 + m2, k = k1 + A*k2
+template <int A, int B, bool INV, typename C>
+__device__ __forceinline__ void reg_ct(C *v)
+{
+    constexpr int N = A * B;
+    C t[N];
+#pragma unroll
+    for (int m2 = 0; m2 < B; m2++) {
+        C a[A];
+#pragma unroll
+        for (int m1 = 0; m1 < A; m1++) a[m1] = v[B * m1 + m2];
+        RDft<A, INV>::run(a);
+#pragma unroll
+        for (int k1 = 0; k1 < A; k1++) t[m2 * A + k1] = twc<N, INV>(a[k1], m2 * k1);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; k1++) {
+        C b[B];
+#pragma unroll
+        for (int m2 = 0; m2 < B; m2++) b[m2] = t[m2 * A + k1];
+        RDft<B, INV>::run(b);
+#pragma unroll
+        for (int k2 = 0; k2 < B; k2++) v[k1 + A * k2] = b[k2];
+    }
+}
+template <bool INV> struct RDft<8, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<2, 4, INV>(v); } };
+template <bool INV> struct RDft<16, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<4, 4, INV>(v); } };
+template <bool INV> struct RDft<32, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<8, 4, INV>(v); } };
+
+// ---- TMA / mbarrier helpers ------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// bounded wait: returns false (and the caller reports an error) if the
+// barrier phase does not complete within the iteration limit
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    for (long it = 0; it < (1L << 24); it++) {
+        unsigned ok;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// ---- the kernel --------------------------------------------------------------------
+// DIR 0: x lines (a tile = 2S contiguous rows), DIR 1: y lines (a tile = 2S
+// adjacent columns over all ny rows).
+template <typename R, int DIR, int N1, int N2, int S>
+__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2))
+line_ct(JobPackCT<R> jobs, LineTables<R> tb, int nx, int ny, int nz, int tpp, int total, int *err)
+{
+    using C = typename CT<R>::T;
+    constexpr int N = N1 * N2;
+    constexpr int NP = N1 > N2 ? N1 : N2;
+    constexpr int NT = S * NP;
+    constexpr int TILE = 2 * S * N;                   // reals per tile
+    constexpr int LX = (N1 > N2 ? N1 : N2) + 1;       // padded exchange row
+    constexpr int LDS = ((NP * LX) / 16) * 16 + 17;   // per-sequence exchange stride (== 1 mod 16)
+
+    extern __shared__ __align__(128) unsigned char smem[];
+    R *tile0 = reinterpret_cast<R *>(smem);
+    R *tile1 = tile0 + TILE;
+    C *ex = reinterpret_cast<C *>(tile1 + TILE);
+    C *tws = ex + (size_t)S * LDS;
+    __shared__ __align__(8) uint64_t bar[2];
+
+    const int tid = threadIdx.x;
+    const int sidx = DIR == 0 ? tid / NP : tid % S;
+    const int lane = DIR == 0 ? tid % NP : tid / S;
+    const size_t np = (size_t)nx * ny;
+
+    for (int e = tid; e < N; e += NT) tws[e] = tb.tw[e];
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](int t, R *dst, uint64_t *b) {
+        const int job = t / (nz * tpp);
+        const int rem = t - job * (nz * tpp);
+        const int plane = rem / tpp;
+        const int l0 = (rem - plane * tpp) * 2 * S;
+        const R *src = jobs.j[job].in + (size_t)plane * np;
+        if (DIR == 0) {
+            if (tid == 0) {
+                mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
+                tma_load(dst, src + (size_t)l0 * nx, TILE * (unsigned)sizeof(R), b);
+            }
+        } else if (tid < 32) {
+            if (tid == 0) mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
+            __syncwarp();
+            for (int e = tid; e < N; e += 32)
+                tma_load(dst + (size_t)e * 2 * S, src + (size_t)e * nx + l0, 2 * S * (unsigned)sizeof(R), b);
+        }
+    };
+
+    if (blockIdx.x < total) issue(blockIdx.x, tile0, &bar[0]);
+    int it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, it++) {
+        R *cur = (it & 1) ? tile1 : tile0;
+        R *nxt = (it & 1) ? tile0 : tile1;
+        if (t + (int)gridDim.x < total) {
+            if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(t + gridDim.x, nxt, &bar[(it + 1) & 1]);
+        }
+        if (!mbar_wait(&bar[it & 1], (it >> 1) & 1)) {
+            if (tid == 0) atomicExch(err, 1);
+            return;
+        }
+        const int job = t / (nz * tpp);
+        const int rem = t - job * (nz * tpp);
+        const int plane = rem / tpp;
+        const int l0 = (rem - plane * tpp) * 2 * S;
+        const LineJob<R> &jb = jobs.j[job];
+        const size_t pbase = (size_t)plane * np;
+        const int op1 = jb.op1, op2 = jb.op2;
+        C *ex_s = ex + (size_t)sidx * LDS;
+
+        // element e of sequence sidx in the tile
+        auto tile_z = [&](int e) -> C {
+            C z;
+            if (DIR == 0) { z.x = cur[(2 * sidx) * N + e]; z.y = cur[(2 * sidx + 1) * N + e]; }
+            else { z = reinterpret_cast<const C *>(cur)[(size_t)e * S + sidx]; }
+            return z;
+        };
+
+        C X[N2];   // thread lane = k1 holds X[k1 + N1 k2], k2 = 0..N2-1
+        if (op1 != OP_INV) {
+            // forward, first level: thread m2 = lane, N1-point DFT over m1
+            if (lane < N2) {
+                C a[N1];
+#pragma unroll
+                for (int m1 = 0; m1 < N1; m1++) a[m1] = tile_z(N2 * m1 + lane);
+                RDft<N1, false>::run(a);
+#pragma unroll
+                for (int k1 = 0; k1 < N1; k1++) {
+                    C w = tws[(lane * k1) & (N - 1)];
+                    ex_s[k1 * LX + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
+                }
+            }
+            __syncthreads();
+            // second level: thread k1 = lane, N2-point DFT over m2
+            if (lane < N1) {
+#pragma unroll
+                for (int m2 = 0; m2 < N2; m2++) X[m2] = ex_s[lane * LX + m2];
+                RDft<N2, false>::run(X);
+            }
+            __syncthreads();
+        } else if (lane < N1) {
+            // halfcomplex input lines a (re) and b (im): Z_k = A_k + i B_k
+#pragma unroll
+            for (int k2 = 0; k2 < N2; k2++) {
+                const int k = lane + N1 * k2;
+                const int kk = k <= N / 2 ? k : N - k;
+                const bool edge = kk == 0 || 2 * kk == N;
+                C pa = tile_z(kk);                     // (ha[kk], hb[kk])
+                C pb = edge ? C{0, 0} : tile_z(N - kk); // (ha[n-kk], hb[n-kk])
+                R ar = pa.x, br = pa.y, ai = k <= N / 2 ? pb.x : -pb.x, bi = k <= N / 2 ? pb.y : -pb.y;
+                X[k2].x = ar - bi;
+                X[k2].y = ai + br;
+            }
+        }
+
+        if (op1 == OP_FWD) {
+            // separate Z into the halfcomplex spectra of the two real lines
+            if (lane < N1) {
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) ex_s[lane + N1 * k2 + ((lane + N1 * k2) >> 5)] = X[k2];
+            }
+            __syncthreads();
+            for (int p = lane; p < N; p += NP) {
+                const int q = p == 0 ? 0 : N - p;
+                C zp = ex_s[p + (p >> 5)], zq = ex_s[q + (q >> 5)];
+                R va, vb;
+                if (2 * p <= N) { va = (R)0.5 * (zp.x + zq.x); vb = (R)0.5 * (zp.y + zq.y); }
+                else { va = (R)0.5 * (zq.y - zp.y); vb = (R)0.5 * (zp.x - zq.x); }
+                const int la = l0 + 2 * sidx;
+                R *oa, *ob;
+                if (DIR == 0) { oa = jb.out1 + pbase + (size_t)la * nx + p; ob = oa + nx; }
+                else { oa = jb.out1 + pbase + (size_t)p * nx + la; ob = oa + 1; }
+                const R ra = jb.alpha1 * va, rb = jb.alpha1 * vb;
+                *oa = jb.acc1 ? *oa + ra : ra;
+                *ob = jb.acc1 ? *ob + rb : rb;
+            }
+            __syncthreads();
+            continue;
+        }
+
+        // one or two outputs: Y = m(X), inverse transform, store
+        const int nout = (op2 != OP_NONE && op1 != OP_INV) ? 2 : 1;
+        for (int o = 0; o < nout; o++) {
+            const int op = o == 0 ? op1 : op2;
+            R *out = o == 0 ? jb.out1 : jb.out2;
+            const R alpha = o == 0 ? jb.alpha1 : jb.alpha2;
+            const int acc = o == 0 ? jb.acc1 : jb.acc2;
+            if (lane < N1) {
+                C Y[N2];
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) {
+                    const int k = lane + N1 * k2;
+                    C z = X[k2], y;
+                    if (op == OP_D1) { R m = tb.m1[k]; y.x = -m * z.y; y.y = m * z.x; }
+                    else if (op == OP_INV) { y = z; }
+                    else { R m = op == OP_D2 ? tb.m2[k] : tb.mda[k]; y.x = m * z.x; y.y = m * z.y; }
+                    Y[k2] = y;
+                }
+                // inverse, first level: thread k1 = lane, N2-point DFT over k2
+                RDft<N2, true>::run(Y);
+#pragma unroll
+                for (int m2 = 0; m2 < N2; m2++) {
+                    C w = tws[(m2 * lane) & (N - 1)];
+                    w.y = -w.y;
+                    ex_s[m2 * LX + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
+                }
+            }
+            __syncthreads();
+            // second level: thread m2 = lane, N1-point DFT over k1
+            if (lane < N2) {
+                C a[N1];
+#pragma unroll
+                for (int k1 = 0; k1 < N1; k1++) a[k1] = ex_s[lane * LX + k1];
+                RDft<N1, true>::run(a);
+                const R sc = op == OP_INV ? (R)1 / (R)N : (R)1;
+                const int la = l0 + 2 * sidx;
+                R addv = (R)0;
+                if (op == OP_INV && jb.addk) addv = (R)jb.addk[plane];
+                if (op == OP_INV) addv = addv + (R)jb.addc;
+#pragma unroll
+                for (int m1 = 0; m1 < N1; m1++) {
+                    const int e = lane + N2 * m1;
+                    R *oa, *ob;
+                    if (DIR == 0) { oa = out + pbase + (size_t)la * nx + e; ob = oa + nx; }
+                    else { oa = out + pbase + (size_t)e * nx + la; ob = oa + 1; }
+                    R va = alpha * (a[m1].x * sc), vb = alpha * (a[m1].y * sc);
+                    if (acc) { va = *oa + va; vb = *ob + vb; }
+                    if (op == OP_INV) { va = va + addv; vb = vb + addv; }
+                    *oa = va;
+                    *ob = vb;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---- host side ------------------------------------------------------------------------
+int line_ct_configure()
+{
+    float2 tf[32];
+    double2 td[32];
+    for (int q = 0; q < 32; q++) {
+        // exp(-2 pi i q/32) with exact quadrant values
+        double a = 2.0 * M_PI * (double)q / 32.0;
+        double c = cos(a), s = sin(a);
+        if (q % 8 == 0) {
+            c = (q == 0) ? 1.0 : (q == 16 ? -1.0 : 0.0);
+            s = (q == 8) ? 1.0 : (q == 24 ? -1.0 : 0.0);
+        }
+        td[q].x = c; td[q].y = -s;
+        tf[q].x = (float)c; tf[q].y = (float)(-s);
+    }
+    CUDA_TRY(cudaMemcpyToSymbol(c_tw32f, tf, sizeof(tf)));
+    CUDA_TRY(cudaMemcpyToSymbol(c_tw32d, td, sizeof(td)));
+    return VEC_OK;
+}
+
+template <typename R, int DIR, int N1, int N2, int S>
+static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
+{
+    using C = typename CT<R>::T;
+    constexpr int N = N1 * N2;
+    constexpr int NP = N1 > N2 ? N1 : N2;
+    constexpr int TILE = 2 * S * N;
+    constexpr int LX = NP + 1;
+    constexpr int LDS = ((NP * LX) / 16) * 16 + 17;
+    static bool attr_set = false;
+    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + N) * sizeof(C);
+    if (!attr_set) {
+        CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    const int L = DIR == 0 ? E->ny : E->nx;
+    const int tpp = L / (2 * S);
+    JobPackCT<R> pk;
+    memset(&pk, 0, sizeof(pk));
+    double fields = 0.0;
+    for (int j = 0; j < nj; j++) {
+        pk.j[j] = jobs[j];
+        fields += 2.0 + (jobs[j].acc1 ? 1.0 : 0.0);
+        if (jobs[j].op2 != OP_NONE) fields += 1.0 + (jobs[j].acc2 ? 1.0 : 0.0);
+    }
+    const int total = nj * E->nz * tpp;
+    int per_sm = 1;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_ct<R, DIR, N1, N2, S>, S * NP, smem));
+    if (per_sm < 1) per_sm = 1;
+    int grid = E->num_sms * per_sm;
+    if (grid > total) grid = total;
+    E->prof_begin(name, fields * (double)E->n * sizeof(R));
+    line_ct<R, DIR, N1, N2, S><<<grid, S * NP, smem, E->stream>>>(pk, E->tables<R>(DIR), E->nx, E->ny, E->nz, tpp,
+                                                                  total, E->dev_err);
+    E->prof_end();
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+// returns 1 if handled by the specialised kernel, 0 if the caller must use
+// the generic one, <0 on error
+template <typename R>
+int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
+{
+    const int n = dir == 0 ? E->nx : E->ny;
+    const int L = dir == 0 ? E->ny : E->nx;
+    constexpr bool F = sizeof(R) == 4;
+    // sequences per tile
+    int S = 0;
+    switch (n) {
+    case 64: case 128: case 256: S = F ? 16 : 8; break;
+    case 512: S = F ? 8 : 4; break;
+    case 1024: S = F ? 4 : 2; break;
+    default: return 0;
+    }
+    if (L % (2 * S) != 0) return 0;
+    if ((E->nx * (int)sizeof(R)) % 16 != 0) return 0;
+    for (int j = 0; j < njobs; j++) {
+        if (!aligned16(jobs[j].in) || !aligned16(jobs[j].out1) || (jobs[j].out2 && !aligned16(jobs[j].out2)))
+            return 0;
+    }
+    for (int j0 = 0; j0 < njobs; j0 += MAX_JOBS) {
+        const int nj = njobs - j0 < MAX_JOBS ? njobs - j0 : MAX_JOBS;
+        const LineJob<R> *jb = jobs + j0;
+        const char *name = dir == 0 ? (F ? "line_x_f32" : "line_x_f64") : (F ? "line_y_f32" : "line_y_f64");
+        int st = -1;
+#define CT_CASE(NN, A, B, SS)                                                                       \
+    if (n == NN && S == SS) st = dir == 0 ? run_ct<R, 0, A, B, SS>(E, jb, nj, name) : run_ct<R, 1, A, B, SS>(E, jb, nj, name);
+        if constexpr (F) {
+            CT_CASE(64, 8, 8, 16) CT_CASE(128, 16, 8, 16) CT_CASE(256, 16, 16, 16)
+            CT_CASE(512, 32, 16, 8) CT_CASE(1024, 32, 32, 4)
+        } else {
+            CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
+            CT_CASE(512, 32, 16, 4) CT_CASE(1024, 32, 32, 2)
+        }
+#undef CT_CASE
+        if (st < 0) return 0;
+        if (st) return st;
+    }
+    return 1;
+}
+
+template int launch_lines_ct<float>(Engine *, int, const LineJob<float> *, int);
+template int launch_lines_ct<double>(Engine *, int, const LineJob<double> *, int);
