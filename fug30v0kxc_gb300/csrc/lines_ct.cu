@@ -21,10 +21,15 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "engine.h"
 
 template <typename R> struct JobPackCT { LineJob<R> j[MAX_JOBS]; };
+// one TMA descriptor per job input (y lines: 3-D view nx x ny x nz)
+struct TmapPack { CUtensorMap m[MAX_JOBS]; };
 
 // W_32^q = exp(-2 pi i q/32), q = 0..31 (the in-register radix kernels)
 __constant__ float2 c_tw32f[32];
@@ -115,6 +120,12 @@ __device__ __forceinline__ void tma_load(void *dst, const void *src, unsigned by
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
+// 3-D tiled TMA load of one box (c0 innermost) into shared memory
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                 ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar)) : "memory");
+}
 // bounded wait: returns false (and the caller reports an error) if the
 // barrier phase does not complete within the iteration limit
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
@@ -133,8 +144,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
 // DIR 0: x lines (a tile = 2S contiguous rows), DIR 1: y lines (a tile = 2S
 // adjacent columns over all ny rows).
 template <typename R, int DIR, int N1, int N2, int S>
-__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2))
-line_ct(JobPackCT<R> jobs, LineTables<R> tb, int nx, int ny, int nz, int tpp, int total, int *err)
+__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (S * (N1 > N2 ? N1 : N2) <= 256) ? 2 : 1)
+line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R> tb, int nx, int ny, int nz,
+        int tpp, int total, int *err)
 {
     using C = typename CT<R>::T;
     constexpr int N = N1 * N2;
@@ -176,11 +188,14 @@ line_ct(JobPackCT<R> jobs, LineTables<R> tb, int nx, int ny, int nz, int tpp, in
                 mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
                 tma_load(dst, src + (size_t)l0 * nx, TILE * (unsigned)sizeof(R), b);
             }
-        } else if (tid < 32) {
-            if (tid == 0) mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
-            __syncwarp();
-            for (int e = tid; e < N; e += 32)
-                tma_load(dst + (size_t)e * 2 * S, src + (size_t)e * nx + l0, 2 * S * (unsigned)sizeof(R), b);
+        } else if (tid == 0) {
+            // boxes of 2S columns x (up to 256) rows of this plane
+            constexpr int BR = N < 256 ? N : 256;
+            mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
+#pragma unroll
+            for (int c = 0; c < N / BR; c++)
+                tma_load_3d(dst + (size_t)c * BR * 2 * S, &tmaps.m[job], l0, c * BR, plane, b);
+            (void)src;
         }
     };
 
@@ -354,6 +369,42 @@ int line_ct_configure()
     return VEC_OK;
 }
 
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static int get_encoder()
+{
+    if (g_encode) return VEC_OK;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        vec_set_error("cuTensorMapEncodeTiled not available");
+        return VEC_ERR_CUDA;
+    }
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    return VEC_OK;
+}
+
+// TMA descriptor of a (nx, ny, nz) field read in boxes of 2S columns x BR rows
+template <typename R>
+static int encode_ymap(CUtensorMap *m, const R *base, int nx, int ny, int nz, int S, int BR)
+{
+    cuuint64_t dims[3] = { (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz };
+    cuuint64_t strides[2] = { (cuuint64_t)nx * sizeof(R), (cuuint64_t)nx * ny * sizeof(R) };
+    cuuint32_t box[3] = { (cuuint32_t)(2 * S), (cuuint32_t)BR, 1 };
+    cuuint32_t es[3] = { 1, 1, 1 };
+    CUresult r = g_encode(m, sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                          (void *)base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        vec_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return VEC_ERR_CUDA;
+    }
+    return VEC_OK;
+}
+
 template <typename R, int DIR, int N1, int N2, int S>
 static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
 {
@@ -379,6 +430,15 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
         fields += 2.0 + (jobs[j].acc1 ? 1.0 : 0.0);
         if (jobs[j].op2 != OP_NONE) fields += 1.0 + (jobs[j].acc2 ? 1.0 : 0.0);
     }
+    TmapPack tp;
+    memset(&tp, 0, sizeof(tp));
+    if (DIR == 1) {
+        int st = get_encoder();
+        if (st) return st;
+        constexpr int BR = N < 256 ? N : 256;
+        for (int j = 0; j < nj; j++)
+            if ((st = encode_ymap<R>(&tp.m[j], jobs[j].in, E->nx, E->ny, E->nz, S, BR))) return st;
+    }
     const int total = nj * E->nz * tpp;
     int per_sm = 1;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_ct<R, DIR, N1, N2, S>, S * NP, smem));
@@ -386,8 +446,8 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     int grid = E->num_sms * per_sm;
     if (grid > total) grid = total;
     E->prof_begin(name, fields * (double)E->n * sizeof(R));
-    line_ct<R, DIR, N1, N2, S><<<grid, S * NP, smem, E->stream>>>(pk, E->tables<R>(DIR), E->nx, E->ny, E->nz, tpp,
-                                                                  total, E->dev_err);
+    line_ct<R, DIR, N1, N2, S><<<grid, S * NP, smem, E->stream>>>(pk, tp, E->tables<R>(DIR), E->nx, E->ny, E->nz,
+                                                                  tpp, total, E->dev_err);
     E->prof_end();
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;

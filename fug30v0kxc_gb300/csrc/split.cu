@@ -204,7 +204,7 @@ struct SplitHydroArgs {
 
 // the FP32 counterpart of k_hydro_pass2 (src/hydro_deriv.f90 terms without
 // a second-level derivative) on perturbation mirrors
-__global__ void k_split_pass2(SplitHydroArgs a)
+__global__ void __launch_bounds__(256, 4) k_split_pass2(SplitHydroArgs a)
 {
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.np * a.nz) return;
@@ -479,11 +479,11 @@ __global__ void k_split_ab3(SplitAb3Args a)
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * a.nz) return;
     const int k = (int)(idx / np);
-    const double c0 = a.ds->c0, c1 = a.ds->c1, c2 = a.ds->c2;
+    const float c0 = (float)a.ds->c0, c1 = (float)a.ds->c1, c2 = (float)a.ds->c2;
     double xs[7];
 #pragma unroll
     for (int f = 0; f < 5; f++)
-        xs[f] = a.x[f][idx] + c0 * (double)a.h2[f][idx] + c1 * (double)a.h1[f][idx] + c2 * (double)a.h0[f][idx];
+        xs[f] = a.x[f][idx] + (double)(c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx]);
     if (xs[3] < 0.05) {
         xs[3] = 0.05;
         a.r0[idx] = 0.0f;
@@ -497,7 +497,7 @@ __global__ void k_split_ab3(SplitAb3Args a)
     }
 #pragma unroll
     for (int f = 5; f < 7; f++) {
-        double v = a.x[f][idx] + c0 * (double)a.h2[f][idx] + c1 * (double)a.h1[f][idx] + c2 * (double)a.h0[f][idx];
+        double v = a.x[f][idx] + (double)(c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx]);
         xs[f] = trunc ? 0.0 : v;
     }
 #pragma unroll
@@ -509,6 +509,56 @@ __global__ void k_split_ab3(SplitAb3Args a)
     a.m[4][idx] = (float)(xs[4] - a.bg[BG_T0 * a.nz + k]);
     a.m[5][idx] = (float)xs[5];
     a.m[6][idx] = (float)xs[6];
+}
+
+// four consecutive points per thread (x fastest, nx % 4 == 0): 16-byte
+// loads and stores of the FP32 histories/mirrors and of the FP64 state
+__global__ void k_split_ab3_v4(SplitAb3Args a)
+{
+    const size_t np = (size_t)a.nx * a.ny;
+    const size_t i4 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i4 >= np * a.nz) return;
+    const int k = (int)(i4 / np);
+    // the increment c0 h3 + c1 h2 + c2 h1 is formed in FP32 (the precision of
+    // the histories); only the accumulation into the state is FP64
+    const float c0 = (float)a.ds->c0, c1 = (float)a.ds->c1, c2 = (float)a.ds->c2;
+    double xs[7][4];
+#pragma unroll
+    for (int f = 0; f < 7; f++) {
+        const double2 s01 = *reinterpret_cast<const double2 *>(a.x[f] + i4);
+        const double2 s23 = *reinterpret_cast<const double2 *>(a.x[f] + i4 + 2);
+        const float4 h2 = *reinterpret_cast<const float4 *>(a.h2[f] + i4);
+        const float4 h1 = *reinterpret_cast<const float4 *>(a.h1[f] + i4);
+        const float4 h0 = *reinterpret_cast<const float4 *>(a.h0[f] + i4);
+        xs[f][0] = s01.x + (double)(c0 * h2.x + c1 * h1.x + c2 * h0.x);
+        xs[f][1] = s01.y + (double)(c0 * h2.y + c1 * h1.y + c2 * h0.y);
+        xs[f][2] = s23.x + (double)(c0 * h2.z + c1 * h1.z + c2 * h0.z);
+        xs[f][3] = s23.y + (double)(c0 * h2.w + c1 * h1.w + c2 * h0.w);
+    }
+    // density floor (src/main.F90:438-443)
+    const bool fl0 = xs[3][0] < 0.05, fl1 = xs[3][1] < 0.05, fl2 = xs[3][2] < 0.05, fl3 = xs[3][3] < 0.05;
+    if (fl0 | fl1 | fl2 | fl3) {
+        const bool fl[4] = { fl0, fl1, fl2, fl3 };
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (fl[q]) { xs[3][q] = 0.05; a.r0[i4 + q] = 0.0f; a.r1[i4 + q] = 0.0f; }
+    }
+    if (a.magdealias) {
+        const size_t qq = i4 - (size_t)k * np;
+        const int j = (int)(qq / a.nx), i = (int)(qq - (size_t)j * a.nx);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (truncated(i + q, j, a.nx, a.ny, a.cx, a.cy)) { xs[5][q] = 0.0; xs[6][q] = 0.0; }
+    }
+    const double rb = a.bg[BG_RHO0 * a.nz + k], tb = a.bg[BG_T0 * a.nz + k];
+#pragma unroll
+    for (int f = 0; f < 7; f++) {
+        *reinterpret_cast<double2 *>(a.x[f] + i4) = make_double2(xs[f][0], xs[f][1]);
+        *reinterpret_cast<double2 *>(a.x[f] + i4 + 2) = make_double2(xs[f][2], xs[f][3]);
+        const double b = f == 3 ? rb : (f == 4 ? tb : 0.0);
+        *reinterpret_cast<float4 *>(a.m[f] + i4) =
+            make_float4((float)(xs[f][0] - b), (float)(xs[f][1] - b), (float)(xs[f][2] - b), (float)(xs[f][3] - b));
+    }
 }
 
 int split_ab3(Engine *E, int magdealias)
@@ -533,7 +583,11 @@ int split_ab3(Engine *E, int magdealias)
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
     // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B
-    KLAUNCHB(E, "ab3_update_split", (double)E->n * (14 * 8 + 21 * 4 + 7 * 4), k_split_ab3, nblk(E->n), TPB, a);
+    const double bytes = (double)E->n * (14 * 8 + 21 * 4 + 7 * 4);
+    if (E->nx % 4 == 0)
+        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4, nblk(E->n / 4), TPB, a);
+    else
+        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3, nblk(E->n), TPB, a);
     phys_rotate_hist(E);
     return VEC_OK;
 }
