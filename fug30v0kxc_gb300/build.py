@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libvec_gpu.so")
-SOURCES = ["capi.cu", "lines.cu", "lines_ct.cu", "physics.cu", "split.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "lines.cu", "lines_ct.cu", "physics.cu", "split.cu", "noalloc.cu", "netcdf_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -40,11 +40,12 @@ def build(force=False, verbose=False, extra=()):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
-    objs = [os.path.join(OUT, os.path.basename(s).replace(".cu", ".o")) for s in srcs]
+    objs = [os.path.join(OUT, os.path.splitext(os.path.basename(s))[0] + ".o") for s in srcs]
 
     def comp(pair):
         s, o = pair
-        cmd = [nvcc(), "-c", s, "-o", o] + flags(extra)
+        cmd = [nvcc(), "-c", s, "-o", o] + (flags(extra) if s.endswith(".cu") else
+                                            ["-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-std=c++17"])
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -603,6 +603,9 @@ static int line_op(vec_ctx *c, int dir, const double *fin, double *f1, int op1, 
     return VEC_OK;
 }
 
+extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec);
+extern "C" int vec_nc_read(const char *path, vec_snapshot *s);
+
 extern "C" int vec_d1bydx(vec_ctx *c, const double *fin, double *fout) { return line_op(c, 0, fin, fout, OP_D1, nullptr, OP_NONE); }
 extern "C" int vec_d1bydy(vec_ctx *c, const double *fin, double *fout) { return line_op(c, 1, fin, fout, OP_D1, nullptr, OP_NONE); }
 extern "C" int vec_d2bydx(vec_ctx *c, const double *fin, double *a, double *b) { return line_op(c, 0, fin, a, OP_D1, b, OP_D2); }
@@ -816,3 +819,52 @@ extern "C" int vec_profile_reset(vec_ctx *c)
     return VEC_OK;
 }
 extern "C" long long vec_launch_count(vec_ctx *c) { return c ? c->E.launches : 0; }
+
+// ---- snapshots ------------------------------------------------------------------
+static const int SNAP_FIELDS[8] = { VEC_F_R, VEC_F_T, VEC_F_U, VEC_F_V, VEC_F_W, VEC_F_BX, VEC_F_BY, VEC_F_BZ };
+
+extern "C" int vec_write_snapshot(vec_ctx *c, const char *path, int iprec, const char *history)
+{
+    if (!c || !path) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    vec_scalars sc;
+    int st = vec_get_scalars(c, &sc);
+    if (st) return st;
+    vec_snapshot s;
+    memset(&s, 0, sizeof(s));
+    s.nx = E.nx; s.ny = E.ny; s.nz = E.nz;
+    s.iteration = sc.iter; s.time = sc.ttime; s.timestep = sc.dt1; s.version = 3;
+    if (history) strncpy(s.history, history, 79);
+    s.gamma = E.p.gamma; s.sigma = E.p.sigma; s.theta = E.p.theta; s.ck = E.p.ck; s.cm = E.p.cm;
+    s.f = E.p.f; s.tayl = E.p.tayl; s.psi = E.p.psi; s.zeta = E.p.zeta; s.xmax = E.p.xmax; s.ymax = E.p.ymax;
+    std::vector<double> buf(8 * E.n);
+    for (int i = 0; i < 8; i++) {
+        s.fields[i] = buf.data() + (size_t)i * E.n;
+        if ((st = vec_get_field(c, SNAP_FIELDS[i], s.fields[i]))) return st;
+    }
+    return vec_nc_write(path, &s, iprec);
+}
+
+extern "C" int vec_read_restart(vec_ctx *c, const char *path)
+{
+    if (!c || !path) return VEC_ERR_ARG;
+    Engine &E = c->E;
+    vec_snapshot s;
+    memset(&s, 0, sizeof(s));
+    s.nx = E.nx; s.ny = E.ny; s.nz = E.nz;
+    std::vector<double> buf(8 * E.n);
+    for (int i = 0; i < 8; i++) s.fields[i] = buf.data() + (size_t)i * E.n;
+    int st = vec_nc_read(path, &s);
+    if (st) return st;
+    for (int i = 0; i < 8; i++)
+        if ((st = vec_set_field(c, SNAP_FIELDS[i], s.fields[i]))) return st;
+    vec_scalars sc;
+    if ((st = vec_get_scalars(c, &sc))) return st;
+    sc.iter = s.iteration;
+    sc.ttime = s.time;
+    sc.dt1 = s.timestep;
+    sc.nit = 0;
+    sc.first = 1;   // src/main.F90:110: the histories are not restored
+    sc.second = 0;
+    return vec_set_scalars(c, &sc);
+}

@@ -203,18 +203,15 @@ struct SplitHydroArgs {
 };
 
 // the FP32 counterpart of k_hydro_pass2 (src/hydro_deriv.f90 terms without
-// a second-level derivative) on perturbation mirrors
-__global__ void __launch_bounds__(256, 4) k_split_pass2(SplitHydroArgs a)
-{
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.np * a.nz) return;
-    const int nz = a.nz;
-    const size_t np = a.np;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    const float h = a.ho12, s = a.sc1;
-    const double *bg = a.bg;
+// a second-level derivative) on perturbation mirrors, for one point; the z
+// derivatives of t', u, v, w come from the caller (register windows in the
+// interior, direct row formulas near the walls)
+struct ZDer { float tzu, tzp, tzz, wzu, wz, uzu, vzu, uzz, vzz; };
 
+__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer &z)
+{
+    const int nz = a.nz;
+    const double *bg = a.bg;
     const float rho0 = (float)bg[BG_RHO0 * nz + k], t0 = (float)bg[BG_T0 * nz + k];
     const float rp = a.r[idx], tp = a.t[idx], u0 = a.u[idx], v0 = a.v[idx], w0 = a.w[idx];
     const float rr = rho0 + rp, tt = t0 + tp;
@@ -226,15 +223,10 @@ __global__ void __launch_bounds__(256, 4) k_split_pass2(SplitHydroArgs a)
     const float wx = a.wx[idx], wxx = a.wxx[idx], wy = a.wy[idx], wyy = a.wyy[idx];
 
     const bool wpos = w0 >= 0.0f;
-    const float tzu = zd1up(a.t + q, np, k, nz, 5, h, w0) + (float)bg[(wpos ? BG_T0ZU_P : BG_T0ZU_M) * nz + k];
-    const float tzp = zd1(a.t + q, np, k, nz, 5, h);
-    const float tzz = zd2(a.t + q, np, k, nz, 0, s) + (float)bg[BG_T0ZZ0 * nz + k];
-    const float wzu = zd1up(a.w + q, np, k, nz, 1, h, w0);
-    const float wz = zd1(a.w + q, np, k, nz, 1, h);
-    const float uzu = zd1up(a.u + q, np, k, nz, 2, h, w0);
-    const float vzu = zd1up(a.v + q, np, k, nz, 2, h, w0);
-    const float uzz = zd2(a.u + q, np, k, nz, 3, s);
-    const float vzz = zd2(a.v + q, np, k, nz, 3, s);
+    const float tzu = z.tzu + (float)bg[(wpos ? BG_T0ZU_P : BG_T0ZU_M) * nz + k];
+    const float tzp = z.tzp;
+    const float tzz = z.tzz + (float)bg[BG_T0ZZ0 * nz + k];
+    const float wzu = z.wzu, wz = z.wz, uzu = z.uzu, vzu = z.vzu, uzz = z.uzz, vzz = z.vzz;
 
     const float third = 1.0f / 3.0f;
     const float ohm = a.var_eta ? (float)(a.eta[k] / a.zck) : 1.0f;
@@ -280,6 +272,56 @@ __global__ void __launch_bounds__(256, 4) k_split_pass2(SplitHydroArgs a)
     a.q[idx] = a.f * by * bx;
     a.g[idx] = a.f * bz * bx;
     a.hh[idx] = a.f * bz * by;
+}
+
+// z-marching: one thread per (i,j) column and chunk of kc planes, with
+// 7-plane register windows of t', u, v, w
+__global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t np = a.np;
+    if (q >= np) return;
+    const int nz = a.nz;
+    const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
+    const float h = a.ho12, s = a.sc1;
+    float T[7], U[7], V[7], W[7];
+#pragma unroll
+    for (int d = 0; d < 7; d++) {
+        const int kk = k0 - 3 + d;
+        const bool ok = kk >= 0 && kk < nz;
+        const size_t o = (size_t)kk * np + q;
+        T[d] = ok ? a.t[o] : 0.0f;
+        U[d] = ok ? a.u[o] : 0.0f;
+        V[d] = ok ? a.v[o] : 0.0f;
+        W[d] = ok ? a.w[o] : 0.0f;
+    }
+    for (int k = k0; k < k1; k++) {
+        const size_t idx = (size_t)k * np + q;
+        const float w0 = W[3];
+        ZDer z;
+        if (k >= 3 && k <= nz - 4) {
+            z.tzu = wd1up(T, h, w0); z.tzp = wd1(T, h); z.tzz = wd2(T, s);
+            z.wzu = wd1up(W, h, w0); z.wz = wd1(W, h);
+            z.uzu = wd1up(U, h, w0); z.vzu = wd1up(V, h, w0);
+            z.uzz = wd2(U, s); z.vzz = wd2(V, s);
+        } else {
+            z.tzu = zd1up(a.t + q, np, k, nz, 5, h, w0); z.tzp = zd1(a.t + q, np, k, nz, 5, h);
+            z.tzz = zd2(a.t + q, np, k, nz, 0, s);
+            z.wzu = zd1up(a.w + q, np, k, nz, 1, h, w0); z.wz = zd1(a.w + q, np, k, nz, 1, h);
+            z.uzu = zd1up(a.u + q, np, k, nz, 2, h, w0); z.vzu = zd1up(a.v + q, np, k, nz, 2, h, w0);
+            z.uzz = zd2(a.u + q, np, k, nz, 3, s); z.vzz = zd2(a.v + q, np, k, nz, 3, s);
+        }
+        split_pass2_point(a, idx, k, z);
+#pragma unroll
+        for (int d = 0; d < 6; d++) { T[d] = T[d + 1]; U[d] = U[d + 1]; V[d] = V[d + 1]; W[d] = W[d + 1]; }
+        const int kn = k + 4;
+        const bool ok = kn < nz;
+        const size_t o = (size_t)kn * np + q;
+        T[6] = ok ? a.t[o] : 0.0f;
+        U[6] = ok ? a.u[o] : 0.0f;
+        V[6] = ok ? a.v[o] : 0.0f;
+        W[6] = ok ? a.w[o] : 0.0f;
+    }
 }
 
 struct SplitHydro4Args {
@@ -368,7 +410,9 @@ int split_hydro(Engine *E)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar; a.zck = c.zck;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
-    KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, nblk(E->n), TPB, a);
+    const int kc = 16;
+    dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
+    KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
 
     LineJob<float> kx[3] = {
         ljob<float>(W[W_P1], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),

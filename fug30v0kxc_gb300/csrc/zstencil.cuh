@@ -92,3 +92,18 @@ __device__ __forceinline__ R sdy(const R *plane, int i, int j, int nx, int ny, c
     R v = plane[(size_t)(ny - j) * nx + i] * (R)aky1[j];
     return 2 * j < ny ? -v : v;
 }
+
+// Interior rows (3 <= k <= nz-4) from a register window v[d] = f(k-3+d):
+// the same formulas and operation order as zd1 / zd1up / zd2.
+template <typename R>
+__host__ __device__ __forceinline__ R wd1(const R *v, R h)
+{ return h * (v[1] - (R)8 * v[2] + (R)8 * v[4] - v[5]); }
+template <typename R>
+__host__ __device__ __forceinline__ R wd1up(const R *v, R h, R wv)
+{
+    if (wv >= (R)0) return h * (-v[0] + (R)6 * v[1] - (R)18 * v[2] + (R)10 * v[3] + (R)3 * v[4]);
+    return h * (v[6] - (R)6 * v[5] + (R)18 * v[4] - (R)10 * v[3] - (R)3 * v[2]);
+}
+template <typename R>
+__host__ __device__ __forceinline__ R wd2(const R *v, R s)
+{ return s * (-v[1] + (R)16 * v[2] - (R)30 * v[3] + (R)16 * v[4] - v[5]); }

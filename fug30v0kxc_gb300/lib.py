@@ -6,7 +6,7 @@ with an error naming the file.
 import ctypes as C
 import os
 
-from .params import VecDiag, VecParams, VecScalars
+from .params import VecDiag, VecParams, VecScalars, VecSnapshot
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libvec_gpu.so")
@@ -61,6 +61,10 @@ SIGNATURES = {
                                   C.POINTER(C.c_double)]),
     "vec_profile_reset": (C.c_int, [_vp]),
     "vec_launch_count": (C.c_longlong, [_vp]),
+    "vec_nc_write": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int]),
+    "vec_nc_read": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot)]),
+    "vec_write_snapshot": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_char_p]),
+    "vec_read_restart": (C.c_int, [_vp, C.c_char_p]),
     "vec_calcdt_noalloc": (C.c_int, [C.POINTER(VecParams)] + [_dp] * 9 + [_vp]),
 }
 

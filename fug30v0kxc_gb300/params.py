@@ -126,3 +126,12 @@ def config0(**kw):
 def config1(**kw):
     """256x256x129, Ra 1e5, Q 100, eta contrast 20."""
     return convection_params(256, 256, 129, eta_contrast=20.0, **kw)
+
+
+class VecSnapshot(C.Structure):
+    """include/vec.h vec_snapshot (fields: R, T, U, V, W, Bx, By, Bz)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("iteration", C.c_int32),
+                ("version", C.c_int32), ("pad_", C.c_int32), ("time", C.c_double), ("timestep", C.c_double)] + \
+               [(n, C.c_double) for n in ("gamma", "sigma", "theta", "ck", "cm", "f", "tayl", "psi", "zeta",
+                                          "xmax", "ymax")] + \
+               [("history", C.c_char * 80), ("fields", C.c_void_p * 8)]

@@ -12,7 +12,7 @@ import numpy as np
 
 from . import lib as _L
 from .params import (FIELD_NAMES, MEAN_NAMES, STATE_FIELDS, STATUS, VecDiag, VecParams,
-                     VecScalars)
+                     VecScalars, VecSnapshot)
 
 
 class VecError(RuntimeError):
@@ -216,6 +216,14 @@ class P3D:
     def launch_count(self):
         return self.L.vec_launch_count(self.h)
 
+    # -- snapshots (src/netcdf.F90) -------------------------------------------------
+    def write_snapshot(self, path, iprec=8, history=""):
+        self._chk(self.L.vec_write_snapshot(self.h, str(path).encode(), iprec, history.encode()),
+                  "write_snapshot")
+
+    def read_restart(self, path):
+        self._chk(self.L.vec_read_restart(self.h, str(path).encode()), "read_restart")
+
 
 def read_input(path):
     """Parse a reference INPUT file (src/initial.F90:94-201) via the C-ABI."""
@@ -224,3 +232,48 @@ def read_input(path):
     if st != 0:
         raise VecError("vec_params_read_input", st)
     return p
+
+
+SNAP_FIELDS = ("R", "T", "U", "V", "W", "Bx", "By", "Bz")
+SNAP_ATTRS = ("gamma", "sigma", "theta", "ck", "cm", "f", "tayl", "psi", "zeta", "xmax", "ymax")
+
+
+def nc_read(path):
+    """Read a reference-layout NetCDF snapshot (no GPU needed): returns a dict
+    with the 8 fields as (nz, ny, nx) arrays plus scalars and attributes."""
+    L = _L.load()
+    s = VecSnapshot()
+    st = L.vec_nc_read(str(path).encode(), C.byref(s))
+    if st != 0:
+        raise VecError("vec_nc_read", st)
+    shape = (s.nz, s.ny, s.nx)
+    arrs = [np.empty(shape, dtype=np.float64) for _ in SNAP_FIELDS]
+    for i, a in enumerate(arrs):
+        s.fields[i] = a.ctypes.data
+    st = L.vec_nc_read(str(path).encode(), C.byref(s))
+    if st != 0:
+        raise VecError("vec_nc_read", st)
+    out = dict(zip(SNAP_FIELDS, arrs))
+    out.update(time=s.time, iteration=s.iteration, timestep=s.timestep, version=s.version,
+               history=s.history.decode(errors="replace"))
+    out.update({a: getattr(s, a) for a in SNAP_ATTRS})
+    return out
+
+
+def nc_write(path, snap, iprec=8):
+    """Write a dict like nc_read's result as a reference-layout snapshot."""
+    L = _L.load()
+    s = VecSnapshot()
+    nz, ny, nx = np.asarray(snap["R"]).shape
+    s.nx, s.ny, s.nz = nx, ny, nz
+    s.time, s.iteration, s.timestep = snap.get("time", 0.0), snap.get("iteration", 0), snap.get("timestep", 0.0)
+    s.version = snap.get("version", 3)
+    s.history = snap.get("history", "").encode()[:79]
+    for a in SNAP_ATTRS:
+        setattr(s, a, float(snap.get(a, 0.0)))
+    keep = [np.ascontiguousarray(snap[n], dtype=np.float64) for n in SNAP_FIELDS]
+    for i, a in enumerate(keep):
+        s.fields[i] = a.ctypes.data
+    st = L.vec_nc_write(str(path).encode(), C.byref(s), iprec)
+    if st != 0:
+        raise VecError("vec_nc_write", st)

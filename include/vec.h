@@ -188,6 +188,32 @@ int vec_step(vec_ctx *ctx, int nsteps);
 /* last diagnostics computed inside vec_step (valid after an ndu06 step) */
 int vec_last_diag(vec_ctx *ctx, vec_diag_out *out);
 
+/* ---- snapshots: the NetCDF layout of src/netcdf.F90:39-1287 -------------- */
+/* One snapshot in host memory; fields[0..7] = R, T, U, V, W, Bx, By, Bz
+ * (caller-owned nx*ny*nz doubles each, Fortran (nx,ny,nz) order). */
+typedef struct vec_snapshot {
+    int32_t nx, ny, nz, iteration, version, pad_;
+    double time, timestep;
+    double gamma, sigma, theta, ck, cm, f, tayl, psi, zeta, xmax, ymax;
+    char history[80];
+    double *fields[8];
+} vec_snapshot;
+/* Writes a classic (CDF-1) NetCDF file as CreateNetCDF/WriteNetCDF do
+ * (src/netcdf.F90:39-585); iprec 4 (float) or 8 (double), cf.
+ * src/main.F90:695-704. */
+int vec_nc_write(const char *path, const vec_snapshot *s, int iprec);
+/* Reads a classic NetCDF snapshot (OpenNetCDF/ReadNetCDF,
+ * src/netcdf.F90:591-1166): sizes, parameters, time, iteration, timestep;
+ * fields too when s->fields[i] are set and s->nx/ny/nz match the file. */
+int vec_nc_read(const char *path, vec_snapshot *s);
+/* The context's state written as a snapshot (time/iteration/timestep from
+ * the context's scalars; timestep = dt1 as in src/main.F90:729). */
+int vec_write_snapshot(vec_ctx *ctx, const char *path, int iprec, const char *history);
+/* Restart (nframe = 1, src/initial.F90:221-230): loads R..Bz, iteration,
+ * time and timestep (as dt1); the AB3 histories are not stored, so the next
+ * step is an Euler step, as in the reference. */
+int vec_read_restart(vec_ctx *ctx, const char *path);
+
 /* ---- allocation-free entry point ---------------------------------------- */
 /* No counterpart in the reference.  calcdt (src/utils.F90:144-244) for
  * callers that cannot allocate device memory: programs whose device memory

@@ -1,0 +1,130 @@
+"""Host-side logic of the library, run without a GPU: exported symbols, the
+INPUT parser (src/initial.F90:94-201) and the NetCDF snapshot codec
+(src/netcdf.F90 layout) against scipy's independent NetCDF reader."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fug30v0kxc_gb300 import lib
+from fug30v0kxc_gb300.params import ck_from_rayleigh
+from fug30v0kxc_gb300.solver import SNAP_ATTRS, SNAP_FIELDS, nc_read, nc_write, read_input
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_BIN = "/root/reference/VarElecCond/bin"
+
+
+def test_library_exports_every_header_symbol():
+    L = lib.load()
+    hdr = open(os.path.join(ROOT, "include", "vec.h")).read()
+    names = set(re.findall(r"^\s*(?:int|void|const char|long long)\s*\*?\s*(vec_\w+)\s*\(", hdr, re.M))
+    assert len(names) > 40
+    for n in sorted(names):
+        assert hasattr(L, n), n
+        assert n in lib.SIGNATURES, f"{n} has no ctypes signature"
+
+
+INPUT_TEXT = """data file for parallel magnetoconvection program
+
+{flag}\t     INPUT FLAG (1 for CK/F, 2 for Ra/Q)
+
+VALUE        VARIABLE
+1.4      GAMMA
+1.00          SIGMA
+9.0         THETA
+{ck}      CK (if FLAG=1) or Ra (if FLAG=2)
+1.0          CM
+{f}          F (if FLAG=1) or Q (if FLAG=2)
+0.0      TAYL (mid layer)
+1.570796327         PSI
+0.2          ZETA
+4.0          XMAX
+4.0          YMAX
+0.3          SF
+0            NFRAME
+1000       TOTAL
+100          NDU06
+1000        NDU16
+10            NDURESTART
+64\t     NX
+64\t     NY
+65\t     NZ
+"""
+
+
+def test_input_ra_q_conversion(tmp_path):
+    path = tmp_path / "INPUT"
+    path.write_text(INPUT_TEXT.format(flag=2, ck="100000", f="100.0"))
+    p = read_input(str(path))
+    ck = ck_from_rayleigh(1e5, 9.0, 1.0, 1.0, 1.4)
+    assert abs(p.ck - ck) < 1e-15 * ck
+    assert abs(p.f - 100.0 * 0.2 * ck * ck) < 1e-15
+    assert (p.nx, p.ny, p.nz, p.ntotal, p.ndu06) == (64, 64, 65, 1000, 100)
+    assert p.rayl == 1e5 and p.chand == 100.0
+
+
+def test_input_ck_f_and_errors(tmp_path):
+    path = tmp_path / "INPUT"
+    path.write_text(INPUT_TEXT.format(flag=1, ck="0.05d0", f="2.0"))
+    p = read_input(str(path))
+    assert p.ck == 0.05 and p.f == 2.0
+    assert abs(p.chand - 2.0 / (0.2 * 0.05 * 0.05)) < 1e-9
+    path.write_text(INPUT_TEXT.format(flag=3, ck="1", f="1"))
+    with pytest.raises(RuntimeError):
+        read_input(str(path))
+    with pytest.raises(RuntimeError):
+        read_input(str(tmp_path / "missing"))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference inputs not mounted")
+def test_reference_input_files():
+    for sub in ("INPUT", "originalINPUT", "test1/INPUT"):
+        p = read_input(os.path.join(REF_BIN, sub))
+        assert p.nx > 0 and p.ck > 0
+
+
+def _snapshot(nx=12, ny=10, nz=7, seed=0):
+    rng = np.random.default_rng(seed)
+    d = {n: rng.standard_normal((nz, ny, nx)) for n in SNAP_FIELDS}
+    d.update(time=13.875, iteration=105000, timestep=1.25e-4, version=3, history="test snapshot")
+    d.update({a: float(i) + 0.5 for i, a in enumerate(SNAP_ATTRS)})
+    return d
+
+
+@pytest.mark.parametrize("iprec", [4, 8])
+def test_snapshot_roundtrip_and_scipy(tmp_path, iprec):
+    snap = _snapshot()
+    path = tmp_path / "T16_001.nc"
+    nc_write(path, snap, iprec)
+    back = nc_read(path)
+    for n in SNAP_FIELDS:
+        ref = snap[n].astype(np.float32).astype(np.float64) if iprec == 4 else snap[n]
+        assert np.array_equal(back[n], ref), n
+    assert back["iteration"] == 105000 and back["time"] == 13.875 and back["timestep"] == 1.25e-4
+    # an independent reader sees the reference's layout
+    from scipy.io import netcdf_file
+    with netcdf_file(str(path), "r", mmap=False) as f:
+        assert f.dimensions == {"nx": 12, "ny": 10, "nz": 7, "one": 1}
+        assert f.variables["R"].shape == (7, 10, 12)
+        assert f.variables["R"].typecode() == ("d" if iprec == 8 else "f")
+        assert np.array_equal(np.asarray(f.variables["T"][:], dtype=np.float64), back["T"])
+        assert f.variables["time"].units == b"UNKNOWN"
+        assert int(f.variables["iteration"][0]) == 105000
+        assert f.version == 3
+        assert len(f.history) == 79
+        for i, a in enumerate(SNAP_ATTRS):
+            assert getattr(f, a) == float(i) + 0.5
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference inputs not mounted")
+def test_reads_reference_restart():
+    from scipy.io import netcdf_file
+    path = os.path.join(REF_BIN, "restart.nc")
+    d = nc_read(path)
+    with netcdf_file(path, "r", mmap=False) as f:
+        for n in SNAP_FIELDS:
+            assert np.array_equal(d[n], np.asarray(f.variables[n][:], dtype=np.float64)), n
+        assert d["iteration"] == int(f.variables["iteration"][0])
+        assert d["time"] == float(f.variables["time"][0])
+        assert d["ck"] == float(f.ck) and d["f"] == float(f.f)
