@@ -36,8 +36,9 @@ def build(force=False, verbose=False, extra=()):
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "vec.h"))
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
+    deps.append(os.path.join(HERE, "host", "p3d_gpu.c"))
+    if not force and os.path.exists(LIB) and os.path.exists(HOST):
+        t = min(os.path.getmtime(LIB), os.path.getmtime(HOST))
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
     objs = [os.path.join(OUT, os.path.splitext(os.path.basename(s))[0] + ".o") for s in srcs]
@@ -62,7 +63,25 @@ def build(force=False, verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(LIB + ".tmp", LIB)
+    build_host(verbose)
     return LIB
+
+
+HOST = os.path.join(OUT, "p3d_gpu")
+
+
+def build_host(verbose=False):
+    """The C host driver (src/main.F90 on the GPU library)."""
+    src = os.path.join(HERE, "host", "p3d_gpu.c")
+    cc = shutil.which("gcc") or "cc"
+    cmd = [cc, "-O2", "-std=gnu11", "-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include"), src,
+           "-o", HOST, "-L" + OUT, "-lvec_gpu", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host driver build failed:\n{r.stdout}\n{r.stderr}")
+    return HOST
 
 
 if __name__ == "__main__":
