@@ -329,9 +329,16 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     for (auto pp : st64) ALLOC(*pp, sizeof(double) * n);
     const size_t esz = E.split ? sizeof(float) : sizeof(double);
     for (int f = 0; f < 7; f++)
-        for (int s = 0; s < 3; s++) ALLOC(E.hist[f][s], esz * n);
+        for (int s = 0; s < 3; s++) ALLOC(E.hbuf[f][s], esz * n);
     ALLOC(E.bxbar, sizeof(double) * nz); ALLOC(E.bybar, sizeof(double) * nz);
-    for (int s = 0; s < 3; s++) { ALLOC(E.bxbardot[s], sizeof(double) * nz); ALLOC(E.bybardot[s], sizeof(double) * nz); }
+    for (int s = 0; s < 3; s++) { ALLOC(E.bxd_buf[s], sizeof(double) * nz); ALLOC(E.byd_buf[s], sizeof(double) * nz); }
+    {
+        HistTable h;
+        for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) h.p[f][s] = E.hbuf[f][s];
+        for (int s = 0; s < 3; s++) { h.bx[s] = E.bxd_buf[s]; h.by[s] = E.byd_buf[s]; }
+        ALLOC(E.ht, sizeof(HistTable));
+        CUDA_TRY(cudaMemcpy(E.ht, &h, sizeof(h), cudaMemcpyHostToDevice));
+    }
     ALLOC(E.w1d, sizeof(double) * 8 * nz);
     ALLOC(E.wblock, esz * n * W_COUNT);
     for (int i = 0; i < W_COUNT; i++) E.wk[i] = (char *)E.wblock + esz * n * (size_t)i;
@@ -358,13 +365,15 @@ extern "C" int vec_destroy(vec_ctx *c)
     if (!c) return VEC_OK;
     Engine &E = c->E;
     if (E.stream) cudaStreamSynchronize(E.stream);
+    E.drop_graphs();
     void *ptrs[] = { E.r, E.t, E.u, E.v, E.w, E.bx, E.by, E.bz, E.jsq, E.pol, E.tor, E.bxbar, E.bybar,
                      E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds, E.dev_err,
                      E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
                      E.rho0, E.t0, E.hres };
     for (void *q : ptrs) if (q) cudaFree(q);
-    for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hist[f][s]) cudaFree(E.hist[f][s]);
-    for (int s = 0; s < 3; s++) { if (E.bxbardot[s]) cudaFree(E.bxbardot[s]); if (E.bybardot[s]) cudaFree(E.bybardot[s]); }
+    for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hbuf[f][s]) cudaFree(E.hbuf[f][s]);
+    for (int s = 0; s < 3; s++) { if (E.bxd_buf[s]) cudaFree(E.bxd_buf[s]); if (E.byd_buf[s]) cudaFree(E.byd_buf[s]); }
+    if (E.ht) cudaFree(E.ht);
     if (E.wblock) cudaFree(E.wblock);
     for (int i = 0; i < 6; i++) if (E.s64[i]) cudaFree(E.s64[i]);
     if (E.tx64.tw) line_tables_free(&E.tx64);
@@ -466,10 +475,12 @@ extern "C" int vec_set_field(vec_ctx *c, int field, const double *src)
     }
     int f, s;
     if (hist_index(field, &f, &s)) return VEC_ERR_ARG;
-    if (!E.split) return stage_in(E, (double *)E.hist[f][s], src, E.n) ? VEC_ERR_CUDA : vec_sync(c);
-    int st = stage_in(E, E.s64[0], src, E.n);
+    HistTable h;
+    int st = hist_table_host(&E, &h);
     if (st) return st;
-    k_d2f<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>(E.s64[0], (float *)E.hist[f][s], E.n);
+    if (!E.split) return stage_in(E, (double *)h.p[f][s], src, E.n) ? VEC_ERR_CUDA : vec_sync(c);
+    if ((st = stage_in(E, E.s64[0], src, E.n))) return st;
+    k_d2f<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>(E.s64[0], (float *)h.p[f][s], E.n);
     return vec_sync(c);
 }
 
@@ -485,8 +496,11 @@ extern "C" int vec_get_field(vec_ctx *c, int field, double *dst)
     }
     int f, s;
     if (hist_index(field, &f, &s)) return VEC_ERR_ARG;
-    if (!E.split) return stage_out(E, dst, (const double *)E.hist[f][s], E.n);
-    k_f2d<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>((const float *)E.hist[f][s], E.s64[0], E.n);
+    HistTable h;
+    int st = hist_table_host(&E, &h);
+    if (st) return st;
+    if (!E.split) return stage_out(E, dst, (const double *)h.p[f][s], E.n);
+    k_f2d<<<(unsigned)((E.n + 255) / 256), 256, 0, E.stream>>>((const float *)h.p[f][s], E.s64[0], E.n);
     return stage_out(E, dst, E.s64[0], E.n);
 }
 
@@ -497,8 +511,12 @@ static double *mean_ptr(Engine &E, int m)
     case VEC_M_KAPPA: return E.kappa; case VEC_M_DKAPPA: return E.dkappa;
     case VEC_M_ETA: return E.eta; case VEC_M_DETA: return E.deta;
     }
-    if (m >= VEC_M_BXBARDOT && m < VEC_M_BXBARDOT + 3) return E.bxbardot[m - VEC_M_BXBARDOT];
-    if (m >= VEC_M_BYBARDOT && m < VEC_M_BYBARDOT + 3) return E.bybardot[m - VEC_M_BYBARDOT];
+    if ((m >= VEC_M_BXBARDOT && m < VEC_M_BXBARDOT + 3) || (m >= VEC_M_BYBARDOT && m < VEC_M_BYBARDOT + 3)) {
+        HistTable h;
+        if (hist_table_host(&E, &h)) return nullptr;
+        if (m < VEC_M_BYBARDOT) return h.bx[m - VEC_M_BXBARDOT];
+        return h.by[m - VEC_M_BYBARDOT];
+    }
     return nullptr;
 }
 
@@ -525,6 +543,7 @@ extern "C" int vec_set_bzbar(vec_ctx *c, double b)
     int st;
     if (c->E.split && (st = split_sync_b64(&c->E))) return st;
     c->E.bzbar = b;
+    c->E.drop_graphs();
     if (c->E.split && (st = split_refresh(&c->E))) return st;
     return vec_sync(c);
 }
@@ -583,6 +602,7 @@ extern "C" int vec_mag_init(vec_ctx *c)
     if (!c) return VEC_ERR_ARG;
     int st;
     if (c->E.split && (st = split_sync_b64(&c->E))) return st;
+    c->E.drop_graphs();
     st = phys_mag_init(&c->E);
     if (st) return st;
     if (c->E.split && (st = split_refresh(&c->E))) return st;
@@ -744,13 +764,18 @@ extern "C" int vec_diag(vec_ctx *c, vec_diag_out *out)
     return st ? st : s2;
 }
 
-// one iteration of src/main.F90:340-747 (printing and snapshots excluded)
-static int one_step(Engine &E)
+void Engine::drop_graphs()
+{
+    for (int v = 0; v < 2; v++)
+        if (gexec[v]) { cudaGraphExecDestroy(gexec[v]); gexec[v] = nullptr; }
+}
+
+// device work of one iteration of src/main.F90:340-747 (printing and
+// snapshots excluded); host counters are advanced by the caller
+static int enqueue_step(Engine &E, bool diag_now)
 {
     int st;
     const int mag = mag_on(E);
-    E.nit += 1;
-    E.iter += 1;
     if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
     if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
     else st = phys_zero_mag_rhs(&E);
@@ -762,10 +787,59 @@ static int one_step(Engine &E)
     if (mag && (st = E.split ? split_bandj(&E) : phys_bandj64(&E))) return st;
     if ((st = boundary_step(E))) return st;
     if (mag && (st = mag_boundary_step(E))) return st;
-    const bool diag_now = E.p.diag_cadence && E.p.ndu06 > 0 && (E.nit % E.p.ndu06 == 0);
     if (diag_now && (st = diag_step(E, nullptr))) return st;
     if (E.nit % 10 == 0 && (st = E.split ? split_calcdt(&E) : phys_calcdt(&E))) return st;
     return VEC_OK;
+}
+
+static bool diag_due(const Engine &E, int nit)
+{
+    return E.p.diag_cadence && E.p.ndu06 > 0 && (nit % E.p.ndu06 == 0);
+}
+
+// Captures the device work of the next step into graph variant v (or
+// replays it).  Returns VEC_OK with *done = 0 when the step must run
+// eagerly (diagnostics, profiling, graphs disabled).
+static int graph_step(Engine &E, int *done)
+{
+    *done = 0;
+    const int nit = E.nit + 1;
+    if (!E.use_graphs || E.prof_on || diag_due(E, nit)) return VEC_OK;
+    const int v = (nit % 10 == 0) ? 1 : 0;
+    if (!E.gexec[v]) {
+        E.nit = nit;
+        E.iter += 1;
+        cudaGraph_t g = nullptr;
+        const long long l0 = E.launches;
+        CUDA_TRY(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+        int st = enqueue_step(E, false);
+        cudaError_t ce = cudaStreamEndCapture(E.stream, &g);
+        if (st) { if (g) cudaGraphDestroy(g); return st; }
+        if (ce != cudaSuccess) { vec_set_error("step capture failed: %s", cudaGetErrorString(ce)); return VEC_ERR_CUDA; }
+        ce = cudaGraphInstantiate(&E.gexec[v], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { vec_set_error("graph instantiate failed: %s", cudaGetErrorString(ce)); return VEC_ERR_CUDA; }
+        E.g_b32_after[v] = E.b32_auth;
+        E.g_launches[v] = E.launches - l0;
+    } else {
+        E.nit = nit;
+        E.iter += 1;
+        E.b32_auth = E.g_b32_after[v];
+        E.launches += E.g_launches[v];
+    }
+    CUDA_TRY(cudaGraphLaunch(E.gexec[v], E.stream));
+    *done = 1;
+    return VEC_OK;
+}
+
+static int one_step(Engine &E)
+{
+    int done = 0;
+    int st = graph_step(E, &done);
+    if (st || done) return st;
+    E.nit += 1;
+    E.iter += 1;
+    return enqueue_step(E, diag_due(E, E.nit));
 }
 
 extern "C" int vec_step(vec_ctx *c, int nsteps)
@@ -868,3 +942,16 @@ extern "C" int vec_read_restart(vec_ctx *c, const char *path)
     sc.second = 0;
     return vec_set_scalars(c, &sc);
 }
+
+extern "C" int vec_use_graphs(vec_ctx *c, int on)
+{
+    if (!c) return VEC_ERR_ARG;
+    c->E.use_graphs = on != 0;
+    if (!on) c->E.drop_graphs();
+    return VEC_OK;
+}
+
+int engine_enqueue_step(Engine &E, bool diag_now) { return enqueue_step(E, diag_now); }
+int engine_one_step(Engine &E) { return one_step(E); }
+bool engine_diag_due(const Engine &E, int nit) { return diag_due(E, nit); }
+Engine &engine_of(vec_ctx *c) { return c->E; }

@@ -82,6 +82,15 @@ struct DevScalars {
     double res[64];                            // diagnostics results
 };
 
+// RHS histories in logical slot order (0 oldest .. 2 newest), kept in device
+// memory so that kernels read their slot pointers at run time and a one-
+// thread kernel performs the shift of src/main.F90:448-461 by rotating it;
+// kernel arguments are then the same on every step (graph capture).
+struct HistTable {
+    void *p[7][3];          // r, t, u, v, w, pol, tor
+    double *bx[3], *by[3];  // bxbardot, bybardot
+};
+
 // ---- error helper --------------------------------------------------------
 void vec_set_error(const char *fmt, ...);
 

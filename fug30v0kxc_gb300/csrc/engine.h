@@ -51,10 +51,12 @@ struct Engine {
     // FP64 state (src/arrays.f90)
     double *r = nullptr, *t = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
     double *bx = nullptr, *by = nullptr, *bz = nullptr, *jsq = nullptr, *pol = nullptr, *tor = nullptr;
-    // RHS histories [field][slot]: r,t,u,v,w,pol,tor; slot 2 = newest
-    void *hist[7][3] = {};
+    // RHS history buffers (physical; their logical order lives in ht)
+    void *hbuf[7][3] = {};
+    double *bxd_buf[3] = {}, *byd_buf[3] = {};
+    HistTable *ht = nullptr;    // device table of logical slots
     // 1-D
-    double *bxbar = nullptr, *bybar = nullptr, *bxbardot[3] = {}, *bybardot[3] = {};
+    double *bxbar = nullptr, *bybar = nullptr;
     double *kappa = nullptr, *dkappa = nullptr, *eta = nullptr, *deta = nullptr;
     double *akx1 = nullptr, *akx2 = nullptr, *aky1 = nullptr, *aky2 = nullptr;
     double *w1d = nullptr;      // 1-D scratch (8 nz)
@@ -80,6 +82,16 @@ struct Engine {
     vec_diag_out last_diag;
     int have_diag = 0;
 
+    // CUDA graphs of one time step: [0] plain step, [1] step with dealias and
+    // calcdt (nit % 10 == 0); diagnostic steps run without a graph
+    int use_graphs = 1;
+    cudaGraphExec_t gexec[2] = { nullptr, nullptr };
+    int g_b32_after[2] = { 0, 0 };
+    long long g_launches[2] = { 0, 0 };
+    // tunables (the ensemble autotuner sets them per grid)
+    int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
+    int ct_s = 0;               // sequences per line tile (0: default for the size)
+
     // profiling
     bool prof_on = false;
     std::vector<ProfRec> prof;
@@ -96,6 +108,7 @@ struct Engine {
     double *W64(int i) const { return split ? reinterpret_cast<double *>(wblock) + (size_t)i * n : (double *)wk[i]; }
 
     void prof_begin(const char *name, double bytes = 0.0);
+    void drop_graphs();
     void prof_end();
     int prof_flush();
 };
@@ -104,7 +117,7 @@ template <> inline const LineTables<double> &Engine::tables<double>(int dir) con
 template <> inline const LineTables<float> &Engine::tables<float>(int dir) const { return dir == 0 ? tx32 : ty32; }
 
 // lines.cu
-int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl);
+int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl, int force_p = 0);
 template <typename R> int line_tables_make(int n, const double *k1, const double *k2, int icut, LineTables<R> *tb);
 template <typename R> void line_tables_free(LineTables<R> *tb);
 template <typename R> int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
@@ -136,13 +149,19 @@ int phys_boundary(Engine *E);
 int phys_mag_boundary(Engine *E);
 int phys_ab3(Engine *E, int magdealias);
 int phys_ab3_coef(Engine *E);
-void phys_rotate_hist(Engine *E);
+int phys_rotate_hist(Engine *E);
+int hist_table_host(Engine *E, HistTable *h);   // synchronous copy of the table
 int phys_dealias_state(Engine *E);
 int phys_calcdt(Engine *E);
 int phys_diag(Engine *E, vec_diag_out *out);
 int phys_mag_init(Engine *E);
 int phys_static(Engine *E);
 int phys_step_prologue(Engine *E);
+// capi.cu (used by the ensemble)
+int engine_enqueue_step(Engine &E, bool diag_now);
+int engine_one_step(Engine &E);
+bool engine_diag_due(const Engine &E, int nit);
+Engine &engine_of(vec_ctx *c);
 // split form (split.cu)
 int split_setup(Engine *E);
 int split_hydro(Engine *E);

@@ -1,0 +1,293 @@
+// ensemble.cu -- many independent instances (uneven grids and parameters)
+// stepped together as one captured CUDA graph.
+//
+// Every member is a full context (its own arrays and stream).  One ensemble
+// step is captured once per step variant (plain, or the tenth step with
+// dealias and calcdt): the root stream forks to every member stream through
+// an event, each member enqueues its own time step, and the root joins them
+// again, so the graph holds one independent branch per member and the GPU
+// runs small members concurrently.  Steps with diagnostics (a host read-back)
+// run without the graph.
+//
+// The autotuner picks, per distinct grid, the planes per thread of the
+// z-marching hydro kernel and the sequences per tile of the line kernels by
+// timing a scratch context of that grid; results can be cached in a text
+// file (one line per grid: nx ny nz precision kc s).
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+
+struct vec_ens {
+    std::vector<vec_ctx *> m;
+    cudaStream_t root = nullptr;
+    cudaEvent_t ev_root = nullptr;
+    std::vector<cudaEvent_t> ev;
+    cudaGraphExec_t g[2] = { nullptr, nullptr };
+    std::vector<int> b32_after[2];
+    std::vector<long long> launches[2];
+};
+
+static void drop(vec_ens *e)
+{
+    for (int v = 0; v < 2; v++)
+        if (e->g[v]) { cudaGraphExecDestroy(e->g[v]); e->g[v] = nullptr; }
+}
+
+extern "C" int vec_ensemble_destroy(vec_ens *e)
+{
+    if (!e) return VEC_OK;
+    if (e->root) cudaStreamSynchronize(e->root);
+    drop(e);
+    for (auto c : e->m) vec_destroy(c);
+    for (auto ev : e->ev) cudaEventDestroy(ev);
+    if (e->ev_root) cudaEventDestroy(e->ev_root);
+    if (e->root) cudaStreamDestroy(e->root);
+    delete e;
+    return VEC_OK;
+}
+
+extern "C" int vec_ensemble_create(const vec_params *ps, int n, vec_ens **out)
+{
+    if (!ps || n <= 0 || !out) return VEC_ERR_ARG;
+    *out = nullptr;
+    vec_ens *e = new vec_ens();
+    for (int i = 0; i < n; i++) {
+        vec_ctx *c = nullptr;
+        int st = vec_create(&ps[i], &c);
+        if (st) { vec_ensemble_destroy(e); return st; }
+        e->m.push_back(c);
+        cudaEvent_t ev;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { vec_ensemble_destroy(e); return VEC_ERR_CUDA; }
+        e->ev.push_back(ev);
+    }
+    if (cudaStreamCreateWithFlags(&e->root, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ev_root, cudaEventDisableTiming) != cudaSuccess) {
+        vec_ensemble_destroy(e);
+        return VEC_ERR_CUDA;
+    }
+    for (int v = 0; v < 2; v++) { e->b32_after[v].assign(n, 0); e->launches[v].assign(n, 0); }
+    *out = e;
+    return VEC_OK;
+}
+
+extern "C" int vec_ensemble_size(vec_ens *e) { return e ? (int)e->m.size() : 0; }
+
+extern "C" vec_ctx *vec_ensemble_member(vec_ens *e, int i)
+{
+    if (!e || i < 0 || i >= (int)e->m.size()) return nullptr;
+    return e->m[i];
+}
+
+// static state, calcdt and mag_init of every member (src/main.F90:275-333)
+extern "C" int vec_ensemble_start(vec_ens *e)
+{
+    if (!e) return VEC_ERR_ARG;
+    drop(e);
+    for (auto c : e->m) {
+        int st;
+        if ((st = vec_static(c))) return st;
+        if ((st = vec_calcdt(c, nullptr))) return st;
+        Engine &E = engine_of(c);
+        if ((E.p.f != 0.0 || E.p.kinematic) && (st = vec_mag_init(c))) return st;
+    }
+    return VEC_OK;
+}
+
+// Work on the member streams must follow the graph replays queued on the
+// root stream, and later replays must follow it: join in both directions.
+static int root_to_members(vec_ens *e)
+{
+    CUDA_TRY(cudaEventRecord(e->ev_root, e->root));
+    for (auto c : e->m) CUDA_TRY(cudaStreamWaitEvent(engine_of(c).stream, e->ev_root, 0));
+    return VEC_OK;
+}
+
+static int members_to_root(vec_ens *e)
+{
+    for (size_t i = 0; i < e->m.size(); i++) {
+        CUDA_TRY(cudaEventRecord(e->ev[i], engine_of(e->m[i]).stream));
+        CUDA_TRY(cudaStreamWaitEvent(e->root, e->ev[i], 0));
+    }
+    return VEC_OK;
+}
+
+static int ens_eager_step(vec_ens *e)
+{
+    int st = root_to_members(e);
+    if (st) return st;
+    for (auto c : e->m) {
+        if ((st = engine_one_step(engine_of(c)))) return st;
+    }
+    return members_to_root(e);
+}
+
+extern "C" int vec_ensemble_step(vec_ens *e, int nsteps)
+{
+    if (!e || nsteps < 0) return VEC_ERR_ARG;
+    const int nm = (int)e->m.size();
+    int st0 = members_to_root(e);
+    if (st0) return st0;
+    for (int s = 0; s < nsteps; s++) {
+        // all members advance together, so they share nit
+        const int nit = engine_of(e->m[0]).nit + 1;
+        bool eager = false;
+        for (auto c : e->m) {
+            Engine &E = engine_of(c);
+            if (E.nit + 1 != nit || engine_diag_due(E, nit) || E.prof_on || !E.use_graphs) eager = true;
+        }
+        if (eager) {
+            int st = ens_eager_step(e);
+            if (st) return st;
+            continue;
+        }
+        const int v = nit % 10 == 0 ? 1 : 0;
+        if (!e->g[v]) {
+            CUDA_TRY(cudaStreamBeginCapture(e->root, cudaStreamCaptureModeThreadLocal));
+            int st = VEC_OK;
+            if (cudaEventRecord(e->ev_root, e->root) != cudaSuccess) st = VEC_ERR_CUDA;
+            for (int i = 0; i < nm && !st; i++) {
+                Engine &E = engine_of(e->m[i]);
+                if (cudaStreamWaitEvent(E.stream, e->ev_root, 0) != cudaSuccess) { st = VEC_ERR_CUDA; break; }
+                E.nit += 1;
+                E.iter += 1;
+                const long long l0 = E.launches;
+                st = engine_enqueue_step(E, false);
+                e->b32_after[v][i] = E.b32_auth;
+                e->launches[v][i] = E.launches - l0;
+                if (!st && cudaEventRecord(e->ev[i], E.stream) != cudaSuccess) st = VEC_ERR_CUDA;
+                if (!st && cudaStreamWaitEvent(e->root, e->ev[i], 0) != cudaSuccess) st = VEC_ERR_CUDA;
+            }
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(e->root, &g);
+            if (st) { if (g) cudaGraphDestroy(g); return st; }
+            if (ce != cudaSuccess) { vec_set_error("ensemble capture failed: %s", cudaGetErrorString(ce)); return VEC_ERR_CUDA; }
+            ce = cudaGraphInstantiate(&e->g[v], g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) { vec_set_error("ensemble instantiate failed: %s", cudaGetErrorString(ce)); return VEC_ERR_CUDA; }
+        } else {
+            for (int i = 0; i < nm; i++) {
+                Engine &E = engine_of(e->m[i]);
+                E.nit += 1;
+                E.iter += 1;
+                E.b32_auth = e->b32_after[v][i];
+                E.launches += e->launches[v][i];
+            }
+        }
+        CUDA_TRY(cudaGraphLaunch(e->g[v], e->root));
+    }
+    // whatever the caller does next on a member's stream follows the steps
+    return root_to_members(e);
+}
+
+extern "C" int vec_ensemble_sync(vec_ens *e)
+{
+    if (!e) return VEC_ERR_ARG;
+    CUDA_TRY(cudaStreamSynchronize(e->root));
+    for (auto c : e->m) {
+        int st = vec_sync(c);
+        if (st) return st;
+    }
+    return VEC_OK;
+}
+
+// ---- autotuner -------------------------------------------------------------------
+struct TuneKey { int nx, ny, nz, prec; };
+
+static bool same(const TuneKey &a, const TuneKey &b)
+{
+    return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.prec == b.prec;
+}
+
+static int time_config(const vec_params &p, int kc, int s, int steps, float *ms)
+{
+    vec_ctx *c = nullptr;
+    int st = vec_create(&p, &c);
+    if (st) return st;
+    Engine &E = engine_of(c);
+    E.kc_pass2 = kc;
+    E.ct_s = s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if ((st = vec_static(c)) || (st = vec_calcdt(c, nullptr))) goto out;
+    if ((p.f != 0.0 || p.kinematic) && (st = vec_mag_init(c))) goto out;
+    if ((st = vec_step(c, 2)) || (st = vec_sync(c))) goto out;   // warm-up and graph capture
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, E.stream);
+    if ((st = vec_step(c, steps))) goto out;
+    cudaEventRecord(b, E.stream);
+    if ((st = vec_sync(c))) goto out;
+    cudaEventElapsedTime(ms, a, b);
+out:
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    vec_destroy(c);
+    return st;
+}
+
+// Picks kc (z-marching chunk) and s (sequences per line tile) per distinct
+// grid of the ensemble; cache: optional text file read first and rewritten.
+extern "C" int vec_ensemble_tune(vec_ens *e, int steps, const char *cache)
+{
+    if (!e || steps <= 0) return VEC_ERR_ARG;
+    struct Entry { TuneKey k; int kc, s; };
+    std::vector<Entry> tab;
+    if (cache) {
+        FILE *fp = fopen(cache, "r");
+        if (fp) {
+            Entry t;
+            while (fscanf(fp, "%d %d %d %d %d %d", &t.k.nx, &t.k.ny, &t.k.nz, &t.k.prec, &t.kc, &t.s) == 6)
+                tab.push_back(t);
+            fclose(fp);
+        }
+    }
+    for (auto c : e->m) {
+        Engine &E = engine_of(c);
+        TuneKey k = { E.nx, E.ny, E.nz, E.p.precision };
+        const Entry *hit = nullptr;
+        for (auto &t : tab) if (same(t.k, k)) { hit = &t; break; }
+        if (!hit) {
+            const int kcs[3] = { 8, 16, 32 };
+            // sequences per tile: the CT kernel's default or 8; the generic
+            // kernel's default or 4 / 8
+            const bool pow2 = (E.nx & (E.nx - 1)) == 0 && (E.ny & (E.ny - 1)) == 0;
+            std::vector<int> ss = pow2 ? std::vector<int>{ 0, 8 } : std::vector<int>{ 0, 4, 8 };
+            Entry best = { k, 16, 0 };
+            float best_ms = 1e30f;
+            for (int kc : kcs)
+                for (int s : ss) {
+                    float ms = 0.0f;
+                    int st = time_config(E.p, kc, s, steps, &ms);
+                    if (st) return st;
+                    if (ms < best_ms) { best_ms = ms; best.kc = kc; best.s = s; }
+                }
+            tab.push_back(best);
+            hit = &tab.back();
+        }
+        E.kc_pass2 = hit->kc;
+        E.ct_s = hit->s;
+        E.drop_graphs();
+    }
+    drop(e);
+    if (cache) {
+        FILE *fp = fopen(cache, "w");
+        if (fp) {
+            for (auto &t : tab) fprintf(fp, "%d %d %d %d %d %d\n", t.k.nx, t.k.ny, t.k.nz, t.k.prec, t.kc, t.s);
+            fclose(fp);
+        }
+    }
+    return VEC_OK;
+}
+
+extern "C" int vec_tunables(vec_ctx *c, int *kc, int *s)
+{
+    if (!c) return VEC_ERR_ARG;
+    Engine &E = engine_of(c);
+    if (kc) *kc = E.kc_pass2;
+    if (s) *s = E.ct_s;
+    return VEC_OK;
+}

@@ -327,7 +327,7 @@ static void sincos2pi_host(long e, long n, double *c, double *s)
     }
 }
 
-int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl)
+int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl, int force_p)
 {
     memset(pl, 0, sizeof(*pl));
     pl->n = n;
@@ -343,6 +343,7 @@ int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl)
     int P = 2048 / n;
     if (P < 1) P = 1;
     if (P > 16) P = 16;
+    if (force_p > 0) P = force_p;
     if (P > lines / 2) P = lines / 2;
     if (P < 1) P = 1;
     pl->P = P;
@@ -411,7 +412,12 @@ int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
         if (h == 1) return VEC_OK;
         if (h < 0) return h;
     }
-    const LinePlan &pl = dir == 0 ? E->plx : E->ply;
+    LinePlan pl = dir == 0 ? E->plx : E->ply;
+    if (E->ct_s > 0 && E->ct_s != pl.P) {
+        // autotuned sequences per CTA for the generic kernel
+        LinePlan alt;
+        if (line_plan_make(pl.n, pl.lines, sizeof(R), &alt, E->ct_s) == VEC_OK) pl = alt;
+    }
     const LineTables<R> &tb = E->tables<R>(dir);
     for (int j0 = 0; j0 < njobs; j0 += MAX_JOBS) {
         JobPack<R> pk;

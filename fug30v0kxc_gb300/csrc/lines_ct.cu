@@ -471,6 +471,7 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
     case 1024: S = F ? 4 : 2; break;
     default: return 0;
     }
+    if (F && n <= 256 && E->ct_s == 8) S = 8;   // autotuned alternative
     if (L % (2 * S) != 0) return 0;
     if ((E->nx * (int)sizeof(R)) % 16 != 0) return 0;
     for (int j = 0; j < njobs; j++) {
@@ -486,6 +487,7 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
     if (n == NN && S == SS) st = dir == 0 ? run_ct<R, 0, A, B, SS>(E, jb, nj, name) : run_ct<R, 1, A, B, SS>(E, jb, nj, name);
         if constexpr (F) {
             CT_CASE(64, 8, 8, 16) CT_CASE(128, 16, 8, 16) CT_CASE(256, 16, 16, 16)
+            CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
             CT_CASE(512, 32, 16, 8) CT_CASE(1024, 32, 32, 4)
         } else {
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)

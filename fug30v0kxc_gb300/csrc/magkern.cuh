@@ -20,10 +20,11 @@ static __global__ void k_emf(const R *u, const R *v, const R *w, const R *bx, co
 // mean-field RHS (:328-352) on one CTA; ex, ey are the 2-D spectra of the EMF
 template <typename R>
 static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar, const double *bybar,
-                                  const double *eta, const double *deta, double *bxd, double *byd,
+                                  const double *eta, const double *deta, const HistTable *ht,
                                   double *scratch, size_t np, int nz, double xn, double zck, double ho12,
                                   double sc1, int var_eta)
 {
+    double *bxd = ht->bx[2], *byd = ht->by[2];
     double *e1 = scratch, *e2 = scratch + nz;
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
         e1[k] = xn * (double)ex[(size_t)k * np];
@@ -66,7 +67,7 @@ template <typename R>
 struct MagArgs {
     const R *ex, *ey, *ez, *w1, *pol, *tor;
     const double *eta, *deta, *akx1, *aky1, *akx2, *aky2;
-    R *poldot, *tordot;
+    const HistTable *ht;    // poldot / tordot = newest slots
     double zck, ho12, sc1;
     int var_eta, nx, ny, nz;
 };
@@ -90,16 +91,17 @@ static __global__ void k_mag_final(MagArgs<R> a)
     else { w2 = w2 / kk; w3 = w3 / kk; }
     const R d2p = zd2(a.pol + q, np, k, a.nz, 3, (R)a.sc1);
     const R d2t = zd2(a.tor + q, np, k, a.nz, 3, (R)a.sc1);
+    R *poldot = (R *)a.ht->p[5][2], *tordot = (R *)a.ht->p[6][2];
     if (!a.var_eta) {
         const R zck = (R)a.zck;
-        a.poldot[idx] = zck * a.pol[idx] * kk + zck * d2p + w2;
-        a.tordot[idx] = zck * a.tor[idx] * kk + zck * d2t - w3 + a.ez[idx];
+        poldot[idx] = zck * a.pol[idx] * kk + zck * d2p + w2;
+        tordot[idx] = zck * a.tor[idx] * kk + zck * d2t - w3 + a.ez[idx];
     } else {
         // extension: eta(z) replaces zeta*ck, tordot gains eta'(z) d(tor)/dz
         const R e = (R)a.eta[k];
         const R dt = zd1(a.tor + q, np, k, a.nz, 5, (R)a.ho12);
-        a.poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
-        a.tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + (R)a.deta[k] * dt;
+        poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
+        tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + (R)a.deta[k] * dt;
     }
 }
 
@@ -178,4 +180,29 @@ static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, in
         a[idx] = (R)0;
         if (b) b[idx] = (R)0;
     }
+}
+
+// zero the newest magnetic RHS slots (F = 0, src/main.F90:355-376)
+template <typename R>
+static __global__ void k_zero_mag_rhs(const HistTable *ht, size_t n, int nz)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { ((R *)ht->p[5][2])[i] = (R)0; ((R *)ht->p[6][2])[i] = (R)0; }
+    if (i < (size_t)nz) { ht->bx[2][i] = 0.0; ht->by[2][i] = 0.0; }
+}
+
+// the history shift of src/main.F90:448-461 and :473-476 as a rotation of
+// the logical slots: 0 <- 1 <- 2 <- old 0 (reused for the next RHS)
+static __global__ void k_rotate_hist(HistTable *ht)
+{
+    if (threadIdx.x != 0) return;
+    for (int f = 0; f < 7; f++) {
+        void *o = ht->p[f][0];
+        ht->p[f][0] = ht->p[f][1];
+        ht->p[f][1] = ht->p[f][2];
+        ht->p[f][2] = o;
+    }
+    double *x = ht->bx[0], *y = ht->by[0];
+    ht->bx[0] = ht->bx[1]; ht->bx[1] = ht->bx[2]; ht->bx[2] = x;
+    ht->by[0] = ht->by[1]; ht->by[1] = ht->by[2]; ht->by[2] = y;
 }

@@ -100,7 +100,8 @@ struct HydroArgs {
     const double *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
     const double *ry, *ty, *tyy, *uy, *uyy, *vy, *vyy, *wy, *wyy;
     const double *kappa, *dkappa, *eta;
-    double *racc, *tdot, *uacc, *vacc, *wacc;
+    const HistTable *ht;    // tdot = newest slot of t
+    double *racc, *uacc, *vacc, *wacc;
     double *p1, *p2, *q, *g, *hh, *p3, *p4;
     double gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, zck, ho12, sc1;
     int var_eta;
@@ -156,7 +157,7 @@ __global__ void k_hydro_pass2(HydroArgs a)
     td = td + a.sckg * (uy + vx) * (uy + vx);
     td = td + a.sckg * (wx + uzu) * (wx + uzu);
     td = td + a.sckg * (wy + vzu) * (wy + vzu);
-    a.tdot[idx] = td * (1.0 / rr);
+    ((double *)a.ht->p[1][2])[idx] = td * (1.0 / rr);
 
     // momentum: :103-105, :159-161, :213-214, :253-254, :292-306, :363-364, :393-395, :424-426
     double ud = -tt * rx - rr * tx;
@@ -189,7 +190,7 @@ __global__ void k_hydro_pass2(HydroArgs a)
 
 struct Hydro4Args {
     const double *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
-    double *rdot, *udot, *vdot, *wdot;
+    const HistTable *ht;    // rdot, udot, vdot, wdot = newest slots
     double ho12;
     size_t np;
     int nz;
@@ -218,12 +219,12 @@ __global__ void k_hydro_pass4(Hydro4Args a)
         rzu = zd1up(a.r + q, np, k, nz, 0, h, w0);
         rz = zd1(a.r + q, np, k, nz, 0, h);
     }
-    a.rdot[idx] = a.racc[idx] - w0 * rzu;
+    ((double *)a.ht->p[0][2])[idx] = a.racc[idx] - w0 * rzu;
     wd = wd - tt * rz;
     const double ri = 1.0 / rr;
-    a.udot[idx] = ud * ri;
-    a.vdot[idx] = vd * ri;
-    a.wdot[idx] = wd * ri;
+    ((double *)a.ht->p[2][2])[idx] = ud * ri;
+    ((double *)a.ht->p[3][2])[idx] = vd * ri;
+    ((double *)a.ht->p[4][2])[idx] = wd * ri;
 }
 
 int phys_hydro64(Engine *E)
@@ -258,7 +259,7 @@ int phys_hydro64(Engine *E)
     a.ry = W[W_RY]; a.ty = W[W_TY]; a.tyy = W[W_TYY]; a.uy = W[W_UY]; a.uyy = W[W_UYY];
     a.vy = W[W_VY]; a.vyy = W[W_VYY]; a.wy = W[W_WY]; a.wyy = W[W_WYY];
     a.kappa = E->kappa; a.dkappa = E->dkappa; a.eta = E->eta;
-    a.racc = W[W_RACC]; a.tdot = (double *)E->hist[1][2];
+    a.racc = W[W_RACC]; a.ht = E->ht;
     a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
     a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H];
     a.p3 = W[W_P3]; a.p4 = W[W_P4];
@@ -287,8 +288,7 @@ int phys_hydro64(Engine *E)
     Hydro4Args b;
     b.r = E->r; b.t = E->t; b.w = E->w; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
     b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC];
-    b.rdot = (double *)E->hist[0][2]; b.udot = (double *)E->hist[2][2];
-    b.vdot = (double *)E->hist[3][2]; b.wdot = (double *)E->hist[4][2];
+    b.ht = E->ht;
     b.ho12 = c.ho12; b.np = E->np; b.nz = E->nz;
     KLAUNCHB(E, "hydro_pass4_f64", FB(E, 15, 8), k_hydro_pass4, nblk(E->n), TPB, b);
     return VEC_OK;
@@ -312,12 +312,12 @@ int phys_mag64(Engine *E)
     if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
     const Consts &c = E->k;
     KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
-            E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
+            E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
     KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
     MagArgs<double> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol; a.tor = E->tor;
     a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
-    a.poldot = (double *)E->hist[5][2]; a.tordot = (double *)E->hist[6][2];
+    a.ht = E->ht;
     a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
     KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final<double>, nblk(E->n), TPB, a);
@@ -326,11 +326,11 @@ int phys_mag64(Engine *E)
 
 int phys_zero_mag_rhs(Engine *E)
 {
-    size_t esz = E->split ? sizeof(float) : sizeof(double);
-    CUDA_TRY(cudaMemsetAsync(E->hist[5][2], 0, esz * E->n, E->stream));
-    CUDA_TRY(cudaMemsetAsync(E->hist[6][2], 0, esz * E->n, E->stream));
-    CUDA_TRY(cudaMemsetAsync(E->bxbardot[2], 0, sizeof(double) * E->nz, E->stream));
-    CUDA_TRY(cudaMemsetAsync(E->bybardot[2], 0, sizeof(double) * E->nz, E->stream));
+    size_t cnt = E->n > (size_t)E->nz ? E->n : (size_t)E->nz;
+    if (E->split)
+        KLAUNCH(E, "zero_mag_rhs", k_zero_mag_rhs<float>, nblk(cnt), TPB, E->ht, E->n, E->nz);
+    else
+        KLAUNCH(E, "zero_mag_rhs", k_zero_mag_rhs<double>, nblk(cnt), TPB, E->ht, E->n, E->nz);
     return VEC_OK;
 }
 
@@ -459,10 +459,10 @@ int phys_mag_boundary(Engine *E)
 // ============================================================================
 // coefficients (:381-403), dt1/dt2 (:488-489), ttime (:345) and the 1-D mean
 // update (:469-476) on one CTA
-__global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const double *bxd0, const double *bxd1,
-                           const double *bxd2, const double *byd0, const double *byd1, const double *byd2, int nz,
-                           int do_means)
+__global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const HistTable *ht, int nz, int do_means)
 {
+    const double *bxd0 = ht->bx[0], *bxd1 = ht->bx[1], *bxd2 = ht->bx[2];
+    const double *byd0 = ht->by[0], *byd1 = ht->by[1], *byd2 = ht->by[2];
     __shared__ double cc[3];
     if (threadIdx.x == 0) {
         double dt = ds->dt, c0, c1, c2;
@@ -498,8 +498,8 @@ __global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const d
 
 struct Ab3Args {
     double *x[7];
-    const double *h0[7], *h1[7], *h2[7];
-    double *r0, *r1;             // rdot slots 1 and 2 (zeroed at floored points)
+    int hmap[7];                 // history table row of each state field
+    const HistTable *ht;
     const DevScalars *ds;
     int nx, ny, nz, cx, cy, magdealias;
 };
@@ -512,14 +512,15 @@ __global__ void k_ab3_update(Ab3Args a)
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * a.nz) return;
     const double c0 = a.ds->c0, c1 = a.ds->c1, c2 = a.ds->c2;
+#define H(f, s) ((const double *)a.ht->p[a.hmap[f]][s])
 #pragma unroll
     for (int f = 0; f < 5; f++)
-        a.x[f][idx] = a.x[f][idx] + c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx];
+        a.x[f][idx] = a.x[f][idx] + c0 * H(f, 2)[idx] + c1 * H(f, 1)[idx] + c2 * H(f, 0)[idx];
     // order of the reference: u,v,w,r,t then pol,tor; density floor after all
     if (a.x[3][idx] < 0.05) {
         a.x[3][idx] = 0.05;
-        a.r0[idx] = 0.0;
-        a.r1[idx] = 0.0;
+        ((double *)a.ht->p[0][1])[idx] = 0.0;   // become slots 1 and 2 after the shift
+        ((double *)a.ht->p[0][2])[idx] = 0.0;
     }
     bool trunc = false;
     if (a.magdealias) {
@@ -529,28 +530,28 @@ __global__ void k_ab3_update(Ab3Args a)
     }
 #pragma unroll
     for (int f = 5; f < 7; f++) {
-        double xn = a.x[f][idx] + c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx];
+        double xn = a.x[f][idx] + c0 * H(f, 2)[idx] + c1 * H(f, 1)[idx] + c2 * H(f, 0)[idx];
         a.x[f][idx] = trunc ? 0.0 : xn;
     }
+#undef H
 }
 
-void phys_rotate_hist(Engine *E)
+int phys_rotate_hist(Engine *E)
 {
-    for (int f = 0; f < 7; f++) {
-        void *old0 = E->hist[f][0];
-        E->hist[f][0] = E->hist[f][1];
-        E->hist[f][1] = E->hist[f][2];
-        E->hist[f][2] = old0;
-    }
-    double *bx0 = E->bxbardot[0], *by0 = E->bybardot[0];
-    E->bxbardot[0] = E->bxbardot[1]; E->bxbardot[1] = E->bxbardot[2]; E->bxbardot[2] = bx0;
-    E->bybardot[0] = E->bybardot[1]; E->bybardot[1] = E->bybardot[2]; E->bybardot[2] = by0;
+    KLAUNCH(E, "rotate_hist", k_rotate_hist, 1, 32, E->ht);
+    return VEC_OK;
+}
+
+int hist_table_host(Engine *E, HistTable *h)
+{
+    CUDA_TRY(cudaMemcpyAsync(h, E->ht, sizeof(HistTable), cudaMemcpyDeviceToHost, E->stream));
+    CUDA_TRY(cudaStreamSynchronize(E->stream));
+    return VEC_OK;
 }
 
 int phys_ab3_coef(Engine *E)
 {
-    KLAUNCH(E, "ab3_coef", k_ab3_coef, 1, 256, E->ds, E->bxbar, E->bybar, E->bxbardot[0], E->bxbardot[1],
-            E->bxbardot[2], E->bybardot[0], E->bybardot[1], E->bybardot[2], E->nz, 1);
+    KLAUNCH(E, "ab3_coef", k_ab3_coef, 1, 256, E->ds, E->bxbar, E->bybar, E->ht, E->nz, 1);
     return VEC_OK;
 }
 
@@ -564,18 +565,14 @@ int phys_ab3(Engine *E, int magdealias)
     const int hmap[7] = { 2, 3, 4, 0, 1, 5, 6 };
     for (int f = 0; f < 7; f++) {
         a.x[f] = xs[f];
-        a.h0[f] = (const double *)E->hist[hmap[f]][0];
-        a.h1[f] = (const double *)E->hist[hmap[f]][1];
-        a.h2[f] = (const double *)E->hist[hmap[f]][2];
+        a.hmap[f] = hmap[f];
     }
-    a.r0 = (double *)E->hist[0][1];   // become slots 1 and 2 after rotation
-    a.r1 = (double *)E->hist[0][2];
+    a.ht = E->ht;
     a.ds = E->ds;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
     KLAUNCHB(E, "ab3_update_f64", FB(E, 35, 8), k_ab3_update, nblk(E->n), TPB, a);
-    phys_rotate_hist(E);
-    return VEC_OK;
+    return phys_rotate_hist(E);
 }
 
 // dealias(r,t,u,v,w): src/main.F90:495-502 -> src/fft.F90:586-682

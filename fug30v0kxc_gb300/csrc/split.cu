@@ -193,7 +193,8 @@ struct SplitHydroArgs {
     const float *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
     const float *ry, *ty, *tyy, *uy, *uyy, *vy, *vyy, *wy, *wyy;
     const double *kappa, *dkappa, *eta, *bg;
-    float *racc, *tdot, *uacc, *vacc, *wacc;
+    const HistTable *ht;    // tdot = newest slot of t
+    float *racc, *uacc, *vacc, *wacc;
     float *p1, *p2, *q, *g, *hh, *p3, *p4;
     float gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, ho12, sc1, bzbar;
     double zck;
@@ -242,7 +243,7 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     td = td + a.sckg * (uy + vx) * (uy + vx);
     td = td + a.sckg * (wx + uzu) * (wx + uzu);
     td = td + a.sckg * (wy + vzu) * (wy + vzu);
-    a.tdot[idx] = td / rr;
+    ((float *)a.ht->p[1][2])[idx] = td / rr;
 
     float ud = -tt * rx - rr * tx;
     ud = ud - rr * u0 * ux - rr * v0 * uy - rr * w0 * uzu;
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
 struct SplitHydro4Args {
     const float *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
     const double *bg;
-    float *rdot, *udot, *vdot, *wdot;
+    const HistTable *ht;    // rdot, udot, vdot, wdot = newest slots
     float ho12;
     size_t np;
     int nz;
@@ -365,10 +366,10 @@ __global__ void k_split_pass4(SplitHydro4Args a)
                - tp * (float)bg[BG_RHO0Z0 * nz + k] - tp * rzp;
     }
     const float ri = 1.0f / rr;
-    a.rdot[idx] = rdot;
-    a.udot[idx] = ud * ri;
-    a.vdot[idx] = vd * ri;
-    a.wdot[idx] = wfin * ri;
+    ((float *)a.ht->p[0][2])[idx] = rdot;
+    ((float *)a.ht->p[2][2])[idx] = ud * ri;
+    ((float *)a.ht->p[3][2])[idx] = vd * ri;
+    ((float *)a.ht->p[4][2])[idx] = wfin * ri;
 }
 
 int split_hydro(Engine *E)
@@ -402,7 +403,7 @@ int split_hydro(Engine *E)
     a.ry = W[W_RY]; a.ty = W[W_TY]; a.tyy = W[W_TYY]; a.uy = W[W_UY]; a.uyy = W[W_UYY];
     a.vy = W[W_VY]; a.vyy = W[W_VYY]; a.wy = W[W_WY]; a.wyy = W[W_WYY];
     a.kappa = E->kappa; a.dkappa = E->dkappa; a.eta = E->eta; a.bg = E->hres;
-    a.racc = W[W_RACC]; a.tdot = (float *)E->hist[1][2];
+    a.racc = W[W_RACC]; a.ht = E->ht;
     a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
     a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H]; a.p3 = W[W_P3]; a.p4 = W[W_P4];
     a.gck = (float)c.gck; a.fzckg = (float)c.fzckg; a.gm1 = (float)c.gm1; a.sckg = (float)c.sckg;
@@ -410,7 +411,7 @@ int split_hydro(Engine *E)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar; a.zck = c.zck;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
-    const int kc = 16;
+    const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
     dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
     KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
 
@@ -430,8 +431,7 @@ int split_hydro(Engine *E)
     SplitHydro4Args b;
     b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
     b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres;
-    b.rdot = (float *)E->hist[0][2]; b.udot = (float *)E->hist[2][2];
-    b.vdot = (float *)E->hist[3][2]; b.wdot = (float *)E->hist[4][2];
+    b.ht = E->ht;
     b.ho12 = (float)c.ho12; b.np = E->np; b.nz = E->nz;
     KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4, nblk(E->n), TPB, b);
     return VEC_OK;
@@ -453,13 +453,13 @@ int split_mag(Engine *E)
     if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
     const Consts &c = E->k;
     KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
-             E->bxbardot[2], E->bybardot[2], E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
+             E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
     KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx,
              E->ny, E->nz, E->akx1, E->aky1);
     MagArgs<float> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol32; a.tor = E->tor32;
     a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
-    a.poldot = (float *)E->hist[5][2]; a.tordot = (float *)E->hist[6][2];
+    a.ht = E->ht;
     a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
     KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, nblk(E->n), TPB, a);
@@ -508,9 +508,9 @@ int split_bandj(Engine *E)
 // ---- AB3 update in FP64 with FP32 histories ------------------------------------------
 struct SplitAb3Args {
     double *x[7];
-    const float *h0[7], *h1[7], *h2[7];
+    int hmap[7];           // history table row of each state field
+    const HistTable *ht;
     float *m[7];           // mirrors, same order
-    float *r0, *r1;        // rdot slots zeroed at floored points
     const double *bg;
     const DevScalars *ds;
     int nx, ny, nz, cx, cy, magdealias;
@@ -524,14 +524,15 @@ __global__ void k_split_ab3(SplitAb3Args a)
     if (idx >= np * a.nz) return;
     const int k = (int)(idx / np);
     const float c0 = (float)a.ds->c0, c1 = (float)a.ds->c1, c2 = (float)a.ds->c2;
+#define H(f, s) ((const float *)a.ht->p[a.hmap[f]][s])
     double xs[7];
 #pragma unroll
     for (int f = 0; f < 5; f++)
-        xs[f] = a.x[f][idx] + (double)(c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx]);
+        xs[f] = a.x[f][idx] + (double)(c0 * H(f, 2)[idx] + c1 * H(f, 1)[idx] + c2 * H(f, 0)[idx]);
     if (xs[3] < 0.05) {
         xs[3] = 0.05;
-        a.r0[idx] = 0.0f;
-        a.r1[idx] = 0.0f;
+        ((float *)a.ht->p[0][1])[idx] = 0.0f;
+        ((float *)a.ht->p[0][2])[idx] = 0.0f;
     }
     bool trunc = false;
     if (a.magdealias) {
@@ -541,9 +542,10 @@ __global__ void k_split_ab3(SplitAb3Args a)
     }
 #pragma unroll
     for (int f = 5; f < 7; f++) {
-        double v = a.x[f][idx] + (double)(c0 * a.h2[f][idx] + c1 * a.h1[f][idx] + c2 * a.h0[f][idx]);
+        double v = a.x[f][idx] + (double)(c0 * H(f, 2)[idx] + c1 * H(f, 1)[idx] + c2 * H(f, 0)[idx]);
         xs[f] = trunc ? 0.0 : v;
     }
+#undef H
 #pragma unroll
     for (int f = 0; f < 7; f++) a.x[f][idx] = xs[f];
     a.m[0][idx] = (float)xs[0];
@@ -571,9 +573,10 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
     for (int f = 0; f < 7; f++) {
         const double2 s01 = *reinterpret_cast<const double2 *>(a.x[f] + i4);
         const double2 s23 = *reinterpret_cast<const double2 *>(a.x[f] + i4 + 2);
-        const float4 h2 = *reinterpret_cast<const float4 *>(a.h2[f] + i4);
-        const float4 h1 = *reinterpret_cast<const float4 *>(a.h1[f] + i4);
-        const float4 h0 = *reinterpret_cast<const float4 *>(a.h0[f] + i4);
+        const float *const *hp = (const float *const *)a.ht->p[a.hmap[f]];
+        const float4 h2 = *reinterpret_cast<const float4 *>(hp[2] + i4);
+        const float4 h1 = *reinterpret_cast<const float4 *>(hp[1] + i4);
+        const float4 h0 = *reinterpret_cast<const float4 *>(hp[0] + i4);
         xs[f][0] = s01.x + (double)(c0 * h2.x + c1 * h1.x + c2 * h0.x);
         xs[f][1] = s01.y + (double)(c0 * h2.y + c1 * h1.y + c2 * h0.y);
         xs[f][2] = s23.x + (double)(c0 * h2.z + c1 * h1.z + c2 * h0.z);
@@ -583,9 +586,10 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
     const bool fl0 = xs[3][0] < 0.05, fl1 = xs[3][1] < 0.05, fl2 = xs[3][2] < 0.05, fl3 = xs[3][3] < 0.05;
     if (fl0 | fl1 | fl2 | fl3) {
         const bool fl[4] = { fl0, fl1, fl2, fl3 };
+        float *r1 = (float *)a.ht->p[0][1], *r2 = (float *)a.ht->p[0][2];
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if (fl[q]) { xs[3][q] = 0.05; a.r0[i4 + q] = 0.0f; a.r1[i4 + q] = 0.0f; }
+            if (fl[q]) { xs[3][q] = 0.05; r1[i4 + q] = 0.0f; r2[i4 + q] = 0.0f; }
     }
     if (a.magdealias) {
         const size_t qq = i4 - (size_t)k * np;
@@ -616,12 +620,9 @@ int split_ab3(Engine *E, int magdealias)
     for (int f = 0; f < 7; f++) {
         a.x[f] = xs[f];
         a.m[f] = ms[f];
-        a.h0[f] = (const float *)E->hist[hmap[f]][0];
-        a.h1[f] = (const float *)E->hist[hmap[f]][1];
-        a.h2[f] = (const float *)E->hist[hmap[f]][2];
+        a.hmap[f] = hmap[f];
     }
-    a.r0 = (float *)E->hist[0][1];
-    a.r1 = (float *)E->hist[0][2];
+    a.ht = E->ht;
     a.bg = E->hres;
     a.ds = E->ds;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
@@ -632,8 +633,7 @@ int split_ab3(Engine *E, int magdealias)
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4, nblk(E->n / 4), TPB, a);
     else
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3, nblk(E->n), TPB, a);
-    phys_rotate_hist(E);
-    return VEC_OK;
+    return phys_rotate_hist(E);
 }
 
 // ---- dealias of r,t,u,v,w (every 10 steps) -----------------------------------------

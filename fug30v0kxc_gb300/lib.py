@@ -61,6 +61,16 @@ SIGNATURES = {
                                   C.POINTER(C.c_double)]),
     "vec_profile_reset": (C.c_int, [_vp]),
     "vec_launch_count": (C.c_longlong, [_vp]),
+    "vec_use_graphs": (C.c_int, [_vp, C.c_int]),
+    "vec_ensemble_create": (C.c_int, [C.POINTER(VecParams), C.c_int, C.POINTER(_vp)]),
+    "vec_ensemble_destroy": (C.c_int, [_vp]),
+    "vec_ensemble_size": (C.c_int, [_vp]),
+    "vec_ensemble_member": (_vp, [_vp, C.c_int]),
+    "vec_ensemble_start": (C.c_int, [_vp]),
+    "vec_ensemble_step": (C.c_int, [_vp, C.c_int]),
+    "vec_ensemble_sync": (C.c_int, [_vp]),
+    "vec_ensemble_tune": (C.c_int, [_vp, C.c_int, C.c_char_p]),
+    "vec_tunables": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "vec_nc_write": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int]),
     "vec_nc_read": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot)]),
     "vec_write_snapshot": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_char_p]),

@@ -34,20 +34,23 @@ def _ptr(a):
 class P3D:
     """One device-resident VarElecCond context (src/arrays.f90 in HBM)."""
 
-    def __init__(self, params: VecParams):
+    def __init__(self, params: VecParams, handle=None):
         self.L = _L.load()
         self.p = params.copy()
-        h = C.c_void_p()
-        st = self.L.vec_create(C.byref(self.p), C.byref(h))
-        if st != 0:
-            raise VecError("vec_create", st)
-        self.h = h
+        self.owned = handle is None
+        if handle is None:
+            h = C.c_void_p()
+            st = self.L.vec_create(C.byref(self.p), C.byref(h))
+            if st != 0:
+                raise VecError("vec_create", st)
+            handle = h
+        self.h = handle
         self.shape = (self.p.nz, self.p.ny, self.p.nx)
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "owned", True):
             self.L.vec_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -216,6 +219,14 @@ class P3D:
     def launch_count(self):
         return self.L.vec_launch_count(self.h)
 
+    def use_graphs(self, on=True):
+        self._chk(self.L.vec_use_graphs(self.h, 1 if on else 0), "use_graphs")
+
+    def tunables(self):
+        kc, s = C.c_int(), C.c_int()
+        self._chk(self.L.vec_tunables(self.h, C.byref(kc), C.byref(s)), "tunables")
+        return kc.value, s.value
+
     # -- snapshots (src/netcdf.F90) -------------------------------------------------
     def write_snapshot(self, path, iprec=8, history=""):
         self._chk(self.L.vec_write_snapshot(self.h, str(path).encode(), iprec, history.encode()),
@@ -277,3 +288,47 @@ def nc_write(path, snap, iprec=8):
     st = L.vec_nc_write(str(path).encode(), C.byref(s), iprec)
     if st != 0:
         raise VecError("vec_nc_write", st)
+
+
+class Ensemble:
+    """Independent instances stepped together as one captured CUDA graph."""
+
+    def __init__(self, params_list):
+        self.L = _L.load()
+        arr = (VecParams * len(params_list))(*[p.copy() for p in params_list])
+        h = C.c_void_p()
+        st = self.L.vec_ensemble_create(arr, len(params_list), C.byref(h))
+        if st != 0:
+            raise VecError("vec_ensemble_create", st)
+        self.h = h
+        self.members = [P3D(params_list[i], handle=C.c_void_p(self.L.vec_ensemble_member(h, i)))
+                        for i in range(len(params_list))]
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.L.vec_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st, where):
+        if st != 0:
+            raise VecError(where, st)
+
+    def start(self):
+        self._chk(self.L.vec_ensemble_start(self.h), "ensemble_start")
+
+    def step(self, n=1):
+        return self.L.vec_ensemble_step(self.h, n)
+
+    def sync(self):
+        self._chk(self.L.vec_ensemble_sync(self.h), "ensemble_sync")
+
+    def tune(self, steps=3, cache=None):
+        self._chk(self.L.vec_ensemble_tune(self.h, steps, cache.encode() if cache else None), "ensemble_tune")

@@ -185,6 +185,10 @@ int vec_diag(vec_ctx *ctx, vec_diag_out *out);
  * diagnostics every ndu06 steps, calcdt every 10, dealias every 10.
  * Returns VEC_ERR_DIVB / VEC_ERR_NAN if a check fails. */
 int vec_step(vec_ctx *ctx, int nsteps);
+/* Steps without diagnostics run as replays of a captured CUDA graph of one
+ * step (two variants: plain, and the tenth step with dealias and calcdt);
+ * on by default, off while profiling.  on = 0 launches every kernel. */
+int vec_use_graphs(vec_ctx *ctx, int on);
 /* last diagnostics computed inside vec_step (valid after an ndu06 step) */
 int vec_last_diag(vec_ctx *ctx, vec_diag_out *out);
 
@@ -229,6 +233,27 @@ int vec_read_restart(vec_ctx *ctx, const char *path);
 int vec_calcdt_noalloc(const vec_params *p, const double *u, const double *v, const double *w,
                        const double *r, const double *t, const double *bx, const double *by,
                        const double *bz, double *dt_out, void *stream);
+
+/* ---- batched ensemble (independent instances, uneven grids) ------------- */
+typedef struct vec_ens vec_ens;
+/* n members with their own parameters (grids and physics may differ) */
+int vec_ensemble_create(const vec_params *ps, int n, vec_ens **ens);
+int vec_ensemble_destroy(vec_ens *ens);
+int vec_ensemble_size(vec_ens *ens);
+vec_ctx *vec_ensemble_member(vec_ens *ens, int i);
+/* static state, calcdt and mag_init of every member */
+int vec_ensemble_start(vec_ens *ens);
+/* nsteps time steps of every member; steps without diagnostics replay one
+ * captured CUDA graph holding an independent branch per member */
+int vec_ensemble_step(vec_ens *ens, int nsteps);
+int vec_ensemble_sync(vec_ens *ens);
+/* autotuner: per distinct grid, time candidate tile shapes (z-marching
+ * chunk, sequences per FFT tile) on a scratch context for `steps` steps and
+ * apply the fastest; `cache` (may be NULL) is a text file read first and
+ * rewritten with the results */
+int vec_ensemble_tune(vec_ens *ens, int steps, const char *cache);
+/* the tile shapes in use by a context */
+int vec_tunables(vec_ctx *ctx, int *kc, int *s);
 
 /* ---- instrumentation --------------------------------------------------- */
 /* When on, every kernel launch of the context is bracketed by CUDA events
