@@ -29,6 +29,7 @@ sys.path.insert(0, ROOT)
 NX, NY, NZ = 256, 256, 129
 WORKLOAD = "VarElecCond 256x256x129 Ra1e5 Q100 eta-contrast-20"
 METRIC = "grid-point-steps/s at 256^2x129"
+LARGE = {"on": False}
 
 
 def peaks():
@@ -102,8 +103,8 @@ def dist_env():
 
 
 def make_params(precision):
-    from fug30v0kxc_gb300.params import config1
-    p = config1(precision=precision)
+    from fug30v0kxc_gb300.params import config1, config4
+    p = (config4 if LARGE["on"] else config1)(precision=precision)
     p.nx, p.ny, p.nz = NX, NY, NZ
     p.ndu06 = 1000000          # diagnostics printing cadence of bin/INPUT is 5000 steps
     return p
@@ -170,6 +171,59 @@ def time_e2e(g, args):
     dt = reduce_max(dt * 1e3) / 1e3
     nbytes = sum(host[n].nbytes for n in names)
     return dt, nbytes, C.sizeof(VecScalars)
+
+
+def time_ensemble(args):
+    """The 48-member ensemble (16 x 64^2x65, 16 x 128^2x97, 16 x 192^2x129,
+    split form) stepped as one captured graph after the autotuner picked the
+    tile shapes per grid.  Aggregate grid-point-steps/s over all members."""
+    import torch
+    from fug30v0kxc_gb300.params import config2_members
+    from fug30v0kxc_gb300.solver import Ensemble
+    ps = config2_members()
+    npts = sum(p.nx * p.ny * p.nz for p in ps)
+    ens = Ensemble(ps)
+    ens.start()
+    t0 = time.perf_counter()
+    ens.tune(steps=3)
+    tune_s = time.perf_counter() - t0
+    assert ens.step(args.warmup) == 0
+    ens.sync()
+    m0 = ens.members[0]
+    stream = torch.cuda.ExternalStream(m0.stream())
+    launches0 = sum(m.launch_count() for m in ens.members)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    # the ensemble step joins every member stream into its root stream
+    # first and forks back at the end, so events on member 0's stream
+    # bracket all members' work
+    ev0.record(stream)
+    st = ens.step(args.steps)
+    ev1.record(stream)
+    ens.sync()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    assert st == 0, f"ensemble step failed: {st}"
+    ms = reduce_max(ev0.elapsed_time(ev1))
+    launches = sum(m.launch_count() for m in ens.members) - launches0
+    tun = sorted({(m.p.nx, m.p.nz) + tuple(m.tunables()) for m in ens.members})
+    ens.close()
+    return npts, ms, launches, clocks, tune_s, tun
+
+
+def ensemble_line(args, ws, hbm, pk):
+    npts, ms, launches, clocks, tune_s, tun = time_ensemble(args)
+    value = npts * args.steps * ws / (ms * 1e-3)
+    alg = 196
+    return {"value": value, "unit": "grid-point-steps/s", "ms_per_step": ms / args.steps,
+            "members": 48, "points": npts, "gpu_launches": launches, "clocks": clocks,
+            "step_roofline": {"alg_bytes_per_gps": alg, "achieved_gbs": round(value / ws * alg / 1e9, 1),
+                              "peak": hbm, "frac": round(value / ws * alg / 1e9 / hbm, 4), "peak_kind": pk},
+            "autotune_s": round(tune_s, 2),
+            "tunables": [{"n": t[0], "nz": t[1], "kc": t[2], "s": t[3]} for t in tun]}
 
 
 def cpu_baseline(nsteps, precision_note=""):
@@ -282,6 +336,7 @@ def measure(args, precision, ws, hbm, pk, with_e2e):
 
 
 def main():
+    global NX, NY, NZ, WORKLOAD, METRIC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -291,13 +346,26 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", default=None, help="NX,NY,NZ (smaller cases for ncu captures)")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large"],
+                    help="ensemble: the 48-member batched ensemble as the headline line; "
+                         "large: one 1024^2x513 instance, Ra 1e7, Q 1e4, eta contrast 50 (split)")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the host-buffer measurement (very large grids)")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the ensemble sub-measurement of the single-instance line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.grid:
-        global NX, NY, NZ, WORKLOAD
         NX, NY, NZ = (int(x) for x in args.grid.split(","))
         WORKLOAD = f"VarElecCond {NX}x{NY}x{NZ} Ra1e5 Q100 eta-contrast-20"
+        METRIC = f"grid-point-steps/s at {NX}x{NY}x{NZ}"
 
+    if args.workload == "large":
+        LARGE["on"] = True
+        NX, NY, NZ = 1024, 1024, 513
+        WORKLOAD = "VarElecCond 1024x1024x513 Ra1e7 Q1e4 eta-contrast-50 theta19"
+        METRIC = "grid-point-steps/s at 1024^2x513"
+        args.precision, args.no_e2e, args.no_ensemble, args.no_cpu = "split", True, True, True
     ws, rank, local = dist_env()
     if ws > 1:
         import torch
@@ -318,8 +386,29 @@ def main():
     torch.cuda.set_device(local)
     from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
     hbm, pk = peaks()
+    if args.workload == "ensemble":
+        e = ensemble_line(args, ws, hbm, pk)
+        line = {"metric": "aggregate grid-point-steps/s, 48-instance ensemble", "value": e["value"],
+                "unit": e["unit"], "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": e["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32/f64",
+                "data": "synthetic (seeded static polytropes + uniform +-1e-3 T noise)",
+                "config": {"workload": "ensemble 16x64^2x65 + 16x128^2x97 + 16x192^2x129, Ra log-uniform "
+                                       "[1e4,1e6], Q {0,100,1000}, eta contrast {1,5,20}, split",
+                           "parallelism": f"replicas{ws}", "l2": "no flush: resident state ~100 GB"},
+                "roofline": {"bound": "hbm", "achieved": e["step_roofline"]["achieved_gbs"], "peak": hbm,
+                             "unit": "GB/s", "frac": e["step_roofline"]["frac"], "traffic": None,
+                             "basis": "196 B/gps compulsory state traffic of the whole step"},
+                "clocks": e["clocks"], "gpu_launches": e["gpu_launches"], "ensemble": e}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if _dist["on"]:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     head_prec = VEC_PREC_FP64 if args.precision == "fp64" else VEC_PREC_SPLIT
-    head = measure(args, head_prec, ws, hbm, pk, with_e2e=True)
+    head = measure(args, head_prec, ws, hbm, pk, with_e2e=not args.no_e2e)
     line = {
         "metric": METRIC, "value": head["value"], "unit": "grid-point-steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
@@ -333,7 +422,7 @@ def main():
         "roofline": head["roofline"],
         "step_roofline": head["step_roofline"],
         "clocks": head["clocks"],
-        "e2e": head["e2e"],
+        "e2e": head.get("e2e"),
         "gpu_launches": head["launches"],
         "kernels": head["kernels"],
     }
@@ -343,6 +432,11 @@ def main():
                         "roofline": f64["roofline"], "step_roofline": f64["step_roofline"],
                         "clocks": f64["clocks"], "gpu_launches": f64["launches"]}
         line["split_over_fp64"] = head["value"] / f64["value"]
+    if not args.no_ensemble and not args.grid:
+        try:
+            line["ensemble"] = ensemble_line(args, ws, hbm, pk)
+        except Exception as ex:  # reported, never hides the headline
+            line["ensemble"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0 and not args.no_cpu:
         v, cores, dt = cpu_baseline(args.cpu_steps)
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",

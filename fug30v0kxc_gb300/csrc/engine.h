@@ -117,6 +117,8 @@ template <> inline const LineTables<double> &Engine::tables<double>(int dir) con
 template <> inline const LineTables<float> &Engine::tables<float>(int dir) const { return dir == 0 ? tx32 : ty32; }
 
 // lines.cu
+// exp(-2 pi i e/n) on the host in double, exact at multiples of n/4
+void sincos2pi_host(long e, long n, double *c, double *s);
 int line_plan_make(int n, int lines, int elem_bytes, LinePlan *pl, int force_p = 0);
 template <typename R> int line_tables_make(int n, const double *k1, const double *k2, int icut, LineTables<R> *tb);
 template <typename R> void line_tables_free(LineTables<R> *tb);

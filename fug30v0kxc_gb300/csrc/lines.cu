@@ -311,7 +311,7 @@ line_kernel(JobPack<R> jobs, LinePlan pl, LineTables<R> tb, int nx, int ny, int 
 // ---- host side ------------------------------------------------------------------
 // Twiddles exp(-2 pi i e/n) computed on the host in double, exact at
 // multiples of n/4 (quadrant reduction of the angle).
-static void sincos2pi_host(long e, long n, double *c, double *s)
+void sincos2pi_host(long e, long n, double *c, double *s)
 {
     e %= n;
     if (e < 0) e += n;

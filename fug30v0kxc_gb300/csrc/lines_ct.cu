@@ -1,5 +1,5 @@
-// lines_ct.cu -- horizontal spectral operators (src/fft.F90) for power-of-two
-// line lengths n = N1*N2 (64..1024), the hot path of the time step.
+// lines_ct.cu -- horizontal spectral operators (src/fft.F90) for line
+// lengths n = N1*N2 = 2^a or 3*2^a (64..1024), the hot path of the time step.
 //
 // Per tile a CTA owns 2S real lines of one z-plane (S complex sequences
 // z = a + ib).  The tile is brought into shared memory by TMA bulk copies
@@ -31,13 +31,22 @@ template <typename R> struct JobPackCT { LineJob<R> j[MAX_JOBS]; };
 // one TMA descriptor per job input (y lines: 3-D view nx x ny x nz)
 struct TmapPack { CUtensorMap m[MAX_JOBS]; };
 
-// W_32^q = exp(-2 pi i q/32), q = 0..31 (the in-register radix kernels)
+// W_32^q = exp(-2 pi i q/32), q = 0..31, and W_96^q (the in-register radix
+// kernels; radix-3 factors take their twiddles from the second table)
 __constant__ float2 c_tw32f[32];
 __constant__ double2 c_tw32d[32];
+__constant__ float2 c_tw96f[96];
+__constant__ double2 c_tw96d[96];
 
 template <typename C> __device__ __forceinline__ C tw32(int q);
 template <> __device__ __forceinline__ float2 tw32<float2>(int q) { return c_tw32f[q]; }
 template <> __device__ __forceinline__ double2 tw32<double2>(int q) { return c_tw32d[q]; }
+template <typename C> __device__ __forceinline__ C tw96(int q);
+template <> __device__ __forceinline__ float2 tw96<float2>(int q) { return c_tw96f[q]; }
+template <> __device__ __forceinline__ double2 tw96<double2>(int q) { return c_tw96d[q]; }
+
+// x mod N for x >= 0 (N a compile-time constant)
+template <int N> __device__ __forceinline__ int modn(int x) { return (N & (N - 1)) == 0 ? (x & (N - 1)) : x % N; }
 
 template <typename C>
 __device__ __forceinline__ C cmul_(C a, C b) { C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
@@ -52,14 +61,26 @@ __device__ __forceinline__ C rot_(C a) { C r; if (INV) { r.x = -a.y; r.y = a.x; 
 template <int N, bool INV, typename C>
 __device__ __forceinline__ C twc(C a, int e)
 {
-    const int q = (e * (32 / N)) & 31;
-    if (q == 0) return a;
-    if (q == 8) return rot_<INV>(a);                           // -i (fwd)
-    if (q == 16) { C r; r.x = -a.x; r.y = -a.y; return r; }
-    if (q == 24) return rot_<!INV>(a);                         // +i (fwd)
-    C w = tw32<C>(q);
-    if (INV) w.y = -w.y;
-    return cmul_(a, w);
+    if constexpr (32 % N == 0) {
+        const int q = (e * (32 / N)) & 31;
+        if (q == 0) return a;
+        if (q == 8) return rot_<INV>(a);                           // -i (fwd)
+        if (q == 16) { C r; r.x = -a.x; r.y = -a.y; return r; }
+        if (q == 24) return rot_<!INV>(a);                         // +i (fwd)
+        C w = tw32<C>(q);
+        if (INV) w.y = -w.y;
+        return cmul_(a, w);
+    } else {
+        static_assert(96 % N == 0, "radix kernels cover divisors of 32 and 96");
+        const int q = (e * (96 / N)) % 96;
+        if (q == 0) return a;
+        if (q == 24) return rot_<INV>(a);
+        if (q == 48) { C r; r.x = -a.x; r.y = -a.y; return r; }
+        if (q == 72) return rot_<!INV>(a);
+        C w = tw96<C>(q);
+        if (INV) w.y = -w.y;
+        return cmul_(a, w);
+    }
 }
 
 // in-register natural-order DFT of N points
@@ -67,6 +88,20 @@ template <int N, bool INV> struct RDft;
 template <bool INV> struct RDft<1, INV> { template <typename C> static __device__ __forceinline__ void run(C *) {} };
 template <bool INV> struct RDft<2, INV> {
     template <typename C> static __device__ __forceinline__ void run(C *v) { C a = v[0], b = v[1]; v[0] = cadd_(a, b); v[1] = csub_(a, b); }
+};
+// X1,2 = a - (b+c)/2 -+ i (sqrt(3)/2)(b-c) (forward; conjugate for INV)
+template <bool INV> struct RDft<3, INV> {
+    template <typename C> static __device__ __forceinline__ void run(C *v) {
+        using R = decltype(v[0].x);
+        const R h = (R)0.8660254037844386;
+        C t1 = cadd_(v[1], v[2]), d = csub_(v[1], v[2]);
+        C t2; t2.x = v[0].x - (R)0.5 * t1.x; t2.y = v[0].y - (R)0.5 * t1.y;
+        C r = rot_<INV>(d);
+        r.x *= h; r.y *= h;
+        v[0] = cadd_(v[0], t1);
+        v[1] = cadd_(t2, r);
+        v[2] = csub_(t2, r);
+    }
 };
 template <bool INV> struct RDft<4, INV> {
     template <typename C> static __device__ __forceinline__ void run(C *v) {
@@ -103,6 +138,9 @@ __device__ __forceinline__ void reg_ct(C *v)
 template <bool INV> struct RDft<8, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<2, 4, INV>(v); } };
 template <bool INV> struct RDft<16, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<4, 4, INV>(v); } };
 template <bool INV> struct RDft<32, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<8, 4, INV>(v); } };
+template <bool INV> struct RDft<6, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<3, 2, INV>(v); } };
+template <bool INV> struct RDft<12, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<4, 3, INV>(v); } };
+template <bool INV> struct RDft<24, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<8, 3, INV>(v); } };
 
 // ---- TMA / mbarrier helpers ------------------------------------------------------
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -139,6 +177,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
     }
     return false;
 }
+
+// rows per TMA box of a y tile: TMA boxes are at most 256 rows, and the box
+// must divide the line length
+__host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 
 // ---- the kernel --------------------------------------------------------------------
 // DIR 0: x lines (a tile = 2S contiguous rows), DIR 1: y lines (a tile = 2S
@@ -190,7 +232,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             }
         } else if (tid == 0) {
             // boxes of 2S columns x (up to 256) rows of this plane
-            constexpr int BR = N < 256 ? N : 256;
+            constexpr int BR = ybox_rows(N);
             mbar_expect_tx(b, TILE * (unsigned)sizeof(R));
 #pragma unroll
             for (int c = 0; c < N / BR; c++)
@@ -239,7 +281,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 RDft<N1, false>::run(a);
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
-                    C w = tws[(lane * k1) & (N - 1)];
+                    C w = tws[modn<N>(lane * k1)];
                     ex_s[k1 * LX + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
                 }
             }
@@ -313,7 +355,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 RDft<N2, true>::run(Y);
 #pragma unroll
                 for (int m2 = 0; m2 < N2; m2++) {
-                    C w = tws[(m2 * lane) & (N - 1)];
+                    C w = tws[modn<N>(m2 * lane)];
                     w.y = -w.y;
                     ex_s[m2 * LX + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
                 }
@@ -366,6 +408,16 @@ int line_ct_configure()
     }
     CUDA_TRY(cudaMemcpyToSymbol(c_tw32f, tf, sizeof(tf)));
     CUDA_TRY(cudaMemcpyToSymbol(c_tw32d, td, sizeof(td)));
+    float2 uf[96];
+    double2 ud[96];
+    for (int q = 0; q < 96; q++) {
+        double c, s;
+        sincos2pi_host(q, 96, &c, &s);
+        ud[q].x = c; ud[q].y = -s;
+        uf[q].x = (float)c; uf[q].y = (float)(-s);
+    }
+    CUDA_TRY(cudaMemcpyToSymbol(c_tw96f, uf, sizeof(uf)));
+    CUDA_TRY(cudaMemcpyToSymbol(c_tw96d, ud, sizeof(ud)));
     return VEC_OK;
 }
 
@@ -435,7 +487,7 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     if (DIR == 1) {
         int st = get_encoder();
         if (st) return st;
-        constexpr int BR = N < 256 ? N : 256;
+        constexpr int BR = ybox_rows(N);
         for (int j = 0; j < nj; j++)
             if ((st = encode_ymap<R>(&tp.m[j], jobs[j].in, E->nx, E->ny, E->nz, S, BR))) return st;
     }
@@ -466,9 +518,9 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
     // sequences per tile
     int S = 0;
     switch (n) {
-    case 64: case 128: case 256: S = F ? 16 : 8; break;
-    case 512: S = F ? 8 : 4; break;
-    case 1024: S = F ? 4 : 2; break;
+    case 64: case 96: case 128: case 192: case 256: S = F ? 16 : 8; break;
+    case 384: case 512: S = F ? 8 : 4; break;
+    case 768: case 1024: S = F ? 4 : 2; break;
     default: return 0;
     }
     if (F && n <= 256 && E->ct_s == 8) S = 8;   // autotuned alternative
@@ -489,9 +541,12 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
             CT_CASE(64, 8, 8, 16) CT_CASE(128, 16, 8, 16) CT_CASE(256, 16, 16, 16)
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
             CT_CASE(512, 32, 16, 8) CT_CASE(1024, 32, 32, 4)
+            CT_CASE(96, 8, 12, 16) CT_CASE(192, 16, 12, 16) CT_CASE(96, 8, 12, 8) CT_CASE(192, 16, 12, 8)
+            CT_CASE(384, 16, 24, 8) CT_CASE(768, 32, 24, 4)
         } else {
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
             CT_CASE(512, 32, 16, 4) CT_CASE(1024, 32, 32, 2)
+            CT_CASE(96, 8, 12, 8) CT_CASE(192, 16, 12, 8) CT_CASE(384, 16, 24, 4) CT_CASE(768, 32, 24, 2)
         }
 #undef CT_CASE
         if (st < 0) return 0;

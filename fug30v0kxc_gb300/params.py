@@ -128,6 +128,34 @@ def config1(**kw):
     return convection_params(256, 256, 129, eta_contrast=20.0, **kw)
 
 
+def config4(**kw):
+    """1024x1024x513, Ra 1e7, Q 1e4, eta contrast 50, theta 19 (density
+    contrast 20), +-1e-4 temperature noise."""
+    return convection_params(1024, 1024, 513, ra=1.0e7, q=1.0e4, theta=19.0, eta_contrast=50.0,
+                             noise=1.0e-4, **kw)
+
+
+def config2_members(seed=20240, precision=VEC_PREC_SPLIT):
+    """The 48-member ensemble: 16 each at 64^2 x 65, 128^2 x 97 and
+    192^2 x 129; Ra log-uniform in [1e4, 1e6], Q in {0, 100, 1000}, eta
+    contrast in {1, 5, 20}, drawn from a seeded generator; m=1, density
+    contrast 10; seeded +-1e-3 temperature noise (a distinct noise seed per
+    member)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for g, (n, nz) in enumerate(((64, 65), (128, 97), (192, 129))):
+        for i in range(16):
+            ra = float(10.0 ** rng.uniform(4.0, 6.0))
+            q = float(rng.choice([0.0, 100.0, 1000.0]))
+            eta = float(rng.choice([1.0, 5.0, 20.0]))
+            p = convection_params(n, n, nz, ra=ra, q=q, eta_contrast=eta, precision=precision)
+            p.seed_base = 1996 + 7919 * (16 * g + i)
+            p.ntotal, p.ndu06 = 5000, 1000000
+            out.append(p)
+    return out
+
+
 class VecSnapshot(C.Structure):
     """include/vec.h vec_snapshot (fields: R, T, U, V, W, Bx, By, Bz)."""
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("iteration", C.c_int32),

@@ -17,7 +17,8 @@ from tests.helpers import rel_err
 pytestmark = pytest.mark.gpu
 
 SIZES = [(30, 30, 8), (64, 48, 7), (4, 4, 6), (96, 60, 9), (256, 256, 6), (10, 250, 6),
-         (128, 128, 6), (512, 64, 6), (64, 1024, 6), (1024, 32, 6), (64, 64, 7)]
+         (128, 128, 6), (512, 64, 6), (64, 1024, 6), (1024, 32, 6), (64, 64, 7),
+         (192, 96, 6), (384, 64, 6), (96, 768, 6)]
 TOL = 1e-12
 
 
@@ -101,9 +102,10 @@ def test_bad_sizes():
         assert e.value.status == code
 
 
-@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 7), (64, 128, 6), (1024, 64, 6), (128, 512, 6)])
+@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 7), (64, 128, 6), (1024, 64, 6), (128, 512, 6),
+                                      (192, 192, 7), (96, 384, 6), (768, 96, 6)])
 def test_specialised_lines_match_generic(nx, ny, nz, monkeypatch):
-    """The power-of-two line kernel (TMA-fed, register four-step FFT) and the
+    """The 2^a / 3*2^a line kernel (TMA-fed, register four-step FFT) and the
     generic shared-memory Stockham kernel agree on every operator."""
     rng = np.random.default_rng(nx + ny)
     f = rng.standard_normal((nz, ny, nx))

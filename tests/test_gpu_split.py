@@ -36,9 +36,9 @@ def rel_l2(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
 
-@pytest.mark.parametrize("eta", [1.0, 20.0])
-def test_split_rhs(eta):
-    g, o, p = _pair(64, 64, 33, eta)
+@pytest.mark.parametrize("eta,grid", [(1.0, (64, 64, 33)), (20.0, (64, 64, 33)), (20.0, (192, 96, 17))])
+def test_split_rhs(eta, grid):
+    g, o, p = _pair(*grid, eta)
     g.hydro_deriv(); o.hydro_deriv()
     for n in ("rdot3", "tdot3", "udot3", "vdot3", "wdot3"):
         e = rel_err(g.get(n), o.get(n))
