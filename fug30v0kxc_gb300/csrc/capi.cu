@@ -369,7 +369,7 @@ extern "C" int vec_destroy(vec_ctx *c)
     void *ptrs[] = { E.r, E.t, E.u, E.v, E.w, E.bx, E.by, E.bz, E.jsq, E.pol, E.tor, E.bxbar, E.bybar,
                      E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds, E.dev_err,
                      E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
-                     E.rho0, E.t0, E.hres };
+                     E.rho0, E.t0, E.hres, E.corr, E.corr_bx };
     for (void *q : ptrs) if (q) cudaFree(q);
     for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hbuf[f][s]) cudaFree(E.hbuf[f][s]);
     for (int s = 0; s < 3; s++) { if (E.bxd_buf[s]) cudaFree(E.bxd_buf[s]); if (E.byd_buf[s]) cudaFree(E.byd_buf[s]); }
@@ -780,6 +780,7 @@ static int enqueue_step(Engine &E, bool diag_now)
     if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
     else st = phys_zero_mag_rhs(&E);
     if (st) return st;
+    if (E.corr_on && (st = closure_apply_corr(&E))) return st;
     const int mdeal = E.p.dalias && mag;
     if ((st = E.split ? split_ab3(&E, mdeal) : phys_ab3(&E, mdeal))) return st;
     const bool dealias_now = E.p.dalias && (E.nit % 10 == 0);

@@ -1,0 +1,640 @@
+// closure_net.cu -- the learned closure's network: four 3x3x3 convolutions
+// (16 -> 32 -> 32 -> 32 -> 16 channels, GELU between them) with BF16 weights
+// and activations and FP32 accumulation on the tensor cores (mma.sync
+// m16n8k16), trained with Adam.  Every convolution pass -- forward, input
+// gradient and weight gradient -- is an implicit GEMM over channel-last
+// activations staged in shared memory.
+//
+// Layout: activations [sample][z][y][x][channel], channel fastest, BF16;
+// periodic in x and y, zero padding in z (the walls).  Tap t = 9(dz+1) +
+// 3(dy+1) + (dx+1) multiplies X[x+dx, y+dy, z+dz] (a correlation).  Forward
+// weights are [27][cout][cin]; the input-gradient pass uses the same weights
+// flipped in the tap and transposed, [27][cin][cout], so it runs through the
+// forward kernel.
+//
+// A tile is 128 consecutive points of one z-plane (128/nx rows of nx points;
+// nx in {16, 32, 64, 128}).  Its halo -- 3 planes x (rows + 2) x (nx + 2)
+// points, wrapped in x and y, zero outside the walls -- is copied into
+// shared memory with cp.async; rows are padded by 8 channels (16 bytes), so
+// the ldmatrix row addresses of eight consecutive points fall in distinct
+// bank groups.  CTAs are persistent over tiles and keep the weights of their
+// layer in shared memory.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "closure_net.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+constexpr int TP = 128;       // points per tile
+constexpr int NTAP = 27;
+
+__device__ __forceinline__ unsigned su32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// 16-byte asynchronous copy global -> shared, zero-filled when !valid
+__device__ __forceinline__ void cp16(unsigned dst, const void *src, bool valid)
+{
+    const int sz = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ void ldsm4(unsigned a, uint32_t *r)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm4t(unsigned a, uint32_t *r)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+// D += A(16x16, row) * B(16x8, col), BF16 in, FP32 accumulate
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// GELU with the Gaussian CDF, and its derivative
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float x)
+{
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+struct TileAt {
+    int b, z, y0;
+    size_t plane0;    // global point index of (b, z, 0, 0)
+    int q0;           // first point of the tile within the plane
+};
+
+__device__ __forceinline__ TileAt tile_at(const NetGeom &g, long long t)
+{
+    const int tpp = g.nx * g.ny / TP;
+    TileAt a;
+    a.b = (int)(t / ((long long)g.nz * tpp));
+    const int rem = (int)(t - (long long)a.b * g.nz * tpp);
+    a.z = rem / tpp;
+    const int tip = rem - a.z * tpp;
+    a.y0 = tip * g.R;
+    a.q0 = tip * TP;
+    a.plane0 = ((size_t)a.b * g.nz + a.z) * (size_t)g.ny * g.nx;
+    return a;
+}
+
+// halo [3][R+2][nx+2] points of C channels (row stride C + 8)
+template <int C>
+__device__ __forceinline__ void load_halo(bf16 *h, const bf16 *src, const NetGeom &g, const TileAt &a)
+{
+    constexpr int CS = C + 8, CH = C / 8;
+    const int W = g.nx + 2, RR = g.R + 2;
+    const int total = 3 * RR * W * CH;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int c = e % CH;
+        const int pt = e / CH;
+        const int xi = pt % W;
+        const int rr = (pt / W) % RR;
+        const int dz = pt / (W * RR);
+        const int zz = a.z + dz - 1;
+        int yy = a.y0 + rr - 1;
+        yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
+        int xx = xi - 1;
+        xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+        const bool ok = zz >= 0 && zz < g.nz;
+        const size_t gp = ok ? ((((size_t)a.b * g.nz + zz) * g.ny + yy) * g.nx + xx) : 0;
+        cp16(su32(h + (size_t)pt * CS + c * 8), src + gp * C + c * 8, ok);
+    }
+}
+
+// ---- forward / input-gradient convolution -------------------------------------------
+// EPI_ACT: pre = acc + bias -> o_pre (BF16), gelu(pre) -> o_act (BF16)
+// EPI_OUT: acc + bias -> o_f32 (FP32, first cout_real channels)
+// EPI_GATE: acc * gelu'(gate) -> o_act (BF16)      (input gradient)
+enum { EPI_ACT = 0, EPI_OUT = 1, EPI_GATE = 2 };
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(256, 1)
+k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
+       bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
+       const bf16 *__restrict__ gate)
+{
+    constexpr int CSI = CIN + 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    bf16 *ws = reinterpret_cast<bf16 *>(smem);               // [27][COUT][CSI]
+    bf16 *hs = ws + (size_t)NTAP * COUT * CSI;               // halo
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+
+    for (int e = tid; e < NTAP * COUT * (CIN / 8); e += blockDim.x) {
+        const int row = e / (CIN / 8), c = e % (CIN / 8);
+        cp16(su32(ws + (size_t)row * CSI + c * 8), wt + (size_t)row * CIN + c * 8, true);
+    }
+    const int yl = (16 * w) / g.nx, x0 = (16 * w) % g.nx;
+    const int W2 = g.nx + 2, RR = g.R + 2;
+    for (long long t = blockIdx.x; t < g.tiles; t += gridDim.x) {
+        const TileAt a = tile_at(g, t);
+        __syncthreads();                      // previous tile's reads of hs are done
+        load_halo<CIN>(hs, x, g, a);
+        cp_wait_all();
+        __syncthreads();
+        float acc[COUT / 8][4];
+#pragma unroll
+        for (int j = 0; j < COUT / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        const int pa = (lane & 7) + ((lane >> 3) & 1) * 8, ca = (lane >> 4) * 8;    // A: point, channel
+        const int nb_ = (lane & 7) + (lane >> 4) * 8, kb = ((lane >> 3) & 1) * 8;   // B: row n, column k
+#pragma unroll 1
+        for (int tap = 0; tap < NTAP; tap++) {
+            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+            const int hrow = (dz * RR + yl + dy) * W2 + x0 + dx;
+#pragma unroll
+            for (int kk = 0; kk < CIN / 16; kk++) {
+                uint32_t af[4];
+                ldsm4(su32(hs + (size_t)(hrow + pa) * CSI + kk * 16 + ca), af);
+#pragma unroll
+                for (int np = 0; np < COUT / 16; np++) {
+                    uint32_t bfr[4];
+                    ldsm4(su32(ws + (size_t)(tap * COUT + np * 16 + nb_) * CSI + kk * 16 + kb), bfr);
+                    mma16816(acc[2 * np], af, bfr[0], bfr[1]);
+                    mma16816(acc[2 * np + 1], af, bfr[2], bfr[3]);
+                }
+            }
+        }
+        // epilogue: c0,c1 at (row g, n 2t', 2t'+1), c2,c3 at row g+8
+        const int gr = lane >> 2, tq = lane & 3;
+#pragma unroll
+        for (int j = 0; j < COUT / 8; j++) {
+            const int n = 8 * j + 2 * tq;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const size_t gp = a.plane0 + a.q0 + 16 * w + gr + 8 * h;
+                float v0 = acc[j][2 * h], v1 = acc[j][2 * h + 1];
+                if (EPI == EPI_ACT) {
+                    v0 += bias[n];
+                    v1 += bias[n + 1];
+                    *reinterpret_cast<__nv_bfloat162 *>(o_pre + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
+                    *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) =
+                        __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+                } else if (EPI == EPI_OUT) {
+                    if (n < cout_real) o_f32[gp * cout_real + n] = v0 + bias[n];
+                    if (n + 1 < cout_real) o_f32[gp * cout_real + n + 1] = v1 + bias[n + 1];
+                } else {
+                    const __nv_bfloat162 gg = *reinterpret_cast<const __nv_bfloat162 *>(gate + gp * COUT + n);
+                    v0 *= gelu_d(__bfloat162float(gg.x));
+                    v1 *= gelu_d(__bfloat162float(gg.y));
+                    *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+        }
+    }
+}
+
+// ---- weight gradient ----------------------------------------------------------------------
+// dW[tap][co][ci] = sum_p dY[p][co] X[p + d(tap)][ci], db[co] = sum_p dY[p][co].
+// Nine warps; warp w = 3 dz + dy owns the three taps (dz, dy, dx = -1..1).
+// Per-CTA partial sums go to part[block][27*CO*CI + CO].
+template <int CI, int CO>
+__global__ void __launch_bounds__(288, 1)
+k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, float *__restrict__ part)
+{
+    constexpr int CSI = CI + 8, CSO = CO + 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    bf16 *hs = reinterpret_cast<bf16 *>(smem);
+    const int W2 = g.nx + 2, RR = g.R + 2;
+    bf16 *ds = hs + (size_t)3 * RR * W2 * CSI;              // [TP][CSO]
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int wz = w / 3, wy = w % 3;
+
+    float acc[3][CO / 16][CI / 8][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int m = 0; m < CO / 16; m++)
+#pragma unroll
+            for (int n = 0; n < CI / 8; n++) acc[d][m][n][0] = acc[d][m][n][1] = acc[d][m][n][2] = acc[d][m][n][3] = 0.0f;
+    float bsum = 0.0f;
+
+    for (long long t = blockIdx.x; t < g.tiles; t += gridDim.x) {
+        const TileAt a = tile_at(g, t);
+        __syncthreads();
+        load_halo<CI>(hs, x, g, a);
+        for (int e = tid; e < TP * (CO / 8); e += blockDim.x) {
+            const int p = e / (CO / 8), c = e % (CO / 8);
+            cp16(su32(ds + (size_t)p * CSO + c * 8), dy + (a.plane0 + a.q0 + p) * CO + c * 8, true);
+        }
+        cp_wait_all();
+        __syncthreads();
+        if (tid < CO) {
+            float s = 0.0f;
+            for (int p = 0; p < TP; p++) s += __bfloat162float(ds[(size_t)p * CSO + tid]);
+            bsum += s;
+        }
+        const int pa = (lane & 7) + (lane >> 4) * 8, ca = ((lane >> 3) & 1) * 8;   // A^T: point, co
+        const int pb = (lane & 7) + ((lane >> 3) & 1) * 8, cb = (lane >> 4) * 8;   // B^T: point, ci
+#pragma unroll 1
+        for (int s = 0; s < TP / 16; s++) {
+            const int yl = (16 * s) / g.nx, x0 = (16 * s) % g.nx;
+            uint32_t af[CO / 16][4];
+#pragma unroll
+            for (int m = 0; m < CO / 16; m++) ldsm4t(su32(ds + (size_t)(16 * s + pa) * CSO + 16 * m + ca), af[m]);
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const int hrow = (wz * RR + yl + wy) * W2 + x0 + d;
+#pragma unroll
+                for (int np = 0; np < CI / 16; np++) {
+                    uint32_t bfr[4];
+                    ldsm4t(su32(hs + (size_t)(hrow + pb) * CSI + 16 * np + cb), bfr);
+#pragma unroll
+                    for (int m = 0; m < CO / 16; m++) {
+                        mma16816(acc[d][m][2 * np], af[m], bfr[0], bfr[1]);
+                        mma16816(acc[d][m][2 * np + 1], af[m], bfr[2], bfr[3]);
+                    }
+                }
+            }
+        }
+    }
+    float *pp = part + (size_t)blockIdx.x * (NTAP * CO * CI + CO);
+    const int gr = lane >> 2, tq = lane & 3;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int tap = 3 * w + d;
+#pragma unroll
+        for (int m = 0; m < CO / 16; m++)
+#pragma unroll
+            for (int n = 0; n < CI / 8; n++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int co = 16 * m + gr + 8 * h, ci = 8 * n + 2 * tq;
+                    pp[((size_t)tap * CO + co) * CI + ci] = acc[d][m][n][2 * h];
+                    pp[((size_t)tap * CO + co) * CI + ci + 1] = acc[d][m][n][2 * h + 1];
+                }
+    }
+    if (tid < CO) pp[NTAP * CO * CI + tid] = bsum;
+}
+
+// out[j] = sum over blocks of part[b][j]
+__global__ void k_reduce_parts(const float *part, int nblocks, int J, float *out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    float s = 0.0f;
+    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * J + j];
+    out[j] = s;
+}
+
+// ---- loss, optimiser, weight packing ---------------------------------------------------
+// mean-squared error over P points x C channels; dout (BF16, 16 channels,
+// the last 16 - C zero) = 2 (out - tgt) / (P C)
+__global__ void k_mse(const float *out, const float *tgt, size_t P, int C, bf16 *dout, double *loss)
+{
+    __shared__ double red[256];
+    double acc = 0.0;
+    const double inv = 1.0 / ((double)P * C);
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+        float g[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) g[c] = 0.0f;
+        for (int c = 0; c < C; c++) {
+            const float d = out[p * C + c] - tgt[p * C + c];
+            acc += (double)d * d;
+            g[c] = (float)(2.0 * inv) * d;
+        }
+#pragma unroll
+        for (int c = 0; c < 16; c += 2)
+            *reinterpret_cast<__nv_bfloat162 *>(dout + p * 16 + c) = __floats2bfloat162_rn(g[c], g[c + 1]);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0] * inv);
+}
+
+// Adam (Kingma & Ba), bias-corrected, step t >= 1
+__global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// wf[tap][co][ci] = W, wb[tap][ci][co] = W[26 - tap][co][ci]
+__global__ void k_pack(const float *W, int CO, int CI, bf16 *wf, bf16 *wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NTAP * CO * CI) return;
+    const int tap = i / (CO * CI), r = i % (CO * CI), co = r / CI, ci = r % CI;
+    const bf16 v = __float2bfloat16_rn(W[i]);
+    wf[i] = v;
+    wb[((size_t)(NTAP - 1 - tap) * CI + ci) * CO + co] = v;
+}
+
+__global__ void k_f32_to_bf16(const float *a, bf16 *b, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+}
+
+template <int CIN, int COUT, int EPI>
+size_t conv_smem(const NetGeom &g)
+{
+    return ((size_t)NTAP * COUT * (CIN + 8) + (size_t)3 * (g.R + 2) * (g.nx + 2) * (CIN + 8)) * sizeof(bf16);
+}
+
+template <int CI, int CO>
+size_t wgrad_smem(const NetGeom &g)
+{
+    return ((size_t)3 * (g.R + 2) * (g.nx + 2) * (CI + 8) + (size_t)TP * (CO + 8)) * sizeof(bf16);
+}
+
+template <int CIN, int COUT, int EPI>
+int run_conv(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre, bf16 *o_act, float *o_f32,
+             int cout_real, const bf16 *gate)
+{
+    const size_t sm = conv_smem<CIN, COUT, EPI>(N->g);
+    static bool set = false;
+    if (!set) {
+        CUDA_TRY(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        set = true;
+    }
+    long long grid = N->num_sms;
+    if (grid > N->g.tiles) grid = N->g.tiles;
+    k_conv<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real, gate);
+    N->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+template <int CI, int CO>
+int run_wgrad(vec_net *N, const bf16 *x, const bf16 *dy, float *gout)
+{
+    const size_t sm = wgrad_smem<CI, CO>(N->g);
+    static bool set = false;
+    if (!set) {
+        CUDA_TRY(cudaFuncSetAttribute(k_wgrad<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        set = true;
+    }
+    long long grid = N->num_sms;
+    if (grid > N->g.tiles) grid = N->g.tiles;
+    k_wgrad<CI, CO><<<(int)grid, 288, sm, N->stream>>>(x, dy, N->g, N->part);
+    const int J = NTAP * CO * CI + CO;
+    k_reduce_parts<<<(J + 255) / 256, 256, 0, N->stream>>>(N->part, (int)grid, J, gout);
+    N->launches += 2;
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+// the layers: (cin, cout) = (16,32), (32,32), (32,32), (32,16)
+const int LCI[4] = { 16, 32, 32, 32 };
+const int LCO[4] = { 32, 32, 32, 16 };
+
+uint64_t splitmix(uint64_t &s)
+{
+    uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+// ---- internal API (used by the closure coupling) ------------------------------------
+int net_pack(vec_net *N)
+{
+    for (int l = 0; l < 4; l++) {
+        const int n = NTAP * LCO[l] * LCI[l];
+        k_pack<<<(n + 255) / 256, 256, 0, N->stream>>>(N->p + N->off_w[l], LCO[l], LCI[l], N->wf[l], N->wb[l]);
+        N->launches++;
+    }
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+// x0 (BF16, [P][16]) -> out (FP32, [P][cout_real])
+int net_forward(vec_net *N)
+{
+    int st;
+    float *p = N->p;
+    if ((st = run_conv<16, 32, EPI_ACT>(N, N->x0, N->wf[0], p + N->off_b[0], N->pre[0], N->act[0], nullptr, 0, nullptr)))
+        return st;
+    if ((st = run_conv<32, 32, EPI_ACT>(N, N->act[0], N->wf[1], p + N->off_b[1], N->pre[1], N->act[1], nullptr, 0, nullptr)))
+        return st;
+    if ((st = run_conv<32, 32, EPI_ACT>(N, N->act[1], N->wf[2], p + N->off_b[2], N->pre[2], N->act[2], nullptr, 0, nullptr)))
+        return st;
+    return run_conv<32, 16, EPI_OUT>(N, N->act[2], N->wf[3], p + N->off_b[3], nullptr, nullptr, N->out, N->cout_real,
+                                     nullptr);
+}
+
+// after net_forward: loss against tgt ([P][cout_real] FP32) and all gradients
+int net_backward(vec_net *N, const float *tgt)
+{
+    int st;
+    CUDA_TRY(cudaMemsetAsync(N->loss_d, 0, sizeof(double), N->stream));
+    const size_t P = (size_t)N->g.nb * N->npts;
+    k_mse<<<N->num_sms * 4, 256, 0, N->stream>>>(N->out, tgt, P, N->cout_real, N->dout, N->loss_d);
+    N->launches++;
+    CUDA_TRY(cudaGetLastError());
+    float *g = N->gr;
+    // layer 4: dW from act3 and dout; dX3 -> gate with pre3
+    if ((st = run_wgrad<32, 16>(N, N->act[2], N->dout, g + N->off_w[3]))) return st;
+    if ((st = run_conv<16, 32, EPI_GATE>(N, N->dout, N->wb[3], nullptr, nullptr, N->d[0], nullptr, 0, N->pre[2])))
+        return st;
+    if ((st = run_wgrad<32, 32>(N, N->act[1], N->d[0], g + N->off_w[2]))) return st;
+    if ((st = run_conv<32, 32, EPI_GATE>(N, N->d[0], N->wb[2], nullptr, nullptr, N->d[1], nullptr, 0, N->pre[1])))
+        return st;
+    if ((st = run_wgrad<32, 32>(N, N->act[0], N->d[1], g + N->off_w[1]))) return st;
+    if ((st = run_conv<32, 32, EPI_GATE>(N, N->d[1], N->wb[1], nullptr, nullptr, N->d[0], nullptr, 0, N->pre[0])))
+        return st;
+    return run_wgrad<16, 32>(N, N->x0, N->d[0], g + N->off_w[0]);
+}
+
+int net_adam(vec_net *N, float lr)
+{
+    N->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - powf(b1, (float)N->step), c2 = 1.0f - powf(b2, (float)N->step);
+    k_adam<<<(unsigned)((N->nparam + 255) / 256), 256, 0, N->stream>>>(N->p, N->gr, N->m, N->v, N->nparam, lr, b1, b2,
+                                                                     1e-8f, c1, c2);
+    N->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return net_pack(N);
+}
+
+// ---- C-ABI ---------------------------------------------------------------------------
+static int nalloc(void **p, size_t bytes)
+{
+    if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) {
+        cudaGetLastError();
+        vec_set_error("cudaMalloc of %zu bytes failed", bytes);
+        return VEC_ERR_ALLOC;
+    }
+    return cudaMemset(*p, 0, bytes ? bytes : 16) == cudaSuccess ? VEC_OK : VEC_ERR_CUDA;
+}
+
+extern "C" int vec_net_destroy(vec_net *N)
+{
+    if (!N) return VEC_OK;
+    if (N->stream) cudaStreamSynchronize(N->stream);
+    void *ps[] = { N->p, N->gr, N->m, N->v, N->x0, N->dout, N->out, N->tgt, N->part, N->loss_d, N->xin };
+    for (void *q : ps) if (q) cudaFree(q);
+    for (int l = 0; l < 4; l++) { if (N->wf[l]) cudaFree(N->wf[l]); if (N->wb[l]) cudaFree(N->wb[l]); }
+    for (int l = 0; l < 3; l++) { if (N->pre[l]) cudaFree(N->pre[l]); if (N->act[l]) cudaFree(N->act[l]); }
+    for (int l = 0; l < 2; l++) if (N->d[l]) cudaFree(N->d[l]);
+    if (N->stream && N->own_stream) cudaStreamDestroy(N->stream);
+    delete N;
+    return VEC_OK;
+}
+
+extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long long seed, vec_net **out)
+{
+    if (!out) return VEC_ERR_ARG;
+    *out = nullptr;
+    if (!(nx == 16 || nx == 32 || nx == 64 || nx == 128) || ny < 2 || (nx * ny) % TP != 0 || nz < 1 || batch < 1) {
+        vec_set_error("closure network: nx must be 16, 32, 64 or 128 and nx*ny a multiple of %d", TP);
+        return VEC_ERR_SIZE;
+    }
+    vec_net *N = new vec_net();
+    N->g.nx = nx; N->g.ny = ny; N->g.nz = nz; N->g.nb = batch;
+    N->g.R = TP / nx;
+    N->g.tiles = (long long)batch * nz * (nx * ny / TP);
+    N->npts = (size_t)nx * ny * nz;
+    N->cout_real = 8;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&N->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking) != cudaSuccess) { delete N; return VEC_ERR_CUDA; }
+    N->own_stream = 1;
+    size_t off = 0;
+    for (int l = 0; l < 4; l++) {
+        N->off_w[l] = off; off += (size_t)NTAP * LCO[l] * LCI[l];
+        N->off_b[l] = off; off += LCO[l];
+    }
+    N->nparam = off;
+    const size_t P = (size_t)batch * N->npts;
+    int st = 0;
+#define NA(ptr, bytes) do { if (!st) st = nalloc((void **)&(ptr), (bytes)); } while (0)
+    NA(N->p, off * 4); NA(N->gr, off * 4); NA(N->m, off * 4); NA(N->v, off * 4);
+    for (int l = 0; l < 4; l++) {
+        NA(N->wf[l], (size_t)NTAP * LCO[l] * LCI[l] * 2);
+        NA(N->wb[l], (size_t)NTAP * LCO[l] * LCI[l] * 2);
+    }
+    NA(N->x0, P * 16 * 2);
+    for (int l = 0; l < 3; l++) { NA(N->pre[l], P * 32 * 2); NA(N->act[l], P * 32 * 2); }
+    for (int l = 0; l < 2; l++) NA(N->d[l], P * 32 * 2);
+    NA(N->dout, P * 16 * 2);
+    NA(N->out, P * 8 * 4);
+    NA(N->tgt, P * 8 * 4);
+    NA(N->xin, P * 16 * 4);
+    NA(N->part, (size_t)N->num_sms * (NTAP * 32 * 32 + 32) * 4);
+    NA(N->loss_d, 8);
+#undef NA
+    if (st) { vec_net_destroy(N); return st; }
+    // initial weights: uniform(-a, a), a = sqrt(6 / fan_in) (He); the output
+    // layer scaled by 0.1; padded input / output channels zero; biases zero
+    std::vector<float> h(off, 0.0f);
+    uint64_t s = seed * 0x2545F4914F6CDD1DULL + 12345;
+    const int creal_in[4] = { 9, 32, 32, 32 }, creal_out[4] = { 32, 32, 32, 8 };
+    for (int l = 0; l < 4; l++) {
+        const double a = sqrt(6.0 / (NTAP * creal_in[l])) * (l == 3 ? 0.1 : 1.0);
+        for (int tap = 0; tap < NTAP; tap++)
+            for (int co = 0; co < LCO[l]; co++)
+                for (int ci = 0; ci < LCI[l]; ci++) {
+                    const double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+                    const bool real = co < creal_out[l] && ci < creal_in[l];
+                    h[N->off_w[l] + ((size_t)tap * LCO[l] + co) * LCI[l] + ci] = real ? (float)((2.0 * u - 1.0) * a) : 0.0f;
+                }
+    }
+    if (cudaMemcpy(N->p, h.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess || net_pack(N) ||
+        cudaStreamSynchronize(N->stream) != cudaSuccess) {
+        vec_net_destroy(N);
+        return VEC_ERR_CUDA;
+    }
+    *out = N;
+    return VEC_OK;
+}
+
+extern "C" long long vec_net_nparams(vec_net *N) { return N ? (long long)N->nparam : 0; }
+
+extern "C" int vec_net_get_params(vec_net *N, float *host)
+{
+    if (!N || !host) return VEC_ERR_ARG;
+    CUDA_TRY(cudaMemcpyAsync(host, N->p, N->nparam * 4, cudaMemcpyDeviceToHost, N->stream));
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}
+
+extern "C" int vec_net_set_params(vec_net *N, const float *host)
+{
+    if (!N || !host) return VEC_ERR_ARG;
+    CUDA_TRY(cudaMemcpyAsync(N->p, host, N->nparam * 4, cudaMemcpyHostToDevice, N->stream));
+    CUDA_TRY(cudaMemsetAsync(N->m, 0, N->nparam * 4, N->stream));
+    CUDA_TRY(cudaMemsetAsync(N->v, 0, N->nparam * 4, N->stream));
+    N->step = 0;
+    int st = net_pack(N);
+    if (st) return st;
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}
+
+extern "C" int vec_net_get_grads(vec_net *N, float *host)
+{
+    if (!N || !host) return VEC_ERR_ARG;
+    CUDA_TRY(cudaMemcpyAsync(host, N->gr, N->nparam * 4, cudaMemcpyDeviceToHost, N->stream));
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}
+
+// x: host [batch][nz][ny][nx][16] FP32 (rounded to BF16 on the device);
+// out (optional): host [batch][nz][ny][nx][8] FP32
+extern "C" int vec_net_forward(vec_net *N, const float *x, float *out)
+{
+    if (!N || !x) return VEC_ERR_ARG;
+    const size_t n = (size_t)N->g.nb * N->npts * 16;
+    CUDA_TRY(cudaMemcpyAsync(N->xin, x, n * 4, cudaMemcpyHostToDevice, N->stream));
+    k_f32_to_bf16<<<(unsigned)((n + 255) / 256), 256, 0, N->stream>>>(N->xin, N->x0, n);
+    N->launches++;
+    int st = net_forward(N);
+    if (st) return st;
+    if (out)
+        CUDA_TRY(cudaMemcpyAsync(out, N->out, (size_t)N->g.nb * N->npts * 8 * 4, cudaMemcpyDeviceToHost, N->stream));
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}
+
+// after vec_net_forward: MSE against tgt (host [batch][...][8]) and the
+// gradients of every parameter
+extern "C" int vec_net_backward(vec_net *N, const float *tgt, double *loss)
+{
+    if (!N || !tgt) return VEC_ERR_ARG;
+    CUDA_TRY(cudaMemcpyAsync(N->tgt, tgt, (size_t)N->g.nb * N->npts * 8 * 4, cudaMemcpyHostToDevice, N->stream));
+    int st = net_backward(N, N->tgt);
+    if (st) return st;
+    if (loss) CUDA_TRY(cudaMemcpyAsync(loss, N->loss_d, 8, cudaMemcpyDeviceToHost, N->stream));
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}
+
+extern "C" int vec_net_adam(vec_net *N, float lr)
+{
+    if (!N) return VEC_ERR_ARG;
+    int st = net_adam(N, lr);
+    if (st) return st;
+    CUDA_TRY(cudaStreamSynchronize(N->stream));
+    return VEC_OK;
+}

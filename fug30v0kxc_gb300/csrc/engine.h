@@ -88,6 +88,13 @@ struct Engine {
     cudaGraphExec_t gexec[2] = { nullptr, nullptr };
     int g_b32_after[2] = { 0, 0 };
     long long g_launches[2] = { 0, 0 };
+    // learned-closure RHS correction (closure.cu): 7 fields in the history
+    // row order (r, t, u, v, w, pol, tor) plus 3 scratch fields, of the RHS
+    // precision, and the mean-field corrections; added to the newest RHS
+    // slots inside the step while corr_on
+    void *corr = nullptr;
+    double *corr_bx = nullptr, *corr_by = nullptr;
+    int corr_on = 0;
     // tunables (the ensemble autotuner sets them per grid)
     int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
     int ct_s = 0;               // sequences per line tile (0: default for the size)
@@ -164,6 +171,8 @@ int engine_enqueue_step(Engine &E, bool diag_now);
 int engine_one_step(Engine &E);
 bool engine_diag_due(const Engine &E, int nit);
 Engine &engine_of(vec_ctx *c);
+// closure.cu
+int closure_apply_corr(Engine *E);
 // split form (split.cu)
 int split_setup(Engine *E);
 int split_hydro(Engine *E);

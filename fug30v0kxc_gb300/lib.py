@@ -6,7 +6,7 @@ with an error naming the file.
 import ctypes as C
 import os
 
-from .params import VecDiag, VecParams, VecScalars, VecSnapshot
+from .params import VecClosureReport, VecDiag, VecParams, VecScalars, VecSnapshot
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libvec_gpu.so")
@@ -71,6 +71,34 @@ SIGNATURES = {
     "vec_ensemble_sync": (C.c_int, [_vp]),
     "vec_ensemble_tune": (C.c_int, [_vp, C.c_int, C.c_char_p]),
     "vec_tunables": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "vec_net_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),
+    "vec_net_destroy": (C.c_int, [_vp]),
+    "vec_net_nparams": (C.c_longlong, [_vp]),
+    "vec_net_get_params": (C.c_int, [_vp, _dp]),
+    "vec_net_set_params": (C.c_int, [_vp, _dp]),
+    "vec_net_get_grads": (C.c_int, [_vp, _dp]),
+    "vec_net_forward": (C.c_int, [_vp, _dp, _dp]),
+    "vec_net_backward": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
+    "vec_net_adam": (C.c_int, [_vp, C.c_float]),
+    "vec_closure_create": (C.c_int, [C.POINTER(VecParams), C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),
+    "vec_closure_destroy": (C.c_int, [_vp]),
+    "vec_closure_net": (_vp, [_vp]),
+    "vec_closure_npairs": (C.c_int, [_vp]),
+    "vec_box_filter": (C.c_int, [_vp, _vp, _vp]),
+    "vec_closure_add_pair": (C.c_int, [_vp, _vp, _vp]),
+    "vec_closure_get_pair": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "vec_closure_fit_norm": (C.c_int, [_vp, C.c_int]),
+    "vec_closure_get_norm": (C.c_int, [_vp, _dp]),
+    "vec_closure_set_norm": (C.c_int, [_vp, _dp]),
+    "vec_closure_train": (C.c_int, [_vp, C.c_int, C.c_float, C.c_int, C.c_ulonglong, _dp]),
+    "vec_closure_eval": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "vec_closure_attach": (C.c_int, [_vp, _vp, C.c_int]),
+    "vec_closure_infer": (C.c_int, [_vp, _vp]),
+    "vec_closure_step": (C.c_int, [_vp, _vp, C.c_int]),
+    "vec_closure_run": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, C.c_double,
+                                  C.POINTER(VecClosureReport)]),
+    "vec_expand": (C.c_int, [_vp, _vp, _dp, _dp]),
+    "vec_upsample": (C.c_int, [_vp, _vp]),
     "vec_nc_write": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int]),
     "vec_nc_read": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot)]),
     "vec_write_snapshot": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_char_p]),

@@ -156,6 +156,13 @@ def config2_members(seed=20240, precision=VEC_PREC_SPLIT):
     return out
 
 
+class VecClosureReport(C.Structure):
+    """include/vec.h vec_closure_report."""
+    _fields_ = [("judges", C.c_int32), ("pad_", C.c_int32), ("coarse_steps", C.c_int64),
+                ("fine_steps", C.c_int64), ("fallback_step", C.c_int64), ("last_err", C.c_double * 3),
+                ("max_err", C.c_double * 3), ("end_time", C.c_double)]
+
+
 class VecSnapshot(C.Structure):
     """include/vec.h vec_snapshot (fields: R, T, U, V, W, Bx, By, Bz)."""
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("iteration", C.c_int32),

@@ -255,6 +255,93 @@ int vec_ensemble_tune(vec_ens *ens, int steps, const char *cache);
 /* the tile shapes in use by a context */
 int vec_tunables(vec_ctx *ctx, int *kc, int *s);
 
+/* ---- learned closure: the network ---------------------------------------
+ * No reference counterpart (an addition to the solver).  Four 3x3x3
+ * convolutions 9(->16 padded) -> 32 -> 32 -> 32 -> 8 channels with GELU,
+ * BF16 weights and activations, FP32 accumulation on the tensor cores,
+ * Adam.  Grids: nx in {16, 32, 64, 128}, nx*ny a multiple of 128; periodic
+ * in x and y, zero padding in z. */
+typedef struct vec_net vec_net;
+int vec_net_create(int nx, int ny, int nz, int batch, unsigned long long seed, vec_net **out);
+int vec_net_destroy(vec_net *net);
+long long vec_net_nparams(vec_net *net);
+/* FP32 master parameters: per layer l = 0..3 weights [27][cout][cin] then
+ * biases [cout], with (cin, cout) = (16,32), (32,32), (32,32), (32,16) */
+int vec_net_get_params(vec_net *net, float *host_out);
+int vec_net_set_params(vec_net *net, const float *host);
+int vec_net_get_grads(vec_net *net, float *host_out);
+/* x: host [batch][nz][ny][nx][16] FP32 (rounded to BF16); out (may be
+ * NULL): host [batch][nz][ny][nx][8] FP32 */
+int vec_net_forward(vec_net *net, const float *x, float *out);
+/* after vec_net_forward: mean-squared error against tgt (host, as out) and
+ * the gradient of every parameter */
+int vec_net_backward(vec_net *net, const float *tgt, double *loss);
+int vec_net_adam(vec_net *net, float lr);
+
+/* ---- learned closure: coupling to the solver ----------------------------
+ * No reference counterpart.  A closure works on a coarse grid r times
+ * coarser than the fine (DNS) grid in x and y, with nz_f - 1 = r (nz_c - 1)
+ * (coarse planes on fine planes); r even.  Network inputs: the box-filtered
+ * state (u, v, w, rho - rho0(z), T - T0(z), Bx, By, Bz - mean Bz) and the
+ * height; outputs: the RHS correction (d/dt of u, v, w, rho, T, Bx, By, Bz)
+ * = filtered fine RHS - coarse RHS at the filtered state. */
+typedef struct vec_closure vec_closure;
+typedef struct {
+    int judges;             /* comparisons made */
+    int pad_;
+    long long coarse_steps, fine_steps;
+    long long fallback_step; /* coarse step at which the run fell back, -1 if never */
+    double last_err[3];     /* relative error of Nu, kinetic, magnetic energy */
+    double max_err[3];
+    double end_time;
+} vec_closure_report;
+/* coarse: the coarse parameters; capacity: training pairs stored (FP32,
+ * 64 bytes per coarse point and pair); batch <= 64 */
+int vec_closure_create(const vec_params *coarse, int factor, int capacity, int batch, unsigned long long seed,
+                       vec_closure **out);
+int vec_closure_destroy(vec_closure *cl);
+vec_net *vec_closure_net(vec_closure *cl);
+int vec_closure_npairs(vec_closure *cl);
+/* coarse context state = box-filtered fine state (then pol/tor, B and the
+ * boundary conditions as after a time step) */
+int vec_box_filter(vec_closure *cl, vec_ctx *fine, vec_ctx *coarse);
+/* one training pair from the fine context's current state (coarse is a
+ * scratch context whose state is overwritten) */
+int vec_closure_add_pair(vec_closure *cl, vec_ctx *fine, vec_ctx *coarse);
+int vec_closure_get_pair(vec_closure *cl, int i, float *in, float *tgt);
+/* per-channel mean / standard deviation of inputs and targets over pairs
+ * [0, n); [32] = input means, input stds, target means, target stds */
+int vec_closure_fit_norm(vec_closure *cl, int n);
+int vec_closure_get_norm(vec_closure *cl, float *out32);
+int vec_closure_set_norm(vec_closure *cl, const float *in32);
+/* iters Adam steps (rate lr) on seeded batches from pairs [0, ntrain);
+ * losses (may be NULL) gets each iteration's mean-squared error */
+int vec_closure_train(vec_closure *cl, int iters, float lr, int ntrain, unsigned long long seed, double *losses);
+/* a-priori error on pairs [first, first + count), normalised units:
+ * mse_net with the network, mse_zero without (the plain coarse RHS) */
+int vec_closure_eval(vec_closure *cl, int first, int count, double *mse_net, double *mse_zero);
+/* the RHS correction of a coarse context on (1) or off (0) */
+int vec_closure_attach(vec_closure *cl, vec_ctx *coarse, int on);
+/* the correction for the coarse context's current state */
+int vec_closure_infer(vec_closure *cl, vec_ctx *coarse);
+/* nsteps steps, the correction recomputed before each */
+int vec_closure_step(vec_closure *cl, vec_ctx *coarse, int nsteps);
+/* judged run to time t_end: every `every` coarse steps a plain fine segment
+ * of nfine steps from the upsampled coarse state; if Nu, kinetic or
+ * magnetic energy of the coarse run at the segment's end time differ by more
+ * than tol (relative), the run continues on the fine solver */
+int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, double t_end, int every, int nfine, double tol,
+                    vec_closure_report *rep);
+
+/* ---- spectral upsampling (interpolate/fft.F90:834-927) -------------------- */
+/* the reference's expand: in (nx, ny, nz) of coarse -> out (r nx, r ny, nz)
+ * of fine (fine has the same nz); host or device arrays */
+int vec_expand(vec_ctx *coarse, vec_ctx *fine, const double *in, double *out);
+/* fine state from the coarse one: expand of u, v, w, rho, T, B, cubic
+ * interpolation between vertex-aligned planes, pol/tor from B, boundary
+ * conditions; the fine run restarts its AB3 history at the coarse time */
+int vec_upsample(vec_ctx *coarse, vec_ctx *fine);
+
 /* ---- instrumentation --------------------------------------------------- */
 /* When on, every kernel launch of the context is bracketed by CUDA events
  * on the context stream and its duration is accumulated per kernel name. */

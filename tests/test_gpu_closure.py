@@ -1,0 +1,151 @@
+"""The learned closure coupled to the solver, on the GPU.
+
+* expand (interpolate/fft.F90:834-927) against its numpy restatement, FP64,
+  to 1e-12 of the field's scale;
+* the upsampler is exact on a resolved Fourier mode times a cubic in z;
+* the box filter against its numpy restatement (FP32 channel storage:
+  2e-6 of the field's scale) on interior planes (the wall planes then get
+  the boundary conditions);
+* a zero correction leaves the coarse run bit-identical to the plain one
+  (eager and graph-replayed steps);
+* the network trained on pairs from a fine run lowers the a-priori error
+  of the coarse RHS on held-out pairs (mse with the closure < 0.5 x mse of
+  the plain coarse RHS);
+* the judged run falls back to the fine solver when the tolerance is
+  unattainable and never when it is loose.
+"""
+import numpy as np
+import pytest
+
+from oracle import closure_oracle as CO
+from fug30v0kxc_gb300.closure import Closure, expand, upsample
+from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT, convection_params
+from fug30v0kxc_gb300.solver import P3D
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_expand_matches_oracle():
+    pc = convection_params(32, 16, 6, precision=VEC_PREC_FP64)
+    pf = convection_params(64, 32, 6, precision=VEC_PREC_FP64)
+    c, f = P3D(pc), P3D(pf)
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal(c.shape)
+    g = expand(c, f, a)
+    assert rel_err(g, CO.expand(a, 2)) < 1e-12
+    # four-fold in one call equals two two-fold expansions
+    pf4 = convection_params(128, 64, 6, precision=VEC_PREC_FP64)
+    f4 = P3D(pf4)
+    assert rel_err(expand(c, f4, a), CO.expand(CO.expand(a, 2), 2)) < 1e-12
+
+
+@pytest.mark.parametrize("prec", [VEC_PREC_FP64, VEC_PREC_SPLIT])
+def test_upsample_exact_on_resolved_fields(prec):
+    pc = convection_params(32, 32, 9, precision=prec)
+    pf = convection_params(128, 128, 33, precision=prec)
+    c, f = P3D(pc), P3D(pf)
+    c.start()
+    f.start()
+
+    def field(nx, ny, nz):
+        x = np.arange(nx) / nx
+        y = np.arange(ny) / ny
+        z = np.arange(nz) / (nz - 1)
+        h = np.cos(2 * np.pi * 3 * x)[None, None, :] * np.sin(2 * np.pi * 2 * y)[None, :, None]
+        pz = (1.0 + z - z ** 2 + 0.5 * z ** 3)[:, None, None]
+        return 2.0 + 0.1 * h * pz
+
+    c.set("r", field(32, 32, 9))
+    upsample(c, f)
+    assert rel_err(f.get("r"), field(128, 128, 33)) < 1e-12
+
+
+def test_box_filter_matches_oracle():
+    pf = convection_params(128, 64, 33, precision=VEC_PREC_FP64)
+    pc = convection_params(32, 16, 9, precision=VEC_PREC_FP64)
+    f, c = P3D(pf), P3D(pc)
+    f.start()
+    c.start()
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal(f.shape)
+    t = f.get("t") + 0.01 * rng.standard_normal(f.shape)
+    f.set("u", u)
+    f.set("t", t)
+    cl = Closure(pc, factor=4, capacity=1, batch=1)
+    cl.box_filter(f, c)
+    gu = c.get("u")[1:-1]
+    assert rel_err(gu, CO.box_filter(u, 4)[1:-1]) < 2e-6
+    z = np.arange(33) / 32.0
+    t0f = (1 + pf.theta * z)[:, None, None]
+    zc = np.arange(9) / 8.0
+    t0c = (1 + pc.theta * zc)[:, None, None]
+    gt = c.get("t")[1:-1] - t0c[1:-1]
+    assert rel_err(gt, CO.box_filter(t - t0f, 4)[1:-1]) < 2e-6
+    cl.close()
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_zero_correction_is_identity(graphs):
+    pc = convection_params(32, 32, 9, precision=VEC_PREC_SPLIT, eta_contrast=5.0)
+    pc.ndu06 = 7
+    a, b = P3D(pc), P3D(pc)
+    a.use_graphs(graphs)
+    b.use_graphs(graphs)
+    a.start()
+    b.start()
+    cl = Closure(pc, factor=4, capacity=1, batch=1)
+    cl.net.set_params(np.zeros(cl.net.n, np.float32))
+    cl.attach(a)
+    assert cl.step(a, 25) == 0
+    assert b.step(25) == 0
+    for n in ("r", "t", "u", "v", "w", "pol", "tor"):
+        assert np.array_equal(a.get(n), b.get(n)), n
+    cl.close()
+
+
+def _fine_run(nsteps=150):
+    pf = convection_params(128, 128, 33, ra=2e5, q=100.0, eta_contrast=5.0, noise=0.05, precision=VEC_PREC_SPLIT)
+    pf.ndu06 = 1000000
+    f = P3D(pf)
+    f.start()
+    assert f.step(nsteps) == 0
+    pc = convection_params(32, 32, 9, ra=2e5, q=100.0, eta_contrast=5.0, noise=0.05, precision=VEC_PREC_SPLIT)
+    pc.ndu06 = 1000000
+    return f, pf, pc
+
+
+def test_closure_learns_a_priori():
+    f, pf, pc = _fine_run()
+    scratch = P3D(pc)
+    cl = Closure(pc, factor=4, capacity=40, batch=8, seed=1)
+    for _ in range(40):
+        cl.add_pair(f, scratch)
+        assert f.step(3) == 0
+    cl.fit_norm(32)
+    losses = cl.train(400, lr=1e-3, ntrain=32, seed=2)
+    mse_net, mse_zero = cl.evaluate(32, 8)
+    print("closure a-priori: train loss %.3e -> %.3e; held-out mse %.3e vs %.3e without"
+          % (losses[:10].mean(), losses[-10:].mean(), mse_net, mse_zero))
+    assert np.all(np.isfinite(losses))
+    assert mse_net < 0.5 * mse_zero
+    cl.close()
+
+
+def test_judged_run_fallback():
+    f, pf, pc = _fine_run(60)
+    c = P3D(pc)
+    cl = Closure(pc, factor=4, capacity=1, batch=1)
+    cl.box_filter(f, c)
+    c.calcdt()
+    t0 = c.scalars().ttime
+    rep = cl.run(c, f, t0 + 40 * c.scalars().dt, every=5, nfine=10, tol=1e-12)
+    assert rep["judges"] >= 1 and rep["fallback_step"] >= 0 and rep["fine_steps"] > 10
+    assert rep["end_time"] >= t0 + 40 * c.scalars().dt * 0.999
+    c2 = P3D(pc)
+    cl.box_filter(f, c2)
+    c2.calcdt()
+    t1 = c2.scalars().ttime
+    rep2 = cl.run(c2, f, t1 + 30 * c2.scalars().dt, every=5, nfine=10, tol=1e12)
+    assert rep2["judges"] >= 1 and rep2["fallback_step"] == -1
+    cl.close()
