@@ -226,6 +226,42 @@ def ensemble_line(args, ws, hbm, pk):
             "tunables": [{"n": t[0], "nz": t[1], "kc": t[2], "s": t[3]} for t in tun]}
 
 
+def closure_line(args, ws):
+    """The learned closure against the filtered DNS (Ra 1e6, Q 1e3, eta
+    contrast 20, split form): errors of the time-averaged top Nusselt number
+    and energies of the judged closure run and of the plain coarse run, and
+    the wall time of the closure run against the DNS over the same time."""
+    from fug30v0kxc_gb300.closure import run_workload
+    if args.closure_scale == "full":
+        kw = dict(nxf=512, nyf=512, nzf=257, pre_time=args.closure_pre_time, spinup=2000, pairs=2000,
+                  pair_every=4, iters=2000, window=8000, diag_every=100, judge_every=args.closure_judge_every,
+                  nfine=50)
+    else:
+        kw = dict(nxf=256, nyf=256, nzf=129, pre_time=args.closure_pre_time, spinup=1000, pairs=200, pair_every=4,
+                  iters=500, window=2000, diag_every=50, judge_every=min(args.closure_judge_every, 100), nfine=50)
+    r = run_workload(log=lambda m: print("#", m, file=sys.stderr, flush=True), **kw)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, pk = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, pk = 1900.0, "fallback"
+    ach = r.get("net_tflops_train")
+    value = r["closure"]["max_err"] if "closure" in r else None
+    return {"metric": "closure: max relative error of the time-averaged top Nusselt number, kinetic and "
+                      "magnetic energy vs the filtered DNS",
+            "value": value, "unit": "fraction", "n_gpus": ws,
+            "steps": r.get("judge", {}).get("coarse_steps"), "warmup": 0, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network / f32-f64 solver",
+            "data": "synthetic (seeded static polytrope + uniform +-0.05 T noise, developed on the coarse grid, "
+                    "upsampled, spun up)",
+            "config": {"workload": "closure %dx%dx%d DNS -> %dx%dx%d, Ra 1e6, Q 1e3, eta contrast 20"
+                                   % tuple(r["fine"] + r["coarse"]), **kw},
+            "roofline": {"bound": "tensor", "kernel": "closure network training step (mma.sync BF16)",
+                         "achieved": round(ach, 2) if ach else None, "peak": peak, "peak_kind": pk, "unit": "TFLOP/s",
+                         "frac": round(ach / peak, 4) if ach else None, "traffic": None},
+            "closure": r}
+
+
 def cpu_baseline(nsteps, precision_note=""):
     """The oracle (plain C restatement, OpenMP over planes) on the host cores."""
     from oracle import oracle as O
@@ -346,7 +382,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", default=None, help="NX,NY,NZ (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large"],
+    ap.add_argument("--closure-scale", default="full", choices=["full", "small"],
+                    help="closure workload: full = DNS 512^2x257 -> 128^2x65, 2000 pairs; small = 256^2x129 "
+                         "-> 64^2x33, 200 pairs")
+    ap.add_argument("--closure-pre-time", type=float, default=1.5,
+                    help="closure workload: model time the coarse solver develops convection before the DNS")
+    ap.add_argument("--closure-judge-every", type=int, default=2000,
+                    help="closure workload: coarse steps between judged fine segments")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large", "closure"],
                     help="ensemble: the 48-member batched ensemble as the headline line; "
                          "large: one 1024^2x513 instance, Ra 1e7, Q 1e4, eta contrast 50 (split)")
     ap.add_argument("--no-e2e", action="store_true",
@@ -386,6 +429,15 @@ def main():
     torch.cuda.set_device(local)
     from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
     hbm, pk = peaks()
+    if args.workload == "closure":
+        line = closure_line(args, ws)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if _dist["on"]:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.workload == "ensemble":
         e = ensemble_line(args, ws, hbm, pk)
         line = {"metric": "aggregate grid-point-steps/s, 48-instance ensemble", "value": e["value"],

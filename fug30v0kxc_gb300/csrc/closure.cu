@@ -80,6 +80,8 @@ struct vec_closure {
     double *rho0f = nullptr, *t0f = nullptr;    // fine background profiles (allocated per fine nz)
     int nzf_bg = 0;
     vec_params pc;                   // coarse parameters
+    float clip = 4.0f;               // |normalised output| limit at inference
+    float gain = 1.0f;               // scale of the applied correction
 };
 
 // ---- background profiles: T0 = 1 + theta z, rho0 = T0^m (src/initial.F90:49-58)
@@ -418,14 +420,19 @@ __global__ void k_pack_state(const double *u, const double *v, const double *w, 
 
 // denormalised network output -> hydro corrections (history rows r, t, u, v,
 // w) and the real-space dB/dt correction (3 arrays)
+// (the normalised output is limited to +-clip standard deviations of the
+// training targets and the correction scaled by gain)
 template <typename R>
-__global__ void k_corr_split(const float *out, const float *nrm, size_t n, R *corr, R *bd)
+__global__ void k_corr_split(const float *out, const float *nrm, size_t n, R *corr, R *bd, float clip, float gain)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float v[8];
 #pragma unroll
-    for (int c = 0; c < 8; c++) v[c] = out[i * 8 + c] * nrm[24 + c] + nrm[16 + c];
+    for (int c = 0; c < 8; c++) {
+        const float o = fminf(fmaxf(out[i * 8 + c], -clip), clip);
+        v[c] = gain * (o * nrm[24 + c] + nrm[16 + c]);
+    }
     corr[0 * n + i] = (R)v[3];   // rho
     corr[1 * n + i] = (R)v[4];   // T
     corr[2 * n + i] = (R)v[0];   // u
@@ -505,11 +512,11 @@ int closure_apply_corr(Engine *E)
 }
 
 template <typename R>
-static int corr_from_out(Engine &E, const float *out, const float *nrm)
+static int corr_from_out(Engine &E, const float *out, const float *nrm, float clip, float gain)
 {
     R *corr = (R *)E.corr;
     R *bd = corr + 7 * E.n;
-    KLAUNCH((&E), "closure_corr", k_corr_split<R>, nblk(E.n), TPB, out, nrm, E.n, corr, bd);
+    KLAUNCH((&E), "closure_corr", k_corr_split<R>, nblk(E.n), TPB, out, nrm, E.n, corr, bd, clip, gain);
     if (!mag_on(E)) return VEC_OK;
     R *ex = bd, *ey = bd + E.n, *ez = bd + 2 * E.n;
     int st;
@@ -566,6 +573,12 @@ __global__ void k_zinterp(double *f, size_t np, int nzf, int r)
         v += l * f[(size_t)(m0 + a) * r * np + q];
     }
     f[idx] = v;
+}
+
+__global__ void k_floor(double *r, size_t n, double lo)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && r[i] < lo) r[i] = lo;
 }
 
 // one FP64 field of C upsampled into the FP64 array dst of F (nz_f planes)
@@ -655,6 +668,33 @@ extern "C" int vec_closure_create(const vec_params *coarse, int factor, int capa
 }
 
 extern "C" vec_net *vec_closure_net(vec_closure *cl) { return cl ? cl->net : nullptr; }
+
+extern "C" int vec_closure_set_output(vec_closure *cl, float clip, float gain)
+{
+    if (!cl || !(clip > 0.0f) || !(gain >= 0.0f)) return VEC_ERR_ARG;
+    cl->clip = clip;
+    cl->gain = gain;
+    return VEC_OK;
+}
+
+// Nusselt number at the fixed-temperature top: the reference's formula
+// (src/dbydz.F90:4877-4925) with the one-sided derivative mirrored to the
+// top plane, (-11 T0 + 18 T1 - 9 T2 + 2 T3) / (6 dz); with a fixed-flux
+// bottom the reference's own (bottom) Nusselt number is identically one
+extern "C" int vec_top_nusselt(vec_ctx *c, double *nu)
+{
+    if (!c || !nu) return VEC_ERR_ARG;
+    Engine &E = engine_of(c);
+    std::vector<double> h(4 * E.np);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), E.t, sizeof(double) * 4 * E.np, cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    double s = 0.0;
+    for (size_t q = 0; q < E.np; q++)
+        s += (-11.0 * h[q] + 18.0 * h[E.np + q] - 9.0 * h[2 * E.np + q] + 2.0 * h[3 * E.np + q]) / (6.0 * E.k.dz);
+    s /= (double)E.np;
+    *nu = (s - E.k.nusstmp) / (E.k.theta - E.k.nusstmp);
+    return VEC_OK;
+}
 extern "C" int vec_closure_npairs(vec_closure *cl) { return cl ? cl->npairs : 0; }
 
 // synchronise s1 after s0
@@ -883,7 +923,8 @@ extern "C" int vec_closure_infer(vec_closure *cl, vec_ctx *coarse)
     N->g = g0;
     if (st) return st;
     if ((st = join(N->stream, E.stream))) return st;
-    st = E.split ? corr_from_out<float>(E, N->out, cl->nrm) : corr_from_out<double>(E, N->out, cl->nrm);
+    st = E.split ? corr_from_out<float>(E, N->out, cl->nrm, cl->clip, cl->gain)
+                 : corr_from_out<double>(E, N->out, cl->nrm, cl->clip, cl->gain);
     if (st) return st;
     return join(E.stream, N->stream);
 }
@@ -934,6 +975,9 @@ extern "C" int vec_upsample(vec_ctx *coarse, vec_ctx *fine)
     double *dst[8] = { F.u, F.v, F.w, F.r, F.t, F.bx, F.by, F.bz };
     for (int f = 0; f < 8; f++)
         if ((st = upsample_field(Cc, F, src[f], dst[f], r, 1))) return st;
+    // the density floor of the AB3 update (src/main.F90:438-442) on the
+    // interpolated density, whose spectral interpolation can undershoot
+    KLAUNCH((&F), "upsample_floor", k_floor, nblk(F.n), TPB, F.r, F.n, 0.05);
     F.bzbar = Cc.bzbar;
     F.b32_auth = 0;
     if (mag_on(F) && (st = phys_mag_init(&F))) return st;
@@ -956,65 +1000,135 @@ extern "C" int vec_upsample(vec_ctx *coarse, vec_ctx *fine)
 // t_end; every `every` steps the current coarse state is upsampled into
 // `fine` and the plain fine solver runs `nfine` steps; when the coarse run
 // reaches that segment's end time its diagnostics are compared with the
-// fine ones, and if the Nusselt number, kinetic or magnetic energy differs
-// by more than tol (relative) the run continues on the fine solver to t_end.
+// fine ones, and if the Nusselt number (at the bottom, as the reference, and
+// at the top), kinetic or magnetic energy differs by more than tol
+// (relative), the coarse state fails the div B check, or the coarse run
+// stops advancing, the run continues on the fine solver to t_end.  The fine
+// context always holds the state the fall-back continues from: the
+// upsampled start of the run, then the end of the last judged segment.
+// With diag_every > 0, rows (time, Nu, kinetic energy, magnetic energy,
+// top Nu) of the running solver are appended to series every diag_every
+// steps (at most cap rows).
 extern "C" int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, double t_end, int every, int nfine,
-                               double tol, vec_closure_report *rep)
+                               double tol, int diag_every, double *series, int cap, vec_closure_report *rep)
 {
     if (!cl || !coarse || !fine || every <= 0 || nfine <= 0 || !rep) return VEC_ERR_ARG;
     memset(rep, 0, sizeof(*rep));
     rep->fallback_step = -1;
     int st;
+    // diagnostics of c (+ the top Nusselt number); the div B check of
+    // src/main.F90:583-590 failing is reported through *divb, not as an error
+    auto diag = [&](vec_ctx *c, vec_diag_out *d, double *nutop, int *divb) -> int {
+        int e = vec_diag(c, d);
+        if (e == VEC_ERR_DIVB) { *divb = 1; e = VEC_OK; }
+        if (e) return e;
+        return vec_top_nusselt(c, nutop);
+    };
+    auto record = [&](vec_ctx *c, int *divb) -> int {
+        if (diag_every <= 0 || !series || rep->nseries >= cap) return VEC_OK;
+        vec_diag_out d;
+        vec_scalars s;
+        double nt = 0.0;
+        int e = diag(c, &d, &nt, divb);
+        if (e) return e;
+        if ((e = vec_get_scalars(c, &s))) return e;
+        double *row = series + 5 * (size_t)rep->nseries;
+        row[0] = s.ttime; row[1] = d.nusselt; row[2] = d.kenergy; row[3] = d.menergy; row[4] = nt;
+        rep->nseries += 1;
+        return VEC_OK;
+    };
+    // a run makes progress while its time advances by finite steps not
+    // below 1e-3 of its first, within 100 times the step count that first
+    // step implies
+    struct Progress {
+        double t_prev, dt0, t0;
+        long long n;
+        bool ok(const vec_scalars &s, double t_end)
+        {
+            if (!(isfinite(s.ttime) && isfinite(s.dt) && s.dt > 0.0)) return false;
+            if (n == 0) { dt0 = s.dt; t0 = s.ttime; t_prev = s.ttime; n = 1; return true; }
+            const bool adv = s.ttime > t_prev && s.dt > 1e-3 * dt0;
+            const bool cap = (double)n < 100.0 * (t_end - t0) / dt0 + 1000.0;
+            t_prev = s.ttime;
+            n += 1;
+            return adv && cap;
+        }
+    };
+    // the fine solver continues to t_end from the last state it holds
+    auto fall_back = [&](long long at) -> int {
+        rep->fallback_step = at;
+        int e;
+        if ((e = vec_closure_attach(cl, coarse, 0))) return e;
+        vec_scalars sf;
+        long long fs = 0;
+        int ignore = 0;
+        Progress pf = { 0.0, 0.0, 0.0, 0 };
+        for (;;) {
+            if ((e = vec_get_scalars(fine, &sf))) return e;
+            if (sf.ttime >= t_end) break;
+            if (!pf.ok(sf, t_end)) {
+                vec_set_error("closure run: the fine solver stopped advancing (t = %g, dt = %g)", sf.ttime, sf.dt);
+                return VEC_ERR_NAN;
+            }
+            if ((e = vec_step(fine, 1))) return e;
+            rep->fine_steps += 1;
+            fs += 1;
+            if (diag_every > 0 && fs % diag_every == 0 && (e = record(fine, &ignore))) return e;
+        }
+        rep->end_time = sf.ttime;
+        return VEC_OK;
+    };
     if ((st = vec_closure_attach(cl, coarse, 1))) return st;
+    if ((st = vec_upsample(coarse, fine))) return st;   // the fall-back start until the first judge
     vec_scalars sc;
     vec_diag_out dfine, dc;
+    double nutf = 0.0, nutc = 0.0;
     int pending = 0;
     double t_check = 0.0;
     long long step = 0;
+    Progress pc = { 0.0, 0.0, 0.0, 0 };
+    auto rel = [](double a, double b) { return fabs(a - b) / fmax(fabs(b), 1e-300); };
     for (;;) {
         if ((st = vec_get_scalars(coarse, &sc))) return st;
         if (sc.ttime >= t_end) break;
+        if (!pc.ok(sc, t_end)) {
+            rep->blowup = 1;
+            return fall_back(step);
+        }
         if (pending && sc.ttime >= t_check) {
-            if ((st = vec_diag(coarse, &dc))) return st;
-            const double e0 = fabs(dc.nusselt - dfine.nusselt) / fmax(fabs(dfine.nusselt), 1e-300);
-            const double e1 = fabs(dc.kenergy - dfine.kenergy) / fmax(fabs(dfine.kenergy), 1e-300);
-            const double e2 = mag_on(engine_of(coarse))
-                                  ? fabs(dc.menergy - dfine.menergy) / fmax(fabs(dfine.menergy), 1e-300)
-                                  : 0.0;
+            int divb = 0;
+            if ((st = diag(coarse, &dc, &nutc, &divb))) return st;
+            const double e0 = fmax(rel(dc.nusselt, dfine.nusselt), rel(nutc, nutf));
+            const double e1 = rel(dc.kenergy, dfine.kenergy);
+            const double e2 = mag_on(engine_of(coarse)) ? rel(dc.menergy, dfine.menergy) : 0.0;
             rep->judges += 1;
             rep->last_err[0] = e0; rep->last_err[1] = e1; rep->last_err[2] = e2;
             rep->max_err[0] = fmax(rep->max_err[0], e0);
             rep->max_err[1] = fmax(rep->max_err[1], e1);
             rep->max_err[2] = fmax(rep->max_err[2], e2);
             pending = 0;
-            if (e0 > tol || e1 > tol || e2 > tol) {
-                // fall back: the fine run continues from a fresh upsampling
-                rep->fallback_step = step;
-                if ((st = vec_closure_attach(cl, coarse, 0))) return st;
-                if ((st = vec_upsample(coarse, fine))) return st;
-                vec_scalars sf;
-                for (;;) {
-                    if ((st = vec_get_scalars(fine, &sf))) return st;
-                    if (sf.ttime >= t_end) break;
-                    if ((st = vec_step(fine, 1))) return st;
-                    rep->fine_steps += 1;
-                }
-                rep->end_time = sf.ttime;
-                return VEC_OK;
-            }
+            if (divb) rep->divb_fail = 1;
+            if (divb || e0 > tol || e1 > tol || e2 > tol) return fall_back(step);
         }
         if (!pending && step > 0 && step % every == 0) {
             if ((st = vec_upsample(coarse, fine))) return st;
             if ((st = vec_step(fine, nfine))) return st;
             rep->fine_steps += nfine;
             vec_scalars sf;
-            if ((st = vec_get_scalars(fine, &sf)) || (st = vec_diag(fine, &dfine))) return st;
+            int ignore = 0;
+            if ((st = vec_get_scalars(fine, &sf)) || (st = diag(fine, &dfine, &nutf, &ignore))) return st;
             t_check = sf.ttime;
             pending = 1;
         }
         if ((st = vec_closure_step(cl, coarse, 1))) return st;
         step += 1;
         rep->coarse_steps += 1;
+        int divb = 0;
+        if (diag_every > 0 && step % diag_every == 0 && (st = record(coarse, &divb))) return st;
+        if (divb) {
+            rep->divb_fail = 1;
+            return fall_back(step);
+        }
     }
     rep->end_time = sc.ttime;
     return vec_closure_attach(cl, coarse, 0);

@@ -638,3 +638,51 @@ extern "C" int vec_net_adam(vec_net *N, float lr)
     CUDA_TRY(cudaStreamSynchronize(N->stream));
     return VEC_OK;
 }
+
+// device time of `reps` forward passes and of `reps` training steps (forward,
+// backward, Adam with rate 0: the parameters stay, the moments move) on the
+// current batch buffers, CUDA events on the network stream; flops_*: the
+// floating-point operations executed per pass (padded channels included)
+extern "C" int vec_net_time(vec_net *N, int reps, float *ms_fwd, float *ms_train, double *flops_fwd,
+                            double *flops_train)
+{
+    if (!N || reps <= 0) return VEC_ERR_ARG;
+    cudaEvent_t a, b, c;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    CUDA_TRY(cudaEventCreate(&c));
+    int st = net_forward(N);   // warm-up
+    if (!st) {
+        cudaEventRecord(a, N->stream);
+        for (int i = 0; i < reps && !st; i++) st = net_forward(N);
+        cudaEventRecord(b, N->stream);
+        for (int i = 0; i < reps && !st; i++) {
+            if ((st = net_forward(N))) break;
+            if ((st = net_backward(N, N->tgt))) break;
+            st = net_adam(N, 0.0f);
+        }
+        cudaEventRecord(c, N->stream);
+        cudaEventSynchronize(c);
+    }
+    float t1 = 0, t2 = 0;
+    if (!st) {
+        cudaEventElapsedTime(&t1, a, b);
+        cudaEventElapsedTime(&t2, b, c);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaEventDestroy(c);
+    if (st) return st;
+    const double P = (double)N->g.nb * (double)N->npts;
+    double fwd = 0.0, dg = 0.0;
+    for (int l = 0; l < 4; l++) {
+        const double f = 2.0 * NTAP * LCI[l] * LCO[l] * P;
+        fwd += f;
+        if (l > 0) dg += f;
+    }
+    if (ms_fwd) *ms_fwd = t1 / reps;
+    if (ms_train) *ms_train = t2 / reps;
+    if (flops_fwd) *flops_fwd = fwd;
+    if (flops_train) *flops_train = 2.0 * fwd + dg;   // forward + weight gradients + input gradients
+    return VEC_OK;
+}

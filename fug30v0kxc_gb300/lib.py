@@ -80,6 +80,8 @@ SIGNATURES = {
     "vec_net_forward": (C.c_int, [_vp, _dp, _dp]),
     "vec_net_backward": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
     "vec_net_adam": (C.c_int, [_vp, C.c_float]),
+    "vec_net_time": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double),
+                               C.POINTER(C.c_double)]),
     "vec_closure_create": (C.c_int, [C.POINTER(VecParams), C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),
     "vec_closure_destroy": (C.c_int, [_vp]),
     "vec_closure_net": (_vp, [_vp]),
@@ -95,8 +97,10 @@ SIGNATURES = {
     "vec_closure_attach": (C.c_int, [_vp, _vp, C.c_int]),
     "vec_closure_infer": (C.c_int, [_vp, _vp]),
     "vec_closure_step": (C.c_int, [_vp, _vp, C.c_int]),
-    "vec_closure_run": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, C.c_double,
+    "vec_closure_run": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int,
                                   C.POINTER(VecClosureReport)]),
+    "vec_closure_set_output": (C.c_int, [_vp, C.c_float, C.c_float]),
+    "vec_top_nusselt": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "vec_expand": (C.c_int, [_vp, _vp, _dp, _dp]),
     "vec_upsample": (C.c_int, [_vp, _vp]),
     "vec_nc_write": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int]),

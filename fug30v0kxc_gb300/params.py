@@ -160,7 +160,8 @@ class VecClosureReport(C.Structure):
     """include/vec.h vec_closure_report."""
     _fields_ = [("judges", C.c_int32), ("pad_", C.c_int32), ("coarse_steps", C.c_int64),
                 ("fine_steps", C.c_int64), ("fallback_step", C.c_int64), ("last_err", C.c_double * 3),
-                ("max_err", C.c_double * 3), ("end_time", C.c_double)]
+                ("max_err", C.c_double * 3), ("end_time", C.c_double), ("nseries", C.c_int32),
+                ("divb_fail", C.c_int32), ("blowup", C.c_int32), ("pad2_", C.c_int32)]
 
 
 class VecSnapshot(C.Structure):

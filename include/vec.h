@@ -277,6 +277,10 @@ int vec_net_forward(vec_net *net, const float *x, float *out);
  * the gradient of every parameter */
 int vec_net_backward(vec_net *net, const float *tgt, double *loss);
 int vec_net_adam(vec_net *net, float lr);
+/* device time of reps forward passes and of reps training steps (Adam with
+ * rate 0) on the current batch, and the floating-point operations each
+ * executes (padded channels included) */
+int vec_net_time(vec_net *net, int reps, float *ms_fwd, float *ms_train, double *flops_fwd, double *flops_train);
 
 /* ---- learned closure: coupling to the solver ----------------------------
  * No reference counterpart.  A closure works on a coarse grid r times
@@ -294,6 +298,11 @@ typedef struct {
     double last_err[3];     /* relative error of Nu, kinetic, magnetic energy */
     double max_err[3];
     double end_time;
+    int nseries;            /* rows written to the diagnostics series */
+    int divb_fail;          /* the coarse run failed the div B check (a fall-back cause) */
+    int blowup;             /* the coarse run stopped advancing: non-finite time or step,
+                             * or a step below 1e-3 of its first (a fall-back cause) */
+    int pad2_;
 } vec_closure_report;
 /* coarse: the coarse parameters; capacity: training pairs stored (FP32,
  * 64 bytes per coarse point and pair); batch <= 64 */
@@ -301,6 +310,14 @@ int vec_closure_create(const vec_params *coarse, int factor, int capacity, int b
                        vec_closure **out);
 int vec_closure_destroy(vec_closure *cl);
 vec_net *vec_closure_net(vec_closure *cl);
+/* at inference the normalised network output is limited to +-clip
+ * standard deviations of the training targets and the correction scaled by
+ * gain (defaults 4 and 1) */
+int vec_closure_set_output(vec_closure *cl, float clip, float gain);
+/* Nusselt number at the fixed-temperature top (the formula of
+ * src/dbydz.F90:4877-4925 mirrored to the top plane); with a fixed-flux
+ * bottom the reference's own Nusselt number is identically one */
+int vec_top_nusselt(vec_ctx *ctx, double *nu);
 int vec_closure_npairs(vec_closure *cl);
 /* coarse context state = box-filtered fine state (then pol/tor, B and the
  * boundary conditions as after a time step) */
@@ -327,11 +344,19 @@ int vec_closure_infer(vec_closure *cl, vec_ctx *coarse);
 /* nsteps steps, the correction recomputed before each */
 int vec_closure_step(vec_closure *cl, vec_ctx *coarse, int nsteps);
 /* judged run to time t_end: every `every` coarse steps a plain fine segment
- * of nfine steps from the upsampled coarse state; if Nu, kinetic or
- * magnetic energy of the coarse run at the segment's end time differ by more
- * than tol (relative), the run continues on the fine solver */
+ * of nfine steps from the upsampled coarse state; if the Nusselt numbers
+ * (bottom and top), kinetic or magnetic energy of the coarse run at the
+ * segment's end time differ by more than tol (relative), or the coarse
+ * state fails the div B check of src/main.F90:583-590, or the coarse run
+ * stops advancing (non-finite time or step, or a step below 1e-3 of its
+ * first), the run continues on the fine solver from the last state it holds
+ * -- the upsampled start of the run, then the end of the last judged
+ * segment -- (returning VEC_ERR_NAN if that stops advancing too).  With
+ * diag_every > 0, rows (time, Nu, kinetic energy, magnetic energy, top Nu)
+ * of the running solver are appended to series[cap][5] every diag_every
+ * steps. */
 int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, double t_end, int every, int nfine, double tol,
-                    vec_closure_report *rep);
+                    int diag_every, double *series, int cap, vec_closure_report *rep);
 
 /* ---- spectral upsampling (interpolate/fft.F90:834-927) -------------------- */
 /* the reference's expand: in (nx, ny, nz) of coarse -> out (r nx, r ny, nz)

@@ -149,3 +149,14 @@ def test_judged_run_fallback():
     rep2 = cl.run(c2, f, t1 + 30 * c2.scalars().dt, every=5, nfine=10, tol=1e12)
     assert rep2["judges"] >= 1 and rep2["fallback_step"] == -1
     cl.close()
+
+
+def test_top_nusselt_of_conductive_state():
+    """T = 1 + theta z (the conductive profile) has top Nusselt number 1."""
+    from fug30v0kxc_gb300.closure import top_nusselt
+    p = convection_params(32, 32, 9, precision=VEC_PREC_FP64)
+    g = P3D(p)
+    g.start()
+    z = np.arange(9) / 8.0
+    g.set("t", np.broadcast_to((1.0 + p.theta * z)[:, None, None], g.shape).copy())
+    assert abs(top_nusselt(g) - 1.0) < 1e-12
