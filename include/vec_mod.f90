@@ -209,5 +209,52 @@ module vec_mod
       type(c_ptr), value :: ctx
       character(kind=c_char), dimension(*), intent(in) :: path
     end function
+    ! additions without a reference counterpart: graphs, ensembles, the
+    ! interpolate step (interpolate/fft.F90:834-927)
+    integer(c_int) function vec_use_graphs(ctx, on) bind(C, name='vec_use_graphs')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function vec_ensemble_create(ps, n, ens) bind(C, name='vec_ensemble_create')
+      import :: c_int, c_ptr, vec_params
+      type(vec_params), dimension(*), intent(in) :: ps
+      integer(c_int), value :: n
+      type(c_ptr), intent(out) :: ens
+    end function
+    integer(c_int) function vec_ensemble_destroy(ens) bind(C, name='vec_ensemble_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ens
+    end function
+    type(c_ptr) function vec_ensemble_member(ens, i) bind(C, name='vec_ensemble_member')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ens
+      integer(c_int), value :: i
+    end function
+    integer(c_int) function vec_ensemble_start(ens) bind(C, name='vec_ensemble_start')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ens
+    end function
+    integer(c_int) function vec_ensemble_step(ens, nsteps) bind(C, name='vec_ensemble_step')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ens
+      integer(c_int), value :: nsteps
+    end function
+    integer(c_int) function vec_ensemble_tune(ens, steps, cache) bind(C, name='vec_ensemble_tune')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: ens
+      integer(c_int), value :: steps
+      character(kind=c_char), dimension(*), intent(in) :: cache
+    end function
+    integer(c_int) function vec_expand(coarse, fine, fin, fout) bind(C, name='vec_expand')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: coarse, fine
+      real(c_double), dimension(*), intent(in) :: fin
+      real(c_double), dimension(*), intent(out) :: fout
+    end function
+    integer(c_int) function vec_upsample(coarse, fine) bind(C, name='vec_upsample')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: coarse, fine
+    end function
   end interface
 end module vec_mod
