@@ -262,6 +262,47 @@ def closure_line(args, ws):
             "closure": r}
 
 
+def net_line(args, ws):
+    """The closure network alone: forward pass and training step (forward,
+    input and weight gradients, Adam) on a seeded synthetic batch of 8 at
+    the coarse grid of the closure workload (128^2x65; --grid overrides),
+    CUDA events on the network's stream."""
+    import numpy as np
+    from fug30v0kxc_gb300.closure import Net
+    nx, ny, nz = (int(v) for v in args.grid.split(",")) if args.grid else (128, 128, 65)
+    nb = 8
+    net = Net(nx, ny, nz, nb, seed=1)
+    rng = np.random.default_rng(0)
+    x = np.zeros((nb, nz, ny, nx, 16), np.float32)
+    x[..., :9] = rng.standard_normal((nb, nz, ny, nx, 9))
+    net.forward(x)
+    net.backward(rng.standard_normal((nb, nz, ny, nx, 8)).astype(np.float32))
+    net.time(args.warmup)
+    l0 = net.launch_count()
+    ms_f, ms_t, fl_f, fl_t = net.time(args.steps)
+    launches = net.launch_count() - l0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, pk = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, pk = 1900.0, "fallback"
+    ach = fl_t / ms_t * 1e-9
+    pts = nb * nx * ny * nz
+    net.close()
+    return {"metric": "closure network training steps/s (batch 8)", "value": 1e3 / ms_t, "unit": "steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic (seeded normal inputs and targets)",
+            "config": {"workload": "closure network 4x Conv3d 3x3x3, 16-32-32-32-16 channels, batch 8, %dx%dx%d"
+                                   % (nx, ny, nz), "points_per_batch": pts,
+                       "l2": "no flush: one activation buffer is %.2f GB" % (pts * 2 * 32 / 1e9)},
+            "roofline": {"bound": "tensor", "kernel": "training step (conv forward, input and weight gradients)",
+                         "achieved": round(ach, 2), "peak": peak, "peak_kind": pk, "unit": "TFLOP/s",
+                         "frac": round(ach / peak, 4), "traffic": None},
+            "forward": {"ms": ms_f, "tflops": fl_f / ms_f * 1e-9, "frac": fl_f / ms_f * 1e-9 / peak},
+            "gpu_launches": launches}
+
+
 def cpu_baseline(nsteps, precision_note=""):
     """The oracle (plain C restatement, OpenMP over planes) on the host cores."""
     from oracle import oracle as O
@@ -389,7 +430,7 @@ def main():
                     help="closure workload: model time the coarse solver develops convection before the DNS")
     ap.add_argument("--closure-judge-every", type=int, default=2000,
                     help="closure workload: coarse steps between judged fine segments")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large", "closure"],
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large", "closure", "net"],
                     help="ensemble: the 48-member batched ensemble as the headline line; "
                          "large: one 1024^2x513 instance, Ra 1e7, Q 1e4, eta contrast 50 (split)")
     ap.add_argument("--no-e2e", action="store_true",
@@ -429,8 +470,8 @@ def main():
     torch.cuda.set_device(local)
     from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
     hbm, pk = peaks()
-    if args.workload == "closure":
-        line = closure_line(args, ws)
+    if args.workload in ("closure", "net"):
+        line = closure_line(args, ws) if args.workload == "closure" else net_line(args, ws)
         if rank == 0:
             print(json.dumps(line), flush=True)
         if _dist["on"]:

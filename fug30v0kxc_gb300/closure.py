@@ -71,6 +71,9 @@ class Net:
     def adam(self, lr=1e-3):
         self._chk(self.L.vec_net_adam(self.h, lr), "vec_net_adam")
 
+    def launch_count(self):
+        return int(self.L.vec_net_launch_count(self.h))
+
     def time(self, reps=10):
         """(ms per forward, ms per training step, flops per forward, flops per
         training step) on the current batch buffers."""

@@ -23,6 +23,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -78,16 +79,17 @@ struct TileAt {
     int q0;           // first point of the tile within the plane
 };
 
-__device__ __forceinline__ TileAt tile_at(const NetGeom &g, long long t)
+// tile t of tp points (g.R = tp / nx rows)
+__device__ __forceinline__ TileAt tile_at(const NetGeom &g, long long t, int tp = TP)
 {
-    const int tpp = g.nx * g.ny / TP;
+    const int tpp = g.nx * g.ny / tp;
     TileAt a;
     a.b = (int)(t / ((long long)g.nz * tpp));
     const int rem = (int)(t - (long long)a.b * g.nz * tpp);
     a.z = rem / tpp;
     const int tip = rem - a.z * tpp;
     a.y0 = tip * g.R;
-    a.q0 = tip * TP;
+    a.q0 = tip * tp;
     a.plane0 = ((size_t)a.b * g.nz + a.z) * (size_t)g.ny * g.nx;
     return a;
 }
@@ -122,7 +124,9 @@ __device__ __forceinline__ void load_halo(bf16 *h, const bf16 *src, const NetGeo
 // EPI_GATE: acc * gelu'(gate) -> o_act (BF16)      (input gradient)
 enum { EPI_ACT = 0, EPI_OUT = 1, EPI_GATE = 2 };
 
-template <int CIN, int COUT, int EPI>
+// MT m-tiles (16 MT points) per warp: a CTA tile is 128 MT points, and g.R
+// and g.tiles describe that tile
+template <int CIN, int COUT, int EPI, int MT>
 __global__ void __launch_bounds__(256, 1)
 k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
        bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
@@ -138,62 +142,77 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
         const int row = e / (CIN / 8), c = e % (CIN / 8);
         cp16(su32(ws + (size_t)row * CSI + c * 8), wt + (size_t)row * CIN + c * 8, true);
     }
-    const int yl = (16 * w) / g.nx, x0 = (16 * w) % g.nx;
     const int W2 = g.nx + 2, RR = g.R + 2;
+    int yl[MT], x0[MT];
+#pragma unroll
+    for (int m = 0; m < MT; m++) {
+        yl[m] = (16 * (MT * w + m)) / g.nx;
+        x0[m] = (16 * (MT * w + m)) % g.nx;
+    }
     for (long long t = blockIdx.x; t < g.tiles; t += gridDim.x) {
-        const TileAt a = tile_at(g, t);
+        const TileAt a = tile_at(g, t, TP * MT);
         __syncthreads();                      // previous tile's reads of hs are done
         load_halo<CIN>(hs, x, g, a);
         cp_wait_all();
         __syncthreads();
-        float acc[COUT / 8][4];
+        float acc[MT][COUT / 8][4];
 #pragma unroll
-        for (int j = 0; j < COUT / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        for (int m = 0; m < MT; m++)
+#pragma unroll
+            for (int j = 0; j < COUT / 8; j++) acc[m][j][0] = acc[m][j][1] = acc[m][j][2] = acc[m][j][3] = 0.0f;
         const int pa = (lane & 7) + ((lane >> 3) & 1) * 8, ca = (lane >> 4) * 8;    // A: point, channel
         const int nb_ = (lane & 7) + (lane >> 4) * 8, kb = ((lane >> 3) & 1) * 8;   // B: row n, column k
 #pragma unroll 1
         for (int tap = 0; tap < NTAP; tap++) {
             const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-            const int hrow = (dz * RR + yl + dy) * W2 + x0 + dx;
 #pragma unroll
             for (int kk = 0; kk < CIN / 16; kk++) {
-                uint32_t af[4];
-                ldsm4(su32(hs + (size_t)(hrow + pa) * CSI + kk * 16 + ca), af);
+                uint32_t af[MT][4];
+#pragma unroll
+                for (int m = 0; m < MT; m++) {
+                    const int hrow = (dz * RR + yl[m] + dy) * W2 + x0[m] + dx;
+                    ldsm4(su32(hs + (size_t)(hrow + pa) * CSI + kk * 16 + ca), af[m]);
+                }
 #pragma unroll
                 for (int np = 0; np < COUT / 16; np++) {
                     uint32_t bfr[4];
                     ldsm4(su32(ws + (size_t)(tap * COUT + np * 16 + nb_) * CSI + kk * 16 + kb), bfr);
-                    mma16816(acc[2 * np], af, bfr[0], bfr[1]);
-                    mma16816(acc[2 * np + 1], af, bfr[2], bfr[3]);
+#pragma unroll
+                    for (int m = 0; m < MT; m++) {
+                        mma16816(acc[m][2 * np], af[m], bfr[0], bfr[1]);
+                        mma16816(acc[m][2 * np + 1], af[m], bfr[2], bfr[3]);
+                    }
                 }
             }
         }
         // epilogue: c0,c1 at (row g, n 2t', 2t'+1), c2,c3 at row g+8
         const int gr = lane >> 2, tq = lane & 3;
 #pragma unroll
-        for (int j = 0; j < COUT / 8; j++) {
-            const int n = 8 * j + 2 * tq;
+        for (int m = 0; m < MT; m++)
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const size_t gp = a.plane0 + a.q0 + 16 * w + gr + 8 * h;
-                float v0 = acc[j][2 * h], v1 = acc[j][2 * h + 1];
-                if (EPI == EPI_ACT) {
-                    v0 += bias[n];
-                    v1 += bias[n + 1];
-                    *reinterpret_cast<__nv_bfloat162 *>(o_pre + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
-                    *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) =
-                        __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
-                } else if (EPI == EPI_OUT) {
-                    if (n < cout_real) o_f32[gp * cout_real + n] = v0 + bias[n];
-                    if (n + 1 < cout_real) o_f32[gp * cout_real + n + 1] = v1 + bias[n + 1];
-                } else {
-                    const __nv_bfloat162 gg = *reinterpret_cast<const __nv_bfloat162 *>(gate + gp * COUT + n);
-                    v0 *= gelu_d(__bfloat162float(gg.x));
-                    v1 *= gelu_d(__bfloat162float(gg.y));
-                    *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
+            for (int j = 0; j < COUT / 8; j++) {
+                const int n = 8 * j + 2 * tq;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const size_t gp = a.plane0 + a.q0 + 16 * (MT * w + m) + gr + 8 * h;
+                    float v0 = acc[m][j][2 * h], v1 = acc[m][j][2 * h + 1];
+                    if (EPI == EPI_ACT) {
+                        v0 += bias[n];
+                        v1 += bias[n + 1];
+                        *reinterpret_cast<__nv_bfloat162 *>(o_pre + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
+                        *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) =
+                            __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+                    } else if (EPI == EPI_OUT) {
+                        if (n < cout_real) o_f32[gp * cout_real + n] = v0 + bias[n];
+                        if (n + 1 < cout_real) o_f32[gp * cout_real + n + 1] = v1 + bias[n + 1];
+                    } else {
+                        const __nv_bfloat162 gg = *reinterpret_cast<const __nv_bfloat162 *>(gate + gp * COUT + n);
+                        v0 *= gelu_d(__bfloat162float(gg.x));
+                        v1 *= gelu_d(__bfloat162float(gg.y));
+                        *reinterpret_cast<__nv_bfloat162 *>(o_act + gp * COUT + n) = __floats2bfloat162_rn(v0, v1);
+                    }
                 }
             }
-        }
     }
 }
 
@@ -232,9 +251,10 @@ k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, floa
         }
         cp_wait_all();
         __syncthreads();
-        if (tid < CO) {
+        if (tid < 8 * CO) {   // bias: channel tid % CO over points tid / CO, +8, ...
             float s = 0.0f;
-            for (int p = 0; p < TP; p++) s += __bfloat162float(ds[(size_t)p * CSO + tid]);
+#pragma unroll 4
+            for (int p = tid / CO; p < TP; p += 8) s += __bfloat162float(ds[(size_t)p * CSO + tid % CO]);
             bsum += s;
         }
         const int pa = (lane & 7) + (lane >> 4) * 8, ca = ((lane >> 3) & 1) * 8;   // A^T: point, co
@@ -277,7 +297,17 @@ k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, floa
                     pp[((size_t)tap * CO + co) * CI + ci + 1] = acc[d][m][n][2 * h + 1];
                 }
     }
-    if (tid < CO) pp[NTAP * CO * CI + tid] = bsum;
+    // sum the eight point groups of each bias channel (hs is free now)
+    __syncthreads();
+    float *red = reinterpret_cast<float *>(hs);
+    if (tid < 8 * CO) red[tid] = bsum;
+    __syncthreads();
+    if (tid < CO) {
+        float b = 0.0f;
+#pragma unroll
+        for (int gq = 0; gq < 8; gq++) b += red[gq * CO + tid];
+        pp[NTAP * CO * CI + tid] = b;
+    }
 }
 
 // out[j] = sum over blocks of part[b][j]
@@ -351,7 +381,7 @@ __global__ void k_f32_to_bf16(const float *a, bf16 *b, size_t n)
     if (i < n) b[i] = __float2bfloat16_rn(a[i]);
 }
 
-template <int CIN, int COUT, int EPI>
+template <int CIN, int COUT>
 size_t conv_smem(const NetGeom &g)
 {
     return ((size_t)NTAP * COUT * (CIN + 8) + (size_t)3 * (g.R + 2) * (g.nx + 2) * (CIN + 8)) * sizeof(bf16);
@@ -363,22 +393,38 @@ size_t wgrad_smem(const NetGeom &g)
     return ((size_t)3 * (g.R + 2) * (g.nx + 2) * (CI + 8) + (size_t)TP * (CO + 8)) * sizeof(bf16);
 }
 
+template <int CIN, int COUT, int EPI, int MT>
+int run_conv_mt(vec_net *N, const NetGeom &gt, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre,
+                bf16 *o_act, float *o_f32, int cout_real, const bf16 *gate)
+{
+    const size_t sm = conv_smem<CIN, COUT>(gt);
+    static bool set = false;
+    if (!set) {
+        CUDA_TRY(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      200 * 1024));
+        set = true;
+    }
+    long long grid = N->num_sms;
+    if (grid > gt.tiles) grid = gt.tiles;
+    k_conv<CIN, COUT, EPI, MT><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, gt, o_pre, o_act, o_f32, cout_real,
+                                                                  gate);
+    N->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+// CTA tiles of 256 points (two m-tiles per warp) where the plane divides
+// into them and their halo fits, else 128
 template <int CIN, int COUT, int EPI>
 int run_conv(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre, bf16 *o_act, float *o_f32,
              int cout_real, const bf16 *gate)
 {
-    const size_t sm = conv_smem<CIN, COUT, EPI>(N->g);
-    static bool set = false;
-    if (!set) {
-        CUDA_TRY(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        set = true;
-    }
-    long long grid = N->num_sms;
-    if (grid > N->g.tiles) grid = N->g.tiles;
-    k_conv<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real, gate);
-    N->launches++;
-    CUDA_TRY(cudaGetLastError());
-    return VEC_OK;
+    NetGeom g2 = N->g;
+    g2.R = 2 * TP / g2.nx;
+    g2.tiles = (long long)g2.nb * g2.nz * (g2.nx * g2.ny / (2 * TP));
+    if (N->conv_mt == 2 && (g2.nx * g2.ny) % (2 * TP) == 0 && conv_smem<CIN, COUT>(g2) <= 200 * 1024)
+        return run_conv_mt<CIN, COUT, EPI, 2>(N, g2, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
+    return run_conv_mt<CIN, COUT, EPI, 1>(N, N->g, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
 }
 
 template <int CI, int CO>
@@ -515,6 +561,10 @@ extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long l
     N->g.tiles = (long long)batch * nz * (nx * ny / TP);
     N->npts = (size_t)nx * ny * nz;
     N->cout_real = 8;
+    {
+        const char *e = getenv("VEC_NET_MT");
+        N->conv_mt = (e && e[0] == '1') ? 1 : 2;
+    }
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&N->num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -686,3 +736,6 @@ extern "C" int vec_net_time(vec_net *N, int reps, float *ms_fwd, float *ms_train
     if (flops_train) *flops_train = 2.0 * fwd + dg;   // forward + weight gradients + input gradients
     return VEC_OK;
 }
+
+// kernels launched by the network since creation
+extern "C" long long vec_net_launch_count(vec_net *N) { return N ? N->launches : 0; }

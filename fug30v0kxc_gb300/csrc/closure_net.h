@@ -15,6 +15,7 @@ struct vec_net {
     size_t npts = 0;        // nx * ny * nz
     int cout_real = 8;      // output channels (padded to 16 inside)
     int num_sms = 152;
+    int conv_mt = 2;        // m-tiles per warp in the convolution kernels (VEC_NET_MT=1: one)
     cudaStream_t stream = nullptr;
     int own_stream = 0;
     long long launches = 0;

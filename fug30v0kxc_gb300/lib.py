@@ -80,6 +80,7 @@ SIGNATURES = {
     "vec_net_forward": (C.c_int, [_vp, _dp, _dp]),
     "vec_net_backward": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
     "vec_net_adam": (C.c_int, [_vp, C.c_float]),
+    "vec_net_launch_count": (C.c_longlong, [_vp]),
     "vec_net_time": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double),
                                C.POINTER(C.c_double)]),
     "vec_closure_create": (C.c_int, [C.POINTER(VecParams), C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),

@@ -281,6 +281,8 @@ int vec_net_adam(vec_net *net, float lr);
  * rate 0) on the current batch, and the floating-point operations each
  * executes (padded channels included) */
 int vec_net_time(vec_net *net, int reps, float *ms_fwd, float *ms_train, double *flops_fwd, double *flops_train);
+/* kernels the network launched since creation */
+long long vec_net_launch_count(vec_net *net);
 
 /* ---- learned closure: coupling to the solver ----------------------------
  * No reference counterpart.  A closure works on a coarse grid r times
