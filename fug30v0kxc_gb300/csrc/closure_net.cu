@@ -125,9 +125,10 @@ __device__ __forceinline__ void load_halo(bf16 *h, const bf16 *src, const NetGeo
 enum { EPI_ACT = 0, EPI_OUT = 1, EPI_GATE = 2 };
 
 // MT m-tiles (16 MT points) per warp: a CTA tile is 128 MT points, and g.R
-// and g.tiles describe that tile
-template <int CIN, int COUT, int EPI, int MT>
-__global__ void __launch_bounds__(256, 1)
+// and g.tiles describe that tile.  KS warp groups of 8 split the 27 taps;
+// groups above the first hand their partial sums over through shared memory
+template <int CIN, int COUT, int EPI, int MT, int KS>
+__global__ void __launch_bounds__(256 * KS, 1)
 k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
        bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
        const bf16 *__restrict__ gate)
@@ -136,7 +137,8 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
     extern __shared__ __align__(128) unsigned char smem[];
     bf16 *ws = reinterpret_cast<bf16 *>(smem);               // [27][COUT][CSI]
     bf16 *hs = ws + (size_t)NTAP * COUT * CSI;               // halo
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, w = (tid >> 5) & 7, gk = tid >> 8;
+    const int tap0 = (NTAP * gk) / KS, tap1 = (NTAP * (gk + 1)) / KS;
 
     for (int e = tid; e < NTAP * COUT * (CIN / 8); e += blockDim.x) {
         const int row = e / (CIN / 8), c = e % (CIN / 8);
@@ -163,7 +165,7 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
         const int pa = (lane & 7) + ((lane >> 3) & 1) * 8, ca = (lane >> 4) * 8;    // A: point, channel
         const int nb_ = (lane & 7) + (lane >> 4) * 8, kb = ((lane >> 3) & 1) * 8;   // B: row n, column k
 #pragma unroll 1
-        for (int tap = 0; tap < NTAP; tap++) {
+        for (int tap = tap0; tap < tap1; tap++) {
             const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
 #pragma unroll
             for (int kk = 0; kk < CIN / 16; kk++) {
@@ -184,6 +186,32 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
                     }
                 }
             }
+        }
+        if (KS > 1) {
+            // the other groups' partial sums through shared memory (the halo
+            // is not read again before the next tile's barrier)
+            float *red = reinterpret_cast<float *>(hs);
+            __syncthreads();
+            if (gk > 0) {
+#pragma unroll
+                for (int m = 0; m < MT; m++)
+#pragma unroll
+                    for (int j = 0; j < COUT / 8; j++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++)
+                            red[((((size_t)(gk - 1) * 8 + w) * MT + m) * (COUT / 8) + j) * 128 + c * 32 + lane] =
+                                acc[m][j][c];
+            }
+            __syncthreads();
+            if (gk > 0) continue;
+            for (int q = 1; q < KS; q++)
+#pragma unroll
+                for (int m = 0; m < MT; m++)
+#pragma unroll
+                    for (int j = 0; j < COUT / 8; j++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++)
+                            acc[m][j][c] += red[((((size_t)(q - 1) * 8 + w) * MT + m) * (COUT / 8) + j) * 128 + c * 32 + lane];
         }
         // epilogue: c0,c1 at (row g, n 2t', 2t'+1), c2,c3 at row g+8
         const int gr = lane >> 2, tq = lane & 3;
@@ -220,8 +248,9 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
 // dW[tap][co][ci] = sum_p dY[p][co] X[p + d(tap)][ci], db[co] = sum_p dY[p][co].
 // Nine warps; warp w = 3 dz + dy owns the three taps (dz, dy, dx = -1..1).
 // Per-CTA partial sums go to part[block][27*CO*CI + CO].
-template <int CI, int CO>
-__global__ void __launch_bounds__(288, 1)
+// TPW taps per warp, 27 / TPW warps: warp w owns taps w TPW .. w TPW + TPW - 1
+template <int CI, int CO, int TPW>
+__global__ void __launch_bounds__(32 * (NTAP / TPW), 1)
 k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, float *__restrict__ part)
 {
     constexpr int CSI = CI + 8, CSO = CO + 8;
@@ -230,11 +259,10 @@ k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, floa
     const int W2 = g.nx + 2, RR = g.R + 2;
     bf16 *ds = hs + (size_t)3 * RR * W2 * CSI;              // [TP][CSO]
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int wz = w / 3, wy = w % 3;
 
-    float acc[3][CO / 16][CI / 8][4];
+    float acc[TPW][CO / 16][CI / 8][4];
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+    for (int d = 0; d < TPW; d++)
 #pragma unroll
         for (int m = 0; m < CO / 16; m++)
 #pragma unroll
@@ -266,8 +294,9 @@ k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, floa
 #pragma unroll
             for (int m = 0; m < CO / 16; m++) ldsm4t(su32(ds + (size_t)(16 * s + pa) * CSO + 16 * m + ca), af[m]);
 #pragma unroll
-            for (int d = 0; d < 3; d++) {
-                const int hrow = (wz * RR + yl + wy) * W2 + x0 + d;
+            for (int d = 0; d < TPW; d++) {
+                const int tap = TPW * w + d;
+                const int hrow = ((tap / 9) * RR + yl + (tap / 3) % 3) * W2 + x0 + tap % 3;
 #pragma unroll
                 for (int np = 0; np < CI / 16; np++) {
                     uint32_t bfr[4];
@@ -284,8 +313,8 @@ k_wgrad(const bf16 *__restrict__ x, const bf16 *__restrict__ dy, NetGeom g, floa
     float *pp = part + (size_t)blockIdx.x * (NTAP * CO * CI + CO);
     const int gr = lane >> 2, tq = lane & 3;
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const int tap = 3 * w + d;
+    for (int d = 0; d < TPW; d++) {
+        const int tap = TPW * w + d;
 #pragma unroll
         for (int m = 0; m < CO / 16; m++)
 #pragma unroll
@@ -393,21 +422,21 @@ size_t wgrad_smem(const NetGeom &g)
     return ((size_t)3 * (g.R + 2) * (g.nx + 2) * (CI + 8) + (size_t)TP * (CO + 8)) * sizeof(bf16);
 }
 
-template <int CIN, int COUT, int EPI, int MT>
+template <int CIN, int COUT, int EPI, int MT, int KS>
 int run_conv_mt(vec_net *N, const NetGeom &gt, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre,
                 bf16 *o_act, float *o_f32, int cout_real, const bf16 *gate)
 {
     const size_t sm = conv_smem<CIN, COUT>(gt);
     static bool set = false;
     if (!set) {
-        CUDA_TRY(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CUDA_TRY(cudaFuncSetAttribute(k_conv<CIN, COUT, EPI, MT, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       200 * 1024));
         set = true;
     }
     long long grid = N->num_sms;
     if (grid > gt.tiles) grid = gt.tiles;
-    k_conv<CIN, COUT, EPI, MT><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, gt, o_pre, o_act, o_f32, cout_real,
-                                                                  gate);
+    k_conv<CIN, COUT, EPI, MT, KS><<<(int)grid, 256 * KS, sm, N->stream>>>(x, wt, bias, gt, o_pre, o_act, o_f32,
+                                                                           cout_real, gate);
     N->launches++;
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;
@@ -422,28 +451,42 @@ int run_conv(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf16 
     NetGeom g2 = N->g;
     g2.R = 2 * TP / g2.nx;
     g2.tiles = (long long)g2.nb * g2.nz * (g2.nx * g2.ny / (2 * TP));
-    if (N->conv_mt == 2 && (g2.nx * g2.ny) % (2 * TP) == 0 && conv_smem<CIN, COUT>(g2) <= 200 * 1024)
-        return run_conv_mt<CIN, COUT, EPI, 2>(N, g2, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
-    return run_conv_mt<CIN, COUT, EPI, 1>(N, N->g, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
+    if (N->conv_mt == 2 && (g2.nx * g2.ny) % (2 * TP) == 0 && conv_smem<CIN, COUT>(g2) <= 200 * 1024) {
+        // two warp groups split the taps when the halo holds one group's partials
+        const size_t halo = (size_t)3 * (g2.R + 2) * (g2.nx + 2) * (CIN + 8) * sizeof(bf16);
+        if (halo >= (size_t)8 * 2 * (COUT / 8) * 128 * sizeof(float))
+            return run_conv_mt<CIN, COUT, EPI, 2, 2>(N, g2, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
+        return run_conv_mt<CIN, COUT, EPI, 2, 1>(N, g2, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
+    }
+    return run_conv_mt<CIN, COUT, EPI, 1, 1>(N, N->g, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
 }
 
-template <int CI, int CO>
-int run_wgrad(vec_net *N, const bf16 *x, const bf16 *dy, float *gout)
+// one warp per tap (27 warps) where its registers fit, else three taps per
+// warp (9 warps)
+template <int CI, int CO, int TPW>
+int run_wgrad_t(vec_net *N, const bf16 *x, const bf16 *dy, float *gout)
 {
     const size_t sm = wgrad_smem<CI, CO>(N->g);
     static bool set = false;
     if (!set) {
-        CUDA_TRY(cudaFuncSetAttribute(k_wgrad<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        CUDA_TRY(cudaFuncSetAttribute(k_wgrad<CI, CO, TPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         set = true;
     }
     long long grid = N->num_sms;
     if (grid > N->g.tiles) grid = N->g.tiles;
-    k_wgrad<CI, CO><<<(int)grid, 288, sm, N->stream>>>(x, dy, N->g, N->part);
+    k_wgrad<CI, CO, TPW><<<(int)grid, 32 * (NTAP / TPW), sm, N->stream>>>(x, dy, N->g, N->part);
     const int J = NTAP * CO * CI + CO;
     k_reduce_parts<<<(J + 255) / 256, 256, 0, N->stream>>>(N->part, (int)grid, J, gout);
     N->launches += 2;
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;
+}
+
+template <int CI, int CO>
+int run_wgrad(vec_net *N, const bf16 *x, const bf16 *dy, float *gout)
+{
+    if (N->conv_mt == 2) return run_wgrad_t<CI, CO, 1>(N, x, dy, gout);
+    return run_wgrad_t<CI, CO, 3>(N, x, dy, gout);
 }
 
 // the layers: (cin, cout) = (16,32), (32,32), (32,32), (32,16)
