@@ -244,6 +244,244 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
     }
 }
 
+// ---- forward / input gradient on the 5th-generation tensor cores ---------------------
+// For nx = 128 a tile is one row of 128 points: one M = 128 tcgen05.mma per
+// tap and 16-channel K step, accumulating in 32 TMEM columns.  Operands sit
+// in shared memory in the canonical K-major, non-swizzled layout (core
+// matrices of 8 rows x 16 bytes): the halo as [halo row][8-channel block]
+// [130 points][8 channels], so each tap's A operand is the same descriptor
+// shifted by (row, dx); the weights as [tap][8-channel block][n][8].  One
+// thread issues the 27 x CIN/16 MMAs and commits them to an mbarrier; the
+// four warps read the accumulator back with tcgen05.ld (warp w owns TMEM
+// lanes 32w..32w+31, i.e. points 32w..32w+31) and run the epilogue of
+// k_conv.  The halo is double-buffered: the next tile's copies run while
+// the MMAs of the current one execute.
+
+// shared-memory matrix descriptor: start, leading (K-direction) and stride
+// (M/N-direction) byte offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_sdesc(unsigned saddr, unsigned lbo, unsigned sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+           ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(unsigned tmem_d, uint64_t a, uint64_t b, uint32_t idesc, int accum)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accum)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_mbar_init(uint64_t *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// bounded wait on an mbarrier phase; false when the limit ran out
+__device__ __forceinline__ bool tc_mbar_wait(uint64_t *bar, unsigned parity)
+{
+    const unsigned a = su32(bar);
+    for (long it = 0; it < (1L << 24); it++) {
+        unsigned ok;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(ok)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <int NC>
+__device__ __forceinline__ void tmem_ld(unsigned taddr, float *v);
+template <>
+__device__ __forceinline__ void tmem_ld<32>(unsigned taddr, float *v)
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+template <>
+__device__ __forceinline__ void tmem_ld<16>(unsigned taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                 "[%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+constexpr int TC_W = 130;          // halo points per row (nx = 128 plus one each side)
+constexpr int TC_ROWS = 9;         // 3 planes x 3 rows
+constexpr int TC_TMEM_COLS = 32;
+
+// halo of row-tile a: [TC_ROWS][C/8][TC_W][8]
+template <int C>
+__device__ __forceinline__ void load_halo_tc(bf16 *h, const bf16 *src, const NetGeom &g, const TileAt &a)
+{
+    constexpr int C8 = C / 8;
+    for (int e = threadIdx.x; e < TC_ROWS * TC_W * C8; e += blockDim.x) {
+        const int c = e % C8;
+        const int pt = e / C8;
+        const int xi = pt % TC_W, row = pt / TC_W;
+        const int zz = a.z + row / 3 - 1;
+        int yy = a.y0 + row % 3 - 1;
+        yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
+        int xx = xi - 1;
+        xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+        const bool ok = zz >= 0 && zz < g.nz;
+        const size_t gp = ok ? ((((size_t)a.b * g.nz + zz) * g.ny + yy) * g.nx + xx) : 0;
+        cp16(su32(h + (((size_t)row * C8 + c) * TC_W + xi) * 8), src + gp * C + c * 8, ok);
+    }
+}
+
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t tc_halo_bytes() { return (size_t)TC_ROWS * TC_W * CIN * sizeof(bf16); }
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t tc_smem_bytes()
+{
+    // two halo buffers, the weights, then 4 KB of slack after the last operand
+    return 2 * tc_halo_bytes<CIN, COUT>() + (size_t)NTAP * COUT * CIN * sizeof(bf16) + 4096;
+}
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(128, 1)
+k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
+          bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
+          const bf16 *__restrict__ gate, int *err)
+{
+    constexpr int C8 = CIN / 8;
+    constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
+    extern __shared__ __align__(128) unsigned char smem[];
+    bf16 *hb[2];
+    hb[0] = reinterpret_cast<bf16 *>(smem);
+    hb[1] = hb[0] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);
+    bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [27][C8][COUT][8]
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int e = tid; e < NTAP * COUT * C8; e += blockDim.x) {
+        const int tap = e / (COUT * C8), r = e % (COUT * C8), n = r / C8, k8 = r % C8;
+        cp16(su32(ws + (((size_t)tap * C8 + k8) * COUT + n) * 8), wt + ((size_t)tap * COUT + n) * CIN + k8 * 8, true);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) tc_mbar_init(&bar);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_slot;
+
+    long long t = blockIdx.x;
+    if (t < g.tiles) load_halo_tc<CIN>(hb[0], x, g, tile_at(g, t, TP));
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    int it = 0;
+    bool failed = false;
+    for (; t < g.tiles; t += gridDim.x, it++) {
+        const TileAt a = tile_at(g, t, TP);
+        bf16 *cur = hb[it & 1];
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> async proxy
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned hbase = su32(cur), wbase = su32(ws);
+#pragma unroll 1
+            for (int tap = 0; tap < NTAP; tap++) {
+                const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+                for (int kk = 0; kk < CIN / 16; kk++) {
+                    const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_W) + dx) * 16),
+                                                   TC_W * 16, 128);
+                    const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16,
+                                                   128);
+                    umma_bf16(tmem, ad, bd, IDESC, (tap | kk) != 0);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar))
+                         : "memory");
+        }
+        // the next tile's halo goes to the other buffer, whose MMAs completed
+        // before the previous epilogue
+        if (t + gridDim.x < g.tiles) load_halo_tc<CIN>(hb[(it + 1) & 1], x, g, tile_at(g, t + gridDim.x, TP));
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        const bool ok = tc_mbar_wait(&bar, it & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(err, 2);
+            failed = true;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float v[COUT];
+        tmem_ld<COUT>(tmem + ((unsigned)(warp * 32) << 16), v);
+        const size_t gp = a.plane0 + a.q0 + warp * 32 + lane;
+        if (EPI == EPI_ACT) {
+            __align__(16) __nv_bfloat162 pr[COUT / 2], ac[COUT / 2];
+#pragma unroll
+            for (int n = 0; n < COUT; n += 2) {
+                const float v0 = v[n] + bias[n], v1 = v[n + 1] + bias[n + 1];
+                pr[n / 2] = __floats2bfloat162_rn(v0, v1);
+                ac[n / 2] = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+            }
+#pragma unroll
+            for (int q = 0; q < COUT / 8; q++) {
+                reinterpret_cast<uint4 *>(o_pre + gp * COUT)[q] = reinterpret_cast<const uint4 *>(pr)[q];
+                reinterpret_cast<uint4 *>(o_act + gp * COUT)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+            }
+        } else if (EPI == EPI_OUT) {
+            for (int n = 0; n < cout_real; n++) o_f32[gp * cout_real + n] = v[n] + bias[n];
+        } else {
+            __align__(16) __nv_bfloat162 gg[COUT / 2], ac[COUT / 2];
+#pragma unroll
+            for (int q = 0; q < COUT / 8; q++)
+                reinterpret_cast<uint4 *>(gg)[q] = reinterpret_cast<const uint4 *>(gate + gp * COUT)[q];
+#pragma unroll
+            for (int n = 0; n < COUT; n += 2)
+                ac[n / 2] = __floats2bfloat162_rn(v[n] * gelu_d(__bfloat162float(gg[n / 2].x)),
+                                                  v[n + 1] * gelu_d(__bfloat162float(gg[n / 2].y)));
+#pragma unroll
+            for (int q = 0; q < COUT / 8; q++)
+                reinterpret_cast<uint4 *>(o_act + gp * COUT)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (failed) tc_mbar_wait(&bar, it & 1);   // once more, bounded, before the accumulator is freed
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
 // ---- weight gradient ----------------------------------------------------------------------
 // dW[tap][co][ci] = sum_p dY[p][co] X[p + d(tap)][ci], db[co] = sum_p dY[p][co].
 // Nine warps; warp w = 3 dz + dy owns the three taps (dz, dy, dx = -1..1).
@@ -445,9 +683,30 @@ int run_conv_mt(vec_net *N, const NetGeom &gt, const bf16 *x, const bf16 *wt, co
 // CTA tiles of 256 points (two m-tiles per warp) where the plane divides
 // into them and their halo fits, else 128
 template <int CIN, int COUT, int EPI>
+int run_conv_tc(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre, bf16 *o_act, float *o_f32,
+                int cout_real, const bf16 *gate)
+{
+    constexpr size_t sm = tc_smem_bytes<CIN, COUT>();
+    static bool set = false;
+    if (!set) {
+        CUDA_TRY(cudaFuncSetAttribute(k_conv_tc<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        set = true;
+    }
+    long long grid = N->num_sms;
+    if (grid > N->g.tiles) grid = N->g.tiles;
+    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 128, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real,
+                                                                 gate, N->err);
+    N->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+template <int CIN, int COUT, int EPI>
 int run_conv(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf16 *o_pre, bf16 *o_act, float *o_f32,
              int cout_real, const bf16 *gate)
 {
+    if (N->conv_tc && N->g.nx == 128)
+        return run_conv_tc<CIN, COUT, EPI>(N, x, wt, bias, o_pre, o_act, o_f32, cout_real, gate);
     NetGeom g2 = N->g;
     g2.R = 2 * TP / g2.nx;
     g2.tiles = (long long)g2.nb * g2.nz * (g2.nx * g2.ny / (2 * TP));
@@ -580,7 +839,7 @@ extern "C" int vec_net_destroy(vec_net *N)
 {
     if (!N) return VEC_OK;
     if (N->stream) cudaStreamSynchronize(N->stream);
-    void *ps[] = { N->p, N->gr, N->m, N->v, N->x0, N->dout, N->out, N->tgt, N->part, N->loss_d, N->xin };
+    void *ps[] = { N->p, N->gr, N->m, N->v, N->x0, N->dout, N->out, N->tgt, N->part, N->loss_d, N->xin, N->err };
     for (void *q : ps) if (q) cudaFree(q);
     for (int l = 0; l < 4; l++) { if (N->wf[l]) cudaFree(N->wf[l]); if (N->wb[l]) cudaFree(N->wb[l]); }
     for (int l = 0; l < 3; l++) { if (N->pre[l]) cudaFree(N->pre[l]); if (N->act[l]) cudaFree(N->act[l]); }
@@ -607,6 +866,8 @@ extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long l
     {
         const char *e = getenv("VEC_NET_MT");
         N->conv_mt = (e && e[0] == '1') ? 1 : 2;
+        const char *t = getenv("VEC_NET_TC");
+        N->conv_tc = (t && t[0] == '1') ? 1 : 0;
     }
     int dev = 0;
     cudaGetDevice(&dev);
@@ -636,6 +897,7 @@ extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long l
     NA(N->xin, P * 16 * 4);
     NA(N->part, (size_t)N->num_sms * (NTAP * 32 * 32 + 32) * 4);
     NA(N->loss_d, 8);
+    NA(N->err, 16);
 #undef NA
     if (st) { vec_net_destroy(N); return st; }
     // initial weights: uniform(-a, a), a = sqrt(6 / fan_in) (He); the output

@@ -35,11 +35,14 @@ def _close(a, b, tol):
 
 
 @pytest.mark.parametrize("nx,ny,nz,nb,mt", [(16, 16, 5, 2, "2"), (32, 8, 4, 1, "2"), (64, 4, 3, 2, "2"),
-                                             (128, 2, 3, 1, "2"), (16, 16, 5, 2, "1"), (128, 3, 3, 1, "2")])
+                                             (128, 2, 3, 1, "2"), (16, 16, 5, 2, "1"), (128, 3, 3, 1, "2"),
+                                             (128, 2, 3, 1, "tc"), (128, 4, 5, 2, "tc")])
 def test_forward_backward_match_oracle(nx, ny, nz, nb, mt, monkeypatch):
-    """mt: m-tiles per warp in the convolution kernels (the 128 x 3 plane
-    does not divide into 256-point tiles and takes the one-tile path)."""
-    monkeypatch.setenv("VEC_NET_MT", mt)
+    """mt: m-tiles per warp in the mma.sync convolution kernels (the
+    128 x 3 plane does not divide into 256-point tiles and takes the one-tile
+    path); "tc": forward and input gradient on tcgen05 (nx = 128)."""
+    monkeypatch.setenv("VEC_NET_MT", "2" if mt == "tc" else mt)
+    monkeypatch.setenv("VEC_NET_TC", "1" if mt == "tc" else "0")
     p, x, tgt = _case(nx, ny, nz, nb, seed=nx + nz)
     net = Net(nx, ny, nz, nb)
     net.set_params(p)
