@@ -251,11 +251,12 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
 // matrices of 8 rows x 16 bytes): the halo as [halo row][8-channel block]
 // [130 points][8 channels], so each tap's A operand is the same descriptor
 // shifted by (row, dx); the weights as [tap][8-channel block][n][8].  One
-// thread issues the 27 x CIN/16 MMAs and commits them to an mbarrier; the
-// four warps read the accumulator back with tcgen05.ld (warp w owns TMEM
-// lanes 32w..32w+31, i.e. points 32w..32w+31) and run the epilogue of
-// k_conv.  The halo is double-buffered: the next tile's copies run while
-// the MMAs of the current one execute.
+// thread issues the 27 x CIN/16 MMAs of a tile and commits them to an
+// mbarrier.  Two accumulators (2 x 32 TMEM columns) and two halo buffers
+// form a pipeline: while the eight warps read tile i back with tcgen05.ld
+// (warp w: TMEM lanes 32 (w % 4).., points; half of the channels) and run
+// the epilogue of k_conv, the MMAs of tile i + 1 execute and the halo of
+// tile i + 2 is copied in.
 
 // shared-memory matrix descriptor: start, leading (K-direction) and stride
 // (M/N-direction) byte offsets, descriptor version 1, no swizzle
@@ -304,22 +305,6 @@ __device__ __forceinline__ bool tc_mbar_wait(uint64_t *bar, unsigned parity)
 template <int NC>
 __device__ __forceinline__ void tmem_ld(unsigned taddr, float *v);
 template <>
-__device__ __forceinline__ void tmem_ld<32>(unsigned taddr, float *v)
-{
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-template <>
 __device__ __forceinline__ void tmem_ld<16>(unsigned taddr, float *v)
 {
     uint32_t r[16];
@@ -334,9 +319,21 @@ __device__ __forceinline__ void tmem_ld<16>(unsigned taddr, float *v)
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+template <>
+__device__ __forceinline__ void tmem_ld<8>(unsigned taddr, float *v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
 constexpr int TC_W = 130;          // halo points per row (nx = 128 plus one each side)
 constexpr int TC_ROWS = 9;         // 3 planes x 3 rows
-constexpr int TC_TMEM_COLS = 32;
+constexpr int TC_TMEM_COLS = 64;   // two 32-column accumulators
 
 // halo of row-tile a: [TC_ROWS][C/8][TC_W][8]
 template <int C>
@@ -368,21 +365,24 @@ __host__ __device__ constexpr size_t tc_smem_bytes()
 }
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
 k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
           bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
           const bf16 *__restrict__ gate, int *err)
 {
-    constexpr int C8 = CIN / 8;
+    constexpr int C8 = CIN / 8, HC = COUT / 2;
     constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
     extern __shared__ __align__(128) unsigned char smem[];
     bf16 *hb[2];
     hb[0] = reinterpret_cast<bf16 *>(smem);
     hb[1] = hb[0] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);
     bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [27][C8][COUT][8]
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bar[2];
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and columns
+    // (w / 4) COUT / 2 .. (channels)
+    const int quad = warp & 3, half = warp >> 2;
 
     for (int e = tid; e < NTAP * COUT * C8; e += blockDim.x) {
         const int tap = e / (COUT * C8), r = e % (COUT * C8), n = r / C8, k8 = r % C8;
@@ -394,87 +394,106 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) tc_mbar_init(&bar);
+    if (tid == 0) {
+        tc_mbar_init(&bar[0]);
+        tc_mbar_init(&bar[1]);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_slot;
+    const long long G = gridDim.x;
+    const long long t0 = blockIdx.x;
 
-    long long t = blockIdx.x;
-    if (t < g.tiles) load_halo_tc<CIN>(hb[0], x, g, tile_at(g, t, TP));
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    int it = 0;
-    bool failed = false;
-    for (; t < g.tiles; t += gridDim.x, it++) {
-        const TileAt a = tile_at(g, t, TP);
-        bf16 *cur = hb[it & 1];
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> async proxy
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned hbase = su32(cur), wbase = su32(ws);
+    // the MMAs of tile i (buffer and accumulator i & 1), issued by one thread
+    auto issue = [&](int i) {
+        const unsigned hbase = su32(hb[i & 1]), wbase = su32(ws), d = tmem + (unsigned)((i & 1) * 32);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll 1
-            for (int tap = 0; tap < NTAP; tap++) {
-                const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
+        for (int tap = 0; tap < NTAP; tap++) {
+            const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
 #pragma unroll
-                for (int kk = 0; kk < CIN / 16; kk++) {
-                    const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_W) + dx) * 16),
-                                                   TC_W * 16, 128);
-                    const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16,
-                                                   128);
-                    umma_bf16(tmem, ad, bd, IDESC, (tap | kk) != 0);
-                }
+            for (int kk = 0; kk < CIN / 16; kk++) {
+                const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_W) + dx) * 16), TC_W * 16, 128);
+                const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
+                umma_bf16(d, ad, bd, IDESC, (tap | kk) != 0);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar))
-                         : "memory");
         }
-        // the next tile's halo goes to the other buffer, whose MMAs completed
-        // before the previous epilogue
-        if (t + gridDim.x < g.tiles) load_halo_tc<CIN>(hb[(it + 1) & 1], x, g, tile_at(g, t + gridDim.x, TP));
-        asm volatile("cp.async.commit_group;" ::: "memory");
-        const bool ok = tc_mbar_wait(&bar, it & 1);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar[i & 1]))
+                     : "memory");
+    };
+
+    // prologue: halo of tile 0, its MMAs, then the halo of tile 1
+    if (t0 < g.tiles) load_halo_tc<CIN>(hb[0], x, g, tile_at(g, t0, TP));
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t0 < g.tiles && tid == 0) issue(0);
+    if (t0 + G < g.tiles) load_halo_tc<CIN>(hb[1], x, g, tile_at(g, t0 + G, TP));
+    asm volatile("cp.async.commit_group;" ::: "memory");
+
+    int i = 0;
+    bool failed = false;
+    for (long long t = t0; t < g.tiles; t += G, i++) {
+        // halo of tile i + 1 in place: issue its MMAs into the other accumulator
+        // (read by the epilogue of tile i - 1, which every thread finished)
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (t + G < g.tiles && tid == 0) issue(i + 1);
+        const bool ok = tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicExch(err, 2);
             failed = true;
             break;
         }
+        // tile i's MMAs are done: its halo buffer takes tile i + 2
+        if (t + 2 * G < g.tiles) load_halo_tc<CIN>(hb[i & 1], x, g, tile_at(g, t + 2 * G, TP));
+        asm volatile("cp.async.commit_group;" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        float v[COUT];
-        tmem_ld<COUT>(tmem + ((unsigned)(warp * 32) << 16), v);
-        const size_t gp = a.plane0 + a.q0 + warp * 32 + lane;
+        const TileAt a = tile_at(g, t, TP);
+        float v[HC];
+        tmem_ld<HC>(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)((i & 1) * 32 + half * HC), v);
+        const size_t gp = a.plane0 + a.q0 + quad * 32 + lane;
+        const int n0 = half * HC;
         if (EPI == EPI_ACT) {
-            __align__(16) __nv_bfloat162 pr[COUT / 2], ac[COUT / 2];
+            __align__(16) __nv_bfloat162 pr[HC / 2], ac[HC / 2];
 #pragma unroll
-            for (int n = 0; n < COUT; n += 2) {
-                const float v0 = v[n] + bias[n], v1 = v[n + 1] + bias[n + 1];
+            for (int n = 0; n < HC; n += 2) {
+                const float v0 = v[n] + bias[n0 + n], v1 = v[n + 1] + bias[n0 + n + 1];
                 pr[n / 2] = __floats2bfloat162_rn(v0, v1);
                 ac[n / 2] = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
             }
 #pragma unroll
-            for (int q = 0; q < COUT / 8; q++) {
-                reinterpret_cast<uint4 *>(o_pre + gp * COUT)[q] = reinterpret_cast<const uint4 *>(pr)[q];
-                reinterpret_cast<uint4 *>(o_act + gp * COUT)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+            for (int q = 0; q < HC / 8; q++) {
+                reinterpret_cast<uint4 *>(o_pre + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(pr)[q];
+                reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
             }
         } else if (EPI == EPI_OUT) {
-            for (int n = 0; n < cout_real; n++) o_f32[gp * cout_real + n] = v[n] + bias[n];
+#pragma unroll
+            for (int n = 0; n < HC; n++)
+                if (n0 + n < cout_real) o_f32[gp * cout_real + n0 + n] = v[n] + bias[n0 + n];
         } else {
-            __align__(16) __nv_bfloat162 gg[COUT / 2], ac[COUT / 2];
+            __align__(16) __nv_bfloat162 gg[HC / 2], ac[HC / 2];
 #pragma unroll
-            for (int q = 0; q < COUT / 8; q++)
-                reinterpret_cast<uint4 *>(gg)[q] = reinterpret_cast<const uint4 *>(gate + gp * COUT)[q];
+            for (int q = 0; q < HC / 8; q++)
+                reinterpret_cast<uint4 *>(gg)[q] = reinterpret_cast<const uint4 *>(gate + gp * COUT + n0)[q];
 #pragma unroll
-            for (int n = 0; n < COUT; n += 2)
+            for (int n = 0; n < HC; n += 2)
                 ac[n / 2] = __floats2bfloat162_rn(v[n] * gelu_d(__bfloat162float(gg[n / 2].x)),
                                                   v[n + 1] * gelu_d(__bfloat162float(gg[n / 2].y)));
 #pragma unroll
-            for (int q = 0; q < COUT / 8; q++)
-                reinterpret_cast<uint4 *>(o_act + gp * COUT)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+            for (int q = 0; q < HC / 8; q++)
+                reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
-    if (failed) tc_mbar_wait(&bar, it & 1);   // once more, bounded, before the accumulator is freed
+    if (failed) {   // the MMAs issued for tiles i and i + 1, bounded, before the accumulator is freed
+        tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
+        tc_mbar_wait(&bar[(i + 1) & 1], ((i + 1) >> 1) & 1);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -694,7 +713,7 @@ int run_conv_tc(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf
     }
     long long grid = N->num_sms;
     if (grid > N->g.tiles) grid = N->g.tiles;
-    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 128, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real,
+    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real,
                                                                  gate, N->err);
     N->launches++;
     CUDA_TRY(cudaGetLastError());
