@@ -19,6 +19,8 @@
 // the ldmatrix row addresses of eight consecutive points fall in distinct
 // bank groups.  CTAs are persistent over tiles and keep the weights of their
 // layer in shared memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
@@ -331,32 +333,72 @@ __device__ __forceinline__ void tmem_ld<8>(unsigned taddr, float *v)
     for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 
-constexpr int TC_W = 130;          // halo points per row (nx = 128 plus one each side)
+// halo row: 144 slots per (row, 8-channel block): x = -1 at slot 7, x = 0..127
+// at slots 8..135 (a 128-byte aligned TMA box), x = 128 at slot 136
+constexpr int TC_RL = 144;
+constexpr int TC_X0 = 8;
 constexpr int TC_ROWS = 9;         // 3 planes x 3 rows
 constexpr int TC_TMEM_COLS = 64;   // two 32-column accumulators
 
-// halo of row-tile a: [TC_ROWS][C/8][TC_W][8]
+// halo of row-tile a into h: [TC_ROWS][C/8][TC_RL][8].  One thread issues a
+// TMA box (8 channels x 128 points, 2 KB) per row and channel block within
+// the walls, counted on the mbarrier tb; all threads copy the two wrapped
+// edge points per row and block with cp.async and zero the rows outside the
+// walls.
+__device__ __forceinline__ void tma_load_5d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            int c4, unsigned bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+                 "%5, %6}], [%7];" ::"r"(dst),
+                 "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+                 : "memory");
+}
+
 template <int C>
-__device__ __forceinline__ void load_halo_tc(bf16 *h, const bf16 *src, const NetGeom &g, const TileAt &a)
+__device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, const bf16 *src, const NetGeom &g,
+                                             const TileAt &a, uint64_t *tb)
 {
     constexpr int C8 = C / 8;
-    for (int e = threadIdx.x; e < TC_ROWS * TC_W * C8; e += blockDim.x) {
-        const int c = e % C8;
-        const int pt = e / C8;
-        const int xi = pt % TC_W, row = pt / TC_W;
+    if (threadIdx.x == 0) {
+        int nr = 0;
+        for (int row = 0; row < TC_ROWS; row++) {
+            const int zz = a.z + row / 3 - 1;
+            nr += (zz >= 0 && zz < g.nz) ? 1 : 0;
+        }
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(tb)),
+                     "r"((unsigned)(nr * C8 * 128 * 16))
+                     : "memory");
+        for (int row = 0; row < TC_ROWS; row++) {
+            const int zz = a.z + row / 3 - 1;
+            if (zz < 0 || zz >= g.nz) continue;
+            int yy = a.y0 + row % 3 - 1;
+            yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
+            for (int c = 0; c < C8; c++)
+                tma_load_5d(su32(h + (((size_t)row * C8 + c) * TC_RL + TC_X0) * 8), tm, 0, c, 0, yy, a.b * g.nz + zz,
+                            su32(tb));
+        }
+    }
+    for (int e = threadIdx.x; e < TC_ROWS * C8 * 2; e += blockDim.x) {
+        const int row = e / (C8 * 2), c = (e / 2) % C8, side = e & 1;
         const int zz = a.z + row / 3 - 1;
         int yy = a.y0 + row % 3 - 1;
         yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
-        int xx = xi - 1;
-        xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+        const int xx = side ? 0 : g.nx - 1;
         const bool ok = zz >= 0 && zz < g.nz;
         const size_t gp = ok ? ((((size_t)a.b * g.nz + zz) * g.ny + yy) * g.nx + xx) : 0;
-        cp16(su32(h + (((size_t)row * C8 + c) * TC_W + xi) * 8), src + gp * C + c * 8, ok);
+        cp16(su32(h + (((size_t)row * C8 + c) * TC_RL + (side ? TC_X0 + 128 : TC_X0 - 1)) * 8), src + gp * C + c * 8, ok);
+    }
+    for (int e = threadIdx.x; e < TC_ROWS * C8 * 128; e += blockDim.x) {
+        const int row = e / (C8 * 128);
+        const int zz = a.z + row / 3 - 1;
+        if (zz >= 0 && zz < g.nz) continue;
+        const int c = (e / 128) % C8, xi = e % 128;
+        *reinterpret_cast<uint4 *>(h + (((size_t)row * C8 + c) * TC_RL + TC_X0 + xi) * 8) = make_uint4(0, 0, 0, 0);
     }
 }
 
 template <int CIN, int COUT>
-__host__ __device__ constexpr size_t tc_halo_bytes() { return (size_t)TC_ROWS * TC_W * CIN * sizeof(bf16); }
+__host__ __device__ constexpr size_t tc_halo_bytes() { return (size_t)TC_ROWS * TC_RL * CIN * sizeof(bf16); }
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_smem_bytes()
 {
@@ -366,9 +408,9 @@ __host__ __device__ constexpr size_t tc_smem_bytes()
 
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(256, 1)
-k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__restrict__ bias, NetGeom g,
-          bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act, float *__restrict__ o_f32, int cout_real,
-          const bf16 *__restrict__ gate, int *err)
+k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, const bf16 *__restrict__ wt,
+          const float *__restrict__ bias, NetGeom g, bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act,
+          float *__restrict__ o_f32, int cout_real, const bf16 *__restrict__ gate, int *err)
 {
     constexpr int C8 = CIN / 8, HC = COUT / 2;
     constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
@@ -377,7 +419,7 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
     hb[0] = reinterpret_cast<bf16 *>(smem);
     hb[1] = hb[0] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);
     bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [27][C8][COUT][8]
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[2], tbar[2];
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and columns
@@ -397,6 +439,8 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
     if (tid == 0) {
         tc_mbar_init(&bar[0]);
         tc_mbar_init(&bar[1]);
+        tc_mbar_init(&tbar[0]);
+        tc_mbar_init(&tbar[1]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -414,7 +458,8 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
             const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
 #pragma unroll
             for (int kk = 0; kk < CIN / 16; kk++) {
-                const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_W) + dx) * 16), TC_W * 16, 128);
+                const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16),
+                                               TC_RL * 16, 128);
                 const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
                 umma_bf16(d, ad, bd, IDESC, (tap | kk) != 0);
             }
@@ -424,13 +469,17 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
     };
 
     // prologue: halo of tile 0, its MMAs, then the halo of tile 1
-    if (t0 < g.tiles) load_halo_tc<CIN>(hb[0], x, g, tile_at(g, t0, TP));
+    bool tok = true;
+    if (t0 < g.tiles) load_halo_tc<CIN>(hb[0], &tmx, x, g, tile_at(g, t0, TP), &tbar[0]);
     asm volatile("cp.async.commit_group;" ::: "memory");
     asm volatile("cp.async.wait_all;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (t0 < g.tiles && tid == 0) issue(0);
-    if (t0 + G < g.tiles) load_halo_tc<CIN>(hb[1], x, g, tile_at(g, t0 + G, TP));
+    if (t0 < g.tiles && tid == 0) {
+        tok = tc_mbar_wait(&tbar[0], 0);
+        if (tok) issue(0);
+    }
+    if (t0 + G < g.tiles) load_halo_tc<CIN>(hb[1], &tmx, x, g, tile_at(g, t0 + G, TP), &tbar[1]);
     asm volatile("cp.async.commit_group;" ::: "memory");
 
     int i = 0;
@@ -441,15 +490,18 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
         asm volatile("cp.async.wait_all;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (t + G < g.tiles && tid == 0) issue(i + 1);
+        if (t + G < g.tiles && tid == 0 && tok) {
+            tok = tc_mbar_wait(&tbar[(i + 1) & 1], ((i + 1) >> 1) & 1);
+            if (tok) issue(i + 1);
+        }
         const bool ok = tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
-        if (__syncthreads_or(!ok)) {
+        if (__syncthreads_or(!ok || !tok)) {
             if (tid == 0) atomicExch(err, 2);
             failed = true;
             break;
         }
         // tile i's MMAs are done: its halo buffer takes tile i + 2
-        if (t + 2 * G < g.tiles) load_halo_tc<CIN>(hb[i & 1], x, g, tile_at(g, t + 2 * G, TP));
+        if (t + 2 * G < g.tiles) load_halo_tc<CIN>(hb[i & 1], &tmx, x, g, tile_at(g, t + 2 * G, TP), &tbar[i & 1]);
         asm volatile("cp.async.commit_group;" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const TileAt a = tile_at(g, t, TP);
@@ -490,9 +542,11 @@ k_conv_tc(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
-    if (failed) {   // the MMAs issued for tiles i and i + 1, bounded, before the accumulator is freed
+    if (failed && tid == 0) {   // copies and MMAs in flight, bounded, before the accumulator is freed
         tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
         tc_mbar_wait(&bar[(i + 1) & 1], ((i + 1) >> 1) & 1);
+        tc_mbar_wait(&tbar[i & 1], ((i + 2) >> 1) & 1);
+        tc_mbar_wait(&tbar[(i + 1) & 1], ((i + 1) >> 1) & 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -711,9 +765,26 @@ int run_conv_tc(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf
         CUDA_TRY(cudaFuncSetAttribute(k_conv_tc<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         set = true;
     }
+    // x as (8 channels, channel block, x, y, z and sample): boxes of 8 x 1 x 128 x 1 x 1
+    PFN_cuTensorMapEncodeTiled_v12000 enc = (PFN_cuTensorMapEncodeTiled_v12000)tma_encode_fn();
+    if (!enc) return VEC_ERR_CUDA;
+    CUtensorMap tm;
+    const NetGeom &g = N->g;
+    cuuint64_t dims[5] = { 8, (cuuint64_t)(CIN / 8), (cuuint64_t)g.nx, (cuuint64_t)g.ny,
+                           (cuuint64_t)g.nz * (cuuint64_t)g.nb };
+    cuuint64_t strides[4] = { 16, (cuuint64_t)CIN * 2, (cuuint64_t)g.nx * CIN * 2, (cuuint64_t)g.ny * g.nx * CIN * 2 };
+    cuuint32_t box[5] = { 8, 1, 128, 1, 1 };
+    cuuint32_t es[5] = { 1, 1, 1, 1, 1 };
+    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)x, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        vec_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return VEC_ERR_CUDA;
+    }
     long long grid = N->num_sms;
-    if (grid > N->g.tiles) grid = N->g.tiles;
-    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, wt, bias, N->g, o_pre, o_act, o_f32, cout_real,
+    if (grid > g.tiles) grid = g.tiles;
+    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, tm, wt, bias, g, o_pre, o_act, o_f32, cout_real,
                                                                  gate, N->err);
     N->launches++;
     CUDA_TRY(cudaGetLastError());

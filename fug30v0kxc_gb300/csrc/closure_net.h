@@ -41,6 +41,9 @@ struct vec_net {
     double *loss_d = nullptr;
 };
 
+// cuTensorMapEncodeTiled (lines_ct.cu), null if unavailable
+void *tma_encode_fn();
+
 int net_pack(vec_net *N);
 int net_forward(vec_net *N);
 int net_backward(vec_net *N, const float *tgt);

@@ -422,6 +422,10 @@ int line_ct_configure()
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static int get_encoder();
+
+// cuTensorMapEncodeTiled for other translation units (null if unavailable)
+void *tma_encode_fn() { return get_encoder() == VEC_OK ? (void *)g_encode : nullptr; }
 
 static int get_encoder()
 {
