@@ -253,8 +253,9 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
 // matrices of 8 rows x 16 bytes): the halo as [halo row][8-channel block]
 // [130 points][8 channels], so each tap's A operand is the same descriptor
 // shifted by (row, dx); the weights as [tap][8-channel block][n][8].  One
-// thread issues the 27 x CIN/16 MMAs of a tile and commits them to an
-// mbarrier.  Two accumulators (2 x 32 TMEM columns) and two halo buffers
+// thread issues the 27 x CIN/16 MMAs of a tile, spread over four independent
+// accumulator chains that the epilogue sums, and commits them to an
+// mbarrier.  Two sets of accumulators (2 x 4 x 32 TMEM columns) and two halo buffers
 // form a pipeline: while the eight warps read tile i back with tcgen05.ld
 // (warp w: TMEM lanes 32 (w % 4).., points; half of the channels) and run
 // the epilogue of k_conv, the MMAs of tile i + 1 execute and the halo of
@@ -338,7 +339,8 @@ __device__ __forceinline__ void tmem_ld<8>(unsigned taddr, float *v)
 constexpr int TC_RL = 144;
 constexpr int TC_X0 = 8;
 constexpr int TC_ROWS = 9;         // 3 planes x 3 rows
-constexpr int TC_TMEM_COLS = 64;   // two 32-column accumulators
+constexpr int TC_NCH = 4;          // independent accumulator chains per tile (taps split 7, 7, 7, 6)
+constexpr int TC_TMEM_COLS = 256;  // two tiles x TC_NCH chains x 32 columns
 
 // halo of row-tile a into h: [TC_ROWS][C/8][TC_RL][8].  One thread issues a
 // TMA box (8 channels x 128 points, 2 KB) per row and channel block within
@@ -449,19 +451,27 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
     const long long G = gridDim.x;
     const long long t0 = blockIdx.x;
 
-    // the MMAs of tile i (buffer and accumulator i & 1), issued by one thread
+    // the MMAs of tile i (halo buffer i & 1, accumulators (i & 1) TC_NCH ..),
+    // issued by one thread: chain c sums taps 7c .. 7c + 6, and the chains
+    // are interleaved so consecutive MMAs do not depend on each other
     auto issue = [&](int i) {
-        const unsigned hbase = su32(hb[i & 1]), wbase = su32(ws), d = tmem + (unsigned)((i & 1) * 32);
+        const unsigned hbase = su32(hb[i & 1]), wbase = su32(ws);
+        const unsigned d0 = tmem + (unsigned)((i & 1) * TC_NCH * 32);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll 1
-        for (int tap = 0; tap < NTAP; tap++) {
-            const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
+        for (int st = 0; st < 7; st++) {
 #pragma unroll
-            for (int kk = 0; kk < CIN / 16; kk++) {
-                const uint64_t ad = umma_sdesc(hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16),
-                                               TC_RL * 16, 128);
-                const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
-                umma_bf16(d, ad, bd, IDESC, (tap | kk) != 0);
+            for (int c = 0; c < TC_NCH; c++) {
+                const int tap = 7 * c + st;
+                if (tap >= NTAP) continue;
+                const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+                for (int kk = 0; kk < CIN / 16; kk++) {
+                    const uint64_t ad = umma_sdesc(
+                        hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16), TC_RL * 16, 128);
+                    const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
+                    umma_bf16(d0 + (unsigned)(c * 32), ad, bd, IDESC, (st | kk) != 0);
+                }
             }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar[i & 1]))
@@ -506,7 +516,17 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const TileAt a = tile_at(g, t, TP);
         float v[HC];
-        tmem_ld<HC>(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)((i & 1) * 32 + half * HC), v);
+        {
+            const unsigned ta = tmem + ((unsigned)(quad * 32) << 16) + (unsigned)((i & 1) * TC_NCH * 32 + half * HC);
+            tmem_ld<HC>(ta, v);
+#pragma unroll
+            for (int c = 1; c < TC_NCH; c++) {
+                float u[HC];
+                tmem_ld<HC>(ta + (unsigned)(c * 32), u);
+#pragma unroll
+                for (int n = 0; n < HC; n++) v[n] += u[n];
+            }
+        }
         const size_t gp = a.plane0 + a.q0 + quad * 32 + lane;
         const int n0 = half * HC;
         if (EPI == EPI_ACT) {
