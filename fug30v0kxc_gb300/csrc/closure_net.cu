@@ -255,11 +255,10 @@ k_conv(const bf16 *__restrict__ x, const bf16 *__restrict__ wt, const float *__r
 // shifted by (row, dx); the weights as [tap][8-channel block][n][8].  One
 // thread issues the 27 x CIN/16 MMAs of a tile, spread over four independent
 // accumulator chains that the epilogue sums, and commits them to an
-// mbarrier.  Two sets of accumulators (2 x 4 x 32 TMEM columns) and two halo buffers
-// form a pipeline: while the eight warps read tile i back with tcgen05.ld
-// (warp w: TMEM lanes 32 (w % 4).., points; half of the channels) and run
-// the epilogue of k_conv, the MMAs of tile i + 1 execute and the halo of
-// tile i + 2 is copied in.
+// mbarrier.  Two sets of accumulators (2 x 4 x 32 TMEM columns) and two halo
+// buffers form a pipeline between a producer warp (halo copies, MMA issue)
+// and eight epilogue warps (tcgen05.ld, the epilogue of k_conv): while tile
+// i is read back, the halo and MMAs of tile i + 1 proceed.
 
 // shared-memory matrix descriptor: start, leading (K-direction) and stride
 // (M/N-direction) byte offsets, descriptor version 1, no swizzle
@@ -282,12 +281,6 @@ __device__ __forceinline__ void umma_bf16(unsigned tmem_d, uint64_t a, uint64_t 
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
                  ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accum)
                  : "memory");
-}
-
-__device__ __forceinline__ void tc_mbar_init(uint64_t *bar)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
 // bounded wait on an mbarrier phase; false when the limit ran out
@@ -356,12 +349,13 @@ __device__ __forceinline__ void tma_load_5d(unsigned dst, const CUtensorMap *map
                  : "memory");
 }
 
+// (run by a group of nt threads; tl is the thread's index in the group)
 template <int C>
 __device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, const bf16 *src, const NetGeom &g,
-                                             const TileAt &a, uint64_t *tb)
+                                             const TileAt &a, uint64_t *tb, int tl, int nt)
 {
     constexpr int C8 = C / 8;
-    if (threadIdx.x == 0) {
+    if (tl == 0) {
         int nr = 0;
         for (int row = 0; row < TC_ROWS; row++) {
             const int zz = a.z + row / 3 - 1;
@@ -380,7 +374,7 @@ __device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, con
                             su32(tb));
         }
     }
-    for (int e = threadIdx.x; e < TC_ROWS * C8 * 2; e += blockDim.x) {
+    for (int e = tl; e < TC_ROWS * C8 * 2; e += nt) {
         const int row = e / (C8 * 2), c = (e / 2) % C8, side = e & 1;
         const int zz = a.z + row / 3 - 1;
         int yy = a.y0 + row % 3 - 1;
@@ -390,7 +384,7 @@ __device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, con
         const size_t gp = ok ? ((((size_t)a.b * g.nz + zz) * g.ny + yy) * g.nx + xx) : 0;
         cp16(su32(h + (((size_t)row * C8 + c) * TC_RL + (side ? TC_X0 + 128 : TC_X0 - 1)) * 8), src + gp * C + c * 8, ok);
     }
-    for (int e = threadIdx.x; e < TC_ROWS * C8 * 128; e += blockDim.x) {
+    for (int e = tl; e < TC_ROWS * C8 * 128; e += nt) {
         const int row = e / (C8 * 128);
         const int zz = a.z + row / 3 - 1;
         if (zz >= 0 && zz < g.nz) continue;
@@ -408,8 +402,14 @@ __host__ __device__ constexpr size_t tc_smem_bytes()
     return 2 * tc_halo_bytes<CIN, COUT>() + (size_t)NTAP * COUT * CIN * sizeof(bf16) + 4096;
 }
 
+// warp roles: warps 0-7 read the accumulators back and run the epilogue,
+// warp 8 (the producer) copies halos in and issues the MMAs; they meet only
+// at mbarriers (per set b of buffers: tbar halo landed, full MMAs done,
+// empty epilogue done)
+constexpr int TC_THREADS = 288;
+
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, const bf16 *__restrict__ wt,
           const float *__restrict__ bias, NetGeom g, bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act,
           float *__restrict__ o_f32, int cout_real, const bf16 *__restrict__ gate, int *err)
@@ -421,157 +421,156 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
     hb[0] = reinterpret_cast<bf16 *>(smem);
     hb[1] = hb[0] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);
     bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [27][C8][COUT][8]
-    __shared__ __align__(8) uint64_t bar[2], tbar[2];
+    __shared__ __align__(8) uint64_t tbar[2], full[2], empty[2];
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and columns
-    // (w / 4) COUT / 2 .. (channels)
-    const int quad = warp & 3, half = warp >> 2;
 
     for (int e = tid; e < NTAP * COUT * C8; e += blockDim.x) {
         const int tap = e / (COUT * C8), r = e % (COUT * C8), n = r / C8, k8 = r % C8;
         cp16(su32(ws + (((size_t)tap * C8 + k8) * COUT + n) * 8), wt + ((size_t)tap * COUT + n) * CIN + k8 * 8, true);
     }
-    if (warp == 0) {
+    if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
                      "r"(TC_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        tc_mbar_init(&bar[0]);
-        tc_mbar_init(&bar[1]);
-        tc_mbar_init(&tbar[0]);
-        tc_mbar_init(&tbar[1]);
+        for (int b = 0; b < 2; b++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&tbar[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(su32(&empty[b])) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");                 // the weights
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_slot;
-    const long long G = gridDim.x;
-    const long long t0 = blockIdx.x;
+    const long long G = gridDim.x, t0 = blockIdx.x;
+    long long issued = 0;          // producer: tiles whose MMAs were committed
+    bool failed = false;
 
-    // the MMAs of tile i (halo buffer i & 1, accumulators (i & 1) TC_NCH ..),
-    // issued by one thread: chain c sums taps 7c .. 7c + 6, and the chains
-    // are interleaved so consecutive MMAs do not depend on each other
-    auto issue = [&](int i) {
-        const unsigned hbase = su32(hb[i & 1]), wbase = su32(ws);
-        const unsigned d0 = tmem + (unsigned)((i & 1) * TC_NCH * 32);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 8) {
+        int i = 0;
+        for (long long t = t0; t < g.tiles; t += G, i++) {
+            const int b = i & 1;
+            // the epilogue of tile i - 2 released buffer and accumulators b
+            // (lane 0 waits, the warp follows its verdict)
+            bool okw = true;
+            if (i >= 2 && lane == 0) okw = tc_mbar_wait(&empty[b], ((i - 2) >> 1) & 1);
+            if (!__shfl_sync(0xffffffffu, okw ? 1 : 0, 0)) { failed = true; break; }
+            load_halo_tc<CIN>(hb[b], &tmx, x, g, tile_at(g, t, TP), &tbar[b], lane, 32);
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                if (!tc_mbar_wait(&tbar[b], (i >> 1) & 1)) {
+                    failed = true;
+                } else {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const unsigned hbase = su32(hb[b]), wbase = su32(ws);
+                    const unsigned d0 = tmem + (unsigned)(b * TC_NCH * 32);
 #pragma unroll 1
-        for (int st = 0; st < 7; st++) {
+                    for (int st = 0; st < 7; st++) {
 #pragma unroll
-            for (int c = 0; c < TC_NCH; c++) {
-                const int tap = 7 * c + st;
-                if (tap >= NTAP) continue;
-                const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
+                        for (int c = 0; c < TC_NCH; c++) {
+                            const int tap = 7 * c + st;
+                            if (tap >= NTAP) continue;
+                            const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
 #pragma unroll
-                for (int kk = 0; kk < CIN / 16; kk++) {
-                    const uint64_t ad = umma_sdesc(
-                        hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16), TC_RL * 16, 128);
-                    const uint64_t bd = umma_sdesc(wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
-                    umma_bf16(d0 + (unsigned)(c * 32), ad, bd, IDESC, (st | kk) != 0);
+                            for (int kk = 0; kk < CIN / 16; kk++) {
+                                const uint64_t ad = umma_sdesc(
+                                    hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16),
+                                    TC_RL * 16, 128);
+                                const uint64_t bd = umma_sdesc(
+                                    wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
+                                umma_bf16(d0 + (unsigned)(c * 32), ad, bd, IDESC, (st | kk) != 0);
+                            }
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     su32(&full[b]))
+                                 : "memory");
                 }
             }
+            failed = __shfl_sync(0xffffffffu, failed ? 1 : 0, 0) != 0;
+            if (failed) break;
+            issued++;
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar[i & 1]))
-                     : "memory");
-    };
-
-    // prologue: halo of tile 0, its MMAs, then the halo of tile 1
-    bool tok = true;
-    if (t0 < g.tiles) load_halo_tc<CIN>(hb[0], &tmx, x, g, tile_at(g, t0, TP), &tbar[0]);
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and the
+        // channels (w / 4) COUT / 2 .. of the four chains, and sums them
+        const int quad = warp & 3, half = warp >> 2, n0 = half * HC;
+        int i = 0;
+        for (long long t = t0; t < g.tiles; t += G, i++) {
+            const int b = i & 1;
+            bool okw = true;
+            if (lane == 0) okw = tc_mbar_wait(&full[b], (i >> 1) & 1);
+            if (!__shfl_sync(0xffffffffu, okw ? 1 : 0, 0)) { failed = true; break; }
+            __syncwarp();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const TileAt a = tile_at(g, t, TP);
+            float v[HC];
+            {
+                const unsigned ta = tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(b * TC_NCH * 32 + n0);
+                tmem_ld<HC>(ta, v);
+#pragma unroll
+                for (int c = 1; c < TC_NCH; c++) {
+                    float u[HC];
+                    tmem_ld<HC>(ta + (unsigned)(c * 32), u);
+#pragma unroll
+                    for (int n = 0; n < HC; n++) v[n] += u[n];
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)   // accumulators b are free again
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&empty[b])) : "memory");
+            const size_t gp = a.plane0 + a.q0 + quad * 32 + lane;
+            if (EPI == EPI_ACT) {
+                __align__(16) __nv_bfloat162 pr[HC / 2], ac[HC / 2];
+#pragma unroll
+                for (int n = 0; n < HC; n += 2) {
+                    const float v0 = v[n] + bias[n0 + n], v1 = v[n + 1] + bias[n0 + n + 1];
+                    pr[n / 2] = __floats2bfloat162_rn(v0, v1);
+                    ac[n / 2] = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+                }
+#pragma unroll
+                for (int q = 0; q < HC / 8; q++) {
+                    reinterpret_cast<uint4 *>(o_pre + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(pr)[q];
+                    reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+                }
+            } else if (EPI == EPI_OUT) {
+#pragma unroll
+                for (int n = 0; n < HC; n++)
+                    if (n0 + n < cout_real) o_f32[gp * cout_real + n0 + n] = v[n] + bias[n0 + n];
+            } else {
+                __align__(16) __nv_bfloat162 gg[HC / 2], ac[HC / 2];
+#pragma unroll
+                for (int q = 0; q < HC / 8; q++)
+                    reinterpret_cast<uint4 *>(gg)[q] = reinterpret_cast<const uint4 *>(gate + gp * COUT + n0)[q];
+#pragma unroll
+                for (int n = 0; n < HC; n += 2)
+                    ac[n / 2] = __floats2bfloat162_rn(v[n] * gelu_d(__bfloat162float(gg[n / 2].x)),
+                                                      v[n + 1] * gelu_d(__bfloat162float(gg[n / 2].y)));
+#pragma unroll
+                for (int q = 0; q < HC / 8; q++)
+                    reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
+            }
+        }
+    }
+    if (failed && lane == 0) atomicExch(err, 2);
+    // after a failure the producer waits, bounded, for the MMAs it committed
+    if (failed && warp == 8 && lane == 0 && issued > 0)
+        tc_mbar_wait(&full[(issued - 1) & 1], ((issued - 1) >> 1) & 1);
     asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (t0 < g.tiles && tid == 0) {
-        tok = tc_mbar_wait(&tbar[0], 0);
-        if (tok) issue(0);
-    }
-    if (t0 + G < g.tiles) load_halo_tc<CIN>(hb[1], &tmx, x, g, tile_at(g, t0 + G, TP), &tbar[1]);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-
-    int i = 0;
-    bool failed = false;
-    for (long long t = t0; t < g.tiles; t += G, i++) {
-        // halo of tile i + 1 in place: issue its MMAs into the other accumulator
-        // (read by the epilogue of tile i - 1, which every thread finished)
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (t + G < g.tiles && tid == 0 && tok) {
-            tok = tc_mbar_wait(&tbar[(i + 1) & 1], ((i + 1) >> 1) & 1);
-            if (tok) issue(i + 1);
-        }
-        const bool ok = tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
-        if (__syncthreads_or(!ok || !tok)) {
-            if (tid == 0) atomicExch(err, 2);
-            failed = true;
-            break;
-        }
-        // tile i's MMAs are done: its halo buffer takes tile i + 2
-        if (t + 2 * G < g.tiles) load_halo_tc<CIN>(hb[i & 1], &tmx, x, g, tile_at(g, t + 2 * G, TP), &tbar[i & 1]);
-        asm volatile("cp.async.commit_group;" ::: "memory");
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const TileAt a = tile_at(g, t, TP);
-        float v[HC];
-        {
-            const unsigned ta = tmem + ((unsigned)(quad * 32) << 16) + (unsigned)((i & 1) * TC_NCH * 32 + half * HC);
-            tmem_ld<HC>(ta, v);
-#pragma unroll
-            for (int c = 1; c < TC_NCH; c++) {
-                float u[HC];
-                tmem_ld<HC>(ta + (unsigned)(c * 32), u);
-#pragma unroll
-                for (int n = 0; n < HC; n++) v[n] += u[n];
-            }
-        }
-        const size_t gp = a.plane0 + a.q0 + quad * 32 + lane;
-        const int n0 = half * HC;
-        if (EPI == EPI_ACT) {
-            __align__(16) __nv_bfloat162 pr[HC / 2], ac[HC / 2];
-#pragma unroll
-            for (int n = 0; n < HC; n += 2) {
-                const float v0 = v[n] + bias[n0 + n], v1 = v[n + 1] + bias[n0 + n + 1];
-                pr[n / 2] = __floats2bfloat162_rn(v0, v1);
-                ac[n / 2] = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
-            }
-#pragma unroll
-            for (int q = 0; q < HC / 8; q++) {
-                reinterpret_cast<uint4 *>(o_pre + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(pr)[q];
-                reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
-            }
-        } else if (EPI == EPI_OUT) {
-#pragma unroll
-            for (int n = 0; n < HC; n++)
-                if (n0 + n < cout_real) o_f32[gp * cout_real + n0 + n] = v[n] + bias[n0 + n];
-        } else {
-            __align__(16) __nv_bfloat162 gg[HC / 2], ac[HC / 2];
-#pragma unroll
-            for (int q = 0; q < HC / 8; q++)
-                reinterpret_cast<uint4 *>(gg)[q] = reinterpret_cast<const uint4 *>(gate + gp * COUT + n0)[q];
-#pragma unroll
-            for (int n = 0; n < HC; n += 2)
-                ac[n / 2] = __floats2bfloat162_rn(v[n] * gelu_d(__bfloat162float(gg[n / 2].x)),
-                                                  v[n + 1] * gelu_d(__bfloat162float(gg[n / 2].y)));
-#pragma unroll
-            for (int q = 0; q < HC / 8; q++)
-                reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    if (failed && tid == 0) {   // copies and MMAs in flight, bounded, before the accumulator is freed
-        tc_mbar_wait(&bar[i & 1], (i >> 1) & 1);
-        tc_mbar_wait(&bar[(i + 1) & 1], ((i + 1) >> 1) & 1);
-        tc_mbar_wait(&tbar[i & 1], ((i + 2) >> 1) & 1);
-        tc_mbar_wait(&tbar[(i + 1) & 1], ((i + 1) >> 1) & 1);
-    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (warp == 0)
+    if (warp == 8)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 
@@ -804,8 +803,8 @@ int run_conv_tc(vec_net *N, const bf16 *x, const bf16 *wt, const float *bias, bf
     }
     long long grid = N->num_sms;
     if (grid > g.tiles) grid = g.tiles;
-    k_conv_tc<CIN, COUT, EPI><<<(int)grid, 256, sm, N->stream>>>(x, tm, wt, bias, g, o_pre, o_act, o_f32, cout_real,
-                                                                 gate, N->err);
+    k_conv_tc<CIN, COUT, EPI><<<(int)grid, TC_THREADS, sm, N->stream>>>(x, tm, wt, bias, g, o_pre, o_act, o_f32,
+                                                                        cout_real, gate, N->err);
     N->launches++;
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;
