@@ -454,22 +454,21 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
     bool failed = false;
 
     if (warp == 8) {
+        // producer: halo of tile i + 1 is copied while the MMAs of tile i run
+        if (t0 < g.tiles) load_halo_tc<CIN>(hb[0], &tmx, x, g, tile_at(g, t0, TP), &tbar[0], lane, 32);
         int i = 0;
         for (long long t = t0; t < g.tiles; t += G, i++) {
             const int b = i & 1;
-            // the epilogue of tile i - 2 released buffer and accumulators b
-            // (lane 0 waits, the warp follows its verdict)
-            bool okw = true;
-            if (i >= 2 && lane == 0) okw = tc_mbar_wait(&empty[b], ((i - 2) >> 1) & 1);
-            if (!__shfl_sync(0xffffffffu, okw ? 1 : 0, 0)) { failed = true; break; }
-            load_halo_tc<CIN>(hb[b], &tmx, x, g, tile_at(g, t, TP), &tbar[b], lane, 32);
             asm volatile("cp.async.wait_all;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
+            // lane 0 waits (halo i landed, accumulators b released by the
+            // epilogue of tile i - 2) and issues; the warp follows its verdict
+            bool okw = true;
             if (lane == 0) {
-                if (!tc_mbar_wait(&tbar[b], (i >> 1) & 1)) {
-                    failed = true;
-                } else {
+                okw = tc_mbar_wait(&tbar[b], (i >> 1) & 1);
+                if (okw && i >= 2) okw = tc_mbar_wait(&empty[b], ((i - 2) >> 1) & 1);
+                if (okw) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const unsigned hbase = su32(hb[b]), wbase = su32(ws);
                     const unsigned d0 = tmem + (unsigned)(b * TC_NCH * 32);
@@ -496,9 +495,15 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
                                  : "memory");
                 }
             }
-            failed = __shfl_sync(0xffffffffu, failed ? 1 : 0, 0) != 0;
-            if (failed) break;
+            if (!__shfl_sync(0xffffffffu, okw ? 1 : 0, 0)) { failed = true; break; }
             issued++;
+            if (t + G < g.tiles) {
+                // buffer b ^ 1 is free once the MMAs of tile i - 1 completed
+                okw = true;
+                if (lane == 0 && i >= 1) okw = tc_mbar_wait(&full[b ^ 1], ((i - 1) >> 1) & 1);
+                if (!__shfl_sync(0xffffffffu, okw ? 1 : 0, 0)) { failed = true; break; }
+                load_halo_tc<CIN>(hb[b ^ 1], &tmx, x, g, tile_at(g, t + G, TP), &tbar[b ^ 1], lane, 32);
+            }
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and the
