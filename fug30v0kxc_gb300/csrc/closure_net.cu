@@ -283,7 +283,9 @@ __device__ __forceinline__ void umma_bf16(unsigned tmem_d, uint64_t a, uint64_t 
                  : "memory");
 }
 
-// bounded wait on an mbarrier phase; false when the limit ran out
+// bounded wait on an mbarrier phase; false when the limit ran out.  After a
+// few polls the waiting thread sleeps between polls, so waiting warps leave
+// the issue slots to the warp that issues the copies and MMAs.
 __device__ __forceinline__ bool tc_mbar_wait(uint64_t *bar, unsigned parity)
 {
     const unsigned a = su32(bar);
@@ -294,6 +296,7 @@ __device__ __forceinline__ bool tc_mbar_wait(uint64_t *bar, unsigned parity)
                      : "r"(a), "r"(parity)
                      : "memory");
         if (ok) return true;
+        if (it > 4) __nanosleep(64);
     }
     return false;
 }
