@@ -269,6 +269,17 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         delete c;
         return st;
     }
+    if (cudaStreamCreateWithFlags(&E.stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E.ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return VEC_ERR_CUDA;
+    }
+    {
+        const char *sm = getenv("VEC_SERIAL_MAG");
+        E.par_mag = !(sm && sm[0] == '1');
+    }
     if (cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return VEC_ERR_CUDA;
@@ -383,6 +394,9 @@ extern "C" int vec_destroy(vec_ctx *c)
     if (E.hs) cudaFreeHost(E.hs);
     for (auto &pd : E.pending) { cudaEventDestroy(pd.a); cudaEventDestroy(pd.b); }
     for (auto ev : E.ev_pool) cudaEventDestroy(ev);
+    if (E.stream2) { cudaStreamSynchronize(E.stream2); cudaStreamDestroy(E.stream2); }
+    if (E.ev_fork) cudaEventDestroy(E.ev_fork);
+    if (E.ev_join) cudaEventDestroy(E.ev_join);
     if (E.stream) cudaStreamDestroy(E.stream);
     delete c;
     return VEC_OK;
@@ -776,10 +790,25 @@ static int enqueue_step(Engine &E, bool diag_now)
 {
     int st;
     const int mag = mag_on(E);
-    if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
-    if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
-    else st = phys_zero_mag_rhs(&E);
-    if (st) return st;
+    if (mag && E.par_mag) {
+        // mag_deriv on stream2 beside hydro_deriv on stream (disjoint outputs
+        // and work arrays; both only read the state)
+        CUDA_TRY(cudaEventRecord(E.ev_fork, E.stream));
+        CUDA_TRY(cudaStreamWaitEvent(E.stream2, E.ev_fork, 0));
+        cudaStream_t s0 = E.stream;
+        E.stream = E.stream2;
+        st = E.split ? split_mag(&E) : phys_mag64(&E);
+        E.stream = s0;
+        if (st) return st;
+        CUDA_TRY(cudaEventRecord(E.ev_join, E.stream2));
+        if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
+        CUDA_TRY(cudaStreamWaitEvent(E.stream, E.ev_join, 0));
+    } else {
+        if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
+        if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
+        else st = phys_zero_mag_rhs(&E);
+        if (st) return st;
+    }
     if (E.corr_on && (st = closure_apply_corr(&E))) return st;
     const int mdeal = E.p.dalias && mag;
     if ((st = E.split ? split_ab3(&E, mdeal) : phys_ab3(&E, mdeal))) return st;

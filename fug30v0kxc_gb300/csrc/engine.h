@@ -38,6 +38,11 @@ struct Engine {
     size_t np, n;
     int split;                  // VEC_PREC_SPLIT
     cudaStream_t stream = nullptr;
+    // mag_deriv runs on stream2, forked from and joined to stream inside the
+    // step (it shares no output or work array with hydro_deriv)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int par_mag = 1;            // VEC_SERIAL_MAG=1: both on stream
     long long launches = 0;
     int num_sms = 152;
     int *dev_err = nullptr;     // set by kernels whose bounded waits ran out
