@@ -37,8 +37,9 @@ def build(force=False, verbose=False, extra=()):
     deps = srcs + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "vec.h"))
     deps.append(os.path.join(HERE, "host", "p3d_gpu.c"))
-    if not force and os.path.exists(LIB) and os.path.exists(HOST):
-        t = min(os.path.getmtime(LIB), os.path.getmtime(HOST))
+    deps.append(os.path.join(HERE, "host", "interp_gpu.c"))
+    if not force and os.path.exists(LIB) and os.path.exists(HOST) and os.path.exists(INTERP):
+        t = min(os.path.getmtime(LIB), os.path.getmtime(HOST), os.path.getmtime(INTERP))
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
     objs = [os.path.join(OUT, os.path.splitext(os.path.basename(s))[0] + ".o") for s in srcs]
@@ -68,19 +69,22 @@ def build(force=False, verbose=False, extra=()):
 
 
 HOST = os.path.join(OUT, "p3d_gpu")
+INTERP = os.path.join(OUT, "interp_gpu")
 
 
 def build_host(verbose=False):
-    """The C host driver (src/main.F90 on the GPU library)."""
-    src = os.path.join(HERE, "host", "p3d_gpu.c")
+    """The C host programs: p3d_gpu (src/main.F90) and interp_gpu
+    (interpolate/main.F90) on the GPU library."""
     cc = shutil.which("gcc") or "cc"
-    cmd = [cc, "-O2", "-std=gnu11", "-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include"), src,
-           "-o", HOST, "-L" + OUT, "-lvec_gpu", "-Wl,-rpath,$ORIGIN"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"host driver build failed:\n{r.stdout}\n{r.stderr}")
+    for name, exe in (("p3d_gpu.c", HOST), ("interp_gpu.c", INTERP)):
+        src = os.path.join(HERE, "host", name)
+        cmd = [cc, "-O2", "-std=gnu11", "-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include"), src,
+               "-o", exe, "-L" + OUT, "-lvec_gpu", "-lm", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host program build failed:\n{r.stdout}\n{r.stderr}")
     return HOST
 
 

@@ -193,13 +193,15 @@ double att_num(const Att *a)
 
 }  // namespace
 
-extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec)
+// fmt 1: classic (CDF-1, 32-bit offsets, src/netcdf.F90:74); fmt 2: 64-bit
+// offsets (CDF-2, NF_64BIT_OFFSET, interpolate/netcdf.F90:73)
+static int nc_write(const char *path, const vec_snapshot *s, int iprec, int fmt)
 {
-    if (!path || !s || (iprec != 4 && iprec != 8)) return VEC_ERR_ARG;
+    if (!path || !s || (iprec != 4 && iprec != 8) || (fmt != 1 && fmt != 2)) return VEC_ERR_ARG;
     for (int i = 0; i < 8; i++) if (!s->fields[i]) return VEC_ERR_ARG;
     const size_t n = (size_t)s->nx * s->ny * s->nz;
     Buf h;
-    h.b.push_back('C'); h.b.push_back('D'); h.b.push_back('F'); h.b.push_back(1);
+    h.b.push_back('C'); h.b.push_back('D'); h.b.push_back('F'); h.b.push_back((unsigned char)fmt);
     h.u32(0);   // numrecs: no record variables
     h.u32(TAG_DIM); h.u32(4);
     h.name("nx"); h.u32((uint32_t)s->nx);
@@ -228,10 +230,10 @@ extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec)
     for (auto &v : vars) {
         vl += 4 + pad4(v.name.size()) + 4 + 4 * v.dims.size();
         vl += v.units ? 8 + (4 + pad4(5)) + 8 + pad4(7) : 8;
-        vl += 4 + 4 + 4;
+        vl += 4 + 4 + (fmt == 1 ? 4 : 8);
     }
     size_t off = h.b.size() + vl;
-    if (off + 8 * n * iprec + 64 > 0x7fffffffull) {
+    if (fmt == 1 && off + 8 * n * iprec + 64 > 0x7fffffffull) {
         vec_set_error("snapshot larger than the 2 GiB limit of the classic format");
         return VEC_ERR_SIZE;
     }
@@ -244,7 +246,8 @@ extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec)
         else { h.u32(0); h.u32(0); }
         h.u32((uint32_t)v.type);
         h.u32((uint32_t)v.vsize);
-        h.u32((uint32_t)off);
+        if (fmt == 1) h.u32((uint32_t)off);
+        else { h.u32((uint32_t)((uint64_t)off >> 32)); h.u32((uint32_t)off); }
         off += v.vsize;
     }
     // data
@@ -265,6 +268,13 @@ extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec)
     ok = (fclose(fp) == 0) && ok;
     if (!ok) { vec_set_error("write to %s failed", path); return VEC_ERR_INPUT; }
     return VEC_OK;
+}
+
+extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec) { return nc_write(path, s, iprec, 1); }
+
+extern "C" int vec_nc_write_fmt(const char *path, const vec_snapshot *s, int iprec, int fmt)
+{
+    return nc_write(path, s, iprec, fmt);
 }
 
 extern "C" int vec_nc_read(const char *path, vec_snapshot *s)

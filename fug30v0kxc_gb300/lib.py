@@ -105,6 +105,7 @@ SIGNATURES = {
     "vec_expand": (C.c_int, [_vp, _vp, _dp, _dp]),
     "vec_upsample": (C.c_int, [_vp, _vp]),
     "vec_nc_write": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int]),
+    "vec_nc_write_fmt": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot), C.c_int, C.c_int]),
     "vec_nc_read": (C.c_int, [C.c_char_p, C.POINTER(VecSnapshot)]),
     "vec_write_snapshot": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_char_p]),
     "vec_read_restart": (C.c_int, [_vp, C.c_char_p]),

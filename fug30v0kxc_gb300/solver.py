@@ -271,8 +271,9 @@ def nc_read(path):
     return out
 
 
-def nc_write(path, snap, iprec=8):
-    """Write a dict like nc_read's result as a reference-layout snapshot."""
+def nc_write(path, snap, iprec=8, fmt=1):
+    """Write a dict like nc_read's result as a reference-layout snapshot
+    (fmt 1: classic NetCDF; fmt 2: 64-bit offsets)."""
     L = _L.load()
     s = VecSnapshot()
     nz, ny, nx = np.asarray(snap["R"]).shape
@@ -285,7 +286,7 @@ def nc_write(path, snap, iprec=8):
     keep = [np.ascontiguousarray(snap[n], dtype=np.float64) for n in SNAP_FIELDS]
     for i, a in enumerate(keep):
         s.fields[i] = a.ctypes.data
-    st = L.vec_nc_write(str(path).encode(), C.byref(s), iprec)
+    st = L.vec_nc_write_fmt(str(path).encode(), C.byref(s), iprec, fmt)
     if st != 0:
         raise VecError("vec_nc_write", st)
 

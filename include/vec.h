@@ -206,6 +206,10 @@ typedef struct vec_snapshot {
  * (src/netcdf.F90:39-585); iprec 4 (float) or 8 (double), cf.
  * src/main.F90:695-704. */
 int vec_nc_write(const char *path, const vec_snapshot *s, int iprec);
+/* the same with the file format chosen: fmt 1 classic (as above), fmt 2
+ * 64-bit offsets (NF_64BIT_OFFSET, the interpolate program's output,
+ * interpolate/netcdf.F90:73) */
+int vec_nc_write_fmt(const char *path, const vec_snapshot *s, int iprec, int fmt);
 /* Reads a classic NetCDF snapshot (OpenNetCDF/ReadNetCDF,
  * src/netcdf.F90:591-1166): sizes, parameters, time, iteration, timestep;
  * fields too when s->fields[i] are set and s->nx/ny/nz match the file. */

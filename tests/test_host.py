@@ -92,11 +92,14 @@ def _snapshot(nx=12, ny=10, nz=7, seed=0):
     return d
 
 
-@pytest.mark.parametrize("iprec", [4, 8])
-def test_snapshot_roundtrip_and_scipy(tmp_path, iprec):
+@pytest.mark.parametrize("iprec,fmt", [(4, 1), (8, 1), (8, 2)])
+def test_snapshot_roundtrip_and_scipy(tmp_path, iprec, fmt):
+    """fmt 1: classic NetCDF (src/netcdf.F90:74); fmt 2: 64-bit offsets
+    (the interpolate program's output, interpolate/netcdf.F90:73)."""
     snap = _snapshot()
     path = tmp_path / "T16_001.nc"
-    nc_write(path, snap, iprec)
+    nc_write(path, snap, iprec, fmt)
+    assert open(path, "rb").read(4) == b"CDF" + bytes([fmt])
     back = nc_read(path)
     for n in SNAP_FIELDS:
         ref = snap[n].astype(np.float32).astype(np.float64) if iprec == 4 else snap[n]
@@ -105,6 +108,7 @@ def test_snapshot_roundtrip_and_scipy(tmp_path, iprec):
     # an independent reader sees the reference's layout
     from scipy.io import netcdf_file
     with netcdf_file(str(path), "r", mmap=False) as f:
+        assert f.version_byte == fmt
         assert f.dimensions == {"nx": 12, "ny": 10, "nz": 7, "one": 1}
         assert f.variables["R"].shape == (7, 10, 12)
         assert f.variables["R"].typecode() == ("d" if iprec == 8 else "f")
