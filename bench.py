@@ -352,8 +352,11 @@ def dominant_roofline(prof, hbm_peak, peak_kind):
             "alg_bytes_per_launch": per_launch}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from the ncu capture
-# summarised under profiles/ (None until captured for the kernel)
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the split step at
+# 256x256x129, from the ncu capture summarised in
+# profiles/dram_traffic_split_256x256x129.md (other workloads: null)
+TRAFFIC_256x256x129 = {"line_x_f32": 311.8e6, "line_y_f32": 306.6e6, "hydro_pass2_f32": 1298.9e6,
+                       "ab3_update_split": 1838.4e6, "hydro_pass4_f32": 484.2e6}
 TRAFFIC = {}
 
 
@@ -444,6 +447,8 @@ def main():
         WORKLOAD = f"VarElecCond {NX}x{NY}x{NZ} Ra1e5 Q100 eta-contrast-20"
         METRIC = f"grid-point-steps/s at {NX}x{NY}x{NZ}"
 
+    if (NX, NY, NZ) == (256, 256, 129) and args.workload == "single":
+        TRAFFIC.update(TRAFFIC_256x256x129)
     if args.workload == "large":
         LARGE["on"] = True
         NX, NY, NZ = 1024, 1024, 513
