@@ -239,6 +239,8 @@ def closure_line(args, ws):
     else:
         kw = dict(nxf=256, nyf=256, nzf=129, pre_time=args.closure_pre_time, spinup=1000, pairs=200, pair_every=4,
                   iters=500, window=2000, diag_every=50, judge_every=min(args.closure_judge_every, 100), nfine=50)
+    if args.closure_window > 0:
+        kw["window"] = args.closure_window
     r = run_workload(log=lambda m: print("#", m, file=sys.stderr, flush=True), **kw)
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -431,6 +433,8 @@ def main():
                          "-> 64^2x33, 200 pairs")
     ap.add_argument("--closure-pre-time", type=float, default=1.5,
                     help="closure workload: model time the coarse solver develops convection before the DNS")
+    ap.add_argument("--closure-window", type=int, default=0,
+                    help="closure workload: DNS steps of the comparison window (0: 8000 full, 2000 small)")
     ap.add_argument("--closure-judge-every", type=int, default=2000,
                     help="closure workload: coarse steps between judged fine segments")
     ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large", "closure", "net"],
