@@ -249,6 +249,7 @@ def closure_line(args, ws):
         peak, pk = 1900.0, "fallback"
     ach = r.get("net_tflops_train")
     value = r["closure"]["max_err"] if "closure" in r else None
+    # the DNS wall time is the time of the steps it completed
     return {"metric": "closure: max relative error of the time-averaged top Nusselt number, kinetic and "
                       "magnetic energy vs the filtered DNS",
             "value": value, "unit": "fraction", "n_gpus": ws,

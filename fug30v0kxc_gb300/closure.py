@@ -347,18 +347,36 @@ def run_workload(nxf=512, nyf=512, nzf=257, factor=4, ra=1.0e6, q=1.0e3, eta=20.
 
     dns = [filtered_row()]
     tdns = 0.0
+    dt0 = F.scalars().dt
+    res["dns_blowup"] = 0
+    nstep = 0
     for _ in range(0, window, diag_every):
         F.sync()
         t0 = time.perf_counter()
-        assert F.step(diag_every) == 0
+        st = F.step(diag_every)
         F.sync()
         tdns += time.perf_counter() - t0
+        s = F.scalars()
+        # the window ends where the DNS stops advancing by finite steps not
+        # below 1e-3 of its first (an unstable DNS)
+        if st != 0 or not (np.isfinite(s.ttime) and np.isfinite(s.dt)) or s.ttime <= dns[-1][0] \
+                or s.dt < 1e-3 * dt0:
+            res["dns_blowup"] = 1
+            break
+        nstep += diag_every
         dns.append(filtered_row())
     tend = dns[-1][0]
     res["window_time"] = tend - tstart
-    res["dns_steps"] = window
+    res["dns_steps"] = nstep
     res["dns_s"] = tdns
-    say("DNS window", window, "steps", round(tdns, 1), "s, model time", tend - tstart)
+    say("DNS window", nstep, "steps", round(tdns, 1), "s, model time", tend - tstart,
+        "(stopped: the DNS stopped advancing)" if res["dns_blowup"] else "")
+    if nstep == 0:
+        res["error"] = "the DNS stopped advancing at the start of the window"
+        for o in (F, S, C1, C2):
+            o.close()
+        cl.close()
+        return res
     F2 = P3D(pf)
     r1, st1 = _row(C1)
     res["coarse_initial_divb_status"] = st1
