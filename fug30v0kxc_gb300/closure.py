@@ -355,7 +355,7 @@ def run_workload(nxf=512, nyf=512, nzf=257, factor=4, ra=1.0e6, q=1.0e3, eta=20.
         t0 = time.perf_counter()
         st = F.step(diag_every)
         F.sync()
-        tdns += time.perf_counter() - t0
+        tchunk = time.perf_counter() - t0
         s = F.scalars()
         # the window ends where the DNS stops advancing by finite steps not
         # below 1e-3 of its first (an unstable DNS)
@@ -363,6 +363,7 @@ def run_workload(nxf=512, nyf=512, nzf=257, factor=4, ra=1.0e6, q=1.0e3, eta=20.
                 or s.dt < 1e-3 * dt0:
             res["dns_blowup"] = 1
             break
+        tdns += tchunk
         nstep += diag_every
         dns.append(filtered_row())
     tend = dns[-1][0]
