@@ -58,6 +58,8 @@ extern "C" int vec_set_scalars(vec_ctx *c, const vec_scalars *s);
 extern "C" int vec_step(vec_ctx *c, int nsteps);
 extern "C" int vec_diag(vec_ctx *c, vec_diag_out *out);
 extern "C" int vec_calcdt(vec_ctx *c, double *dt);
+extern "C" int vec_create(const vec_params *p, vec_ctx **out);
+extern "C" int vec_destroy(vec_ctx *c);
 extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long long seed, vec_net **out);
 extern "C" int vec_net_destroy(vec_net *N);
 
@@ -82,6 +84,7 @@ struct vec_closure {
     vec_params pc;                   // coarse parameters
     float clip = 4.0f;               // |normalised output| limit at inference
     float gain = 1.0f;               // scale of the applied correction
+    vec_ctx *cs = nullptr;           // scratch coarse context (filtered diagnostics of a fine state)
 };
 
 // ---- background profiles: T0 = 1 + theta z, rho0 = T0^m (src/initial.F90:49-58)
@@ -620,6 +623,7 @@ extern "C" int vec_closure_destroy(vec_closure *cl)
     if (!cl) return VEC_OK;
     cudaDeviceSynchronize();
     if (cl->net) vec_net_destroy(cl->net);
+    if (cl->cs) vec_destroy(cl->cs);
     void *ps[] = { cl->in_ds, cl->tg_ds, cl->nrm, cl->filt_rhs, cl->crhs, cl->stats, cl->acc, cl->rho0c, cl->t0c,
                    cl->rho0f, cl->t0f };
     for (void *p : ps) if (p) cudaFree(p);
@@ -1000,15 +1004,15 @@ extern "C" int vec_upsample(vec_ctx *coarse, vec_ctx *fine)
 // t_end; every `every` steps the current coarse state is upsampled into
 // `fine` and the plain fine solver runs `nfine` steps; when the coarse run
 // reaches that segment's end time its diagnostics are compared with the
-// fine ones, and if the Nusselt number (at the bottom, as the reference, and
-// at the top), kinetic or magnetic energy differs by more than tol
+// box-filtered fine ones, and if the Nusselt number (at the bottom, as the
+// reference, and at the top), kinetic or magnetic energy differs by more than tol
 // (relative), the coarse state fails the div B check, or the coarse run
 // stops advancing, the run continues on the fine solver to t_end.  The fine
 // context always holds the state the fall-back continues from: the
 // upsampled start of the run, then the end of the last judged segment.
 // With diag_every > 0, rows (time, Nu, kinetic energy, magnetic energy,
-// top Nu) of the running solver are appended to series every diag_every
-// steps (at most cap rows).
+// top Nu) of the running solver (the fine one through the box filter) are
+// appended to series every diag_every steps (at most cap rows).
 extern "C" int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, double t_end, int every, int nfine,
                                double tol, int diag_every, double *series, int cap, vec_closure_report *rep)
 {
@@ -1017,9 +1021,18 @@ extern "C" int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, 
     rep->fallback_step = -1;
     int st;
     // diagnostics of c (+ the top Nusselt number); the div B check of
-    // src/main.F90:583-590 failing is reported through *divb, not as an error
+    // src/main.F90:583-590 failing is reported through *divb, not as an
+    // error.  The fine context is measured through the box filter (its state
+    // filtered into a scratch coarse context), so that fine and coarse
+    // diagnostics compare like with like.
+    if (!cl->cs && (st = vec_create(&cl->pc, &cl->cs))) return st;
     auto diag = [&](vec_ctx *c, vec_diag_out *d, double *nutop, int *divb) -> int {
-        int e = vec_diag(c, d);
+        int e;
+        if (c == fine) {
+            if ((e = vec_box_filter(cl, fine, cl->cs))) return e;
+            c = cl->cs;
+        }
+        e = vec_diag(c, d);
         if (e == VEC_ERR_DIVB) { *divb = 1; e = VEC_OK; }
         if (e) return e;
         return vec_top_nusselt(c, nutop);

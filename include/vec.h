@@ -357,10 +357,10 @@ int vec_closure_step(vec_closure *cl, vec_ctx *coarse, int nsteps);
  * stops advancing (non-finite time or step, or a step below 1e-3 of its
  * first), the run continues on the fine solver from the last state it holds
  * -- the upsampled start of the run, then the end of the last judged
- * segment -- (returning VEC_ERR_NAN if that stops advancing too).  With
- * diag_every > 0, rows (time, Nu, kinetic energy, magnetic energy, top Nu)
- * of the running solver are appended to series[cap][5] every diag_every
- * steps. */
+ * segment -- (returning VEC_ERR_NAN if that stops advancing too).  Fine
+ * diagnostics are taken of the box-filtered fine state.  With diag_every >
+ * 0, rows (time, Nu, kinetic energy, magnetic energy, top Nu) of the running
+ * solver are appended to series[cap][5] every diag_every steps. */
 int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, double t_end, int every, int nfine, double tol,
                     int diag_every, double *series, int cap, vec_closure_report *rep);
 
