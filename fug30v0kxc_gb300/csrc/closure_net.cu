@@ -335,8 +335,7 @@ __device__ __forceinline__ void tmem_ld<8>(unsigned taddr, float *v)
 constexpr int TC_RL = 144;
 constexpr int TC_X0 = 8;
 constexpr int TC_ROWS = 9;         // 3 planes x 3 rows
-constexpr int TC_NCH = 4;          // independent accumulator chains per tile (taps split 7, 7, 7, 6)
-constexpr int TC_TMEM_COLS = 256;  // two tiles x TC_NCH chains x 32 columns
+constexpr int TC_TMEM_COLS = 256;  // two tiles x (3 x COUT <= 96) columns
 
 // halo of row-tile a into h: [TC_ROWS][C/8][TC_RL][8].  One thread issues a
 // TMA box (8 channels x 128 points, 2 KB) per row and channel block within
@@ -398,17 +397,28 @@ __device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, con
 
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_halo_bytes() { return (size_t)TC_ROWS * TC_RL * CIN * sizeof(bf16); }
+// epilogue exchange at the warp boundaries: [2 tiles][4 quads][2 halves][3][COUT/2] floats
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t tc_xch_bytes() { return (size_t)2 * 4 * 2 * 3 * (COUT / 2) * sizeof(float); }
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_smem_bytes()
 {
-    // two halo buffers, the weights, then 4 KB of slack after the last operand
-    return 2 * tc_halo_bytes<CIN, COUT>() + (size_t)NTAP * COUT * CIN * sizeof(bf16) + 4096;
+    // two halo buffers, the weights, the epilogue exchange
+    return 2 * tc_halo_bytes<CIN, COUT>() + (size_t)NTAP * COUT * CIN * sizeof(bf16) + tc_xch_bytes<CIN, COUT>();
 }
 
 // warp roles: warps 0-7 read the accumulators back and run the epilogue,
 // warp 8 (the producer) copies halos in and issues the MMAs; they meet only
 // at mbarriers (per set b of buffers: tbar halo landed, full MMAs done,
-// empty epilogue done)
+// empty epilogue done).
+//
+// One MMA per input row r = (dz, dy) and 16-channel step computes the three
+// dx taps at once: A = the 128 halo points x = -1..126 of row r, B = the
+// weights of taps (r, dx = 0, 1, 2) stacked as N = 3 COUT rows.  TMEM row j
+// (point x = j - 1) then holds D_dx[j] for all dx, and by the periodicity in
+// x the output is out[x] = D_0[x] + D_1[(x + 1) mod 128] + D_2[(x + 2) mod
+// 128]: a circular shift that the epilogue does with warp shuffles and, at
+// the warp boundaries, a small shared-memory exchange.
 constexpr int TC_THREADS = 288;
 
 template <int CIN, int COUT, int EPI>
@@ -417,20 +427,24 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
           const float *__restrict__ bias, NetGeom g, bf16 *__restrict__ o_pre, bf16 *__restrict__ o_act,
           float *__restrict__ o_f32, int cout_real, const bf16 *__restrict__ gate, int *err)
 {
-    constexpr int C8 = CIN / 8, HC = COUT / 2;
-    constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
+    constexpr int C8 = CIN / 8, HC = COUT / 2, N3 = 3 * COUT;
+    constexpr uint32_t IDESC = umma_idesc_bf16(128, N3);
     extern __shared__ __align__(128) unsigned char smem[];
     bf16 *hb[2];
     hb[0] = reinterpret_cast<bf16 *>(smem);
     hb[1] = hb[0] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);
-    bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [27][C8][COUT][8]
+    bf16 *ws = hb[1] + tc_halo_bytes<CIN, COUT>() / sizeof(bf16);   // [9 rows][C8][3 COUT][8]
+    float *xch = reinterpret_cast<float *>(ws + (size_t)NTAP * COUT * CIN);
     __shared__ __align__(8) uint64_t tbar[2], full[2], empty[2];
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
+    // B rows of input row r: dx * COUT + n, from wt[tap = 3 r + dx][n][k]
     for (int e = tid; e < NTAP * COUT * C8; e += blockDim.x) {
-        const int tap = e / (COUT * C8), r = e % (COUT * C8), n = r / C8, k8 = r % C8;
-        cp16(su32(ws + (((size_t)tap * C8 + k8) * COUT + n) * 8), wt + ((size_t)tap * COUT + n) * CIN + k8 * 8, true);
+        const int tap = e / (COUT * C8), rr = e % (COUT * C8), n = rr / C8, k8 = rr % C8;
+        const int r = tap / 3, dx = tap % 3;
+        cp16(su32(ws + (((size_t)r * C8 + k8) * N3 + dx * COUT + n) * 8), wt + ((size_t)tap * COUT + n) * CIN + k8 * 8,
+             true);
     }
     if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
@@ -474,23 +488,16 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
                 if (okw) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const unsigned hbase = su32(hb[b]), wbase = su32(ws);
-                    const unsigned d0 = tmem + (unsigned)(b * TC_NCH * 32);
+                    const unsigned d = tmem + (unsigned)(b * 128);
 #pragma unroll 1
-                    for (int st = 0; st < 7; st++) {
+                    for (int r = 0; r < TC_ROWS; r++) {
 #pragma unroll
-                        for (int c = 0; c < TC_NCH; c++) {
-                            const int tap = 7 * c + st;
-                            if (tap >= NTAP) continue;
-                            const int row = (tap / 9) * 3 + (tap / 3) % 3, dx = tap % 3;
-#pragma unroll
-                            for (int kk = 0; kk < CIN / 16; kk++) {
-                                const uint64_t ad = umma_sdesc(
-                                    hbase + (unsigned)((((row * C8 + 2 * kk) * TC_RL) + TC_X0 - 1 + dx) * 16),
-                                    TC_RL * 16, 128);
-                                const uint64_t bd = umma_sdesc(
-                                    wbase + (unsigned)(((tap * C8 + 2 * kk) * COUT) * 16), COUT * 16, 128);
-                                umma_bf16(d0 + (unsigned)(c * 32), ad, bd, IDESC, (st | kk) != 0);
-                            }
+                        for (int kk = 0; kk < CIN / 16; kk++) {
+                            const uint64_t ad = umma_sdesc(
+                                hbase + (unsigned)((((r * C8 + 2 * kk) * TC_RL) + TC_X0 - 1) * 16), TC_RL * 16, 128);
+                            const uint64_t bd =
+                                umma_sdesc(wbase + (unsigned)(((r * C8 + 2 * kk) * N3) * 16), N3 * 16, 128);
+                            umma_bf16(d, ad, bd, IDESC, (r | kk) != 0);
                         }
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -509,8 +516,8 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
             }
         }
     } else {
-        // epilogue: warp w reads TMEM lanes 32 (w % 4).. (points) and the
-        // channels (w / 4) COUT / 2 .. of the four chains, and sums them
+        // epilogue: warp w owns TMEM lanes 32 (w % 4).. (quad q) and the
+        // channels (w / 4) COUT / 2 .. (half h)
         const int quad = warp & 3, half = warp >> 2, n0 = half * HC;
         int i = 0;
         for (long long t = t0; t < g.tiles; t += G, i++) {
@@ -521,22 +528,38 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const TileAt a = tile_at(g, t, TP);
-            float v[HC];
+            float v[HC], d1[HC], d2[HC];
             {
-                const unsigned ta = tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(b * TC_NCH * 32 + n0);
+                const unsigned ta = tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(b * 128 + n0);
                 tmem_ld<HC>(ta, v);
-#pragma unroll
-                for (int c = 1; c < TC_NCH; c++) {
-                    float u[HC];
-                    tmem_ld<HC>(ta + (unsigned)(c * 32), u);
-#pragma unroll
-                    for (int n = 0; n < HC; n++) v[n] += u[n];
-                }
+                tmem_ld<HC>(ta + (unsigned)COUT, d1);
+                tmem_ld<HC>(ta + (unsigned)(2 * COUT), d2);
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0)   // accumulators b are free again
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&empty[b])) : "memory");
+            // rows 32 q and 32 q + 1 to the previous quad's lanes 30 and 31
+            float *xo = xch + (((size_t)b * 4 + quad) * 2 + half) * 3 * HC;
+            if (lane == 0) {
+#pragma unroll
+                for (int n = 0; n < HC; n++) { xo[n] = d1[n]; xo[HC + n] = d2[n]; }
+            }
+            if (lane == 1) {
+#pragma unroll
+                for (int n = 0; n < HC; n++) xo[2 * HC + n] = d2[n];
+            }
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            const float *xi = xch + (((size_t)b * 4 + ((quad + 1) & 3)) * 2 + half) * 3 * HC;
+#pragma unroll
+            for (int n = 0; n < HC; n++) {
+                float s1 = __shfl_down_sync(0xffffffffu, d1[n], 1);
+                float s2 = __shfl_down_sync(0xffffffffu, d2[n], 2);
+                if (lane == 31) s1 = xi[n];
+                if (lane == 30) s2 = xi[HC + n];
+                if (lane == 31) s2 = xi[2 * HC + n];
+                v[n] += s1 + s2;
+            }
             const size_t gp = a.plane0 + a.q0 + quad * 32 + lane;
             if (EPI == EPI_ACT) {
                 __align__(16) __nv_bfloat162 pr[HC / 2], ac[HC / 2];
@@ -568,6 +591,10 @@ k_conv_tc(const bf16 *__restrict__ x, const __grid_constant__ CUtensorMap tmx, c
                 for (int q = 0; q < HC / 8; q++)
                     reinterpret_cast<uint4 *>(o_act + gp * COUT + n0)[q] = reinterpret_cast<const uint4 *>(ac)[q];
             }
+        }
+        // a warp that stopped early keeps the named barrier count of the others
+        if (failed) {
+            for (long long t = t0 + (long long)i * G; t < g.tiles; t += G) asm volatile("bar.sync 1, 256;" ::: "memory");
         }
     }
     if (failed && lane == 0) atomicExch(err, 2);
