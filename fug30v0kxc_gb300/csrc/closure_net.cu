@@ -386,12 +386,15 @@ __device__ __forceinline__ void load_halo_tc(bf16 *h, const CUtensorMap *tm, con
         const size_t gp = ok ? ((((size_t)a.b * g.nz + zz) * g.ny + yy) * g.nx + xx) : 0;
         cp16(su32(h + (((size_t)row * C8 + c) * TC_RL + (side ? TC_X0 + 128 : TC_X0 - 1)) * 8), src + gp * C + c * 8, ok);
     }
-    for (int e = tl; e < TC_ROWS * C8 * 128; e += nt) {
-        const int row = e / (C8 * 128);
-        const int zz = a.z + row / 3 - 1;
+    // rows outside the walls: only the first and last planes have any
+    for (int dzr = 0; dzr < 3; dzr++) {
+        const int zz = a.z + dzr - 1;
         if (zz >= 0 && zz < g.nz) continue;
-        const int c = (e / 128) % C8, xi = e % 128;
-        *reinterpret_cast<uint4 *>(h + (((size_t)row * C8 + c) * TC_RL + TC_X0 + xi) * 8) = make_uint4(0, 0, 0, 0);
+        for (int e = tl; e < 3 * C8 * 128; e += nt) {
+            const int row = dzr * 3 + e / (C8 * 128);
+            const int c = (e / 128) % C8, xi = e % 128;
+            *reinterpret_cast<uint4 *>(h + (((size_t)row * C8 + c) * TC_RL + TC_X0 + xi) * 8) = make_uint4(0, 0, 0, 0);
+        }
     }
 }
 
