@@ -1014,7 +1014,7 @@ extern "C" int vec_net_create(int nx, int ny, int nz, int batch, unsigned long l
         const char *e = getenv("VEC_NET_MT");
         N->conv_mt = (e && e[0] == '1') ? 1 : 2;
         const char *t = getenv("VEC_NET_TC");
-        N->conv_tc = (t && t[0] == '1') ? 1 : 0;
+        N->conv_tc = (t && t[0] == '0') ? 0 : 1;
     }
     int dev = 0;
     cudaGetDevice(&dev);

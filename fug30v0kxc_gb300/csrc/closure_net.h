@@ -16,7 +16,7 @@ struct vec_net {
     int cout_real = 8;      // output channels (padded to 16 inside)
     int num_sms = 152;
     int conv_mt = 2;        // m-tiles per warp in the convolution kernels (VEC_NET_MT=1: one)
-    int conv_tc = 0;        // forward / input gradient on tcgen05 for nx = 128 (VEC_NET_TC=1)
+    int conv_tc = 1;        // forward / input gradient on tcgen05 for nx = 128 (VEC_NET_TC=0: mma.sync)
     int *err = nullptr;     // set by a kernel whose bounded wait ran out
     cudaStream_t stream = nullptr;
     int own_stream = 0;
