@@ -261,6 +261,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     {
         const char *g = getenv("VEC_GENERIC_LINES");
         E.generic_lines = g && g[0] == '1';
+        const char *cw = getenv("VEC_CT_WARP");
+        E.ct_warp = !(cw && cw[0] == '0');
     }
     set_consts(E);
     int st;
@@ -790,7 +792,9 @@ static int enqueue_step(Engine &E, bool diag_now)
 {
     int st;
     const int mag = mag_on(E);
-    if (mag && E.par_mag) {
+    // (with per-kernel profiling on, the branches run one after the other so
+    // that no two timed kernels overlap)
+    if (mag && E.par_mag && !E.prof_on) {
         // mag_deriv on stream2 beside hydro_deriv on stream (disjoint outputs
         // and work arrays; both only read the state)
         CUDA_TRY(cudaEventRecord(E.ev_fork, E.stream));

@@ -103,6 +103,7 @@ struct Engine {
     // tunables (the ensemble autotuner sets them per grid)
     int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
     int ct_s = 0;               // sequences per line tile (0: default for the size)
+    bool ct_warp = true;        // x-line tiles synchronised per warp (VEC_CT_WARP=0: per CTA)
 
     // profiling
     bool prof_on = false;

@@ -149,6 +149,10 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
@@ -185,7 +189,13 @@ __host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 
 // ---- the kernel --------------------------------------------------------------------
 // DIR 0: x lines (a tile = 2S contiguous rows), DIR 1: y lines (a tile = 2S
 // adjacent columns over all ny rows).
-template <typename R, int DIR, int N1, int N2, int S>
+//
+// WS (x lines with NP dividing 32): the NP threads of a sequence sit in one
+// warp, so the exchanges need only warp barriers.  The warps then run
+// through their tiles independently; an "empty" mbarrier per tile buffer
+// (one arrival per warp once it has read the tile) tells the thread that
+// issues the TMA copies when a buffer may be refilled.
+template <typename R, int DIR, int N1, int N2, int S, bool WSYNC>
 __global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (S * (N1 > N2 ? N1 : N2) <= 256) ? 2 : 1)
 line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R> tb, int nx, int ny, int nz,
         int tpp, int total, int *err)
@@ -197,23 +207,38 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     constexpr int TILE = 2 * S * N;                   // reals per tile
     constexpr int LX = (N1 > N2 ? N1 : N2) + 1;       // padded exchange row
     constexpr int LDS = ((NP * LX) / 16) * 16 + 17;   // per-sequence exchange stride (== 1 mod 16)
+    constexpr bool WS = WSYNC && DIR == 0 && (32 % NP == 0) && NT % 32 == 0;
 
     extern __shared__ __align__(128) unsigned char smem[];
     R *tile0 = reinterpret_cast<R *>(smem);
     R *tile1 = tile0 + TILE;
     C *ex = reinterpret_cast<C *>(tile1 + TILE);
     C *tws = ex + (size_t)S * LDS;
-    __shared__ __align__(8) uint64_t bar[2];
+    R *sm1 = reinterpret_cast<R *>(tws + N);          // spectral multipliers
+    R *sm2 = sm1 + N;
+    R *smda = sm2 + N;
+    __shared__ __align__(8) uint64_t bar[4];          // full[2], empty[2]
 
     const int tid = threadIdx.x;
     const int sidx = DIR == 0 ? tid / NP : tid % S;
     const int lane = DIR == 0 ? tid % NP : tid / S;
     const size_t np = (size_t)nx * ny;
+    auto sync = [&]() {
+        if constexpr (WS) __syncwarp();
+        else __syncthreads();
+    };
 
-    for (int e = tid; e < N; e += NT) tws[e] = tb.tw[e];
+    for (int e = tid; e < N; e += NT) {
+        tws[e] = tb.tw[e];
+        sm1[e] = tb.m1[e];
+        sm2[e] = tb.m2[e];
+        smda[e] = tb.mda[e];
+    }
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], NT / 32);
+        mbar_init(&bar[3], NT / 32);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -247,6 +272,13 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
         R *cur = (it & 1) ? tile1 : tile0;
         R *nxt = (it & 1) ? tile0 : tile1;
         if (t + (int)gridDim.x < total) {
+            if (WS && it >= 1 && tid == 0) {
+                // every warp has read buffer nxt (its use in iteration it - 1)
+                if (!mbar_wait(&bar[2 + ((it + 1) & 1)], ((it - 1) >> 1) & 1)) {
+                    atomicExch(err, 1);
+                    return;
+                }
+            }
             if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(t + gridDim.x, nxt, &bar[(it + 1) & 1]);
         }
@@ -285,14 +317,14 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                     ex_s[k1 * LX + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
                 }
             }
-            __syncthreads();
+            sync();
             // second level: thread k1 = lane, N2-point DFT over m2
             if (lane < N1) {
 #pragma unroll
                 for (int m2 = 0; m2 < N2; m2++) X[m2] = ex_s[lane * LX + m2];
                 RDft<N2, false>::run(X);
             }
-            __syncthreads();
+            sync();
         } else if (lane < N1) {
             // halfcomplex input lines a (re) and b (im): Z_k = A_k + i B_k
 #pragma unroll
@@ -307,6 +339,11 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 X[k2].y = ai + br;
             }
         }
+        if constexpr (WS) {
+            // this warp is done with the tile buffer
+            __syncwarp();
+            if ((tid & 31) == 0) mbar_arrive(&bar[2 + (it & 1)]);
+        }
 
         if (op1 == OP_FWD) {
             // separate Z into the halfcomplex spectra of the two real lines
@@ -314,7 +351,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
 #pragma unroll
                 for (int k2 = 0; k2 < N2; k2++) ex_s[lane + N1 * k2 + ((lane + N1 * k2) >> 5)] = X[k2];
             }
-            __syncthreads();
+            sync();
             for (int p = lane; p < N; p += NP) {
                 const int q = p == 0 ? 0 : N - p;
                 C zp = ex_s[p + (p >> 5)], zq = ex_s[q + (q >> 5)];
@@ -322,14 +359,20 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 if (2 * p <= N) { va = (R)0.5 * (zp.x + zq.x); vb = (R)0.5 * (zp.y + zq.y); }
                 else { va = (R)0.5 * (zq.y - zp.y); vb = (R)0.5 * (zp.x - zq.x); }
                 const int la = l0 + 2 * sidx;
-                R *oa, *ob;
-                if (DIR == 0) { oa = jb.out1 + pbase + (size_t)la * nx + p; ob = oa + nx; }
-                else { oa = jb.out1 + pbase + (size_t)p * nx + la; ob = oa + 1; }
                 const R ra = jb.alpha1 * va, rb = jb.alpha1 * vb;
-                *oa = jb.acc1 ? *oa + ra : ra;
-                *ob = jb.acc1 ? *ob + rb : rb;
+                if (DIR == 0) {
+                    R *oa = jb.out1 + pbase + (size_t)la * nx + p, *ob = oa + nx;
+                    *oa = jb.acc1 ? *oa + ra : ra;
+                    *ob = jb.acc1 ? *ob + rb : rb;
+                } else {
+                    // the two lines are adjacent columns: one vector store
+                    C *o = reinterpret_cast<C *>(jb.out1 + pbase + (size_t)p * nx + la);
+                    C v = { ra, rb };
+                    if (jb.acc1) { const C q = *o; v.x += q.x; v.y += q.y; }
+                    *o = v;
+                }
             }
-            __syncthreads();
+            sync();
             continue;
         }
 
@@ -346,9 +389,9 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 for (int k2 = 0; k2 < N2; k2++) {
                     const int k = lane + N1 * k2;
                     C z = X[k2], y;
-                    if (op == OP_D1) { R m = tb.m1[k]; y.x = -m * z.y; y.y = m * z.x; }
+                    if (op == OP_D1) { R m = sm1[k]; y.x = -m * z.y; y.y = m * z.x; }
                     else if (op == OP_INV) { y = z; }
-                    else { R m = op == OP_D2 ? tb.m2[k] : tb.mda[k]; y.x = m * z.x; y.y = m * z.y; }
+                    else { R m = op == OP_D2 ? sm2[k] : smda[k]; y.x = m * z.x; y.y = m * z.y; }
                     Y[k2] = y;
                 }
                 // inverse, first level: thread k1 = lane, N2-point DFT over k2
@@ -360,7 +403,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                     ex_s[m2 * LX + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
                 }
             }
-            __syncthreads();
+            sync();
             // second level: thread m2 = lane, N1-point DFT over k1
             if (lane < N2) {
                 C a[N1];
@@ -375,17 +418,22 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
 #pragma unroll
                 for (int m1 = 0; m1 < N1; m1++) {
                     const int e = lane + N2 * m1;
-                    R *oa, *ob;
-                    if (DIR == 0) { oa = out + pbase + (size_t)la * nx + e; ob = oa + nx; }
-                    else { oa = out + pbase + (size_t)e * nx + la; ob = oa + 1; }
                     R va = alpha * (a[m1].x * sc), vb = alpha * (a[m1].y * sc);
-                    if (acc) { va = *oa + va; vb = *ob + vb; }
-                    if (op == OP_INV) { va = va + addv; vb = vb + addv; }
-                    *oa = va;
-                    *ob = vb;
+                    if (DIR == 0) {
+                        R *oa = out + pbase + (size_t)la * nx + e, *ob = oa + nx;
+                        if (acc) { va = *oa + va; vb = *ob + vb; }
+                        if (op == OP_INV) { va = va + addv; vb = vb + addv; }
+                        *oa = va;
+                        *ob = vb;
+                    } else {
+                        C *o = reinterpret_cast<C *>(out + pbase + (size_t)e * nx + la);
+                        if (acc) { const C q = *o; va = q.x + va; vb = q.y + vb; }
+                        if (op == OP_INV) { va = va + addv; vb = vb + addv; }
+                        *o = C{ va, vb };
+                    }
                 }
             }
-            __syncthreads();
+            sync();
         }
     }
 }
@@ -461,7 +509,7 @@ static int encode_ymap(CUtensorMap *m, const R *base, int nx, int ny, int nz, in
     return VEC_OK;
 }
 
-template <typename R, int DIR, int N1, int N2, int S>
+template <typename R, int DIR, int N1, int N2, int S, bool WSYNC>
 static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
 {
     using C = typename CT<R>::T;
@@ -471,9 +519,10 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     constexpr int LX = NP + 1;
     constexpr int LDS = ((NP * LX) / 16) * 16 + 17;
     static bool attr_set = false;
-    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + N) * sizeof(C);
+    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + N) * sizeof(C) + 3 * (size_t)N * sizeof(R);
     if (!attr_set) {
-        CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S, WSYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
         attr_set = true;
     }
     const int L = DIR == 0 ? E->ny : E->nx;
@@ -497,13 +546,13 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     }
     const int total = nj * E->nz * tpp;
     int per_sm = 1;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_ct<R, DIR, N1, N2, S>, S * NP, smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_ct<R, DIR, N1, N2, S, WSYNC>, S * NP, smem));
     if (per_sm < 1) per_sm = 1;
     int grid = E->num_sms * per_sm;
     if (grid > total) grid = total;
     E->prof_begin(name, fields * (double)E->n * sizeof(R));
-    line_ct<R, DIR, N1, N2, S><<<grid, S * NP, smem, E->stream>>>(pk, tp, E->tables<R>(DIR), E->nx, E->ny, E->nz,
-                                                                  tpp, total, E->dev_err);
+    line_ct<R, DIR, N1, N2, S, WSYNC><<<grid, S * NP, smem, E->stream>>>(pk, tp, E->tables<R>(DIR), E->nx, E->ny,
+                                                                         E->nz, tpp, total, E->dev_err);
     E->prof_end();
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;
@@ -534,13 +583,17 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
         if (!aligned16(jobs[j].in) || !aligned16(jobs[j].out1) || (jobs[j].out2 && !aligned16(jobs[j].out2)))
             return 0;
     }
+    const bool ws = E->ct_warp;
     for (int j0 = 0; j0 < njobs; j0 += MAX_JOBS) {
         const int nj = njobs - j0 < MAX_JOBS ? njobs - j0 : MAX_JOBS;
         const LineJob<R> *jb = jobs + j0;
         const char *name = dir == 0 ? (F ? "line_x_f32" : "line_x_f64") : (F ? "line_y_f32" : "line_y_f64");
         int st = -1;
 #define CT_CASE(NN, A, B, SS)                                                                       \
-    if (n == NN && S == SS) st = dir == 0 ? run_ct<R, 0, A, B, SS>(E, jb, nj, name) : run_ct<R, 1, A, B, SS>(E, jb, nj, name);
+    if (n == NN && S == SS)                                                                         \
+        st = dir == 1 ? run_ct<R, 1, A, B, SS, false>(E, jb, nj, name)                            \
+                      : (ws ? run_ct<R, 0, A, B, SS, true>(E, jb, nj, name)                       \
+                            : run_ct<R, 0, A, B, SS, false>(E, jb, nj, name));
         if constexpr (F) {
             CT_CASE(64, 8, 8, 16) CT_CASE(128, 16, 8, 16) CT_CASE(256, 16, 16, 16)
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
