@@ -263,6 +263,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         E.generic_lines = g && g[0] == '1';
         const char *cw = getenv("VEC_CT_WARP");
         E.ct_warp = !(cw && cw[0] == '0');
+        const char *hc = getenv("VEC_HW_CVT");
+        E.int_cvt = !(hc && hc[0] == '1');
     }
     set_consts(E);
     int st;
@@ -315,6 +317,33 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         vec_destroy(c);
         return VEC_ERR_CUDA;
     }
+    {
+        // the wavenumber tables per precision; kh2 = akx2[i] + aky2[j] per plane point
+        std::vector<double> kh2(E.np);
+        std::vector<float> kx1f(E.nx), ky1f(E.ny), kh2f(E.np);
+        for (int j = 0; j < E.ny; j++)
+            for (int i = 0; i < E.nx; i++) {
+                kh2[(size_t)j * E.nx + i] = akx2[i] + aky2[j];
+                kh2f[(size_t)j * E.nx + i] = (float)kh2[(size_t)j * E.nx + i];
+            }
+        for (int i = 0; i < E.nx; i++) kx1f[i] = (float)akx1[i];
+        for (int j = 0; j < E.ny; j++) ky1f[j] = (float)aky1[j];
+        float *fx = nullptr, *fy = nullptr, *fk = nullptr;
+        double *dk = nullptr;
+        ALLOC(fx, sizeof(float) * E.nx); E.hf.kx1 = fx;
+        ALLOC(fy, sizeof(float) * E.ny); E.hf.ky1 = fy;
+        ALLOC(fk, sizeof(float) * E.np); E.hf.kh2 = fk;
+        ALLOC(dk, sizeof(double) * E.np); E.hd.kh2 = dk;
+        E.hd.kx1 = E.akx1;
+        E.hd.ky1 = E.aky1;
+        if (cudaMemcpy(fx, kx1f.data(), sizeof(float) * E.nx, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(fy, ky1f.data(), sizeof(float) * E.ny, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(fk, kh2f.data(), sizeof(float) * E.np, cudaMemcpyHostToDevice) != cudaSuccess ||
+            upload(dk, kh2)) {
+            vec_destroy(c);
+            return VEC_ERR_CUDA;
+        }
+    }
     // kappa(z): src/trans_params.f90:36-62; eta(z): the extension
     std::vector<double> kap(nz), dkap(nz), eta(nz), deta(nz);
     double emax = 0.0;
@@ -359,6 +388,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     E.red_blocks = 152 * 4;
     ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 24 + 64));
     ALLOC(E.ds, sizeof(DevScalars));
+    ALLOC(E.cdt, sizeof(float) * (4 + 3 * (size_t)cdt_chunks(E.n)));
+    if ((st = cdt_init(E.cdt))) { vec_destroy(c); return st; }
     ALLOC(E.dev_err, sizeof(int) * 4);
     if (cudaMallocHost(&E.hs, sizeof(DevScalars)) != cudaSuccess) { vec_destroy(c); return VEC_ERR_ALLOC; }
     memset(E.hs, 0, sizeof(DevScalars));
@@ -380,10 +411,12 @@ extern "C" int vec_destroy(vec_ctx *c)
     if (E.stream) cudaStreamSynchronize(E.stream);
     E.drop_graphs();
     void *ptrs[] = { E.r, E.t, E.u, E.v, E.w, E.bx, E.by, E.bz, E.jsq, E.pol, E.tor, E.bxbar, E.bybar,
-                     E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds, E.dev_err,
+                     E.kappa, E.dkappa, E.eta, E.deta, E.akx1, E.akx2, E.aky1, E.aky2, E.w1d, E.red, E.ds, E.dev_err, E.cdt,
                      E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
                      E.rho0, E.t0, E.hres, E.corr, E.corr_bx };
     for (void *q : ptrs) if (q) cudaFree(q);
+    const void *tabs[] = { E.hf.kx1, E.hf.ky1, E.hf.kh2, E.hd.kh2, E.pcf };
+    for (const void *q : tabs) if (q) cudaFree((void *)q);
     for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hbuf[f][s]) cudaFree(E.hbuf[f][s]);
     for (int s = 0; s < 3; s++) { if (E.bxd_buf[s]) cudaFree(E.bxd_buf[s]); if (E.byd_buf[s]) cudaFree(E.byd_buf[s]); }
     if (E.ht) cudaFree(E.ht);
@@ -485,7 +518,7 @@ extern "C" int vec_set_field(vec_ctx *c, int field, const double *src)
         int st;
         if (E.split && (st = split_sync_b64(&E))) return st;
         if ((st = stage_in(E, d, src, E.n))) return st;
-        if (E.split && (st = split_refresh(&E))) return st;
+        if (E.split && (st = split_refresh_field(&E, field))) return st;
         CUDA_TRY(cudaStreamSynchronize(E.stream));
         return VEC_OK;
     }
@@ -542,6 +575,8 @@ extern "C" int vec_set_mean(vec_ctx *c, int m, const double *src)
     double *d = mean_ptr(c->E, m);
     if (!d) return VEC_ERR_ARG;
     int st = stage_in(c->E, d, src, c->E.nz);
+    if (!st && c->E.split && (m == VEC_M_KAPPA || m == VEC_M_DKAPPA || m == VEC_M_ETA || m == VEC_M_DETA))
+        st = split_refresh_coefs(&c->E);   // their FP32 per-plane copies
     return st ? st : vec_sync(c);
 }
 

@@ -207,10 +207,10 @@ static int bandj_linear(Engine *E, const R *pol, const R *tor, const double *bxm
     int st;
     KLAUNCH(E, "closure_d1z", k_d1z_t<R>, nblk(E->n), TPB, pol, W[W_M1], E->np, E->nz, (R)E->k.ho12);
     BandjArgs<R> a;
-    a.dzs = W[W_M1]; a.pol = pol; a.tor = tor; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.dzs = W[W_M1]; a.pol = pol; a.tor = tor; a.h = htab<R>(*E);
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCH(E, "closure_bandj_spec", k_bandj_spec<R>, nblk(E->n), TPB, a);
+    KLAUNCH(E, "closure_bandj_spec", k_bandj_spec<R>, plane_grid(*E), TPB, a);
     LineJob<R> ix[3] = { ljob<R>(W[W_EX], W[W_EX], OP_INV), ljob<R>(W[W_EY], W[W_EY], OP_INV),
                          ljob<R>(W[W_EZ], W[W_EZ], OP_INV) };
     if ((st = launch_lines<R>(E, 0, ix, 3))) return st;
@@ -527,7 +527,7 @@ static int corr_from_out(Engine &E, const float *out, const float *nrm, float cl
     if ((st = launch_lines<R>(&E, 0, fx, 3))) return st;
     if ((st = launch_lines<R>(&E, 1, fx, 3))) return st;
     for (int f = 0; f < 3; f++)
-        KLAUNCH((&E), "closure_truncate", k_truncate<R>, nblk(E.n), TPB, bd + (size_t)f * E.n, (R *)nullptr, E.nx,
+        KLAUNCH((&E), "closure_truncate", k_truncate<R>, plane_grid(E), TPB, bd + (size_t)f * E.n, (R *)nullptr, E.nx,
                 E.ny, E.nz, E.k.icutoffx, E.k.icutoffy);
     KLAUNCH((&E), "closure_corr_means", k_corr_means<R>, 1, 256, ex, ey, E.corr_bx, E.corr_by, E.np, E.nz, E.k.xn);
     KLAUNCH((&E), "closure_corr_poltor", k_corr_poltor<R>, nblk(E.n), TPB, ex, ey, ez, corr + 5 * E.n,

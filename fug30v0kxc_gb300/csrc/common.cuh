@@ -56,6 +56,13 @@ struct LineTables {
     R *mda;                 // dealias mask (1/n or 0)
 };
 
+// horizontal wavenumber tables in one precision: akx1, aky1 and the
+// plane table akx2[i] + aky2[j] (summed in FP64, then rounded once)
+template <typename R>
+struct HTab {
+    const R *kx1, *ky1, *kh2;
+};
+
 // ---- per-context derived constants: src/constants.f90:56-109 -----------
 struct Consts {
     double dx, dy, dz, dd, xn, xzn, taylt, cpsi, spsi, cor;

@@ -64,6 +64,9 @@ struct Engine {
     double *bxbar = nullptr, *bybar = nullptr;
     double *kappa = nullptr, *dkappa = nullptr, *eta = nullptr, *deta = nullptr;
     double *akx1 = nullptr, *akx2 = nullptr, *aky1 = nullptr, *aky2 = nullptr;
+    HTab<float> hf = {};        // the same wavenumbers in FP32 (kh2: np values)
+    HTab<double> hd = {};       // FP64 (kx1, ky1 alias akx1, aky1)
+    float *pcf = nullptr;       // split: per-plane FP32 coefficients [PC_COUNT][nz]
     double *w1d = nullptr;      // 1-D scratch (8 nz)
     double bzbar = 0.0;
     // work arrays (bulk precision), carved from one contiguous block
@@ -79,6 +82,7 @@ struct Engine {
     int b32_auth = 0;           // split form: the FP32 B/jsq are newer than the FP64 ones
     // reductions scratch
     double *red = nullptr;      // per-block partials
+    float *cdt = nullptr;       // calcdt: 3 global estimate keys (+1 pad), then [3][chunks] estimates
     int red_blocks = 0;
     DevScalars *ds = nullptr;   // device scalars
     DevScalars *hs = nullptr;   // pinned host mirror
@@ -104,6 +108,8 @@ struct Engine {
     int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
     int ct_s = 0;               // sequences per line tile (0: default for the size)
     bool ct_warp = true;        // x-line tiles synchronised per warp (VEC_CT_WARP=0: per CTA)
+    bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
+                                // (VEC_HW_CVT=1: hardware conversions; the same bits)
 
     // profiling
     bool prof_on = false;
@@ -127,6 +133,11 @@ struct Engine {
 };
 
 template <> inline const LineTables<double> &Engine::tables<double>(int dir) const { return dir == 0 ? tx64 : ty64; }
+template <typename R> inline HTab<R> htab(const Engine &E);
+// one CTA row of 256 threads per plane (the spectral kernels of magkern.cuh)
+inline dim3 plane_grid(const Engine &E) { return dim3((unsigned)((E.np + 255) / 256), (unsigned)E.nz); }
+template <> inline HTab<float> htab<float>(const Engine &E) { return E.hf; }
+template <> inline HTab<double> htab<double>(const Engine &E) { return E.hd; }
 template <> inline const LineTables<float> &Engine::tables<float>(int dir) const { return dir == 0 ? tx32 : ty32; }
 
 // lines.cu
@@ -137,6 +148,9 @@ template <typename R> int line_tables_make(int n, const double *k1, const double
 template <typename R> void line_tables_free(LineTables<R> *tb);
 template <typename R> int launch_lines(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
 int line_kernels_configure();
+// physics.cu: calcdt scratch (floats per context, initialisation of its keys)
+int cdt_chunks(size_t n);
+int cdt_init(float *cdt);
 int line_ct_configure();
 template <typename R> int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs);
 
@@ -181,10 +195,12 @@ Engine &engine_of(vec_ctx *c);
 int closure_apply_corr(Engine *E);
 // split form (split.cu)
 int split_setup(Engine *E);
+int split_refresh_coefs(Engine *E);   // after kappa / eta change
 int split_hydro(Engine *E);
 int split_mag(Engine *E);
 int split_bandj(Engine *E);
 int split_refresh(Engine *E);
+int split_refresh_field(Engine *E, int field);   // one field's mirror (VEC_F_*)
 int split_refresh_planes(Engine *E, int mask);
 int split_refresh_uv(Engine *E);
 int split_sync_b64(Engine *E);

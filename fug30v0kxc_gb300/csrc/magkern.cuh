@@ -48,67 +48,71 @@ static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar,
     }
 }
 
+// The spectral kernels below run one CTA row per plane (grid (np/256, nz)):
+// k = blockIdx.y, the in-plane index in 32 bits, and the wavenumber tables
+// in the kernel's precision (HTab), so that no FP64 arithmetic or 64-bit
+// division is spent per point.
+
 // wk1 = dEx/dx + dEy/dy in spectral space (:362-407)
 template <typename R>
-static __global__ void k_mag_div(const R *ex, const R *ey, R *w1, int nx, int ny, int nz, const double *akx1,
-                                 const double *aky1)
+static __global__ void k_mag_div(const R *ex, const R *ey, R *w1, int nx, int ny, HTab<R> h)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t np = (size_t)nx * ny;
-    if (idx >= np * nz) return;
-    int k = (int)(idx / np);
-    size_t q = idx - (size_t)k * np;
-    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
-    const R *px = ex + (size_t)k * np, *py = ey + (size_t)k * np;
-    w1[idx] = sdx(px, i, j, nx, akx1) + sdy(py, i, j, nx, ny, aky1);
+    const unsigned np = (unsigned)nx * ny;
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const size_t pb = (size_t)blockIdx.y * np;
+    const int j = (int)(q / (unsigned)nx), i = (int)(q - (unsigned)j * nx);
+    w1[pb + q] = sdx(ex + pb, i, j, nx, h.kx1) + sdy(ey + pb, i, j, nx, ny, h.ky1);
 }
 
 template <typename R>
 struct MagArgs {
     const R *ex, *ey, *ez, *w1, *pol, *tor;
-    const double *eta, *deta, *akx1, *aky1, *akx2, *aky2;
+    const R *eta, *deta;    // eta(z), eta'(z) in the kernel's precision
+    HTab<R> h;
     const HistTable *ht;    // poldot / tordot = newest slots
-    double zck, ho12, sc1;
+    R zck, ho12, sc1;
     int var_eta, nx, ny, nz;
 };
 
 // :400-479 -- wk2 = dEx/dy - dEy/dx, wk3 = d/dz(wk1), inverse horizontal
-// Laplacian, d2/dz2 of pol and tor, and the final poldot / tordot.
+// Laplacian, d2/dz2 of pol and tor, and the final poldot / tordot.  One
+// thread per point (grid (np/256, nz)); the neighbouring planes of the z
+// stencils come from L1/L2.
 template <typename R>
 static __global__ void k_mag_final(MagArgs<R> a)
 {
-    const size_t np = (size_t)a.nx * a.ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * a.nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
-    const R *px = a.ex + (size_t)k * np, *py = a.ey + (size_t)k * np;
-    R w2 = sdy(px, i, j, a.nx, a.ny, a.aky1) - sdx(py, i, j, a.nx, a.akx1);
-    R w3 = zd1(a.w1 + q, np, k, a.nz, 5, (R)a.ho12);
-    const R kk = (R)(a.akx2[i] + a.aky2[j]);
-    if (i == 0 && j == 0) { w2 = (R)0; w3 = (R)0; }
+    const unsigned np = (unsigned)a.nx * a.ny;
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int k = blockIdx.y;
+    const size_t pb = (size_t)k * np, idx = pb + q;
+    const int j = (int)(q / (unsigned)a.nx), i = (int)(q - (unsigned)j * a.nx);
+    R w2 = sdy(a.ex + pb, i, j, a.nx, a.ny, a.h.ky1) - sdx(a.ey + pb, i, j, a.nx, a.h.kx1);
+    R w3 = zd1(a.w1 + q, (size_t)np, k, a.nz, 5, a.ho12);
+    const R kk = a.h.kh2[q];
+    if (q == 0) { w2 = (R)0; w3 = (R)0; }
     else { w2 = w2 / kk; w3 = w3 / kk; }
-    const R d2p = zd2(a.pol + q, np, k, a.nz, 3, (R)a.sc1);
-    const R d2t = zd2(a.tor + q, np, k, a.nz, 3, (R)a.sc1);
+    const R d2p = zd2(a.pol + q, (size_t)np, k, a.nz, 3, a.sc1);
+    const R d2t = zd2(a.tor + q, (size_t)np, k, a.nz, 3, a.sc1);
     R *poldot = (R *)a.ht->p[5][2], *tordot = (R *)a.ht->p[6][2];
     if (!a.var_eta) {
-        const R zck = (R)a.zck;
+        const R zck = a.zck;
         poldot[idx] = zck * a.pol[idx] * kk + zck * d2p + w2;
         tordot[idx] = zck * a.tor[idx] * kk + zck * d2t - w3 + a.ez[idx];
     } else {
         // extension: eta(z) replaces zeta*ck, tordot gains eta'(z) d(tor)/dz
-        const R e = (R)a.eta[k];
-        const R dt = zd1(a.tor + q, np, k, a.nz, 5, (R)a.ho12);
+        const R e = a.eta[k];
+        const R dt = zd1(a.tor + q, (size_t)np, k, a.nz, 5, a.ho12);
         poldot[idx] = e * a.pol[idx] * kk + e * d2p + w2;
-        tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + (R)a.deta[k] * dt;
+        tordot[idx] = e * a.tor[idx] * kk + e * d2t - w3 + a.ez[idx] + a.deta[k] * dt;
     }
 }
 
 template <typename R>
 struct BandjArgs {
     const R *dzs, *pol, *tor;
-    const double *akx1, *aky1, *akx2, *aky2;
+    HTab<R> h;
     R *bxh, *byh, *bzh, *dybz, *dxbz, *jzh;
     int nx, ny, nz;
 };
@@ -117,30 +121,29 @@ struct BandjArgs {
 template <typename R>
 static __global__ void k_bandj_spec(BandjArgs<R> a)
 {
-    const size_t np = (size_t)a.nx * a.ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * a.nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
-    const int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
-    const size_t pb = (size_t)k * np;
+    const unsigned np = (unsigned)a.nx * a.ny;
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const size_t pb = (size_t)blockIdx.y * np, idx = pb + q;
+    const int j = (int)(q / (unsigned)a.nx), i = (int)(q - (unsigned)j * a.nx);
     const R *s = a.dzs + pb, *tp = a.tor + pb, *pp = a.pol + pb;
-    a.bxh[idx] = sdx(s, i, j, a.nx, a.akx1) + sdy(tp, i, j, a.nx, a.ny, a.aky1);
-    a.byh[idx] = sdy(s, i, j, a.nx, a.ny, a.aky1) - sdx(tp, i, j, a.nx, a.akx1);
-    a.bzh[idx] = (R)-1 * a.pol[idx] * (R)(a.akx2[i] + a.aky2[j]);
-    a.jzh[idx] = (R)-1 * a.tor[idx] * (R)(a.akx2[i] + a.aky2[j]);
+    a.bxh[idx] = sdx(s, i, j, a.nx, a.h.kx1) + sdy(tp, i, j, a.nx, a.ny, a.h.ky1);
+    a.byh[idx] = sdy(s, i, j, a.nx, a.ny, a.h.ky1) - sdx(tp, i, j, a.nx, a.h.kx1);
+    const R kk = a.h.kh2[q];
+    a.bzh[idx] = (R)-1 * pp[q] * kk;
+    a.jzh[idx] = (R)-1 * tp[q] * kk;
     // d/dy and d/dx of ez = -pol*(akx2+aky2), evaluated at the mirrored index
     R dy = (R)0, dx = (R)0;
     if (!(j == 0 || 2 * j == a.ny)) {
-        int jm = a.ny - j;
-        R ezm = (R)-1 * pp[(size_t)jm * a.nx + i] * (R)(a.akx2[i] + a.aky2[jm]);
-        dy = ezm * (R)a.aky1[j];
+        const unsigned m = (unsigned)(a.ny - j) * a.nx + i;
+        R ezm = (R)-1 * pp[m] * a.h.kh2[m];
+        dy = ezm * a.h.ky1[j];
         if (2 * j < a.ny) dy = -dy;
     }
     if (!(i == 0 || 2 * i == a.nx)) {
-        int im = a.nx - i;
-        R ezm = (R)-1 * pp[(size_t)j * a.nx + im] * (R)(a.akx2[im] + a.aky2[j]);
-        dx = ezm * (R)a.akx1[i];
+        const unsigned m = (unsigned)j * a.nx + (a.nx - i);
+        R ezm = (R)-1 * pp[m] * a.h.kh2[m];
+        dx = ezm * a.h.kx1[i];
         if (2 * i < a.nx) dx = -dx;
     }
     a.dybz[idx] = dy;
@@ -148,18 +151,26 @@ static __global__ void k_bandj_spec(BandjArgs<R> a)
 }
 
 // :630-645: jsq from Jz, dBz/dy, dBz/dx and the z derivatives of Bx, By
+// (grid (np/256, nz))
 template <typename R>
 static __global__ void k_jsq(const R *jz, const R *dybz, const R *dxbz, const R *bx, const R *by, R *jsq,
                              size_t np, int nz, R h)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * nz) return;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int k = blockIdx.y;
+    const size_t idx = (size_t)k * np + q;
     R wk1 = zd1(by + q, np, k, nz, 5, h);
     R wk2 = zd1(bx + q, np, k, nz, 5, h);
     R ez = jz[idx], ex = dybz[idx], ey = dxbz[idx];
     jsq[idx] = ez * ez + ((ex - wk1) * (ex - wk1)) + ((wk2 - ey) * (wk2 - ey));
+}
+
+// planes per z-marching chunk and its grid
+#define ZCHUNK 16
+inline dim3 zmarch_grid(size_t np, int nz, int kc = ZCHUNK)
+{
+    return dim3((unsigned)((np + 255) / 256), (unsigned)((nz + kc - 1) / kc));
 }
 
 // spectral truncation of the 2/3 rule, src/magnetic.f90:666-717
@@ -168,14 +179,15 @@ __host__ __device__ __forceinline__ bool truncated(int i, int j, int nx, int ny,
     return (i >= nx / 2 - cx && i <= nx / 2 + cx) || (j >= ny / 2 - cy && j <= ny / 2 + cy);
 }
 
+// (grid (np/256, nz))
 template <typename R>
 static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, int cy)
 {
-    size_t np = (size_t)nx * ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * nz) return;
-    size_t q = idx % np;
-    int j = (int)(q / nx), i = (int)(q - (size_t)j * nx);
+    const unsigned np = (unsigned)nx * ny;
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const size_t idx = (size_t)blockIdx.y * np + q;
+    const int j = (int)(q / (unsigned)nx), i = (int)(q - (unsigned)j * nx);
     if (truncated(i, j, nx, ny, cx, cy)) {
         a[idx] = (R)0;
         if (b) b[idx] = (R)0;

@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "fpconv.cuh"
 #include "zstencil.cuh"
 #include "magkern.cuh"
 
@@ -313,14 +314,15 @@ int phys_mag64(Engine *E)
     const Consts &c = E->k;
     KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
             E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
-    KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->nz, E->akx1, E->aky1);
+    KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
+             E->nx, E->ny, E->hd);
     MagArgs<double> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol; a.tor = E->tor;
-    a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.eta = E->eta; a.deta = E->deta; a.h = E->hd;
     a.ht = E->ht;
     a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final<double>, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "mag_final_f64", FB(E, 8, 8), k_mag_final<double>, plane_grid(*E), TPB, a);
     return VEC_OK;
 }
 
@@ -344,11 +346,10 @@ int phys_bandj64(Engine *E)
     int st;
     if ((st = op_d1z(E, E->pol, W[W_M1], 5, (int)E->np, E->nz))) return st;   // :519
     BandjArgs<double> a;
-    a.dzs = W[W_M1]; a.pol = E->pol; a.tor = E->tor; a.akx1 = E->akx1; a.aky1 = E->aky1;
-    a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.dzs = W[W_M1]; a.pol = E->pol; a.tor = E->tor; a.h = E->hd;
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "bandj_spec_f64", FB(E, 9, 8), k_bandj_spec<double>, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "bandj_spec_f64", FB(E, 9, 8), k_bandj_spec<double>, plane_grid(*E), TPB, a);
     // six inverse 2-D transforms (:575-577, :623-625): x pass in place, then y
     LineJob<double> ix[6] = { ljob<double>(W[W_EX], W[W_EX], OP_INV), ljob<double>(W[W_EY], W[W_EY], OP_INV),
                               ljob<double>(W[W_EZ], W[W_EZ], OP_INV), ljob<double>(W[W_M2], W[W_M2], OP_INV),
@@ -361,7 +362,8 @@ int phys_bandj64(Engine *E)
     iy[1].addk = E->bybar;
     iy[2].addc = E->bzbar;
     if ((st = launch_lines<double>(E, 1, iy, 6))) return st;
-    KLAUNCHB(E, "jsq_f64", FB(E, 6, 8), k_jsq<double>, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx, E->by, E->jsq, E->np, E->nz, E->k.ho12);
+    KLAUNCHB(E, "jsq_f64", FB(E, 6, 8), k_jsq<double>, plane_grid(*E), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx,
+             E->by, E->jsq, E->np, E->nz, E->k.ho12);
     return VEC_OK;
 }
 
@@ -370,7 +372,7 @@ int phys_bandj64(Engine *E)
 // ============================================================================
 int phys_magdealias(Engine *E)
 {
-    KLAUNCH(E, "magdealias_f64", k_truncate<double>, nblk(E->n), TPB, E->pol, E->tor, E->nx, E->ny, E->nz,
+    KLAUNCH(E, "magdealias_f64", k_truncate<double>, plane_grid(*E), TPB, E->pol, E->tor, E->nx, E->ny, E->nz,
             E->k.icutoffx, E->k.icutoffy);
     return VEC_OK;
 }
@@ -604,20 +606,142 @@ __device__ __forceinline__ double okey_dec(unsigned long long e)
     return __longlong_as_double((long long)u);
 }
 
-template <typename R>
-__global__ void k_calcdt_red(const R *u, const R *v, const R *w, const R *r, const R *t, const R *bx, const R *by,
-                             const R *bz, size_t n, double g1, double f, DevScalars *ds)
+// The maxima of src/utils.F90:190-214 need the FP64 expression only at the
+// points that can hold them, and GB300's FP64 square roots are slow.  So:
+//
+// pass 1 (k_calcdt_est): per chunk of CDT_CHUNK points, FP32 estimates of
+//   xx = |u_h| + g1 sqrt(T) + sqrt(f B^2 / rho) and xz (|w| in place of |u_h|)
+//   and the minimum density, their chunk extrema, and the global extrema;
+// pass 2 (k_calcdt_exact): the few chunks whose estimate lies within
+//   CDT_MARGIN of the global one evaluate the FP64 expression at every point
+//   whose estimate does, and reduce those exact values.
+//
+// The estimates carry a relative error of a few FP32 ulps (all terms are
+// non-negative), far below CDT_MARGIN, so the point holding the exact
+// maximum (minimum) always passes both filters.  Estimates only choose
+// points; the results are the same FP64 extrema as a full FP64 pass.
+#define CDT_CHUNK 8192
+#define CDT_MARGIN 1.0e-3f
+
+// order-preserving keys of floats (as okey for doubles)
+__device__ __forceinline__ unsigned okey32(float x)
 {
+    unsigned u = __float_as_uint(x);
+    return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float okey32_dec(unsigned e)
+{
+    unsigned u = (e >> 31) ? (e & 0x7fffffffu) : ~e;
+    return __uint_as_float(u);
+}
+
+// initial values of the three global estimate keys
+__device__ __forceinline__ void cdt_reset_keys(unsigned *gkey)
+{
+    gkey[0] = 0u;              // below every float's key
+    gkey[1] = 0u;
+    gkey[2] = 0xffffffffu;     // above every float's key
+}
+__global__ void k_cdt_init(unsigned *gkey) { cdt_reset_keys(gkey); }
+int cdt_init(float *cdt)
+{
+    k_cdt_init<<<1, 1>>>(reinterpret_cast<unsigned *>(cdt));
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
+struct CdtArgs {
+    const double *u, *v, *w, *r, *t, *bx, *by, *bz;
+    size_t n;
+    double g1, f;
+    float *chunk;           // [3][nchunks]: xx max, xz max, rho min estimates
+    unsigned *gkey;         // [3]: keys of the global estimates
+    int nchunks;
+    DevScalars *ds;
+};
+
+struct CdtEst { float xx, xz, r; };
+
+__device__ __forceinline__ CdtEst cdt_estimate(const CdtArgs &a, size_t i)
+{
+    // (conversions by truncation on the integer pipe: relative error < 2^-23)
+    const float u0 = d2f_est(a.u[i]), v0 = d2f_est(a.v[i]), w0 = d2f_est(a.w[i]), r0 = d2f_est(a.r[i]);
+    const float t0 = d2f_est(a.t[i]), bx0 = d2f_est(a.bx[i]), by0 = d2f_est(a.by[i]), bz0 = d2f_est(a.bz[i]);
+    const float bsq = bx0 * bx0 + by0 * by0 + bz0 * bz0;
+    const float c = (float)a.g1 * sqrtf(t0) + sqrtf((bsq * (float)a.f) / r0);
+    CdtEst e;
+    e.xx = sqrtf(u0 * u0 + v0 * v0) + c;
+    e.xz = fabsf(w0) + c;
+    e.r = r0;
+    return e;
+}
+
+__device__ __forceinline__ void block_reduce3(float &mx, float &mz, float &mn, float *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mz = fmaxf(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[wid] = mx; sh[32 + wid] = mz; sh[64 + wid] = mn; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < nw; q++) { mx = fmaxf(mx, sh[q]); mz = fmaxf(mz, sh[32 + q]); mn = fminf(mn, sh[64 + q]); }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
+{
+    __shared__ float sh[96];
+    const size_t i0 = (size_t)blockIdx.x * CDT_CHUNK;
+    const size_t i1 = i0 + CDT_CHUNK < a.n ? i0 + CDT_CHUNK : a.n;
+    float mx = -INFINITY, mz = -INFINITY, mn = INFINITY;
+    for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const CdtEst e = cdt_estimate(a, i);
+        mx = fmaxf(mx, e.xx);
+        mz = fmaxf(mz, e.xz);
+        mn = fminf(mn, e.r);
+    }
+    block_reduce3(mx, mz, mn, sh);
+    if (threadIdx.x == 0) {
+        a.chunk[blockIdx.x] = mx;
+        a.chunk[a.nchunks + blockIdx.x] = mz;
+        a.chunk[2 * a.nchunks + blockIdx.x] = mn;
+        atomicMax(&a.gkey[0], okey32(mx));
+        atomicMax(&a.gkey[1], okey32(mz));
+        atomicMin(&a.gkey[2], okey32(mn));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_calcdt_exact(CdtArgs a)
+{
+    const float gx = okey32_dec(a.gkey[0]), gz = okey32_dec(a.gkey[1]), gr = okey32_dec(a.gkey[2]);
+    // thresholds a relative margin below (above) the estimates; scaling
+    // keeps infinite estimates infinite
+    const float tx = gx * (gx >= 0.0f ? 1.0f - CDT_MARGIN : 1.0f + CDT_MARGIN);
+    const float tz = gz * (gz >= 0.0f ? 1.0f - CDT_MARGIN : 1.0f + CDT_MARGIN);
+    const float tr = gr * (gr >= 0.0f ? 1.0f + CDT_MARGIN : 1.0f - CDT_MARGIN);
+    const int c = blockIdx.x;
+    const bool fx = a.chunk[c] >= tx, fz = a.chunk[a.nchunks + c] >= tz, fr = a.chunk[2 * a.nchunks + c] <= tr;
+    if (!(fx || fz || fr)) return;
+    const size_t i0 = (size_t)c * CDT_CHUNK;
+    const size_t i1 = i0 + CDT_CHUNK < a.n ? i0 + CDT_CHUNK : a.n;
     double mxx = -1.0e-50, mxz = -1.0e-50, mn = 1.0e300;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double u0 = u[i], v0 = v[i], w0 = w[i], r0 = r[i], t0 = t[i];
-        double bz0 = bz[i], bx0 = bx[i], by0 = by[i];
-        double bsq0 = bx0 * bx0 + by0 * by0 + bz0 * bz0;
-        double xx = sqrt(u0 * u0 + v0 * v0) + g1 * sqrt(t0) + sqrt((bsq0 * f) / r0);
-        double xz = sqrt(w0 * w0) + g1 * sqrt(t0) + sqrt((bsq0 * f) / r0);
-        mn = fmin(mn, r0);
-        mxx = fmax(mxx, xx);
-        mxz = fmax(mxz, xz);
+    for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const CdtEst e = cdt_estimate(a, i);
+        const bool px = fx && e.xx >= tx, pz = fz && e.xz >= tz;
+        if (px || pz) {
+            // src/utils.F90:190-205, in FP64
+            const double u0 = a.u[i], v0 = a.v[i], w0 = a.w[i], r0 = a.r[i], t0 = a.t[i];
+            const double bz0 = a.bz[i], bx0 = a.bx[i], by0 = a.by[i];
+            const double bsq0 = bx0 * bx0 + by0 * by0 + bz0 * bz0;
+            const double cc = a.g1 * sqrt(t0);
+            const double cb = sqrt((bsq0 * a.f) / r0);
+            if (px) mxx = fmax(mxx, sqrt(u0 * u0 + v0 * v0) + cc + cb);
+            if (pz) mxz = fmax(mxz, sqrt(w0 * w0) + cc + cb);
+        }
+        if (fr && e.r <= tr) mn = fmin(mn, a.r[i]);
     }
     for (int o = 16; o > 0; o >>= 1) {
         mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
@@ -625,14 +749,15 @@ __global__ void k_calcdt_red(const R *u, const R *v, const R *w, const R *r, con
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     }
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(&ds->velmxx, okey(mxx));
-        atomicMax(&ds->velmxz, okey(mxz));
-        atomicMin(&ds->denmn, okey(mn));
+        atomicMax(&a.ds->velmxx, okey(mxx));
+        atomicMax(&a.ds->velmxz, okey(mxz));
+        atomicMin(&a.ds->denmn, okey(mn));
     }
 }
 
-__global__ void k_calcdt_fin(DevScalars *ds, double dd, double dz, double dtvisc0x, double dtvisc0z,
-                             double dtdiff0x, double dtdiff0z, double sf, int var_eta, double eta_max)
+__global__ void k_calcdt_fin(DevScalars *ds, unsigned *gkey, double dd, double dz, double dtvisc0x,
+                             double dtvisc0z, double dtdiff0x, double dtdiff0z, double sf, int var_eta,
+                             double eta_max)
 {
     double velmxx = okey_dec(ds->velmxx);
     double velmxz = okey_dec(ds->velmxz);
@@ -650,18 +775,25 @@ __global__ void k_calcdt_fin(DevScalars *ds, double dd, double dz, double dtvisc
     ds->dt = sf * m;
     ds->res[60] = velmxx; ds->res[61] = velmxz; ds->res[62] = denmn;
     ds->velmxx = OKEY_NEG_HUGE; ds->velmxz = OKEY_NEG_HUGE; ds->denmn = OKEY_POS_HUGE;
+    cdt_reset_keys(gkey);
 }
+
+int cdt_chunks(size_t n) { return (int)((n + CDT_CHUNK - 1) / CDT_CHUNK); }
 
 int phys_calcdt(Engine *E)
 {
-    unsigned blocks = (unsigned)(152 * 8);
-    size_t nb = nblk(E->n);
-    if (nb < blocks) blocks = (unsigned)nb;
-    KLAUNCHB(E, "calcdt_red_f64", FB(E, 8, 8), k_calcdt_red<double>, blocks, TPB, E->u, E->v, E->w, E->r, E->t, E->bx, E->by, E->bz,
-            E->n, E->k.g1, E->k.f, E->ds);
+    CdtArgs a;
+    a.u = E->u; a.v = E->v; a.w = E->w; a.r = E->r; a.t = E->t; a.bx = E->bx; a.by = E->by; a.bz = E->bz;
+    a.n = E->n; a.g1 = E->k.g1; a.f = E->k.f;
+    a.nchunks = cdt_chunks(E->n);
+    a.gkey = reinterpret_cast<unsigned *>(E->cdt);
+    a.chunk = E->cdt + 4;
+    a.ds = E->ds;
+    KLAUNCHB(E, "calcdt_est_f64", FB(E, 8, 8), k_calcdt_est, (unsigned)a.nchunks, 256, a);
+    KLAUNCH(E, "calcdt_exact", k_calcdt_exact, (unsigned)a.nchunks, 256, a);
     const Consts &c = E->k;
-    KLAUNCH(E, "calcdt_fin", k_calcdt_fin, 1, 1, E->ds, c.dd, c.dz, c.dtvisc0x, c.dtvisc0z, c.dtdiff0x, c.dtdiff0z,
-            c.sf, c.var_eta, c.eta_max);
+    KLAUNCH(E, "calcdt_fin", k_calcdt_fin, 1, 1, E->ds, a.gkey, c.dd, c.dz, c.dtvisc0x, c.dtvisc0z, c.dtdiff0x,
+            c.dtdiff0z, c.sf, c.var_eta, c.eta_max);
     return VEC_OK;
 }
 
@@ -973,7 +1105,7 @@ int phys_mag_init(Engine *E)
                               ljob<double>(W[W_EZ], W[W_EZ], OP_FWD) };
     if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
     for (int f = 0; f < 3; f++)     // :70-103
-        KLAUNCH(E, "truncate_f64", k_truncate<double>, nblk(E->n), TPB, W[W_EX + f], (double *)nullptr, E->nx, E->ny,
+        KLAUNCH(E, "truncate_f64", k_truncate<double>, plane_grid(*E), TPB, W[W_EX + f], (double *)nullptr, E->nx, E->ny,
                 E->nz, E->k.icutoffx, E->k.icutoffy);
     KLAUNCH(E, "mag_init_means", k_mag_init_means, 1, 256, W[W_EX], W[W_EY], W[W_EZ], E->bxbar, E->bybar,
             E->w1d + 7 * E->nz, E->np, E->nz, E->k.xn);
@@ -991,7 +1123,7 @@ int phys_mag_init(Engine *E)
     if ((st = launch_lines<double>(E, 0, ix, 3))) return st;
     if ((st = launch_lines<double>(E, 1, ix, 3))) return st;
     // jsq (:246-261): ex = inv(dBz/dy), ey = inv(dBz/dx), ez = inv(Jz)
-    KLAUNCH(E, "jsq_f64", k_jsq<double>, nblk(E->n), TPB, W[W_M3], W[W_M1], W[W_M2], E->bx, E->by, E->jsq, E->np, E->nz,
-            E->k.ho12);
+    KLAUNCH(E, "jsq_f64", k_jsq<double>, plane_grid(*E), TPB, W[W_M3], W[W_M1], W[W_M2], E->bx, E->by,
+            E->jsq, E->np, E->nz, E->k.ho12);
     return phys_mag_boundary(E);
 }

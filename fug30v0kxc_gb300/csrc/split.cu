@@ -29,6 +29,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "fpconv.cuh"
 #include "magkern.cuh"
 #include "zstencil.cuh"
 
@@ -49,6 +50,42 @@ enum Bg {
     BG_RHO0, BG_T0, BG_T0Z5, BG_T0ZU_P, BG_T0ZU_M, BG_T0ZZ0, BG_RHO0Z0, BG_RHO0ZU_P, BG_RHO0ZU_M,
     BG_A, BG_B, BG_COUNT
 };
+
+// The same profiles (and kappa, eta) rounded once to FP32, per plane: the
+// FP32 kernels read these instead of converting FP64 values at every point
+// (identical values; GB300's FP64 and conversion rates are low)
+enum Pc {
+    PC_RHO0, PC_T0, PC_T0Z5, PC_T0ZU_P, PC_T0ZU_M, PC_T0ZZ0, PC_RHO0Z0, PC_RHO0ZU_P, PC_RHO0ZU_M,
+    PC_AB,       // A + B, summed in FP64
+    PC_KAPPA, PC_DKAPPA,
+    PC_OHM,      // eta / (zeta ck), divided in FP64
+    PC_ETA, PC_DETA,
+    PC_COUNT
+};
+
+__global__ void k_make_pcf(const double *bg, const double *kappa, const double *dkappa, const double *eta,
+                           const double *deta, double zck, int nz, float *pc)
+{
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        const int from[9] = { BG_RHO0, BG_T0, BG_T0Z5, BG_T0ZU_P, BG_T0ZU_M, BG_T0ZZ0, BG_RHO0Z0, BG_RHO0ZU_P,
+                              BG_RHO0ZU_M };
+        for (int q = 0; q < 9; q++) pc[q * nz + k] = (float)bg[from[q] * nz + k];
+        pc[PC_AB * nz + k] = (float)(bg[BG_A * nz + k] + bg[BG_B * nz + k]);
+        pc[PC_KAPPA * nz + k] = (float)kappa[k];
+        pc[PC_DKAPPA * nz + k] = (float)dkappa[k];
+        pc[PC_OHM * nz + k] = (float)(eta[k] / zck);
+        pc[PC_ETA * nz + k] = (float)eta[k];
+        pc[PC_DETA * nz + k] = (float)deta[k];
+    }
+}
+
+// (re)builds the FP32 plane coefficients from the FP64 profiles
+int split_refresh_coefs(Engine *E)
+{
+    k_make_pcf<<<1, 256, 0, E->stream>>>(E->hres, E->kappa, E->dkappa, E->eta, E->deta, E->k.zck, E->nz, E->pcf);
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
 
 static int falloc(float **p, size_t n)
 {
@@ -98,6 +135,12 @@ int split_setup(Engine *E)
         return VEC_ERR_ALLOC;
     }
     CUDA_TRY(cudaMemcpy(E->hres, bg.data(), sizeof(double) * bg.size(), cudaMemcpyHostToDevice));
+    {
+        int st = falloc(&E->pcf, (size_t)PC_COUNT * nz);
+        if (st) return st;
+        if ((st = split_refresh_coefs(E))) return st;
+        CUDA_TRY(cudaStreamSynchronize(E->stream));
+    }
     E->b32_auth = 0;
     return VEC_OK;
 }
@@ -108,32 +151,38 @@ struct MirrorArgs {
     float *r32, *t32, *u32, *v32, *w32, *pol32, *tor32, *bx32, *by32, *bz32, *jsq32;
     double bzbar;
     size_t np;
-    int nz, k0, k1, mask;   // planes [k0,k1); mask: 1 state, 2 uv only, 4 B, 8 pol/tor only
+    int nz, k0, k1, mask;   // planes [k0,k1); mask: MIR_* bits
 };
 
+// mirror masks: whole groups, or single fields
+enum {
+    MIR_STATE = 1,          // r, t, u, v, w, pol, tor
+    MIR_UV = 2, MIR_B = 4,  // u and v; bx, by, bz, jsq
+    MIR_POLTOR = 8,
+    MIR_R = 16, MIR_T = 32, MIR_W = 64, MIR_U = 128, MIR_V = 256, MIR_POL = 512, MIR_TOR = 1024,
+};
+
+// FP32 mirrors of the FP64 fields, grid (np/256, k1-k0); conversions on the
+// integer pipe (the same bits as the casts)
 __global__ void k_mirror(MirrorArgs a)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x + (size_t)a.k0 * a.np;
-    if (idx >= (size_t)a.k1 * a.np) return;
-    const int k = (int)(idx / a.np);
-    if (a.mask & 1) {
-        a.r32[idx] = (float)(a.r[idx] - a.bg[BG_RHO0 * a.nz + k]);
-        a.t32[idx] = (float)(a.t[idx] - a.bg[BG_T0 * a.nz + k]);
-        a.w32[idx] = (float)a.w[idx];
-    }
-    if (a.mask & 3) {
-        a.u32[idx] = (float)a.u[idx];
-        a.v32[idx] = (float)a.v[idx];
-    }
-    if (a.mask & 9) {
-        a.pol32[idx] = (float)a.pol[idx];
-        a.tor32[idx] = (float)a.tor[idx];
-    }
-    if (a.mask & 4) {
-        a.bx32[idx] = (float)a.bx[idx];
-        a.by32[idx] = (float)a.by[idx];
-        a.bz32[idx] = (float)(a.bz[idx] - a.bzbar);
-        a.jsq32[idx] = (float)a.jsq[idx];
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.np) return;
+    const int k = a.k0 + blockIdx.y;
+    const size_t idx = (size_t)k * a.np + q;
+    const int m = a.mask;
+    if (m & (MIR_STATE | MIR_R)) a.r32[idx] = d2f_rn(a.r[idx] - a.bg[BG_RHO0 * a.nz + k]);
+    if (m & (MIR_STATE | MIR_T)) a.t32[idx] = d2f_rn(a.t[idx] - a.bg[BG_T0 * a.nz + k]);
+    if (m & (MIR_STATE | MIR_W)) a.w32[idx] = d2f_rn(a.w[idx]);
+    if (m & (MIR_STATE | MIR_UV | MIR_U)) a.u32[idx] = d2f_rn(a.u[idx]);
+    if (m & (MIR_STATE | MIR_UV | MIR_V)) a.v32[idx] = d2f_rn(a.v[idx]);
+    if (m & (MIR_STATE | MIR_POLTOR | MIR_POL)) a.pol32[idx] = d2f_rn(a.pol[idx]);
+    if (m & (MIR_STATE | MIR_POLTOR | MIR_TOR)) a.tor32[idx] = d2f_rn(a.tor[idx]);
+    if (m & MIR_B) {
+        a.bx32[idx] = d2f_rn(a.bx[idx]);
+        a.by32[idx] = d2f_rn(a.by[idx]);
+        a.bz32[idx] = d2f_rn(a.bz[idx] - a.bzbar);
+        a.jsq32[idx] = d2f_rn(a.jsq[idx]);
     }
 }
 
@@ -145,7 +194,7 @@ static int mirror(Engine *E, int mask, int k0, int k1)
     a.r32 = E->r32; a.t32 = E->t32; a.u32 = E->u32; a.v32 = E->v32; a.w32 = E->w32;
     a.pol32 = E->pol32; a.tor32 = E->tor32; a.bx32 = E->bx32; a.by32 = E->by32; a.bz32 = E->bz32;
     a.jsq32 = E->jsq32; a.bzbar = E->bzbar; a.np = E->np; a.nz = E->nz; a.k0 = k0; a.k1 = k1; a.mask = mask;
-    KLAUNCHB(E, "mirror", 0, k_mirror, nblk((size_t)(k1 - k0) * E->np), TPB, a);
+    KLAUNCHB(E, "mirror", 0, k_mirror, dim3((unsigned)nblk(E->np), (unsigned)(k1 - k0)), TPB, a);
     return VEC_OK;
 }
 
@@ -175,7 +224,24 @@ int split_refresh(Engine *E)
 {
     int st = split_sync_b64(E);
     if (st) return st;
-    return mirror(E, 1 | 4 | 8, 0, E->nz);
+    return mirror(E, MIR_STATE | MIR_B, 0, E->nz);
+}
+
+// the mirror of one state field (VEC_F_*) after that field was set
+int split_refresh_field(Engine *E, int field)
+{
+    int m = 0;
+    switch (field) {
+    case VEC_F_R: m = MIR_R; break;
+    case VEC_F_T: m = MIR_T; break;
+    case VEC_F_U: m = MIR_U; break;
+    case VEC_F_V: m = MIR_V; break;
+    case VEC_F_W: m = MIR_W; break;
+    case VEC_F_POL: m = MIR_POL; break;
+    case VEC_F_TOR: m = MIR_TOR; break;
+    default: m = MIR_B; break;   // bx, by, bz, jsq
+    }
+    return mirror(E, m, 0, E->nz);
 }
 
 int split_refresh_planes(Engine *E, int mask)
@@ -185,19 +251,18 @@ int split_refresh_planes(Engine *E, int mask)
     return mirror(E, mask, E->nz - 1, E->nz);
 }
 
-int split_refresh_uv(Engine *E) { return mirror(E, 2, 0, E->nz); }
+int split_refresh_uv(Engine *E) { return mirror(E, MIR_UV, 0, E->nz); }
 
 // ---- hydro_deriv ------------------------------------------------------------
 struct SplitHydroArgs {
     const float *r, *t, *u, *v, *w, *bx, *by, *bz, *jsq;
     const float *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
     const float *ry, *ty, *tyy, *uy, *uyy, *vy, *vyy, *wy, *wyy;
-    const double *kappa, *dkappa, *eta, *bg;
+    const float *pc;        // per-plane FP32 coefficients [PC_COUNT][nz]
     const HistTable *ht;    // tdot = newest slot of t
     float *racc, *uacc, *vacc, *wacc;
     float *p1, *p2, *q, *g, *hh, *p3, *p4;
     float gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, ho12, sc1, bzbar;
-    double zck;
     int var_eta;
     size_t np;
     int nz;
@@ -212,8 +277,8 @@ struct ZDer { float tzu, tzp, tzz, wzu, wz, uzu, vzu, uzz, vzz; };
 __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer &z)
 {
     const int nz = a.nz;
-    const double *bg = a.bg;
-    const float rho0 = (float)bg[BG_RHO0 * nz + k], t0 = (float)bg[BG_T0 * nz + k];
+    const float *pc = a.pc;
+    const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
     const float rp = a.r[idx], tp = a.t[idx], u0 = a.u[idx], v0 = a.v[idx], w0 = a.w[idx];
     const float rr = rho0 + rp, tt = t0 + tp;
     const float bx = a.bx[idx], by = a.by[idx], bzp = a.bz[idx], bz = a.bzbar + bzp;
@@ -224,20 +289,20 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     const float wx = a.wx[idx], wxx = a.wxx[idx], wy = a.wy[idx], wyy = a.wyy[idx];
 
     const bool wpos = w0 >= 0.0f;
-    const float tzu = z.tzu + (float)bg[(wpos ? BG_T0ZU_P : BG_T0ZU_M) * nz + k];
+    const float tzu = z.tzu + pc[(wpos ? PC_T0ZU_P : PC_T0ZU_M) * nz + k];
     const float tzp = z.tzp;
-    const float tzz = z.tzz + (float)bg[BG_T0ZZ0 * nz + k];
+    const float tzz = z.tzz + pc[PC_T0ZZ0 * nz + k];
     const float wzu = z.wzu, wz = z.wz, uzu = z.uzu, vzu = z.vzu, uzz = z.uzz, vzz = z.vzz;
 
     const float third = 1.0f / 3.0f;
-    const float ohm = a.var_eta ? (float)(a.eta[k] / a.zck) : 1.0f;
+    const float ohm = a.var_eta ? pc[PC_OHM * nz + k] : 1.0f;
     const float divu = ux + vy + wz;
 
     a.racc[idx] = -u0 * rx - v0 * ry - rr * divu;
 
     float td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
-               + a.gck * (float)a.kappa[k] * (txx + tyy + tzz)
-               + a.gck * (float)a.dkappa[k] * tzu
+               + a.gck * pc[PC_KAPPA * nz + k] * (txx + tyy + tzz)
+               + a.gck * pc[PC_DKAPPA * nz + k] * tzu
                + a.fzckg * ohm * a.jsq[idx];
     td = td - a.gm1 * tt * divu * rr + 2.0f * a.sckg * (ux * ux + vy * vy + wz * wz - third * divu * divu);
     td = td + a.sckg * (uy + vx) * (uy + vx);
@@ -254,7 +319,7 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     vd = vd - rr * a.cor * (-u0 * a.spsi);
     vd = vd + a.sck * (vzz + vxx + vyy);
     // -rho dT/dz + theta(m+1) rho minus its FP64 background part
-    const float t0z = (float)bg[BG_T0Z5 * nz + k];
+    const float t0z = pc[PC_T0Z5 * nz + k];
     float wd = -rho0 * tzp - rp * t0z - rp * tzp + a.thmplus1 * rp;
     wd = wd - rr * w0 * wzu - rr * u0 * wx - rr * v0 * wy;
     wd = wd - rr * a.cor * (-u0 * a.cpsi);
@@ -328,23 +393,26 @@ __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
 struct SplitHydro4Args {
     const float *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
     const double *bg;
+    const float *pc;
     const HistTable *ht;    // rdot, udot, vdot, wdot = newest slots
     float ho12;
     size_t np;
     int nz;
 };
 
+// one thread per point, grid (np/256, nz): k = blockIdx.y
 __global__ void k_split_pass4(SplitHydro4Args a)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.np * a.nz) return;
-    const int nz = a.nz;
     const size_t np = a.np;
-    const int k = (int)(idx / np);
-    const size_t q = idx - (size_t)k * np;
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int nz = a.nz;
+    const int k = blockIdx.y;
+    const size_t idx = (size_t)k * np + q;
     const float h = a.ho12;
     const double *bg = a.bg;
-    const float rho0 = (float)bg[BG_RHO0 * nz + k], t0 = (float)bg[BG_T0 * nz + k];
+    const float *pc = a.pc;
+    const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
     const float rp = a.r[idx], tp = a.t[idx], w0 = a.w[idx];
     const float rr = rho0 + rp, tt = t0 + tp;
     float wd = a.wacc[idx] + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
@@ -359,11 +427,10 @@ __global__ void k_split_pass4(SplitHydro4Args a)
         wfin = (float)(wdn - (double)tt * rz);
     } else {
         const bool wpos = w0 >= 0.0f;
-        const float rzu = zd1up(a.r + q, np, k, nz, 0, h, w0) + (float)bg[(wpos ? BG_RHO0ZU_P : BG_RHO0ZU_M) * nz + k];
+        const float rzu = zd1up(a.r + q, np, k, nz, 0, h, w0) + pc[(wpos ? PC_RHO0ZU_P : PC_RHO0ZU_M) * nz + k];
         const float rzp = zd1(a.r + q, np, k, nz, 0, h);
         rdot = a.racc[idx] - w0 * rzu;
-        wfin = wd + (float)(bg[BG_A * nz + k] + bg[BG_B * nz + k]) - t0 * rzp
-               - tp * (float)bg[BG_RHO0Z0 * nz + k] - tp * rzp;
+        wfin = wd + pc[PC_AB * nz + k] - t0 * rzp - tp * pc[PC_RHO0Z0 * nz + k] - tp * rzp;
     }
     const float ri = 1.0f / rr;
     ((float *)a.ht->p[0][2])[idx] = rdot;
@@ -402,14 +469,14 @@ int split_hydro(Engine *E)
     a.vx = W[W_VX]; a.vxx = W[W_VXX]; a.wx = W[W_WX]; a.wxx = W[W_WXX];
     a.ry = W[W_RY]; a.ty = W[W_TY]; a.tyy = W[W_TYY]; a.uy = W[W_UY]; a.uyy = W[W_UYY];
     a.vy = W[W_VY]; a.vyy = W[W_VYY]; a.wy = W[W_WY]; a.wyy = W[W_WYY];
-    a.kappa = E->kappa; a.dkappa = E->dkappa; a.eta = E->eta; a.bg = E->hres;
+    a.pc = E->pcf;
     a.racc = W[W_RACC]; a.ht = E->ht;
     a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
     a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H]; a.p3 = W[W_P3]; a.p4 = W[W_P4];
     a.gck = (float)c.gck; a.fzckg = (float)c.fzckg; a.gm1 = (float)c.gm1; a.sckg = (float)c.sckg;
     a.fo2 = (float)c.fo2; a.scko3 = (float)c.scko3; a.f = (float)c.f; a.thmplus1 = (float)c.thmplus1;
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
-    a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar; a.zck = c.zck;
+    a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
     const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
     dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
@@ -430,10 +497,10 @@ int split_hydro(Engine *E)
 
     SplitHydro4Args b;
     b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
-    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres;
+    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres; b.pc = E->pcf;
     b.ht = E->ht;
     b.ho12 = (float)c.ho12; b.np = E->np; b.nz = E->nz;
-    KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4, nblk(E->n), TPB, b);
+    KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4, plane_grid(*E), TPB, b);
     return VEC_OK;
 }
 
@@ -454,25 +521,32 @@ int split_mag(Engine *E)
     const Consts &c = E->k;
     KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
              E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
-    KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, nblk(E->n), TPB, W[W_EX], W[W_EY], W[W_M4], E->nx,
-             E->ny, E->nz, E->akx1, E->aky1);
+    KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
+             E->nx, E->ny, E->hf);
     MagArgs<float> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol32; a.tor = E->tor32;
-    a.eta = E->eta; a.deta = E->deta; a.akx1 = E->akx1; a.aky1 = E->aky1; a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.eta = E->pcf + PC_ETA * E->nz; a.deta = E->pcf + PC_DETA * E->nz; a.h = E->hf;
     a.ht = E->ht;
-    a.zck = c.zck; a.ho12 = c.ho12; a.sc1 = c.sc1; a.var_eta = c.var_eta;
+    a.zck = (float)c.zck; a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, plane_grid(*E), TPB, a);
     return VEC_OK;
 }
 
 // ---- bandj --------------------------------------------------------------------
-__global__ void k_d1z_f(const float *in, float *out, int fl, size_t np, int nz, float h)
+// z-marching, grid (np/256, nz/kc)
+__global__ void __launch_bounds__(256) k_d1z_f(const float *in, float *out, int fl, size_t np, int nz, float h,
+                                               int kc)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= np * nz) return;
-    int k = (int)(idx / np);
-    out[idx] = zd1(in + (idx - (size_t)k * np), np, k, nz, fl, h);
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
+    float v[7];
+    zwin_init(v, in + q, np, k0, nz);
+    for (int k = k0; k < k1; k++) {
+        out[(size_t)k * np + q] = (k >= 3 && k <= nz - 4) ? wd1(v, h) : zd1(in + q, np, k, nz, fl, h);
+        zwin_next(v, in + q, np, k, nz);
+    }
 }
 
 int split_bandj(Engine *E)
@@ -480,14 +554,13 @@ int split_bandj(Engine *E)
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
     int st;
-    KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, nblk(E->n), TPB, E->pol32, W[W_M1], 5, E->np, E->nz,
-             (float)E->k.ho12);
+    KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, W[W_M1], 5, E->np,
+             E->nz, (float)E->k.ho12, ZCHUNK);
     BandjArgs<float> a;
-    a.dzs = W[W_M1]; a.pol = E->pol32; a.tor = E->tor32; a.akx1 = E->akx1; a.aky1 = E->aky1;
-    a.akx2 = E->akx2; a.aky2 = E->aky2;
+    a.dzs = W[W_M1]; a.pol = E->pol32; a.tor = E->tor32; a.h = E->hf;
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, plane_grid(*E), TPB, a);
     LineJob<float> ix[6] = { ljob<float>(W[W_EX], W[W_EX], OP_INV), ljob<float>(W[W_EY], W[W_EY], OP_INV),
                              ljob<float>(W[W_EZ], W[W_EZ], OP_INV), ljob<float>(W[W_M2], W[W_M2], OP_INV),
                              ljob<float>(W[W_M3], W[W_M3], OP_INV), ljob<float>(W[W_M4], W[W_M4], OP_INV) };
@@ -499,8 +572,8 @@ int split_bandj(Engine *E)
     iy[0].addk = E->bxbar;
     iy[1].addk = E->bybar;
     if ((st = launch_lines<float>(E, 1, iy, 6))) return st;
-    KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq<float>, nblk(E->n), TPB, W[W_M4], W[W_M2], W[W_M3], E->bx32,
-             E->by32, E->jsq32, E->np, E->nz, (float)E->k.ho12);
+    KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq<float>, plane_grid(*E), TPB, W[W_M4], W[W_M2], W[W_M3],
+             E->bx32, E->by32, E->jsq32, E->np, E->nz, (float)E->k.ho12);
     E->b32_auth = 1;
     return VEC_OK;
 }
@@ -558,7 +631,10 @@ __global__ void k_split_ab3(SplitAb3Args a)
 }
 
 // four consecutive points per thread (x fastest, nx % 4 == 0): 16-byte
-// loads and stores of the FP32 histories/mirrors and of the FP64 state
+// loads and stores of the FP32 histories/mirrors and of the FP64 state.
+// ICVT: the float <-> double conversions on the integer pipe (fpconv.cuh),
+// leaving the FP64 pipe only the additions; same bits as the casts.
+template <bool ICVT>
 __global__ void k_split_ab3_v4(SplitAb3Args a)
 {
     const size_t np = (size_t)a.nx * a.ny;
@@ -577,10 +653,19 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
         const float4 h2 = *reinterpret_cast<const float4 *>(hp[2] + i4);
         const float4 h1 = *reinterpret_cast<const float4 *>(hp[1] + i4);
         const float4 h0 = *reinterpret_cast<const float4 *>(hp[0] + i4);
-        xs[f][0] = s01.x + (double)(c0 * h2.x + c1 * h1.x + c2 * h0.x);
-        xs[f][1] = s01.y + (double)(c0 * h2.y + c1 * h1.y + c2 * h0.y);
-        xs[f][2] = s23.x + (double)(c0 * h2.z + c1 * h1.z + c2 * h0.z);
-        xs[f][3] = s23.y + (double)(c0 * h2.w + c1 * h1.w + c2 * h0.w);
+        const float i0 = c0 * h2.x + c1 * h1.x + c2 * h0.x, i1 = c0 * h2.y + c1 * h1.y + c2 * h0.y;
+        const float i2 = c0 * h2.z + c1 * h1.z + c2 * h0.z, i3 = c0 * h2.w + c1 * h1.w + c2 * h0.w;
+        if (ICVT) {
+            xs[f][0] = s01.x + f2d_exact(i0);
+            xs[f][1] = s01.y + f2d_exact(i1);
+            xs[f][2] = s23.x + f2d_exact(i2);
+            xs[f][3] = s23.y + f2d_exact(i3);
+        } else {
+            xs[f][0] = s01.x + (double)i0;
+            xs[f][1] = s01.y + (double)i1;
+            xs[f][2] = s23.x + (double)i2;
+            xs[f][3] = s23.y + (double)i3;
+        }
     }
     // density floor (src/main.F90:438-443)
     const bool fl0 = xs[3][0] < 0.05, fl1 = xs[3][1] < 0.05, fl2 = xs[3][2] < 0.05, fl3 = xs[3][3] < 0.05;
@@ -603,9 +688,16 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
     for (int f = 0; f < 7; f++) {
         *reinterpret_cast<double2 *>(a.x[f] + i4) = make_double2(xs[f][0], xs[f][1]);
         *reinterpret_cast<double2 *>(a.x[f] + i4 + 2) = make_double2(xs[f][2], xs[f][3]);
-        const double b = f == 3 ? rb : (f == 4 ? tb : 0.0);
-        *reinterpret_cast<float4 *>(a.m[f] + i4) =
-            make_float4((float)(xs[f][0] - b), (float)(xs[f][1] - b), (float)(xs[f][2] - b), (float)(xs[f][3] - b));
+        float4 m;
+        if (f == 3 || f == 4) {
+            const double b = f == 3 ? rb : tb;
+            if (ICVT) m = make_float4(d2f_rn(xs[f][0] - b), d2f_rn(xs[f][1] - b), d2f_rn(xs[f][2] - b), d2f_rn(xs[f][3] - b));
+            else m = make_float4((float)(xs[f][0] - b), (float)(xs[f][1] - b), (float)(xs[f][2] - b), (float)(xs[f][3] - b));
+        } else {
+            if (ICVT) m = make_float4(d2f_rn(xs[f][0]), d2f_rn(xs[f][1]), d2f_rn(xs[f][2]), d2f_rn(xs[f][3]));
+            else m = make_float4((float)xs[f][0], (float)xs[f][1], (float)xs[f][2], (float)xs[f][3]);
+        }
+        *reinterpret_cast<float4 *>(a.m[f] + i4) = m;
     }
 }
 
@@ -629,8 +721,10 @@ int split_ab3(Engine *E, int magdealias)
     a.magdealias = magdealias;
     // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B
     const double bytes = (double)E->n * (14 * 8 + 21 * 4 + 7 * 4);
-    if (E->nx % 4 == 0)
-        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4, nblk(E->n / 4), TPB, a);
+    if (E->nx % 4 == 0 && E->int_cvt)
+        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4<true>, nblk(E->n / 4), TPB, a);
+    else if (E->nx % 4 == 0)
+        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4<false>, nblk(E->n / 4), TPB, a);
     else
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3, nblk(E->n), TPB, a);
     return phys_rotate_hist(E);

@@ -78,19 +78,40 @@ __host__ __device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, 
 
 // spectral d/dx of a 2-D halfcomplex plane at (i,j): index shuffle of
 // src/fft.F90:292-302 (the reference's "+ik" on the x halfcomplex index).
-template <typename R>
-__device__ __forceinline__ R sdx(const R *plane, int i, int j, int nx, const double *akx1)
+// (K: the table's type; a table in the plane's precision needs no conversion)
+template <typename R, typename K>
+__device__ __forceinline__ R sdx(const R *plane, int i, int j, int nx, const K *akx1)
 {
     if (i == 0 || 2 * i == nx) return (R)0;
-    R v = plane[(size_t)j * nx + (nx - i)] * (R)akx1[i];
+    R v = plane[(unsigned)j * nx + (nx - i)] * (R)akx1[i];
     return 2 * i < nx ? -v : v;
 }
-template <typename R>
-__device__ __forceinline__ R sdy(const R *plane, int i, int j, int nx, int ny, const double *aky1)
+template <typename R, typename K>
+__device__ __forceinline__ R sdy(const R *plane, int i, int j, int nx, int ny, const K *aky1)
 {
     if (j == 0 || 2 * j == ny) return (R)0;
-    R v = plane[(size_t)(ny - j) * nx + i] * (R)aky1[j];
+    R v = plane[(unsigned)(ny - j) * nx + i] * (R)aky1[j];
     return 2 * j < ny ? -v : v;
+}
+
+// z-marching register windows: v[d] = f(k-3+d) for the current plane k of a
+// column (f points at the column's plane 0), zero outside [0, nz)
+template <typename R>
+__device__ __forceinline__ void zwin_init(R *v, const R *f, size_t np, int k0, int nz)
+{
+#pragma unroll
+    for (int d = 0; d < 7; d++) {
+        const int kk = k0 - 3 + d;
+        v[d] = (kk >= 0 && kk < nz) ? f[(size_t)kk * np] : (R)0;
+    }
+}
+// advance the window from plane k to k + 1
+template <typename R>
+__device__ __forceinline__ void zwin_next(R *v, const R *f, size_t np, int k, int nz)
+{
+#pragma unroll
+    for (int d = 0; d < 6; d++) v[d] = v[d + 1];
+    v[6] = k + 4 < nz ? f[(size_t)(k + 4) * np] : (R)0;
 }
 
 // Interior rows (3 <= k <= nz-4) from a register window v[d] = f(k-3+d):

@@ -148,3 +148,67 @@ def test_f_zero_skips_magnetics():
     assert g.step(12) == 0 and o.step(12) == 0
     _cmp(g, o, ["r", "t", "u", "v", "w"], 1e-9)
     assert np.array_equal(g.get("poldot2"), np.zeros_like(g.get("poldot2")))
+
+
+def _near_tie_state(p, which, seed=3):
+    """A state whose CFL (or density) extremum sits among values that agree
+    to 1e-9: FP32 estimates cannot tell the points apart, so calcdt must
+    evaluate them all in FP64."""
+    rng = np.random.default_rng(seed)
+    shape = (p.nz, p.ny, p.nx)
+    n = p.nx * p.ny * p.nz
+    s = smooth_state(p, seed=seed)
+    s["bx"] = np.full(shape, 0.3); s["by"] = np.full(shape, 0.2); s["bz"] = np.full(shape, 1.0)
+    s["t"] = np.full(shape, 2.0)
+    s["r"] = np.full(shape, 1.5)
+    jitter = 1.0 + 0.5e-9 * rng.random(shape)
+    peak = np.unravel_index(int(rng.integers(n)), shape)
+    if which == "xx":
+        s["u"] = 1000.0 * jitter; s["v"] = np.zeros(shape); s["w"] = np.zeros(shape)
+        s["u"][peak] = 1000.0 * (1.0 + 1e-9)
+    elif which == "xz":
+        s["u"] = np.zeros(shape); s["v"] = np.zeros(shape); s["w"] = 1000.0 * jitter
+        s["w"][peak] = 1000.0 * (1.0 + 1e-9)
+    else:
+        # no flow, no field, cold: the viscous / diffusive limits times the
+        # minimum density set dt
+        s["u"] = np.zeros(shape); s["v"] = np.zeros(shape); s["w"] = np.zeros(shape)
+        s["bx"] = np.zeros(shape); s["by"] = np.zeros(shape); s["bz"] = np.zeros(shape)
+        s["t"] = np.full(shape, 1e-8)
+        s["r"] = 1.5 * (2.0 - jitter)
+        s["r"][peak] = 1.5 * (1.0 - 1e-9)
+    return s
+
+
+@pytest.mark.parametrize("which", ["xx", "xz", "rho"])
+def test_calcdt_near_ties(which):
+    """The FP32 pre-pass of calcdt only selects points; the extrema stay the
+    FP64 ones (tolerance 1e-14: a wrong pick would be off by ~5e-10)."""
+    # 64 x 48 x 33 = 101376 points: 12 full chunks of 8192 and a partial one
+    p = convection_params(64, 48, 33, eta_contrast=1.0)
+    g, o = P3D(p), O.Oracle(p)
+    s = _near_tie_state(p, which)
+    for n, a in s.items():
+        g.set(n, a)
+        o.set(n, a)
+    dg, do = g.calcdt(), o.calcdt()
+    assert abs(dg - do) <= 1e-14 * do, (dg, do)
+
+
+@pytest.mark.parametrize("pos", [0, 8191, 8192, 64 * 48 * 33 - 1])
+def test_calcdt_spike_at_chunk_edges(pos):
+    """One fast point at a chunk boundary of the pre-pass, in a smooth state."""
+    p = convection_params(64, 48, 33, eta_contrast=1.0)
+    g, o = P3D(p), O.Oracle(p)
+    s = smooth_state(p, seed=5)
+    shape = s["u"].shape
+    idx = np.unravel_index(pos, shape)
+    s["u"] = s["u"].copy()
+    s["u"][idx] = 50.0
+    s["r"] = s["r"].copy()
+    s["r"][np.unravel_index((pos + 1) % s["r"].size, shape)] = 0.06
+    for n, a in s.items():
+        g.set(n, a)
+        o.set(n, a)
+    dg, do = g.calcdt(), o.calcdt()
+    assert abs(dg - do) <= 1e-14 * do, (dg, do)
