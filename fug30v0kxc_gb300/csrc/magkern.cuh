@@ -173,6 +173,158 @@ inline dim3 zmarch_grid(size_t np, int nz, int kc = ZCHUNK)
     return dim3((unsigned)((np + 255) / 256), (unsigned)((nz + kc - 1) / kc));
 }
 
+// ---- four consecutive x points per thread (FP32, nx % 4 == 0) -----------------
+// Same arithmetic per component as the one-point kernels above, with 16-byte
+// loads and stores; grid (np/4/256, nz).
+
+__device__ __forceinline__ V4 ld4(const float *p, size_t i) { return reinterpret_cast<const V4 *>(p)[i]; }
+__device__ __forceinline__ void st4(float *p, size_t i, V4 v) { reinterpret_cast<V4 *>(p)[i] = v; }
+
+// sdx for points i0..i0+3 of row j: plane[j nx + (nx - i)] * akx1[i], negated
+// for 2i < nx, zero at i = 0 and 2i = nx.  The mirrored points nx-i0-3 ..
+// nx-i0 straddle two aligned 4-vectors.
+__device__ __forceinline__ V4 sdx4(const float *plane, int i0, int j, int nx, const float *kx1)
+{
+    const float *row = plane + (size_t)j * nx;
+    const V4 A = *reinterpret_cast<const V4 *>(row + nx - i0 - 4);
+    const float b = i0 == 0 ? 0.0f : row[nx - i0];
+    const V4 k = *reinterpret_cast<const V4 *>(kx1 + i0);
+    const float m[4] = { b, A.w, A.z, A.y }, kk[4] = { k.x, k.y, k.z, k.w };
+    float r[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int i = i0 + c;
+        float v = m[c] * kk[c];
+        v = 2 * i < nx ? -v : v;
+        r[c] = (i == 0 || 2 * i == nx) ? 0.0f : v;
+    }
+    return V4(r[0], r[1], r[2], r[3]);
+}
+// sdy for points i0..i0+3 of row j: plane[(ny - j) nx + i] * aky1[j]
+__device__ __forceinline__ V4 sdy4(const float *plane, int i0, int j, int nx, int ny, const float *ky1)
+{
+    if (j == 0 || 2 * j == ny) return V4(0.0f);
+    const V4 v = *reinterpret_cast<const V4 *>(plane + (size_t)(ny - j) * nx + i0) * V4(ky1[j]);
+    return 2 * j < ny ? -v : v;
+}
+
+static __global__ void k_emf4(const float *u, const float *v, const float *w, const float *bx, const float *by,
+                              const float *bz, float *e1, float *e2, float *e3, size_t n4, float bzoff)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n4) return;
+    const V4 U = ld4(u, i), Vv = ld4(v, i), W = ld4(w, i), BX = ld4(bx, i), BY = ld4(by, i);
+    const V4 BZ = ld4(bz, i) + V4(bzoff);
+    st4(e1, i, Vv * BZ - W * BY);
+    st4(e2, i, W * BX - U * BZ);
+    st4(e3, i, U * BY - Vv * BX);
+}
+
+static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h)
+{
+    const unsigned np4 = (unsigned)nx * ny / 4;
+    const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const size_t pb = (size_t)blockIdx.y * np4 * 4;
+    const unsigned q = 4 * q4;
+    const int j = (int)(q / (unsigned)nx), i0 = (int)(q - (unsigned)j * nx);
+    st4(w1 + pb, q4, sdx4(ex + pb, i0, j, nx, h.kx1) + sdy4(ey + pb, i0, j, nx, ny, h.ky1));
+}
+
+static __global__ void k_mag_final4(MagArgs<float> a)
+{
+    const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
+    const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const int k = blockIdx.y;
+    const size_t pb = (size_t)k * np, i4 = (size_t)k * np4 + q4;
+    const unsigned q = 4 * q4;
+    const int j = (int)(q / (unsigned)a.nx), i0 = (int)(q - (unsigned)j * a.nx);
+    const V4 w2a = sdy4(a.ex + pb, i0, j, a.nx, a.ny, a.h.ky1) - sdx4(a.ey + pb, i0, j, a.nx, a.h.kx1);
+    const V4 *w1c = reinterpret_cast<const V4 *>(a.w1) + q4;
+    const V4 *polc = reinterpret_cast<const V4 *>(a.pol) + q4, *torc = reinterpret_cast<const V4 *>(a.tor) + q4;
+    const V4 w3a = zd1(w1c, (size_t)np4, k, a.nz, 5, V4(a.ho12));
+    const V4 kk = ld4(a.h.kh2, q4);
+    V4 w2, w3;
+    w2.x = q == 0 ? 0.0f : w2a.x / kk.x; w3.x = q == 0 ? 0.0f : w3a.x / kk.x;
+    w2.y = w2a.y / kk.y; w3.y = w3a.y / kk.y;
+    w2.z = w2a.z / kk.z; w3.z = w3a.z / kk.z;
+    w2.w = w2a.w / kk.w; w3.w = w3a.w / kk.w;
+    const V4 d2p = zd2(polc, (size_t)np4, k, a.nz, 3, V4(a.sc1));
+    const V4 d2t = zd2(torc, (size_t)np4, k, a.nz, 3, V4(a.sc1));
+    float *poldot = (float *)a.ht->p[5][2], *tordot = (float *)a.ht->p[6][2];
+    const V4 pc = polc[(size_t)k * np4], tc = torc[(size_t)k * np4], ez = ld4(a.ez, i4);
+    if (!a.var_eta) {
+        const V4 zck(a.zck);
+        st4(poldot, i4, zck * pc * kk + zck * d2p + w2);
+        st4(tordot, i4, zck * tc * kk + zck * d2t - w3 + ez);
+    } else {
+        const V4 e(a.eta[k]);
+        const V4 dt = zd1(torc, (size_t)np4, k, a.nz, 5, V4(a.ho12));
+        st4(poldot, i4, e * pc * kk + e * d2p + w2);
+        st4(tordot, i4, e * tc * kk + e * d2t - w3 + ez + V4(a.deta[k]) * dt);
+    }
+}
+
+static __global__ void k_bandj_spec4(BandjArgs<float> a)
+{
+    const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
+    const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const size_t pb = (size_t)blockIdx.y * np, i4 = (size_t)blockIdx.y * np4 + q4;
+    const unsigned q = 4 * q4;
+    const int j = (int)(q / (unsigned)a.nx), i0 = (int)(q - (unsigned)j * a.nx);
+    const float *s = a.dzs + pb, *tp = a.tor + pb, *pp = a.pol + pb;
+    st4(a.bxh, i4, sdx4(s, i0, j, a.nx, a.h.kx1) + sdy4(tp, i0, j, a.nx, a.ny, a.h.ky1));
+    st4(a.byh, i4, sdy4(s, i0, j, a.nx, a.ny, a.h.ky1) - sdx4(tp, i0, j, a.nx, a.h.kx1));
+    const V4 kk = ld4(a.h.kh2, q4);
+    st4(a.bzh, i4, V4(-1.0f) * ld4(pp, q4) * kk);
+    st4(a.jzh, i4, V4(-1.0f) * ld4(tp, q4) * kk);
+    // d/dy of ez = -pol*(akx2+aky2) at the mirrored row
+    V4 dy(0.0f);
+    if (!(j == 0 || 2 * j == a.ny)) {
+        const unsigned m = (unsigned)(a.ny - j) * a.nx + i0;
+        const V4 ezm = V4(-1.0f) * *reinterpret_cast<const V4 *>(pp + m) * *reinterpret_cast<const V4 *>(a.h.kh2 + m);
+        dy = ezm * V4(a.h.ky1[j]);
+        if (2 * j < a.ny) dy = -dy;
+    }
+    // d/dx at the mirrored column nx - i (four reversed points, two aligned loads)
+    const float *prow = pp + (size_t)j * a.nx, *krow = a.h.kh2 + (size_t)j * a.nx;
+    const V4 PA = *reinterpret_cast<const V4 *>(prow + a.nx - i0 - 4), KA = *reinterpret_cast<const V4 *>(krow + a.nx - i0 - 4);
+    const float pbv = i0 == 0 ? 0.0f : prow[a.nx - i0], kbv = i0 == 0 ? 0.0f : krow[a.nx - i0];
+    const float pm[4] = { pbv, PA.w, PA.z, PA.y }, km[4] = { kbv, KA.w, KA.z, KA.y };
+    const V4 k1 = ld4(a.h.kx1, (size_t)i0 / 4);
+    const float k1v[4] = { k1.x, k1.y, k1.z, k1.w };
+    float dx[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int i = i0 + c;
+        float v = 0.0f;
+        if (!(i == 0 || 2 * i == a.nx)) {
+            const float ezm = -1.0f * pm[c] * km[c];
+            v = ezm * k1v[c];
+            if (2 * i < a.nx) v = -v;
+        }
+        dx[c] = v;
+    }
+    st4(a.dybz, i4, dy);
+    st4(a.dxbz, i4, V4(dx[0], dx[1], dx[2], dx[3]));
+}
+
+static __global__ void k_jsq4(const float *jz, const float *dybz, const float *dxbz, const float *bx, const float *by,
+                              float *jsq, size_t np, int nz, float h)
+{
+    const size_t np4 = np / 4;
+    const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const int k = blockIdx.y;
+    const size_t i4 = (size_t)k * np4 + q4;
+    const V4 wk1 = zd1(reinterpret_cast<const V4 *>(by) + q4, np4, k, nz, 5, V4(h));
+    const V4 wk2 = zd1(reinterpret_cast<const V4 *>(bx) + q4, np4, k, nz, 5, V4(h));
+    const V4 ez = ld4(jz, i4), ex = ld4(dybz, i4), ey = ld4(dxbz, i4);
+    st4(jsq, i4, ez * ez + ((ex - wk1) * (ex - wk1)) + ((wk2 - ey) * (wk2 - ey)));
+}
+
 // spectral truncation of the 2/3 rule, src/magnetic.f90:666-717
 __host__ __device__ __forceinline__ bool truncated(int i, int j, int nx, int ny, int cx, int cy)
 {

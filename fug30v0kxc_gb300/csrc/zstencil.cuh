@@ -114,6 +114,43 @@ __device__ __forceinline__ void zwin_next(R *v, const R *f, size_t np, int k, in
     v[6] = k + 4 < nz ? f[(size_t)(k + 4) * np] : (R)0;
 }
 
+// Four consecutive x points as one value: 16-byte loads and stores, and the
+// templates above (zd1, zd2) evaluate the same formulas per component.
+struct __align__(16) V4 {
+    float x, y, z, w;
+    __host__ __device__ __forceinline__ V4() {}
+    __host__ __device__ __forceinline__ V4(float s) : x(s), y(s), z(s), w(s) {}
+    __host__ __device__ __forceinline__ V4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+};
+__host__ __device__ __forceinline__ V4 operator+(V4 a, V4 b) { return V4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__host__ __device__ __forceinline__ V4 operator-(V4 a, V4 b) { return V4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+__host__ __device__ __forceinline__ V4 operator*(V4 a, V4 b) { return V4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__host__ __device__ __forceinline__ V4 operator-(V4 a) { return V4(-a.x, -a.y, -a.z, -a.w); }
+// per component: w >= 0 ? p : m
+__host__ __device__ __forceinline__ V4 upsel(V4 w, V4 p, V4 m)
+{
+    return V4(w.x >= 0.0f ? p.x : m.x, w.y >= 0.0f ? p.y : m.y, w.z >= 0.0f ? p.z : m.z, w.w >= 0.0f ? p.w : m.w);
+}
+
+// zd1up for four points: both one-sided stencils of each row, chosen per
+// component by the sign of w (the same formulas and operation order as the
+// scalar zd1up)
+__host__ __device__ __forceinline__ V4 zd1up(const V4 *f, size_t np, int k, int nz, int fl, V4 h, V4 wv)
+{
+    typedef V4 R;
+#define F(kk) zld(f, np, kk)
+    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k == 2)
+        return upsel(wv, h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3)),
+                     h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1)));
+    if (k == nz - 3)
+        return upsel(wv, h * (-F(nz - 6) + (R)6 * F(nz - 5) - (R)18 * F(nz - 4) + (R)10 * F(nz - 3) + (R)3 * F(nz - 2)),
+                     h * ((R)-2 * F(nz - 1) + (R)12 * F(nz - 2) - (R)6 * F(nz - 3) - (R)4 * F(nz - 4)));
+    return upsel(wv, h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1)),
+                 h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1)));
+#undef F
+}
+
 // Interior rows (3 <= k <= nz-4) from a register window v[d] = f(k-3+d):
 // the same formulas and operation order as zd1 / zd1up / zd2.
 template <typename R>
