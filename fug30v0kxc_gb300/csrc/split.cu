@@ -23,6 +23,7 @@
 // a constant; the spectral derivative drops the mean and every z stencil
 // annihilates constants).
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -272,72 +273,105 @@ struct SplitHydroArgs {
 // a second-level derivative) on perturbation mirrors, for one point; the z
 // derivatives of t', u, v, w come from the caller (register windows in the
 // interior, direct row formulas near the walls)
-struct ZDer { float tzu, tzp, tzz, wzu, wz, uzu, vzu, uzz, vzz; };
+template <typename T> struct ZDer { T tzu, tzp, tzz, wzu, wz, uzu, vzu, uzz, vzz; };
 
-__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer &z)
+// loads and stores of one point (float) or four consecutive points (V4)
+template <typename T> __device__ __forceinline__ T ldv(const float *p, size_t i);
+template <> __device__ __forceinline__ float ldv<float>(const float *p, size_t i) { return p[i]; }
+template <> __device__ __forceinline__ V4 ldv<V4>(const float *p, size_t i) { return reinterpret_cast<const V4 *>(p)[i]; }
+__device__ __forceinline__ void stv(float *p, size_t i, float v) { p[i] = v; }
+__device__ __forceinline__ void stv(float *p, size_t i, V4 v) { reinterpret_cast<V4 *>(p)[i] = v; }
+__device__ __forceinline__ float upsel(float w, float p, float m) { return w >= 0.0f ? p : m; }
+__host__ __device__ __forceinline__ V4 operator/(V4 a, V4 b) { return V4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
+
+// one point (T = float, idx a point index) or four (T = V4, idx a 4-vector
+// index) of the terms without second-level derivatives
+template <typename T>
+__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z)
 {
     const int nz = a.nz;
     const float *pc = a.pc;
-    const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
-    const float rp = a.r[idx], tp = a.t[idx], u0 = a.u[idx], v0 = a.v[idx], w0 = a.w[idx];
-    const float rr = rho0 + rp, tt = t0 + tp;
-    const float bx = a.bx[idx], by = a.by[idx], bzp = a.bz[idx], bz = a.bzbar + bzp;
-    const float rx = a.rx[idx], ry = a.ry[idx];
-    const float tx = a.tx[idx], txx = a.txx[idx], ty = a.ty[idx], tyy = a.tyy[idx];
-    const float ux = a.ux[idx], uxx = a.uxx[idx], uy = a.uy[idx], uyy = a.uyy[idx];
-    const float vx = a.vx[idx], vxx = a.vxx[idx], vy = a.vy[idx], vyy = a.vyy[idx];
-    const float wx = a.wx[idx], wxx = a.wxx[idx], wy = a.wy[idx], wyy = a.wyy[idx];
+    const T rho0 = T(pc[PC_RHO0 * nz + k]), t0 = T(pc[PC_T0 * nz + k]);
+    const T rp = ldv<T>(a.r, idx), tp = ldv<T>(a.t, idx), u0 = ldv<T>(a.u, idx), v0 = ldv<T>(a.v, idx);
+    const T w0 = ldv<T>(a.w, idx);
+    const T rr = rho0 + rp, tt = t0 + tp;
+    const T bx = ldv<T>(a.bx, idx), by = ldv<T>(a.by, idx), bzp = ldv<T>(a.bz, idx), bz = T(a.bzbar) + bzp;
+    const T rx = ldv<T>(a.rx, idx), ry = ldv<T>(a.ry, idx);
+    const T tx = ldv<T>(a.tx, idx), txx = ldv<T>(a.txx, idx), ty = ldv<T>(a.ty, idx), tyy = ldv<T>(a.tyy, idx);
+    const T ux = ldv<T>(a.ux, idx), uxx = ldv<T>(a.uxx, idx), uy = ldv<T>(a.uy, idx), uyy = ldv<T>(a.uyy, idx);
+    const T vx = ldv<T>(a.vx, idx), vxx = ldv<T>(a.vxx, idx), vy = ldv<T>(a.vy, idx), vyy = ldv<T>(a.vyy, idx);
+    const T wx = ldv<T>(a.wx, idx), wxx = ldv<T>(a.wxx, idx), wy = ldv<T>(a.wy, idx), wyy = ldv<T>(a.wyy, idx);
 
-    const bool wpos = w0 >= 0.0f;
-    const float tzu = z.tzu + pc[(wpos ? PC_T0ZU_P : PC_T0ZU_M) * nz + k];
-    const float tzp = z.tzp;
-    const float tzz = z.tzz + pc[PC_T0ZZ0 * nz + k];
-    const float wzu = z.wzu, wz = z.wz, uzu = z.uzu, vzu = z.vzu, uzz = z.uzz, vzz = z.vzz;
+    const T tzu = z.tzu + upsel(w0, T(pc[PC_T0ZU_P * nz + k]), T(pc[PC_T0ZU_M * nz + k]));
+    const T tzp = z.tzp;
+    const T tzz = z.tzz + T(pc[PC_T0ZZ0 * nz + k]);
+    const T wzu = z.wzu, wz = z.wz, uzu = z.uzu, vzu = z.vzu, uzz = z.uzz, vzz = z.vzz;
 
-    const float third = 1.0f / 3.0f;
-    const float ohm = a.var_eta ? pc[PC_OHM * nz + k] : 1.0f;
-    const float divu = ux + vy + wz;
+    const T third = T(1.0f / 3.0f);
+    const T ohm = T(a.var_eta ? pc[PC_OHM * nz + k] : 1.0f);
+    const T divu = ux + vy + wz;
 
-    a.racc[idx] = -u0 * rx - v0 * ry - rr * divu;
+    stv(a.racc, idx, -u0 * rx - v0 * ry - rr * divu);
 
-    float td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
-               + a.gck * pc[PC_KAPPA * nz + k] * (txx + tyy + tzz)
-               + a.gck * pc[PC_DKAPPA * nz + k] * tzu
-               + a.fzckg * ohm * a.jsq[idx];
-    td = td - a.gm1 * tt * divu * rr + 2.0f * a.sckg * (ux * ux + vy * vy + wz * wz - third * divu * divu);
-    td = td + a.sckg * (uy + vx) * (uy + vx);
-    td = td + a.sckg * (wx + uzu) * (wx + uzu);
-    td = td + a.sckg * (wy + vzu) * (wy + vzu);
-    ((float *)a.ht->p[1][2])[idx] = td / rr;
+    T td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
+           + T(a.gck) * T(pc[PC_KAPPA * nz + k]) * (txx + tyy + tzz)
+           + T(a.gck) * T(pc[PC_DKAPPA * nz + k]) * tzu
+           + T(a.fzckg) * ohm * ldv<T>(a.jsq, idx);
+    td = td - T(a.gm1) * tt * divu * rr + T(2.0f) * T(a.sckg) * (ux * ux + vy * vy + wz * wz - third * divu * divu);
+    td = td + T(a.sckg) * (uy + vx) * (uy + vx);
+    td = td + T(a.sckg) * (wx + uzu) * (wx + uzu);
+    td = td + T(a.sckg) * (wy + vzu) * (wy + vzu);
+    stv((float *)a.ht->p[1][2], idx, td / rr);
 
-    float ud = -tt * rx - rr * tx;
+    T ud = -tt * rx - rr * tx;
     ud = ud - rr * u0 * ux - rr * v0 * uy - rr * w0 * uzu;
-    ud = ud - rr * a.cor * (w0 * a.cpsi + v0 * a.spsi);
-    ud = ud + a.sck * (uzz + uxx + uyy);
-    float vd = -tt * ry - rr * ty;
+    ud = ud - rr * T(a.cor) * (w0 * T(a.cpsi) + v0 * T(a.spsi));
+    ud = ud + T(a.sck) * (uzz + uxx + uyy);
+    T vd = -tt * ry - rr * ty;
     vd = vd - rr * v0 * vy - rr * u0 * vx - rr * w0 * vzu;
-    vd = vd - rr * a.cor * (-u0 * a.spsi);
-    vd = vd + a.sck * (vzz + vxx + vyy);
+    vd = vd - rr * T(a.cor) * (-u0 * T(a.spsi));
+    vd = vd + T(a.sck) * (vzz + vxx + vyy);
     // -rho dT/dz + theta(m+1) rho minus its FP64 background part
-    const float t0z = pc[PC_T0Z5 * nz + k];
-    float wd = -rho0 * tzp - rp * t0z - rp * tzp + a.thmplus1 * rp;
+    const T t0z = T(pc[PC_T0Z5 * nz + k]);
+    T wd = -rho0 * tzp - rp * t0z - rp * tzp + T(a.thmplus1) * rp;
     wd = wd - rr * w0 * wzu - rr * u0 * wx - rr * v0 * wy;
-    wd = wd - rr * a.cor * (-u0 * a.cpsi);
-    wd = wd + a.sck * (wxx + wyy);
-    a.uacc[idx] = ud;
-    a.vacc[idx] = vd;
-    a.wacc[idx] = wd;
+    wd = wd - rr * T(a.cor) * (-u0 * T(a.cpsi));
+    wd = wd + T(a.sck) * (wxx + wyy);
+    stv(a.uacc, idx, ud);
+    stv(a.vacc, idx, vd);
+    stv(a.wacc, idx, wd);
 
-    const float b2z = bzp * (2.0f * a.bzbar + bzp);          // bz^2 - bzbar^2
-    const float temp1 = a.fo2 * bx * bx, temp2 = a.fo2 * by * by, temp3 = a.fo2 * b2z;
-    const float dv = a.scko3 * divu;
-    a.p1[idx] = dv + temp1 - temp2 - temp3;
-    a.p2[idx] = dv + temp2 - temp1 - temp3;
-    a.p3[idx] = a.scko3 * ux + a.scko3 * vy + temp3 - temp1 - temp2;
-    a.p4[idx] = 4.0f * a.scko3 * wz;
-    a.q[idx] = a.f * by * bx;
-    a.g[idx] = a.f * bz * bx;
-    a.hh[idx] = a.f * bz * by;
+    const T b2z = bzp * (T(2.0f) * T(a.bzbar) + bzp);          // bz^2 - bzbar^2
+    const T temp1 = T(a.fo2) * bx * bx, temp2 = T(a.fo2) * by * by, temp3 = T(a.fo2) * b2z;
+    const T dv = T(a.scko3) * divu;
+    stv(a.p1, idx, dv + temp1 - temp2 - temp3);
+    stv(a.p2, idx, dv + temp2 - temp1 - temp3);
+    stv(a.p3, idx, T(a.scko3) * ux + T(a.scko3) * vy + temp3 - temp1 - temp2);
+    stv(a.p4, idx, T(4.0f) * T(a.scko3) * wz);
+    stv(a.q, idx, T(a.f) * by * bx);
+    stv(a.g, idx, T(a.f) * bz * bx);
+    stv(a.hh, idx, T(a.f) * bz * by);
+}
+
+// four consecutive x points per thread, one plane per CTA row (grid
+// (np/4/256, nz)); the z neighbours come through L1/L2
+__global__ void __launch_bounds__(256, 2) k_split_pass2_v4(SplitHydroArgs a)
+{
+    const size_t np4 = a.np / 4;
+    const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const int nz = a.nz;
+    const int k = blockIdx.y;
+    const V4 h(a.ho12), s(a.sc1);
+    const V4 *t4 = reinterpret_cast<const V4 *>(a.t) + q4, *u4 = reinterpret_cast<const V4 *>(a.u) + q4;
+    const V4 *v4 = reinterpret_cast<const V4 *>(a.v) + q4, *w4 = reinterpret_cast<const V4 *>(a.w) + q4;
+    const V4 w0 = w4[(size_t)k * np4];
+    ZDer<V4> z;
+    z.tzu = zd1up(t4, np4, k, nz, 5, h, w0); z.tzp = zd1(t4, np4, k, nz, 5, h); z.tzz = zd2(t4, np4, k, nz, 0, s);
+    z.wzu = zd1up(w4, np4, k, nz, 1, h, w0); z.wz = zd1(w4, np4, k, nz, 1, h);
+    z.uzu = zd1up(u4, np4, k, nz, 2, h, w0); z.vzu = zd1up(v4, np4, k, nz, 2, h, w0);
+    z.uzz = zd2(u4, np4, k, nz, 3, s); z.vzz = zd2(v4, np4, k, nz, 3, s);
+    split_pass2_point<V4>(a, (size_t)k * np4 + q4, k, z);
 }
 
 // z-marching: one thread per (i,j) column and chunk of kc planes, with
@@ -364,7 +398,7 @@ __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
     for (int k = k0; k < k1; k++) {
         const size_t idx = (size_t)k * np + q;
         const float w0 = W[3];
-        ZDer z;
+        ZDer<float> z;
         if (k >= 3 && k <= nz - 4) {
             z.tzu = wd1up(T, h, w0); z.tzp = wd1(T, h); z.tzz = wd2(T, s);
             z.wzu = wd1up(W, h, w0); z.wz = wd1(W, h);
@@ -377,7 +411,7 @@ __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
             z.uzu = zd1up(a.u + q, np, k, nz, 2, h, w0); z.vzu = zd1up(a.v + q, np, k, nz, 2, h, w0);
             z.uzz = zd2(a.u + q, np, k, nz, 3, s); z.vzz = zd2(a.v + q, np, k, nz, 3, s);
         }
-        split_pass2_point(a, idx, k, z);
+        split_pass2_point<float>(a, idx, k, z);
 #pragma unroll
         for (int d = 0; d < 6; d++) { T[d] = T[d + 1]; U[d] = U[d + 1]; V[d] = V[d + 1]; W[d] = W[d + 1]; }
         const int kn = k + 4;
@@ -532,9 +566,16 @@ int split_hydro(Engine *E)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
-    const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
-    dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
-    KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
+    if (E->nx % 4 == 0 && E->vec4) {
+        // (two CTAs per SM: 128 registers with a few spilled values beat
+        // 175 registers at one CTA per SM, 4.8 against 3.8 TB/s)
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v4,
+                 dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), TPB, a);
+    } else {
+        const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
+        dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
+    }
 
     LineJob<float> kx[3] = {
         ljob<float>(W[W_P1], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
