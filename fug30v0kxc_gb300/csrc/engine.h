@@ -108,6 +108,7 @@ struct Engine {
     int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
     int ct_s = 0;               // sequences per line tile (0: default for the size)
     bool ct_warp = true;        // x-line tiles synchronised per warp (VEC_CT_WARP=0: per CTA)
+    bool prof_kinds = false;    // VEC_PROF_KINDS=1: line launches profiled per job kind
     bool vec4 = true;           // four-point (16-byte) forms of the split pointwise kernels (VEC_VEC4=0: one point)
     bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
                                 // (VEC_HW_CVT=1: hardware conversions; the same bits)

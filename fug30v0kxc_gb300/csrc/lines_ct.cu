@@ -588,6 +588,16 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
         const int nj = njobs - j0 < MAX_JOBS ? njobs - j0 : MAX_JOBS;
         const LineJob<R> *jb = jobs + j0;
         const char *name = dir == 0 ? (F ? "line_x_f32" : "line_x_f64") : (F ? "line_y_f32" : "line_y_f64");
+        if (E->prof_kinds) {
+            // per job kind (profiling aid): forward, inverse, accumulate, derivative pair, other
+            static const char *kinds[2][2][5] = {
+                { { "line_x_f64_fwd", "line_x_f64_inv", "line_x_f64_acc", "line_x_f64_d12", "line_x_f64_op" },
+                  { "line_x_f32_fwd", "line_x_f32_inv", "line_x_f32_acc", "line_x_f32_d12", "line_x_f32_op" } },
+                { { "line_y_f64_fwd", "line_y_f64_inv", "line_y_f64_acc", "line_y_f64_d12", "line_y_f64_op" },
+                  { "line_y_f32_fwd", "line_y_f32_inv", "line_y_f32_acc", "line_y_f32_d12", "line_y_f32_op" } } };
+            const int kd = jb[0].op1 == OP_FWD ? 0 : jb[0].op1 == OP_INV ? 1 : jb[0].acc1 ? 2 : jb[0].op2 != OP_NONE ? 3 : 4;
+            name = kinds[dir][F ? 1 : 0][kd];
+        }
         int st = -1;
 #define CT_CASE(NN, A, B, SS)                                                                       \
     if (n == NN && S == SS)                                                                         \

@@ -426,6 +426,9 @@ __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
 
 struct SplitHydro4Args {
     const float *r, *t, *w, *p3, *p4, *g, *hh, *racc, *uacc, *vacc, *wacc;
+    // horizontal derivatives of the second-level fluxes: d(p1)/dx, d(q)/dy into
+    // u; d(q)/dx, d(p2)/dy into v; d(g)/dx, d(h)/dy into w
+    const float *dxu, *dyu, *dxv, *dyv, *dxw, *dyw;
     const double *bg;
     const float *pc;
     const HistTable *ht;    // rdot, udot, vdot, wdot = newest slots
@@ -449,9 +452,13 @@ __global__ void k_split_pass4(SplitHydro4Args a)
     const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
     const float rp = a.r[idx], tp = a.t[idx], w0 = a.w[idx];
     const float rr = rho0 + rp, tt = t0 + tp;
-    float wd = a.wacc[idx] + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
-    const float ud = a.uacc[idx] + zd1(a.g + q, np, k, nz, 5, h);
-    const float vd = a.vacc[idx] + zd1(a.hh + q, np, k, nz, 5, h);
+    // (sums in the order of the reference's accumulation: x, then y, then z)
+    const float wacc = (a.wacc[idx] + a.dxw[idx]) + a.dyw[idx];
+    const float uacc = (a.uacc[idx] + a.dxu[idx]) + a.dyu[idx];
+    const float vacc = (a.vacc[idx] + a.dxv[idx]) + a.dyv[idx];
+    float wd = wacc + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
+    const float ud = uacc + zd1(a.g + q, np, k, nz, 5, h);
+    const float vd = vacc + zd1(a.hh + q, np, k, nz, 5, h);
     float rdot, wfin;
     if (k == 0 || k == nz - 1) {
         // src/hydro_deriv.f90:455-470: d(rho)/dz chosen so that dw/dt = 0
@@ -493,9 +500,12 @@ __global__ void k_split_pass4_v4(SplitHydro4Args a)
     const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
     const V4 rp = ld(a.r, i4), tp = ld(a.t, i4), w0 = ld(a.w, i4);
     const V4 rr = V4(rho0) + rp, tt = V4(t0) + tp;
-    V4 wd = ld(a.wacc, i4) + zd1(p3, np4, k, nz, 2, h) + zd1(p4, np4, k, nz, 5, h);
-    const V4 ud = ld(a.uacc, i4) + zd1(g, np4, k, nz, 5, h);
-    const V4 vd = ld(a.vacc, i4) + zd1(hh, np4, k, nz, 5, h);
+    const V4 wacc = (ld(a.wacc, i4) + ld(a.dxw, i4)) + ld(a.dyw, i4);
+    const V4 uacc = (ld(a.uacc, i4) + ld(a.dxu, i4)) + ld(a.dyu, i4);
+    const V4 vacc = (ld(a.vacc, i4) + ld(a.dxv, i4)) + ld(a.dyv, i4);
+    V4 wd = wacc + zd1(p3, np4, k, nz, 2, h) + zd1(p4, np4, k, nz, 5, h);
+    const V4 ud = uacc + zd1(g, np4, k, nz, 5, h);
+    const V4 vd = vacc + zd1(hh, np4, k, nz, 5, h);
     const V4 racc = ld(a.racc, i4);
     V4 rdot, wfin;
     if (k == 0 || k == nz - 1) {
@@ -577,29 +587,37 @@ int split_hydro(Engine *E)
         KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
     }
 
+    // The second-level horizontal derivatives go to separate arrays (the
+    // first-level derivative arrays, free once pass 2 has run) and pass 4
+    // adds them: a line pass that accumulates into its output reads each
+    // output element before writing it, and that dependent read made those
+    // two launches the slowest line passes of the step.
+    float *dxu = W[W_TXX], *dxv = W[W_UXX], *dxw = W[W_VXX];
+    float *dyu = W[W_TYY], *dyv = W[W_UYY], *dyw = W[W_VYY];
     LineJob<float> kx[3] = {
-        ljob<float>(W[W_P1], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
-        ljob<float>(W[W_Q], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
-        ljob<float>(W[W_G], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_P1], dxu, OP_D1),
+        ljob<float>(W[W_Q], dxv, OP_D1),
+        ljob<float>(W[W_G], dxw, OP_D1),
     };
     if ((st = launch_lines<float>(E, 0, kx, 3))) return st;
     LineJob<float> ky[3] = {
-        ljob<float>(W[W_P2], W[W_VACC], OP_D1, nullptr, OP_NONE, 1),
-        ljob<float>(W[W_Q], W[W_UACC], OP_D1, nullptr, OP_NONE, 1),
-        ljob<float>(W[W_H], W[W_WACC], OP_D1, nullptr, OP_NONE, 1),
+        ljob<float>(W[W_P2], dyv, OP_D1),
+        ljob<float>(W[W_Q], dyu, OP_D1),
+        ljob<float>(W[W_H], dyw, OP_D1),
     };
     if ((st = launch_lines<float>(E, 1, ky, 3))) return st;
 
     SplitHydro4Args b;
     b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
     b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres; b.pc = E->pcf;
+    b.dxu = dxu; b.dyu = dyu; b.dxv = dxv; b.dyv = dyv; b.dxw = dxw; b.dyw = dyw;
     b.ht = E->ht;
     b.ho12 = (float)c.ho12; b.np = E->np; b.nz = E->nz;
     if (E->nx % 4 == 0 && E->vec4)
-        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4_v4,
+        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 21, 4), k_split_pass4_v4,
                  dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), TPB, b);
     else
-        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 15, 4), k_split_pass4, plane_grid(*E), TPB, b);
+        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 21, 4), k_split_pass4, plane_grid(*E), TPB, b);
     return VEC_OK;
 }
 
