@@ -204,10 +204,11 @@ __global__ void k_b64(const float *bx32, const float *by32, const float *bz32, c
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    bx[i] = (double)bx32[i];
-    by[i] = (double)by32[i];
-    bz[i] = bzbar + (double)bz32[i];
-    jsq[i] = (double)jsq32[i];
+    // (conversions on the integer pipe, the same bits as the casts)
+    bx[i] = f2d_exact(bx32[i]);
+    by[i] = f2d_exact(by32[i]);
+    bz[i] = bzbar + f2d_exact(bz32[i]);
+    jsq[i] = f2d_exact(jsq32[i]);
 }
 
 // FP64 B and jsq from the FP32 ones when the FP32 copy is the newer one
@@ -876,17 +877,20 @@ struct DealiasArgs {
     int nz;
 };
 
+// grid (np/256, nz); float <-> double conversions on the integer pipe (the
+// same bits as the casts; the FP64 pipe keeps only the subtractions)
 __global__ void k_split_dealias_apply(DealiasArgs a)
 {
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.np * a.nz) return;
-    const int k = (int)(idx / a.np);
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.np) return;
+    const int k = blockIdx.y;
+    const size_t idx = (size_t)k * a.np + q;
 #pragma unroll
     for (int f = 0; f < 5; f++) {
-        double xn = a.x[f][idx] - ((double)a.m[f][idx] - (double)a.d[f][idx]);
+        double xn = a.x[f][idx] - (f2d_exact(a.m[f][idx]) - f2d_exact(a.d[f][idx]));
         a.x[f][idx] = xn;
-        double b = f == 0 ? a.bg[BG_RHO0 * a.nz + k] : f == 1 ? a.bg[BG_T0 * a.nz + k] : 0.0;
-        a.m[f][idx] = (float)(xn - b);
+        if (f < 2) a.m[f][idx] = d2f_rn(xn - a.bg[(f == 0 ? BG_RHO0 : BG_T0) * a.nz + k]);
+        else a.m[f][idx] = d2f_rn(xn);
     }
 }
 
@@ -907,7 +911,7 @@ int split_dealias(Engine *E)
     DealiasArgs a;
     for (int i = 0; i < 5; i++) { a.x[i] = xs[i]; a.m[i] = ms[i]; a.d[i] = tmp[i]; }
     a.bg = E->hres; a.np = E->np; a.nz = E->nz;
-    KLAUNCHB(E, "dealias_apply_split", FB(E, 5, 24), k_split_dealias_apply, nblk(E->n), TPB, a);
+    KLAUNCHB(E, "dealias_apply_split", FB(E, 5, 24), k_split_dealias_apply, plane_grid(*E), TPB, a);
     return VEC_OK;
 }
 
