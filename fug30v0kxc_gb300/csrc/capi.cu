@@ -265,6 +265,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         E.ct_warp = !(cw && cw[0] == '0');
         const char *pk = getenv("VEC_PROF_KINDS");
         E.prof_kinds = pk && pk[0] == '1';
+        const char *pd = getenv("VEC_PDL");
+        E.pdl = !(pd && pd[0] == '0');
         const char *v4 = getenv("VEC_VEC4");
         E.vec4 = !(v4 && v4[0] == '0');
         const char *hc = getenv("VEC_HW_CVT");

@@ -98,6 +98,12 @@ struct HistTable {
     double *bx[3], *by[3];  // bxbardot, bybardot
 };
 
+// First statement of the step's kernels: with programmatic dependent launch
+// a kernel may be started while its predecessor in the stream still runs,
+// and this waits until every predecessor grid has completed and its memory
+// is visible (a no-op for an ordinary launch).
+#define PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
 // ---- error helper --------------------------------------------------------
 void vec_set_error(const char *fmt, ...);
 

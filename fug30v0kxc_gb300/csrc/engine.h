@@ -7,6 +7,7 @@
 // itself, the 1-D backgrounds and the diagnostics stay double.
 #pragma once
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -109,6 +110,7 @@ struct Engine {
     int ct_s = 0;               // sequences per line tile (0: default for the size)
     bool ct_warp = true;        // x-line tiles synchronised per warp (VEC_CT_WARP=0: per CTA)
     bool prof_kinds = false;    // VEC_PROF_KINDS=1: line launches profiled per job kind
+    bool pdl = true;            // programmatic dependent launches (VEC_PDL=0: ordinary launches)
     bool vec4 = true;           // four-point (16-byte) forms of the split pointwise kernels (VEC_VEC4=0: one point)
     bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
                                 // (VEC_HW_CVT=1: hardware conversions; the same bits)
@@ -135,6 +137,27 @@ struct Engine {
 };
 
 template <> inline const LineTables<double> &Engine::tables<double>(int dir) const { return dir == 0 ? tx64 : ty64; }
+// A kernel launch on the engine's stream.  With E.pdl (the default) it is a
+// programmatic dependent launch: the launch of the next kernel overlaps the
+// end of this one, which hides most of the gap between the step's kernels;
+// every kernel launched this way starts with PDL_WAIT().
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(const Engine &E, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            Args &&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = E.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = E.pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <typename R> inline HTab<R> htab(const Engine &E);
 // one CTA row of 256 threads per plane (the spectral kernels of magkern.cuh)
 inline dim3 plane_grid(const Engine &E) { return dim3((unsigned)((E.np + 255) / 256), (unsigned)E.nz); }

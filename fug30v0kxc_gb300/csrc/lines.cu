@@ -172,6 +172,7 @@ template <typename R, int DIR>
 __global__ void __launch_bounds__(512, 1)
 line_kernel(JobPack<R> jobs, LinePlan pl, LineTables<R> tb, int nx, int ny, int nz)
 {
+    PDL_WAIT();
     using C = typename CT<R>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = pl.n, P = pl.P, ld = n + 1;

@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (S * (N1 > N2 ? N1 : 
 line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R> tb, int nx, int ny, int nz,
         int tpp, int total, int *err)
 {
+    PDL_WAIT();
     using C = typename CT<R>::T;
     constexpr int N = N1 * N2;
     constexpr int NP = N1 > N2 ? N1 : N2;
@@ -551,8 +552,8 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     int grid = E->num_sms * per_sm;
     if (grid > total) grid = total;
     E->prof_begin(name, fields * (double)E->n * sizeof(R));
-    line_ct<R, DIR, N1, N2, S, WSYNC><<<grid, S * NP, smem, E->stream>>>(pk, tp, E->tables<R>(DIR), E->nx, E->ny,
-                                                                         E->nz, tpp, total, E->dev_err);
+    CUDA_TRY(launch_k(*E, line_ct<R, DIR, N1, N2, S, WSYNC>, dim3(grid), dim3(S * NP), smem, pk, tp,
+                      E->tables<R>(DIR), E->nx, E->ny, E->nz, tpp, total, E->dev_err));
     E->prof_end();
     CUDA_TRY(cudaGetLastError());
     return VEC_OK;

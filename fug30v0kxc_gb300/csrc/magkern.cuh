@@ -9,6 +9,7 @@ template <typename R>
 static __global__ void k_emf(const R *u, const R *v, const R *w, const R *bx, const R *by, const R *bz, R *e1,
                              R *e2, R *e3, size_t n, R bzoff)
 {
+    PDL_WAIT();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R bzv = bz[i] + bzoff;
@@ -24,6 +25,7 @@ static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar,
                                   double *scratch, size_t np, int nz, double xn, double zck, double ho12,
                                   double sc1, int var_eta)
 {
+    PDL_WAIT();
     double *bxd = ht->bx[2], *byd = ht->by[2];
     double *e1 = scratch, *e2 = scratch + nz;
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
@@ -57,6 +59,7 @@ static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar,
 template <typename R>
 static __global__ void k_mag_div(const R *ex, const R *ey, R *w1, int nx, int ny, HTab<R> h)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)nx * ny;
     const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
@@ -82,6 +85,7 @@ struct MagArgs {
 template <typename R>
 static __global__ void k_mag_final(MagArgs<R> a)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)a.nx * a.ny;
     const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
@@ -121,6 +125,7 @@ struct BandjArgs {
 template <typename R>
 static __global__ void k_bandj_spec(BandjArgs<R> a)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)a.nx * a.ny;
     const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
@@ -156,6 +161,7 @@ template <typename R>
 static __global__ void k_jsq(const R *jz, const R *dybz, const R *dxbz, const R *bx, const R *by, R *jsq,
                              size_t np, int nz, R h)
 {
+    PDL_WAIT();
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     const int k = blockIdx.y;
@@ -211,6 +217,7 @@ __device__ __forceinline__ V4 sdy4(const float *plane, int i0, int j, int nx, in
 static __global__ void k_emf4(const float *u, const float *v, const float *w, const float *bx, const float *by,
                               const float *bz, float *e1, float *e2, float *e3, size_t n4, float bzoff)
 {
+    PDL_WAIT();
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n4) return;
     const V4 U = ld4(u, i), Vv = ld4(v, i), W = ld4(w, i), BX = ld4(bx, i), BY = ld4(by, i);
@@ -222,6 +229,7 @@ static __global__ void k_emf4(const float *u, const float *v, const float *w, co
 
 static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h)
 {
+    PDL_WAIT();
     const unsigned np4 = (unsigned)nx * ny / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -233,6 +241,7 @@ static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, i
 
 static __global__ void k_mag_final4(MagArgs<float> a)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -268,6 +277,7 @@ static __global__ void k_mag_final4(MagArgs<float> a)
 
 static __global__ void k_bandj_spec4(BandjArgs<float> a)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -314,6 +324,7 @@ static __global__ void k_bandj_spec4(BandjArgs<float> a)
 static __global__ void k_jsq4(const float *jz, const float *dybz, const float *dxbz, const float *bx, const float *by,
                               float *jsq, size_t np, int nz, float h)
 {
+    PDL_WAIT();
     const size_t np4 = np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -335,6 +346,7 @@ __host__ __device__ __forceinline__ bool truncated(int i, int j, int nx, int ny,
 template <typename R>
 static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, int cy)
 {
+    PDL_WAIT();
     const unsigned np = (unsigned)nx * ny;
     const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
@@ -350,6 +362,7 @@ static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, in
 template <typename R>
 static __global__ void k_zero_mag_rhs(const HistTable *ht, size_t n, int nz)
 {
+    PDL_WAIT();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) { ((R *)ht->p[5][2])[i] = (R)0; ((R *)ht->p[6][2])[i] = (R)0; }
     if (i < (size_t)nz) { ht->bx[2][i] = 0.0; ht->by[2][i] = 0.0; }
@@ -359,6 +372,7 @@ static __global__ void k_zero_mag_rhs(const HistTable *ht, size_t n, int nz)
 // the logical slots: 0 <- 1 <- 2 <- old 0 (reused for the next RHS)
 static __global__ void k_rotate_hist(HistTable *ht)
 {
+    PDL_WAIT();
     if (threadIdx.x != 0) return;
     for (int f = 0; f < 7; f++) {
         void *o = ht->p[f][0];

@@ -35,7 +35,7 @@ static inline unsigned nblk(size_t n, int tpb = TPB)
 #define KLAUNCHB(E, name, bytes, kern, grid, block, ...)         \
     do {                                                         \
         (E)->prof_begin(name, (double)(bytes));                  \
-        kern<<<(grid), (block), 0, (E)->stream>>>(__VA_ARGS__);  \
+        CUDA_TRY(launch_k(*(E), kern, dim3(grid), dim3(block), 0, __VA_ARGS__)); \
         (E)->prof_end();                                         \
         CUDA_TRY(cudaGetLastError());                            \
     } while (0)
@@ -49,6 +49,7 @@ static inline unsigned nblk(size_t n, int tpb = TPB)
 template <typename R>
 __global__ void k_d1z(const R *in, R *out, int fl, size_t np, int nz, R h)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * nz) return;
     int k = (int)(idx / np);
@@ -58,6 +59,7 @@ __global__ void k_d1z(const R *in, R *out, int fl, size_t np, int nz, R h)
 template <typename R>
 __global__ void k_d1upz(const R *in, const R *w, R *out, int fl, size_t np, int nz, R h)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * nz) return;
     int k = (int)(idx / np);
@@ -67,6 +69,7 @@ __global__ void k_d1upz(const R *in, const R *w, R *out, int fl, size_t np, int 
 template <typename R>
 __global__ void k_d2z(const R *in, R *out, int fl, size_t np, int nz, R s)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * nz) return;
     int k = (int)(idx / np);
@@ -115,6 +118,7 @@ struct HydroArgs {
 // derivative); the energy equation is complete here.
 __global__ void k_hydro_pass2(HydroArgs a)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.np * a.nz) return;
     const int nz = a.nz;
@@ -201,6 +205,7 @@ struct Hydro4Args {
 // :443-497 (d(rho)/dz with the boundary override, division by rho)
 __global__ void k_hydro_pass4(Hydro4Args a)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.np * a.nz) return;
     const int nz = a.nz;
@@ -383,6 +388,7 @@ int phys_magdealias(Engine *E)
 __global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
                            double dz, int radbc, int constflux)
 {
+    PDL_WAIT();
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     const double elf = 1.0 / 11.0;
@@ -421,6 +427,7 @@ int phys_boundary(Engine *E)
 
 __global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect)
 {
+    PDL_WAIT();
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const double elf = 1.0 / 11.0;
     if (q == 0) {
@@ -463,6 +470,7 @@ int phys_mag_boundary(Engine *E)
 // update (:469-476) on one CTA
 __global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const HistTable *ht, int nz, int do_means)
 {
+    PDL_WAIT();
     const double *bxd0 = ht->bx[0], *bxd1 = ht->bx[1], *bxd2 = ht->bx[2];
     const double *byd0 = ht->by[0], *byd1 = ht->by[1], *byd2 = ht->by[2];
     __shared__ double cc[3];
@@ -510,6 +518,7 @@ struct Ab3Args {
 // magdealias (:503-509) applied to the new pol/tor
 __global__ void k_ab3_update(Ab3Args a)
 {
+    PDL_WAIT();
     const size_t np = (size_t)a.nx * a.ny;
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * a.nz) return;
@@ -642,7 +651,8 @@ __device__ __forceinline__ void cdt_reset_keys(unsigned *gkey)
     gkey[1] = 0u;
     gkey[2] = 0xffffffffu;     // above every float's key
 }
-__global__ void k_cdt_init(unsigned *gkey) { cdt_reset_keys(gkey); }
+__global__ void k_cdt_init(unsigned *gkey) {
+    PDL_WAIT(); cdt_reset_keys(gkey); }
 int cdt_init(float *cdt)
 {
     k_cdt_init<<<1, 1>>>(reinterpret_cast<unsigned *>(cdt));
@@ -693,6 +703,7 @@ __device__ __forceinline__ void block_reduce3(float &mx, float &mz, float &mn, f
 
 __global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
 {
+    PDL_WAIT();
     __shared__ float sh[96];
     const size_t i0 = (size_t)blockIdx.x * CDT_CHUNK;
     const size_t i1 = i0 + CDT_CHUNK < a.n ? i0 + CDT_CHUNK : a.n;
@@ -716,6 +727,7 @@ __global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
 
 __global__ void __launch_bounds__(256) k_calcdt_exact(CdtArgs a)
 {
+    PDL_WAIT();
     const float gx = okey32_dec(a.gkey[0]), gz = okey32_dec(a.gkey[1]), gr = okey32_dec(a.gkey[2]);
     // thresholds a relative margin below (above) the estimates; scaling
     // keeps infinite estimates infinite
@@ -759,6 +771,7 @@ __global__ void k_calcdt_fin(DevScalars *ds, unsigned *gkey, double dd, double d
                              double dtvisc0z, double dtdiff0x, double dtdiff0z, double sf, int var_eta,
                              double eta_max)
 {
+    PDL_WAIT();
     double velmxx = okey_dec(ds->velmxx);
     double velmxz = okey_dec(ds->velmxz);
     double denmn = okey_dec(ds->denmn);
@@ -805,6 +818,7 @@ int phys_calcdt(Engine *E)
 __global__ void k_plane_sums(const double *r, const double *u, const double *v, const double *w,
                              const double *bx, const double *by, const double *bz, size_t np, double *out)
 {
+    PDL_WAIT();
     const int k = blockIdx.x;
     const size_t base = (size_t)k * np;
     double s[5] = { 0, 0, 0, 0, 0 };
@@ -830,6 +844,7 @@ __global__ void k_plane_sums(const double *r, const double *u, const double *v, 
 
 __global__ void k_sub_mean(double *u, double *v, size_t n, const DevScalars *ds)
 {
+    PDL_WAIT();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     u[i] = u[i] - ds->res[0];
@@ -838,6 +853,7 @@ __global__ void k_sub_mean(double *u, double *v, size_t n, const DevScalars *ds)
 
 __global__ void k_globalavg_fin(const double *ps, int nz, double xzn, DevScalars *ds)
 {
+    PDL_WAIT();
     double urbar = 0, vrbar = 0, rbar = 0, me = 0, ke = 0;
     for (int k = 0; k < nz; k++) {
         const double *p = ps + (size_t)k * 8;
@@ -860,6 +876,7 @@ __global__ void k_minmax(const double *r, const double *t, const double *u, cons
                          const double *bx, const double *by, const double *bz, const double *dxbx,
                          const double *dyby, size_t np, int nz, double ho12, double *out)
 {
+    PDL_WAIT();
     double mn[NMM], mx[NMM];
     for (int m = 0; m < NMM; m++) { mn[m] = 1.0e300; mx[m] = -1.0e300; }
     const size_t n = np * nz;
@@ -897,6 +914,7 @@ __global__ void k_minmax(const double *r, const double *t, const double *u, cons
 
 __global__ void k_nusselt_sum(const double *t, size_t np, int nz, double dz, double *out)
 {
+    PDL_WAIT();
     double s = 0.0;
     for (size_t i = threadIdx.x; i < np; i += blockDim.x)
         s += ((1.0 / (6.0 * dz)) * (11.0 * t[(size_t)(nz - 1) * np + i] - 18.0 * t[(size_t)(nz - 2) * np + i]
@@ -983,6 +1001,7 @@ __global__ void k_static(double *r, double *t, double *u, double *v, double *w, 
                          double *bz, const double *t0k, const double *r0k, size_t np, int nz, double amp,
                          int seed_base, int perfect)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * nz) return;
     const int k = (int)(idx / np);
@@ -1029,6 +1048,7 @@ int phys_static(Engine *E)
 // ============================================================================
 __global__ void k_dynamo_seed(double *bx, double *by, double *bz, int nx, int ny, size_t n, int perfect)
 {
+    PDL_WAIT();
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n) return;
     size_t np = (size_t)nx * ny;
@@ -1056,6 +1076,7 @@ struct MagInitArgs {
 // :123-233: pol, tor from the truncated spectra; Jz, dBz/dy, dBz/dx spectra
 __global__ void k_mag_init_spec(MagInitArgs a)
 {
+    PDL_WAIT();
     const size_t np = (size_t)a.nx * a.ny;
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * a.nz) return;
@@ -1081,6 +1102,7 @@ __global__ void k_mag_init_spec(MagInitArgs a)
 __global__ void k_mag_init_means(const double *ex, const double *ey, const double *ez, double *bxbar,
                                  double *bybar, double *bzbar_out, size_t np, int nz, double xn)
 {
+    PDL_WAIT();
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
         bxbar[k] = ex[(size_t)k * np] * xn;
         bybar[k] = ey[(size_t)k * np] * xn;

@@ -40,7 +40,7 @@ static inline unsigned nblk(size_t n) { return (unsigned)((n + TPB - 1) / TPB); 
 #define KLAUNCHB(E, name, bytes, kern, grid, block, ...)         \
     do {                                                         \
         (E)->prof_begin(name, (double)(bytes));                  \
-        kern<<<(grid), (block), 0, (E)->stream>>>(__VA_ARGS__);  \
+        CUDA_TRY(launch_k(*(E), kern, dim3(grid), dim3(block), 0, __VA_ARGS__)); \
         (E)->prof_end();                                         \
         CUDA_TRY(cudaGetLastError());                            \
     } while (0)
@@ -67,6 +67,7 @@ enum Pc {
 __global__ void k_make_pcf(const double *bg, const double *kappa, const double *dkappa, const double *eta,
                            const double *deta, double zck, int nz, float *pc)
 {
+    PDL_WAIT();
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
         const int from[9] = { BG_RHO0, BG_T0, BG_T0Z5, BG_T0ZU_P, BG_T0ZU_M, BG_T0ZZ0, BG_RHO0Z0, BG_RHO0ZU_P,
                               BG_RHO0ZU_M };
@@ -167,6 +168,7 @@ enum {
 // integer pipe (the same bits as the casts)
 __global__ void k_mirror(MirrorArgs a)
 {
+    PDL_WAIT();
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.np) return;
     const int k = a.k0 + blockIdx.y;
@@ -202,6 +204,7 @@ static int mirror(Engine *E, int mask, int k0, int k1)
 __global__ void k_b64(const float *bx32, const float *by32, const float *bz32, const float *jsq32, double *bx,
                       double *by, double *bz, double *jsq, double bzbar, size_t n)
 {
+    PDL_WAIT();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     // (conversions on the integer pipe, the same bits as the casts)
@@ -358,6 +361,7 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
 // (np/4/256, nz)); the z neighbours come through L1/L2
 __global__ void __launch_bounds__(256, 2) k_split_pass2_v4(SplitHydroArgs a)
 {
+    PDL_WAIT();
     const size_t np4 = a.np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -379,6 +383,7 @@ __global__ void __launch_bounds__(256, 2) k_split_pass2_v4(SplitHydroArgs a)
 // 7-plane register windows of t', u, v, w
 __global__ void __launch_bounds__(256) k_split_pass2(SplitHydroArgs a, int kc)
 {
+    PDL_WAIT();
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t np = a.np;
     if (q >= np) return;
@@ -441,6 +446,7 @@ struct SplitHydro4Args {
 // one thread per point, grid (np/256, nz): k = blockIdx.y
 __global__ void k_split_pass4(SplitHydro4Args a)
 {
+    PDL_WAIT();
     const size_t np = a.np;
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
@@ -485,6 +491,7 @@ __global__ void k_split_pass4(SplitHydro4Args a)
 // loads and stores, four times fewer memory instructions in flight per point
 __global__ void k_split_pass4_v4(SplitHydro4Args a)
 {
+    PDL_WAIT();
     const size_t np4 = a.np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -666,6 +673,7 @@ int split_mag(Engine *E)
 __global__ void __launch_bounds__(256) k_d1z_f(const float *in, float *out, int fl, size_t np, int nz, float h,
                                                int kc)
 {
+    PDL_WAIT();
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
@@ -727,6 +735,7 @@ struct SplitAb3Args {
 // src/main.F90:413-462 with FP64 accumulation; order u,v,w,r,t,pol,tor
 __global__ void k_split_ab3(SplitAb3Args a)
 {
+    PDL_WAIT();
     const size_t np = (size_t)a.nx * a.ny;
     size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= np * a.nz) return;
@@ -772,6 +781,7 @@ __global__ void k_split_ab3(SplitAb3Args a)
 template <bool ICVT>
 __global__ void k_split_ab3_v4(SplitAb3Args a)
 {
+    PDL_WAIT();
     const size_t np = (size_t)a.nx * a.ny;
     const size_t i4 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (i4 >= np * a.nz) return;
@@ -881,6 +891,7 @@ struct DealiasArgs {
 // same bits as the casts; the FP64 pipe keeps only the subtractions)
 __global__ void k_split_dealias_apply(DealiasArgs a)
 {
+    PDL_WAIT();
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.np) return;
     const int k = blockIdx.y;
