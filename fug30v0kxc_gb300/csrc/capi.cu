@@ -287,8 +287,13 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         return VEC_ERR_CUDA;
     }
     {
+        // mag_deriv beside hydro_deriv on a second stream pays off in the FP64
+        // form (FP64-pipe bound kernels overlap); in the split form both are
+        // HBM bound and the overlap costs more in L2 and DRAM contention than
+        // it hides (1.75 against 1.67 ms per 256^2x129 step).  VEC_SERIAL_MAG
+        // = 1 / 0 forces one or the other.
         const char *sm = getenv("VEC_SERIAL_MAG");
-        E.par_mag = !(sm && sm[0] == '1');
+        E.par_mag = sm ? !(sm[0] == '1') : !E.split;
     }
     if (cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;

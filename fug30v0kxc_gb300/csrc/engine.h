@@ -43,7 +43,7 @@ struct Engine {
     // step (it shares no output or work array with hydro_deriv)
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    int par_mag = 1;            // VEC_SERIAL_MAG=1: both on stream
+    int par_mag = 1;            // mag_deriv on stream2 (FP64 form; VEC_SERIAL_MAG=0/1 forces it)
     long long launches = 0;
     int num_sms = 152;
     int *dev_err = nullptr;     // set by kernels whose bounded waits ran out
