@@ -780,18 +780,10 @@ extern "C" int vec_magdealias(vec_ctx *c)
     if (!st && c->E.split) st = split_refresh(&c->E);
     return finish(c, st);
 }
-static int boundary_step(Engine &E)
-{
-    int st = phys_boundary(&E);
-    if (!st && E.split) st = split_refresh_planes(&E, 1 | 2);
-    return st;
-}
-static int mag_boundary_step(Engine &E)
-{
-    int st = phys_mag_boundary(&E);
-    if (!st && E.split) st = split_refresh_planes(&E, 8);
-    return st;
-}
+// (in the split form the boundary kernels also refresh the FP32 mirrors of
+// the planes they change)
+static int boundary_step(Engine &E) { return phys_boundary(&E); }
+static int mag_boundary_step(Engine &E) { return phys_mag_boundary(&E); }
 extern "C" int vec_boundary(vec_ctx *c)
 {
     if (!c) return VEC_ERR_ARG;

@@ -221,6 +221,12 @@ int closure_apply_corr(Engine *E);
 // split form (split.cu)
 int split_setup(Engine *E);
 int split_refresh_coefs(Engine *E);   // after kappa / eta change
+const double *split_bg_t0(const Engine *E);   // T0(z), FP64
+// FP32 mirrors written by the boundary kernels in the split form (null: FP64 form)
+struct BoundaryMirrors {
+    float *u32, *v32, *w32, *t32, *pol32, *tor32;
+    const double *t0;
+};
 int split_hydro(Engine *E);
 int split_mag(Engine *E);
 int split_bandj(Engine *E);

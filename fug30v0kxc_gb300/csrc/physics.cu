@@ -385,8 +385,10 @@ int phys_magdealias(Engine *E)
 // ============================================================================
 // boundary conditions: src/dbydz.F90:3686-4197 and :4205-4791
 // ============================================================================
+// In the split form (m != nullptr) the FP32 mirrors of the two boundary
+// planes are written here too: m = {u32, v32, w32, t32}, t0 = T0(z).
 __global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
-                           double dz, int radbc, int constflux)
+                           double dz, int radbc, int constflux, BoundaryMirrors mb)
 {
     PDL_WAIT();
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,17 +417,33 @@ __global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np
         P(t, nz - 1) = elf * (18.0 * P(t, nz - 2) - 9.0 * P(t, nz - 3) + 2.0 * P(t, nz - 4) + 6.0 * theta * dz);
     else
         P(t, nz - 1) = 1.0 + theta;
+    if (mb.u32) {
+        const int ks[2] = { 0, nz - 1 };
+        for (int e = 0; e < 2; e++) {
+            const int kk = ks[e];
+            mb.u32[(size_t)kk * np + q] = d2f_rn(P(u, kk));
+            mb.v32[(size_t)kk * np + q] = d2f_rn(P(v, kk));
+            mb.w32[(size_t)kk * np + q] = d2f_rn(P(w, kk));
+            mb.t32[(size_t)kk * np + q] = d2f_rn(P(t, kk) - mb.t0[kk]);
+        }
+    }
 #undef P
 }
 
 int phys_boundary(Engine *E)
 {
+    BoundaryMirrors mb = {};
+    if (E->split) {
+        mb.u32 = E->u32; mb.v32 = E->v32; mb.w32 = E->w32; mb.t32 = E->t32; mb.t0 = split_bg_t0(E);
+        mb.pol32 = E->pol32; mb.tor32 = E->tor32;
+    }
     KLAUNCH(E, "boundary_f64", k_boundary, nblk(E->np), TPB, E->u, E->v, E->w, E->t, E->np, E->nz, E->p.theta,
-            E->k.dz, E->p.radbc, E->p.constflux);
+            E->k.dz, E->p.radbc, E->p.constflux, mb);
     return VEC_OK;
 }
 
-__global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect)
+__global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect,
+                               BoundaryMirrors mb)
 {
     PDL_WAIT();
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -453,13 +471,21 @@ __global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *by
         P(tor, nz - 1) = 0.0;
         P(pol, nz - 1) = elf * (18.0 * P(pol, nz - 2) - 9.0 * P(pol, nz - 3) + 2.0 * P(pol, nz - 4));
     }
+    if (mb.pol32) {
+        mb.pol32[q] = d2f_rn(P(pol, 0));
+        mb.tor32[q] = d2f_rn(P(tor, 0));
+        mb.pol32[(size_t)(nz - 1) * np + q] = d2f_rn(P(pol, nz - 1));
+        mb.tor32[(size_t)(nz - 1) * np + q] = d2f_rn(P(tor, nz - 1));
+    }
 #undef P
 }
 
 int phys_mag_boundary(Engine *E)
 {
+    BoundaryMirrors mb = {};
+    if (E->split) { mb.pol32 = E->pol32; mb.tor32 = E->tor32; }
     KLAUNCH(E, "mag_boundary_f64", k_mag_boundary, nblk(E->np), TPB, E->pol, E->tor, E->bxbar, E->bybar,
-            E->np, E->nz, E->p.perfect);
+            E->np, E->nz, E->p.perfect, mb);
     return VEC_OK;
 }
 

@@ -81,6 +81,8 @@ __global__ void k_make_pcf(const double *bg, const double *kappa, const double *
     }
 }
 
+const double *split_bg_t0(const Engine *E) { return E->hres + (size_t)BG_T0 * E->nz; }
+
 // (re)builds the FP32 plane coefficients from the FP64 profiles
 int split_refresh_coefs(Engine *E)
 {
