@@ -304,13 +304,31 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             return z;
         };
 
+        // The two sequences a warp holds (x lines, 16 threads each) have rows
+        // that start on the same bank; the odd one reads its columns in pairs
+        // swapped (index ^ 1), so that the two half-warps hit different banks,
+        // and swaps the registers back.  The values are the same.
+        constexpr bool XSW = WS && DIR == 0 && NP == 16 && sizeof(R) == 4 && N1 % 2 == 0 && N2 % 2 == 0;
+        const int sw = XSW ? (sidx & 1) : 0;
+        auto unswap = [&](C *v, int n) {
+            if constexpr (XSW) {
+#pragma unroll
+                for (int i = 0; i < n; i += 2) {
+                    const C t0 = v[i], t1 = v[i + 1];
+                    v[i] = sw ? t1 : t0;
+                    v[i + 1] = sw ? t0 : t1;
+                }
+            }
+        };
+
         C X[N2];   // thread lane = k1 holds X[k1 + N1 k2], k2 = 0..N2-1
         if (op1 != OP_INV) {
             // forward, first level: thread m2 = lane, N1-point DFT over m1
             if (lane < N2) {
                 C a[N1];
 #pragma unroll
-                for (int m1 = 0; m1 < N1; m1++) a[m1] = tile_z(N2 * m1 + lane);
+                for (int m1 = 0; m1 < N1; m1++) a[m1] = tile_z(N2 * (m1 ^ sw) + lane);
+                unswap(a, N1);
                 RDft<N1, false>::run(a);
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
@@ -330,7 +348,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             // halfcomplex input lines a (re) and b (im): Z_k = A_k + i B_k
 #pragma unroll
             for (int k2 = 0; k2 < N2; k2++) {
-                const int k = lane + N1 * k2;
+                const int k = lane + N1 * (k2 ^ sw);
                 const int kk = k <= N / 2 ? k : N - k;
                 const bool edge = kk == 0 || 2 * kk == N;
                 C pa = tile_z(kk);                     // (ha[kk], hb[kk])
@@ -339,6 +357,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 X[k2].x = ar - bi;
                 X[k2].y = ai + br;
             }
+            unswap(X, N2);
         }
         if constexpr (WS) {
             // this warp is done with the tile buffer
