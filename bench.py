@@ -429,6 +429,9 @@ def measure(args, precision, ws, hbm, pk, with_e2e):
                             "achieved_gbs": round(value / ws * alg_step / 1e9, 1),
                             "frac": round(value / ws * alg_step / 1e9 / hbm, 4)}
     total_ms = sum(r[2] for r in prof) or 1.0
+    # the kernels' own time per step (profiled pass) beside the replayed step
+    # time: the difference is launch gaps and ramp-up/drain between kernels
+    res["kernel_ms_per_step"] = round(total_ms / args.steps, 4)
     res["kernels"] = sorted(({"kernel": n, "launches": l, "ms": round(m, 3), "share": round(m / total_ms, 4),
                               "gbs": round(b / (m * 1e-3) / 1e9, 1) if m > 0 else None}
                              for n, l, m, b in prof), key=lambda d: -d["ms"])[:12]
@@ -550,6 +553,7 @@ def main():
         "clocks": head["clocks"],
         "e2e": head.get("e2e"),
         "gpu_launches": head["launches"],
+        "kernel_ms_per_step": head["kernel_ms_per_step"],
         "kernels": head["kernels"],
     }
     if args.precision == "both":

@@ -857,8 +857,11 @@ static int enqueue_step(Engine &E, bool diag_now)
     const bool dealias_now = E.p.dalias && (E.nit % 10 == 0);
     if (dealias_now && (st = E.split ? split_dealias(&E) : phys_dealias_state(&E))) return st;
     if (mag && (st = E.split ? split_bandj(&E) : phys_bandj64(&E))) return st;
-    if ((st = boundary_step(E))) return st;
-    if (mag && (st = mag_boundary_step(E))) return st;
+    if (mag) {
+        if ((st = phys_boundaries(&E))) return st;   // boundary and mag_boundary (disjoint fields)
+    } else if ((st = boundary_step(E))) {
+        return st;
+    }
     if (diag_now && (st = diag_step(E, nullptr))) return st;
     if (E.nit % 10 == 0 && (st = E.split ? split_calcdt(&E) : phys_calcdt(&E))) return st;
     return VEC_OK;

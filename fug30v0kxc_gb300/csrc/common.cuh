@@ -89,6 +89,41 @@ struct DevScalars {
     double res[64];                            // diagnostics results
 };
 
+// AB3 coefficients of src/main.F90:381-403 from the step sizes (read-only)
+__device__ __forceinline__ void ab3_coefs(const DevScalars *ds, double *c)
+{
+    const double dt = ds->dt;
+    if (ds->first) {
+        c[0] = dt; c[1] = 0.0; c[2] = 0.0;
+    } else if (ds->second) {
+        c[0] = dt * (1.0 + 0.5 * (dt / ds->dt1));
+        c[1] = -0.5 * dt * (dt / ds->dt1);
+        c[2] = 0.0;
+    } else {
+        const double dt1 = ds->dt1, dt2 = ds->dt2;
+        c[0] = dt + (((dt * dt) / (dt1 * dt2)) * ((dt / 3.0) + 0.5 * (dt1 + dt2)));
+        c[1] = ((dt * dt) / (dt1 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt2);
+        c[2] = -((dt * dt) / (dt2 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt1);
+    }
+}
+// the scalar updates of one step: ttime (:345), the Euler / AB2 start flags
+// and dt1, dt2 (:488-489); c are this step's coefficients
+__device__ __forceinline__ void ab3_advance(DevScalars *ds, const double *c)
+{
+    const double dt = ds->dt;
+    ds->ttime = ds->ttime + dt;
+    if (ds->first) {
+        ds->first = 0; ds->second = 1;
+        ds->dt1 = 0.0; ds->dt2 = 0.0;
+    } else if (ds->second) {
+        ds->first = 0; ds->second = 0;
+        ds->dt2 = 0.0;
+    }
+    ds->c0 = c[0]; ds->c1 = c[1]; ds->c2 = c[2];
+    ds->dt2 = dt + ds->dt1;
+    ds->dt1 = dt;
+}
+
 // RHS histories in logical slot order (0 oldest .. 2 newest), kept in device
 // memory so that kernels read their slot pointers at run time and a one-
 // thread kernel performs the shift of src/main.F90:448-461 by rotating it;

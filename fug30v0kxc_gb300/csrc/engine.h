@@ -201,6 +201,7 @@ int phys_bandj64(Engine *E);
 int phys_magdealias(Engine *E);
 int phys_boundary(Engine *E);
 int phys_mag_boundary(Engine *E);
+int phys_boundaries(Engine *E);   // boundary + mag_boundary in one launch
 int phys_ab3(Engine *E, int magdealias);
 int phys_ab3_coef(Engine *E);
 int phys_rotate_hist(Engine *E);

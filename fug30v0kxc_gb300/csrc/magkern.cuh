@@ -370,10 +370,8 @@ static __global__ void k_zero_mag_rhs(const HistTable *ht, size_t n, int nz)
 
 // the history shift of src/main.F90:448-461 and :473-476 as a rotation of
 // the logical slots: 0 <- 1 <- 2 <- old 0 (reused for the next RHS)
-static __global__ void k_rotate_hist(HistTable *ht)
+__device__ __forceinline__ void rotate_hist_table(HistTable *ht)
 {
-    PDL_WAIT();
-    if (threadIdx.x != 0) return;
     for (int f = 0; f < 7; f++) {
         void *o = ht->p[f][0];
         ht->p[f][0] = ht->p[f][1];
@@ -383,4 +381,9 @@ static __global__ void k_rotate_hist(HistTable *ht)
     double *x = ht->bx[0], *y = ht->by[0];
     ht->bx[0] = ht->bx[1]; ht->bx[1] = ht->bx[2]; ht->bx[2] = x;
     ht->by[0] = ht->by[1]; ht->by[1] = ht->by[2]; ht->by[2] = y;
+}
+static __global__ void k_rotate_hist(HistTable *ht)
+{
+    PDL_WAIT();
+    if (threadIdx.x == 0) rotate_hist_table(ht);
 }

@@ -387,12 +387,10 @@ int phys_magdealias(Engine *E)
 // ============================================================================
 // In the split form (m != nullptr) the FP32 mirrors of the two boundary
 // planes are written here too: m = {u32, v32, w32, t32}, t0 = T0(z).
-__global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
-                           double dz, int radbc, int constflux, BoundaryMirrors mb)
+__device__ __forceinline__ void boundary_column(double *u, double *v, double *w, double *t, size_t np, int nz,
+                                                double theta, double dz, int radbc, int constflux,
+                                                const BoundaryMirrors &mb, size_t q)
 {
-    PDL_WAIT();
-    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= np) return;
     const double elf = 1.0 / 11.0;
 #define P(f, kk) f[(size_t)(kk) * np + q]
     P(w, 0) = 0.0;
@@ -430,6 +428,14 @@ __global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np
 #undef P
 }
 
+__global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
+                           double dz, int radbc, int constflux, BoundaryMirrors mb)
+{
+    PDL_WAIT();
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < np) boundary_column(u, v, w, t, np, nz, theta, dz, radbc, constflux, mb, q);
+}
+
 int phys_boundary(Engine *E)
 {
     BoundaryMirrors mb = {};
@@ -442,11 +448,9 @@ int phys_boundary(Engine *E)
     return VEC_OK;
 }
 
-__global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect,
-                               BoundaryMirrors mb)
+__device__ __forceinline__ void mag_boundary_column(double *pol, double *tor, double *bxb, double *byb, size_t np,
+                                                    int nz, int perfect, const BoundaryMirrors &mb, size_t q)
 {
-    PDL_WAIT();
-    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const double elf = 1.0 / 11.0;
     if (q == 0) {
         if (perfect) {
@@ -480,6 +484,36 @@ __global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *by
 #undef P
 }
 
+__global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *byb, size_t np, int nz, int perfect,
+                               BoundaryMirrors mb)
+{
+    PDL_WAIT();
+    mag_boundary_column(pol, tor, bxb, byb, np, nz, perfect, mb, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// boundary and mag_boundary of one step in one launch (disjoint fields)
+__global__ void k_boundaries(double *u, double *v, double *w, double *t, double *pol, double *tor, double *bxb,
+                             double *byb, size_t np, int nz, double theta, double dz, int radbc, int constflux,
+                             int perfect, BoundaryMirrors mb)
+{
+    PDL_WAIT();
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < np) boundary_column(u, v, w, t, np, nz, theta, dz, radbc, constflux, mb, q);
+    mag_boundary_column(pol, tor, bxb, byb, np, nz, perfect, mb, q);
+}
+
+int phys_boundaries(Engine *E)
+{
+    BoundaryMirrors mb = {};
+    if (E->split) {
+        mb.u32 = E->u32; mb.v32 = E->v32; mb.w32 = E->w32; mb.t32 = E->t32; mb.t0 = split_bg_t0(E);
+        mb.pol32 = E->pol32; mb.tor32 = E->tor32;
+    }
+    KLAUNCH(E, "boundaries", k_boundaries, nblk(E->np), TPB, E->u, E->v, E->w, E->t, E->pol, E->tor, E->bxbar,
+            E->bybar, E->np, E->nz, E->p.theta, E->k.dz, E->p.radbc, E->p.constflux, E->p.perfect, mb);
+    return VEC_OK;
+}
+
 int phys_mag_boundary(Engine *E)
 {
     BoundaryMirrors mb = {};
@@ -501,28 +535,8 @@ __global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const H
     const double *byd0 = ht->by[0], *byd1 = ht->by[1], *byd2 = ht->by[2];
     __shared__ double cc[3];
     if (threadIdx.x == 0) {
-        double dt = ds->dt, c0, c1, c2;
-        ds->ttime = ds->ttime + dt;
-        if (ds->first) {
-            ds->first = 0; ds->second = 1;
-            ds->dt1 = 0.0; ds->dt2 = 0.0;
-            c0 = dt; c1 = 0.0; c2 = 0.0;
-        } else if (ds->second) {
-            ds->first = 0; ds->second = 0;
-            ds->dt2 = 0.0;
-            c0 = dt * (1.0 + 0.5 * (dt / ds->dt1));
-            c1 = -0.5 * dt * (dt / ds->dt1);
-            c2 = 0.0;
-        } else {
-            double dt1 = ds->dt1, dt2 = ds->dt2;
-            c0 = dt + (((dt * dt) / (dt1 * dt2)) * ((dt / 3.0) + 0.5 * (dt1 + dt2)));
-            c1 = ((dt * dt) / (dt1 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt2);
-            c2 = -((dt * dt) / (dt2 * (dt1 - dt2))) * ((dt / 3.0) + 0.5 * dt1);
-        }
-        ds->c0 = c0; ds->c1 = c1; ds->c2 = c2;
-        ds->dt2 = dt + ds->dt1;
-        ds->dt1 = dt;
-        cc[0] = c0; cc[1] = c1; cc[2] = c2;
+        ab3_coefs(ds, cc);
+        ab3_advance(ds, cc);
     }
     __syncthreads();
     if (!do_means) return;
