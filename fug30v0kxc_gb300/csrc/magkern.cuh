@@ -239,7 +239,8 @@ static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, i
     st4(w1 + pb, q4, sdx4(ex + pb, i0, j, nx, h.kx1) + sdy4(ey + pb, i0, j, nx, ny, h.ky1));
 }
 
-static __global__ void k_mag_final4(MagArgs<float> a)
+// (four CTAs per SM: 3.4 TB/s against 2.1 at the compiler's own 90 registers)
+static __global__ void __launch_bounds__(256, 4) k_mag_final4(MagArgs<float> a)
 {
     PDL_WAIT();
     const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
