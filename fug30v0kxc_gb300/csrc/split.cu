@@ -689,6 +689,17 @@ __global__ void __launch_bounds__(256) k_d1z_f(const float *in, float *out, int 
     }
 }
 
+// four consecutive x points per thread, grid (np/4/256, nz)
+__global__ void __launch_bounds__(256) k_d1z4(const float *in, float *out, int fl, size_t np, int nz, float h)
+{
+    PDL_WAIT();
+    const size_t np4 = np / 4;
+    const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q4 >= np4) return;
+    const int k = blockIdx.y;
+    reinterpret_cast<V4 *>(out)[(size_t)k * np4 + q4] = zd1(reinterpret_cast<const V4 *>(in) + q4, np4, k, nz, fl, V4(h));
+}
+
 int split_bandj(Engine *E)
 {
     float *W[W_COUNT];
@@ -696,8 +707,11 @@ int split_bandj(Engine *E)
     int st;
     const bool v4 = E->nx % 4 == 0 && E->vec4;
     const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
-    KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, W[W_M1], 5, E->np,
-             E->nz, (float)E->k.ho12, ZCHUNK);
+    if (v4)
+        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z4, g4, TPB, E->pol32, W[W_M1], 5, E->np, E->nz, (float)E->k.ho12);
+    else
+        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, W[W_M1], 5, E->np,
+                 E->nz, (float)E->k.ho12, ZCHUNK);
     BandjArgs<float> a;
     a.dzs = W[W_M1]; a.pol = E->pol32; a.tor = E->tor32; a.h = E->hf;
     a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
