@@ -214,8 +214,15 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     R *tile0 = reinterpret_cast<R *>(smem);
     R *tile1 = tile0 + TILE;
     C *ex = reinterpret_cast<C *>(tile1 + TILE);
-    C *tws = ex + (size_t)S * LDS;
-    R *sm1 = reinterpret_cast<R *>(tws + N);          // spectral multipliers
+    // FP32: twiddles W_N^(m2 k1) as two N1 x N2 tables, one row per value of
+    // the loop index, so that the 16 threads of a sequence read consecutive
+    // entries (indexed by (m2 k1) mod N, a thread stride of k1 made up to
+    // eight-way bank conflicts).  FP64: one table of N (the second would
+    // cost the second CTA per SM).
+    constexpr bool TW2 = sizeof(R) == 4;
+    C *twf = ex + (size_t)S * LDS;                    // twf[k1 N2 + m2] (FP64: tw[e])
+    C *twi = twf + N;                                 // twi[m2 N1 + k1]
+    R *sm1 = reinterpret_cast<R *>(twi + (TW2 ? N : 0));   // spectral multipliers
     R *sm2 = sm1 + N;
     R *smda = sm2 + N;
     __shared__ __align__(8) uint64_t bar[4];          // full[2], empty[2]
@@ -230,7 +237,14 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     };
 
     for (int e = tid; e < N; e += NT) {
-        tws[e] = tb.tw[e];
+        if constexpr (TW2) {
+            const int k1 = e / N2, m2 = e - k1 * N2;
+            twf[e] = tb.tw[modn<N>(m2 * k1)];
+            const int m2i = e / N1, k1i = e - m2i * N1;
+            twi[e] = tb.tw[modn<N>(m2i * k1i)];
+        } else {
+            twf[e] = tb.tw[e];
+        }
         sm1[e] = tb.m1[e];
         sm2[e] = tb.m2[e];
         smda[e] = tb.mda[e];
@@ -332,7 +346,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 RDft<N1, false>::run(a);
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
-                    C w = tws[modn<N>(lane * k1)];
+                    C w = TW2 ? twf[k1 * N2 + lane] : twf[modn<N>(lane * k1)];
                     ex_s[k1 * LX + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
                 }
             }
@@ -418,7 +432,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 RDft<N2, true>::run(Y);
 #pragma unroll
                 for (int m2 = 0; m2 < N2; m2++) {
-                    C w = tws[modn<N>(m2 * lane)];
+                    C w = TW2 ? twi[m2 * N1 + lane] : twf[modn<N>(m2 * lane)];
                     w.y = -w.y;
                     ex_s[m2 * LX + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
                 }
@@ -539,7 +553,8 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     constexpr int LX = NP + 1;
     constexpr int LDS = ((NP * LX) / 16) * 16 + 17;
     static bool attr_set = false;
-    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + N) * sizeof(C) + 3 * (size_t)N * sizeof(R);
+    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C)
+                        + 3 * (size_t)N * sizeof(R);
     if (!attr_set) {
         CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S, WSYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
