@@ -386,9 +386,9 @@ def dominant_roofline(prof, hbm_peak, peak_kind):
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the split step at
 # 256x256x129, from the ncu capture summarised in
 # profiles/dram_traffic_split_256x256x129.md (other workloads: null)
-TRAFFIC_256x256x129 = {"line_x_f32": 266.8e6, "line_y_f32": 259.1e6, "hydro_pass2_f32": 1350.5e6,
-                       "ab3_update_split": 1835.5e6, "hydro_pass4_f32": 691.3e6, "mag_final_f32": 250.0e6,
-                       "bandj_spec_f32": 246.9e6, "emf_f32": 254.8e6, "jsq_f32": 187.5e6}
+TRAFFIC_256x256x129 = {"line_x_f32": 267.1e6, "line_y_f32": 259.1e6, "hydro_pass2_f32": 1349.5e6,
+                       "ab3_update_split": 1835.3e6, "hydro_pass4_f32": 695.7e6, "mag_final_f32": 249.3e6,
+                       "bandj_spec_f32": 246.9e6, "emf_f32": 254.9e6, "jsq_f32": 187.4e6, "d1bydz_f32": 34.2e6}
 TRAFFIC = {}
 
 
