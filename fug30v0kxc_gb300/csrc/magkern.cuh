@@ -20,34 +20,50 @@ static __global__ void k_emf(const R *u, const R *v, const R *w, const R *bx, co
 
 // mean-field RHS (:328-352) on one CTA; ex, ey are the 2-D spectra of the EMF
 template <typename R>
-static __global__ void k_mean_rhs(const R *ex, const R *ey, const double *bxbar, const double *bybar,
-                                  const double *eta, const double *deta, const HistTable *ht,
-                                  double *scratch, size_t np, int nz, double xn, double zck, double ho12,
-                                  double sc1, int var_eta)
+struct MeanArgs {
+    const R *ex, *ey;
+    const double *bxbar, *bybar, *eta, *deta;
+    const HistTable *ht;
+    double *scratch;
+    size_t np;
+    int nz;
+    double xn, zck, ho12, sc1;
+    int var_eta;
+};
+
+template <typename R>
+__device__ __forceinline__ void mean_rhs_block(const MeanArgs<R> &a)
 {
-    PDL_WAIT();
-    double *bxd = ht->bx[2], *byd = ht->by[2];
-    double *e1 = scratch, *e2 = scratch + nz;
+    const int nz = a.nz;
+    double *bxd = a.ht->bx[2], *byd = a.ht->by[2];
+    double *e1 = a.scratch, *e2 = a.scratch + nz;
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        e1[k] = xn * (double)ex[(size_t)k * np];
-        e2[k] = xn * (double)ey[(size_t)k * np];
+        e1[k] = a.xn * (double)a.ex[(size_t)k * a.np];
+        e2[k] = a.xn * (double)a.ey[(size_t)k * a.np];
     }
     __syncthreads();
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        double dey = zd1(e2, 1, k, nz, 5, ho12);   // :337
-        double dex = zd1(e1, 1, k, nz, 5, ho12);   // :338
-        double d2x = zd2(bxbar, 1, k, nz, 3, sc1); // :343
-        double d2y = zd2(bybar, 1, k, nz, 3, sc1); // :344
-        if (!var_eta) {
-            bxd[k] = zck * d2x - dey;              // :350
-            byd[k] = zck * d2y + dex;              // :351
+        double dey = zd1(e2, 1, k, nz, 5, a.ho12);   // :337
+        double dex = zd1(e1, 1, k, nz, 5, a.ho12);   // :338
+        double d2x = zd2(a.bxbar, 1, k, nz, 3, a.sc1); // :343
+        double d2y = zd2(a.bybar, 1, k, nz, 3, a.sc1); // :344
+        if (!a.var_eta) {
+            bxd[k] = a.zck * d2x - dey;              // :350
+            byd[k] = a.zck * d2y + dex;              // :351
         } else {
             // extension: eta(z) d2b/dz2 + eta'(z) db/dz
-            double gx = zd1(bxbar, 1, k, nz, 5, ho12), gy = zd1(bybar, 1, k, nz, 5, ho12);
-            bxd[k] = eta[k] * d2x - dey + deta[k] * gx;
-            byd[k] = eta[k] * d2y + dex + deta[k] * gy;
+            double gx = zd1(a.bxbar, 1, k, nz, 5, a.ho12), gy = zd1(a.bybar, 1, k, nz, 5, a.ho12);
+            bxd[k] = a.eta[k] * d2x - dey + a.deta[k] * gx;
+            byd[k] = a.eta[k] * d2y + dex + a.deta[k] * gy;
         }
     }
+}
+
+template <typename R>
+static __global__ void k_mean_rhs(MeanArgs<R> a)
+{
+    PDL_WAIT();
+    mean_rhs_block(a);
 }
 
 // The spectral kernels below run one CTA row per plane (grid (np/256, nz)):
@@ -227,9 +243,16 @@ static __global__ void k_emf4(const float *u, const float *v, const float *w, co
     st4(e3, i, U * BY - Vv * BX);
 }
 
-static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h)
+// (grid (np/4/256, nz + 1): the extra row's first CTA computes the mean-field
+// RHS, which reads the same spectra -- one launch instead of two)
+static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h,
+                                  MeanArgs<float> ma)
 {
     PDL_WAIT();
+    if (blockIdx.y == gridDim.y - 1) {
+        if (blockIdx.x == 0) mean_rhs_block(ma);
+        return;
+    }
     const unsigned np4 = (unsigned)nx * ny / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;

@@ -317,8 +317,11 @@ int phys_mag64(Engine *E)
                               ljob<double>(W[W_EZ], W[W_EZ], OP_FWD) };
     if ((st = launch_lines<double>(E, 1, fy, 3))) return st;
     const Consts &c = E->k;
-    KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
-            E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
+    MeanArgs<double> ma;
+    ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
+    ma.ht = E->ht; ma.scratch = E->w1d; ma.np = E->np; ma.nz = E->nz;
+    ma.xn = c.xn; ma.zck = c.zck; ma.ho12 = c.ho12; ma.sc1 = c.sc1; ma.var_eta = c.var_eta;
+    KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, ma);
     KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
              E->nx, E->ny, E->hd);
     MagArgs<double> a;

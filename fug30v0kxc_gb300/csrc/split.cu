@@ -654,13 +654,18 @@ int split_mag(Engine *E)
                              ljob<float>(W[W_EZ], W[W_EZ], OP_FWD) };
     if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
     const Consts &c = E->k;
-    KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, W[W_EX], W[W_EY], E->bxbar, E->bybar, E->eta, E->deta,
-             E->ht, E->w1d, E->np, E->nz, c.xn, c.zck, c.ho12, c.sc1, c.var_eta);
-    if (v4)
-        KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div4, g4, TPB, W[W_EX], W[W_EY], W[W_M4], E->nx, E->ny, E->hf);
-    else
+    MeanArgs<float> ma;
+    ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
+    ma.ht = E->ht; ma.scratch = E->w1d; ma.np = E->np; ma.nz = E->nz;
+    ma.xn = c.xn; ma.zck = c.zck; ma.ho12 = c.ho12; ma.sc1 = c.sc1; ma.var_eta = c.var_eta;
+    if (v4) {
+        KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div4, dim3(g4.x, g4.y + 1), TPB, W[W_EX], W[W_EY], W[W_M4],
+                 E->nx, E->ny, E->hf, ma);
+    } else {
+        KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, ma);
         KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
                  E->nx, E->ny, E->hf);
+    }
     MagArgs<float> a;
     a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol32; a.tor = E->tor32;
     a.eta = E->pcf + PC_ETA * E->nz; a.deta = E->pcf + PC_DETA * E->nz; a.h = E->hf;
