@@ -285,6 +285,8 @@ template <typename T> struct ZDer { T tzu, tzp, tzz, wzu, wz, uzu, vzu, uzz, vzz
 template <typename T> __device__ __forceinline__ T ldv(const float *p, size_t i);
 template <> __device__ __forceinline__ float ldv<float>(const float *p, size_t i) { return p[i]; }
 template <> __device__ __forceinline__ V4 ldv<V4>(const float *p, size_t i) { return reinterpret_cast<const V4 *>(p)[i]; }
+template <> __device__ __forceinline__ V2 ldv<V2>(const float *p, size_t i) { return reinterpret_cast<const V2 *>(p)[i]; }
+__device__ __forceinline__ void stv(float *p, size_t i, V2 v) { reinterpret_cast<V2 *>(p)[i] = v; }
 __device__ __forceinline__ void stv(float *p, size_t i, float v) { p[i] = v; }
 __device__ __forceinline__ void stv(float *p, size_t i, V4 v) { reinterpret_cast<V4 *>(p)[i] = v; }
 __device__ __forceinline__ float upsel(float w, float p, float m) { return w >= 0.0f ? p : m; }
@@ -359,26 +361,28 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     stv(a.hh, idx, T(a.f) * bz * by);
 }
 
-// four consecutive x points per thread, one plane per CTA row (grid
-// (np/4/256, nz)); the z neighbours come through L1/L2
-__global__ void __launch_bounds__(256, 2) k_split_pass2_v4(SplitHydroArgs a)
+// two consecutive x points per thread, one plane per CTA row (grid
+// (np/2/256, nz)); the z neighbours come through L1/L2.  (Three CTAs per
+// SM at 80 registers: 4.9 TB/s, against 4.7 for four points per thread,
+// whose ~175 live registers spill at two CTAs per SM.)
+__global__ void __launch_bounds__(256, 3) k_split_pass2_v2(SplitHydroArgs a)
 {
     PDL_WAIT();
-    const size_t np4 = a.np / 4;
-    const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q4 >= np4) return;
+    const size_t np2 = a.np / 2;
+    const size_t q2 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q2 >= np2) return;
     const int nz = a.nz;
     const int k = blockIdx.y;
-    const V4 h(a.ho12), s(a.sc1);
-    const V4 *t4 = reinterpret_cast<const V4 *>(a.t) + q4, *u4 = reinterpret_cast<const V4 *>(a.u) + q4;
-    const V4 *v4 = reinterpret_cast<const V4 *>(a.v) + q4, *w4 = reinterpret_cast<const V4 *>(a.w) + q4;
-    const V4 w0 = w4[(size_t)k * np4];
-    ZDer<V4> z;
-    z.tzu = zd1up(t4, np4, k, nz, 5, h, w0); z.tzp = zd1(t4, np4, k, nz, 5, h); z.tzz = zd2(t4, np4, k, nz, 0, s);
-    z.wzu = zd1up(w4, np4, k, nz, 1, h, w0); z.wz = zd1(w4, np4, k, nz, 1, h);
-    z.uzu = zd1up(u4, np4, k, nz, 2, h, w0); z.vzu = zd1up(v4, np4, k, nz, 2, h, w0);
-    z.uzz = zd2(u4, np4, k, nz, 3, s); z.vzz = zd2(v4, np4, k, nz, 3, s);
-    split_pass2_point<V4>(a, (size_t)k * np4 + q4, k, z);
+    const V2 h(a.ho12), s(a.sc1);
+    const V2 *t2 = reinterpret_cast<const V2 *>(a.t) + q2, *u2 = reinterpret_cast<const V2 *>(a.u) + q2;
+    const V2 *v2 = reinterpret_cast<const V2 *>(a.v) + q2, *w2 = reinterpret_cast<const V2 *>(a.w) + q2;
+    const V2 w0 = w2[(size_t)k * np2];
+    ZDer<V2> z;
+    z.tzu = zd1up(t2, np2, k, nz, 5, h, w0); z.tzp = zd1(t2, np2, k, nz, 5, h); z.tzz = zd2(t2, np2, k, nz, 0, s);
+    z.wzu = zd1up(w2, np2, k, nz, 1, h, w0); z.wz = zd1(w2, np2, k, nz, 1, h);
+    z.uzu = zd1up(u2, np2, k, nz, 2, h, w0); z.vzu = zd1up(v2, np2, k, nz, 2, h, w0);
+    z.uzz = zd2(u2, np2, k, nz, 3, s); z.vzz = zd2(v2, np2, k, nz, 3, s);
+    split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z);
 }
 
 // z-marching: one thread per (i,j) column and chunk of kc planes, with
@@ -589,10 +593,8 @@ int split_hydro(Engine *E)
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
     if (E->nx % 4 == 0 && E->vec4) {
-        // (two CTAs per SM: 128 registers with a few spilled values beat
-        // 175 registers at one CTA per SM, 4.8 against 3.8 TB/s)
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v4,
-                 dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), TPB, a);
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v2,
+                 dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB, a);
     } else {
         const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
         dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));

@@ -151,6 +151,38 @@ __host__ __device__ __forceinline__ V4 zd1up(const V4 *f, size_t np, int k, int 
 #undef F
 }
 
+// Two consecutive x points (8-byte loads), the same operators as V4
+struct __align__(8) V2 {
+    float x, y;
+    __host__ __device__ __forceinline__ V2() {}
+    __host__ __device__ __forceinline__ V2(float s) : x(s), y(s) {}
+    __host__ __device__ __forceinline__ V2(float a, float b) : x(a), y(b) {}
+};
+__host__ __device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ V2 operator-(V2 a, V2 b) { return V2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ V2 operator*(V2 a, V2 b) { return V2(a.x * b.x, a.y * b.y); }
+__host__ __device__ __forceinline__ V2 operator/(V2 a, V2 b) { return V2(a.x / b.x, a.y / b.y); }
+__host__ __device__ __forceinline__ V2 operator-(V2 a) { return V2(-a.x, -a.y); }
+__host__ __device__ __forceinline__ V2 upsel(V2 w, V2 p, V2 m)
+{
+    return V2(w.x >= 0.0f ? p.x : m.x, w.y >= 0.0f ? p.y : m.y);
+}
+__host__ __device__ __forceinline__ V2 zd1up(const V2 *f, size_t np, int k, int nz, int fl, V2 h, V2 wv)
+{
+    typedef V2 R;
+#define F(kk) zld(f, np, kk)
+    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k == 2)
+        return upsel(wv, h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3)),
+                     h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1)));
+    if (k == nz - 3)
+        return upsel(wv, h * (-F(nz - 6) + (R)6 * F(nz - 5) - (R)18 * F(nz - 4) + (R)10 * F(nz - 3) + (R)3 * F(nz - 2)),
+                     h * ((R)-2 * F(nz - 1) + (R)12 * F(nz - 2) - (R)6 * F(nz - 3) - (R)4 * F(nz - 4)));
+    return upsel(wv, h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1)),
+                 h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1)));
+#undef F
+}
+
 // Interior rows (3 <= k <= nz-4) from a register window v[d] = f(k-3+d):
 // the same formulas and operation order as zd1 / zd1up / zd2.
 template <typename R>
