@@ -23,7 +23,6 @@
 // a constant; the spectral derivative drops the mean and every z stencil
 // annihilates constants).
 #include <math.h>
-#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
