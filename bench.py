@@ -390,6 +390,11 @@ TRAFFIC_256x256x129 = {"line_x_f32": 267.1e6, "line_y_f32": 259.1e6, "hydro_pass
                        "ab3_update_split": 1835.3e6, "hydro_pass4_f32": 695.7e6, "mag_final_f32": 249.3e6,
                        "bandj_spec_f32": 246.9e6, "emf_f32": 254.9e6, "jsq_f32": 187.4e6, "d1bydz_f32": 34.2e6}
 TRAFFIC = {}
+# operation count of one grid-point-step at n = 256 (formula: ~72 real
+# transform passes x 2.5 log2 n, ~200 for the z stencils, ~300 pointwise,
+# ~40 for AB3) and GB300's nominal FP64 rate
+FP64_FLOP_PER_GPS_256 = 1.9e3
+FP64_NOMINAL_TFLOPS = 1.25
 
 
 def run_reference(args):
@@ -567,6 +572,17 @@ def main():
         line["fp64"] = {"value": f64["value"], "ms_per_step": f64["ms_per_step"],
                         "roofline": f64["roofline"], "step_roofline": f64["step_roofline"],
                         "clocks": f64["clocks"], "gpu_launches": f64["launches"]}
+        # The FP64 form is bound by GB300's FP64 pipe, not by HBM: its rate in
+        # FLOP/s, with the step's operation count from the formula for n = 256
+        # (transform passes x 2.5 log2 n + stencils + pointwise + AB3, about
+        # 1.9 kflop per grid-point-step) against the nominal FP64 rate (no
+        # FP64 peak is measured on this machine)
+        if NX == 256 and NY == 256:
+            achieved = FP64_FLOP_PER_GPS_256 * f64["value"] / ws / 1e12
+            line["fp64"]["fp64_roofline"] = {"bound": "fp64", "achieved": round(achieved, 3),
+                                             "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                                             "frac": round(achieved / FP64_NOMINAL_TFLOPS, 3), "peak_kind": "nominal",
+                                             "flop_per_gps": FP64_FLOP_PER_GPS_256}
         line["split_over_fp64"] = head["value"] / f64["value"]
     if not args.no_ensemble and not args.grid:
         try:
