@@ -830,9 +830,15 @@ static int enqueue_step(Engine &E, bool diag_now)
 {
     int st;
     const int mag = mag_on(E);
+    const bool par = mag && E.par_mag && !E.prof_on;
+    // split form, mag branch after hydro and no closure correction before
+    // the update: the AB3 coefficient step rides on the mean-field CTA of
+    // mag_div and the history rotation on the first bandj kernel (two
+    // launches fewer per step)
+    const bool fold = E.split && mag && !par && !E.corr_on;
     // (with per-kernel profiling on, the branches run one after the other so
     // that no two timed kernels overlap)
-    if (mag && E.par_mag && !E.prof_on) {
+    if (par) {
         // mag_deriv on stream2 beside hydro_deriv on stream (disjoint outputs
         // and work arrays; both only read the state)
         CUDA_TRY(cudaEventRecord(E.ev_fork, E.stream));
@@ -847,16 +853,16 @@ static int enqueue_step(Engine &E, bool diag_now)
         CUDA_TRY(cudaStreamWaitEvent(E.stream, E.ev_join, 0));
     } else {
         if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
-        if (mag) st = E.split ? split_mag(&E) : phys_mag64(&E);
+        if (mag) st = E.split ? split_mag(&E, fold) : phys_mag64(&E);
         else st = phys_zero_mag_rhs(&E);
         if (st) return st;
     }
     if (E.corr_on && (st = closure_apply_corr(&E))) return st;
     const int mdeal = E.p.dalias && mag;
-    if ((st = E.split ? split_ab3(&E, mdeal) : phys_ab3(&E, mdeal))) return st;
+    if ((st = E.split ? split_ab3(&E, mdeal, fold) : phys_ab3(&E, mdeal))) return st;
     const bool dealias_now = E.p.dalias && (E.nit % 10 == 0);
     if (dealias_now && (st = E.split ? split_dealias(&E) : phys_dealias_state(&E))) return st;
-    if (mag && (st = E.split ? split_bandj(&E) : phys_bandj64(&E))) return st;
+    if (mag && (st = E.split ? split_bandj(&E, fold) : phys_bandj64(&E))) return st;
     if (mag) {
         if ((st = phys_boundaries(&E))) return st;   // boundary and mag_boundary (disjoint fields)
     } else if ((st = boundary_step(E))) {

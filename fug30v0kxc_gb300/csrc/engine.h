@@ -229,13 +229,17 @@ struct BoundaryMirrors {
     const double *t0;
 };
 int split_hydro(Engine *E);
-int split_mag(Engine *E);
-int split_bandj(Engine *E);
+// In one time step the AB3 coefficient step can ride on the mean-field CTA
+// of split_mag's mag_div kernel (ab3_coef) and the history rotation on the
+// first kernel of split_bandj (rotate_hist); split_ab3 then runs the update
+// alone (folded).
+int split_mag(Engine *E, bool ab3_coef = false);
+int split_bandj(Engine *E, bool rotate_hist = false);
 int split_refresh(Engine *E);
 int split_refresh_field(Engine *E, int field);   // one field's mirror (VEC_F_*)
 int split_refresh_planes(Engine *E, int mask);
 int split_refresh_uv(Engine *E);
 int split_sync_b64(Engine *E);
-int split_ab3(Engine *E, int magdealias);
+int split_ab3(Engine *E, int magdealias, bool folded = false);
 int split_dealias(Engine *E);
 int split_calcdt(Engine *E);

@@ -29,6 +29,11 @@ struct MeanArgs {
     int nz;
     double xn, zck, ho12, sc1;
     int var_eta;
+    // k_mag_div4 only: with ds set, the mean-field CTA goes on with the AB3
+    // coefficient step and the mean update of ab3_coef_block on bxm, bym
+    // (the bxbar, bybar above), which read the history it has just written
+    DevScalars *ds;
+    double *bxm, *bym;
 };
 
 template <typename R>
@@ -82,6 +87,26 @@ static __global__ void k_mag_div(const R *ex, const R *ey, R *w1, int nx, int ny
     const size_t pb = (size_t)blockIdx.y * np;
     const int j = (int)(q / (unsigned)nx), i = (int)(q - (unsigned)j * nx);
     w1[pb + q] = sdx(ex + pb, i, j, nx, h.kx1) + sdy(ey + pb, i, j, nx, ny, h.ky1);
+}
+
+// the AB3 coefficients (src/main.F90:381-403), dt1/dt2 (:488-489), ttime
+// (:345) and the 1-D mean update (:469-476), by one whole CTA
+__device__ __forceinline__ void ab3_coef_block(DevScalars *ds, double *bxbar, double *bybar, const HistTable *ht,
+                                               int nz, int do_means)
+{
+    const double *bxd0 = ht->bx[0], *bxd1 = ht->bx[1], *bxd2 = ht->bx[2];
+    const double *byd0 = ht->by[0], *byd1 = ht->by[1], *byd2 = ht->by[2];
+    __shared__ double cc[3];
+    if (threadIdx.x == 0) {
+        ab3_coefs(ds, cc);
+        ab3_advance(ds, cc);
+    }
+    __syncthreads();
+    if (!do_means) return;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        bxbar[k] = bxbar[k] + cc[0] * bxd2[k] + cc[1] * bxd1[k] + cc[2] * bxd0[k];
+        bybar[k] = bybar[k] + cc[0] * byd2[k] + cc[1] * byd1[k] + cc[2] * byd0[k];
+    }
 }
 
 template <typename R>
@@ -243,20 +268,29 @@ static __global__ void k_emf4(const float *u, const float *v, const float *w, co
     st4(e3, i, U * BY - Vv * BX);
 }
 
-// (grid (np/4/256, nz + 1): the extra row's first CTA computes the mean-field
-// RHS, which reads the same spectra -- one launch instead of two)
+// (grid (np/4/256, nz + 1): the first CTA of the extra first row computes
+// the mean-field RHS, which reads the same spectra -- one launch instead of
+// two; the row is dispatched first, so that the CTA's serial FP64 work is
+// not the grid's tail.  No plane of this kernel, and none of k_mag_final4
+// that follows it, reads ds, bxbar, bybar or the bx/by histories.)
 static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h,
                                   MeanArgs<float> ma)
 {
     PDL_WAIT();
-    if (blockIdx.y == gridDim.y - 1) {
-        if (blockIdx.x == 0) mean_rhs_block(ma);
+    if (blockIdx.y == 0) {
+        if (blockIdx.x == 0) {
+            mean_rhs_block(ma);
+            if (ma.ds) {
+                __syncthreads();   // the new history is written, bxbar and bybar are read
+                ab3_coef_block(ma.ds, ma.bxm, ma.bym, ma.ht, ma.nz, 1);
+            }
+        }
         return;
     }
     const unsigned np4 = (unsigned)nx * ny / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
-    const size_t pb = (size_t)blockIdx.y * np4 * 4;
+    const size_t pb = (size_t)(blockIdx.y - 1) * np4 * 4;
     const unsigned q = 4 * q4;
     const int j = (int)(q / (unsigned)nx), i0 = (int)(q - (unsigned)j * nx);
     st4(w1 + pb, q4, sdx4(ex + pb, i0, j, nx, h.kx1) + sdy4(ey + pb, i0, j, nx, ny, h.ky1));

@@ -321,6 +321,7 @@ int phys_mag64(Engine *E)
     ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
     ma.ht = E->ht; ma.scratch = E->w1d; ma.np = E->np; ma.nz = E->nz;
     ma.xn = c.xn; ma.zck = c.zck; ma.ho12 = c.ho12; ma.sc1 = c.sc1; ma.var_eta = c.var_eta;
+    ma.ds = nullptr; ma.bxm = nullptr; ma.bym = nullptr;
     KLAUNCH(E, "mean_rhs", k_mean_rhs<double>, 1, 256, ma);
     KLAUNCHB(E, "mag_div_f64", FB(E, 3, 8), k_mag_div<double>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
              E->nx, E->ny, E->hd);
@@ -534,19 +535,7 @@ int phys_mag_boundary(Engine *E)
 __global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const HistTable *ht, int nz, int do_means)
 {
     PDL_WAIT();
-    const double *bxd0 = ht->bx[0], *bxd1 = ht->bx[1], *bxd2 = ht->bx[2];
-    const double *byd0 = ht->by[0], *byd1 = ht->by[1], *byd2 = ht->by[2];
-    __shared__ double cc[3];
-    if (threadIdx.x == 0) {
-        ab3_coefs(ds, cc);
-        ab3_advance(ds, cc);
-    }
-    __syncthreads();
-    if (!do_means) return;
-    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        bxbar[k] = bxbar[k] + cc[0] * bxd2[k] + cc[1] * bxd1[k] + cc[2] * bxd0[k];
-        bybar[k] = bybar[k] + cc[0] * byd2[k] + cc[1] * byd1[k] + cc[2] * byd0[k];
-    }
+    ab3_coef_block(ds, bxbar, bybar, ht, nz, do_means);
 }
 
 struct Ab3Args {

@@ -635,7 +635,7 @@ int split_hydro(Engine *E)
 }
 
 // ---- mag_deriv ---------------------------------------------------------------
-int split_mag(Engine *E)
+int split_mag(Engine *E, bool ab3_coef)
 {
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
@@ -659,6 +659,7 @@ int split_mag(Engine *E)
     ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
     ma.ht = E->ht; ma.scratch = E->w1d; ma.np = E->np; ma.nz = E->nz;
     ma.xn = c.xn; ma.zck = c.zck; ma.ho12 = c.ho12; ma.sc1 = c.sc1; ma.var_eta = c.var_eta;
+    ma.ds = v4 && ab3_coef ? E->ds : nullptr; ma.bxm = E->bxbar; ma.bym = E->bybar;
     if (v4) {
         KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div4, dim3(g4.x, g4.y + 1), TPB, W[W_EX], W[W_EY], W[W_M4],
                  E->nx, E->ny, E->hf, ma);
@@ -673,8 +674,12 @@ int split_mag(Engine *E)
     a.ht = E->ht;
     a.zck = (float)c.zck; a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    if (v4) KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final4, g4, TPB, a);
-    else KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, plane_grid(*E), TPB, a);
+    if (v4) {
+        KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final4, g4, TPB, a);
+    } else {
+        KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, plane_grid(*E), TPB, a);
+        if (ab3_coef) return phys_ab3_coef(E);
+    }
     return VEC_OK;
 }
 
@@ -696,25 +701,35 @@ __global__ void __launch_bounds__(256) k_d1z_f(const float *in, float *out, int 
 }
 
 // four consecutive x points per thread, grid (np/4/256, nz)
-__global__ void __launch_bounds__(256) k_d1z4(const float *in, float *out, int fl, size_t np, int nz, float h)
+// with rot set, an extra first CTA row (blockIdx.y == 0) rotates the history
+// table: the first kernel after the AB3 update, and none of its planes reads
+// the table
+__global__ void __launch_bounds__(256) k_d1z4(const float *in, float *out, int fl, size_t np, int nz, float h,
+                                              HistTable *rot)
 {
     PDL_WAIT();
+    if (rot && blockIdx.y == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) rotate_hist_table(rot);
+        return;
+    }
     const size_t np4 = np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
-    const int k = blockIdx.y;
+    const int k = (int)blockIdx.y - (rot ? 1 : 0);
     reinterpret_cast<V4 *>(out)[(size_t)k * np4 + q4] = zd1(reinterpret_cast<const V4 *>(in) + q4, np4, k, nz, fl, V4(h));
 }
 
-int split_bandj(Engine *E)
+int split_bandj(Engine *E, bool rotate_hist)
 {
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
     int st;
     const bool v4 = E->nx % 4 == 0 && E->vec4;
     const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
+    if (!v4 && rotate_hist && (st = phys_rotate_hist(E))) return st;
     if (v4)
-        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z4, g4, TPB, E->pol32, W[W_M1], 5, E->np, E->nz, (float)E->k.ho12);
+        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z4, dim3(g4.x, g4.y + (rotate_hist ? 1 : 0)), TPB, E->pol32,
+                 W[W_M1], 5, E->np, E->nz, (float)E->k.ho12, rotate_hist ? E->ht : nullptr);
     else
         KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, W[W_M1], 5, E->np,
                  E->nz, (float)E->k.ho12, ZCHUNK);
@@ -872,10 +887,10 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
     }
 }
 
-int split_ab3(Engine *E, int magdealias)
+int split_ab3(Engine *E, int magdealias, bool folded)
 {
-    int st = phys_ab3_coef(E);
-    if (st) return st;
+    int st;
+    if (!folded && (st = phys_ab3_coef(E))) return st;
     SplitAb3Args a;
     double *xs[7] = { E->u, E->v, E->w, E->r, E->t, E->pol, E->tor };
     float *ms[7] = { E->u32, E->v32, E->w32, E->r32, E->t32, E->pol32, E->tor32 };
@@ -898,7 +913,7 @@ int split_ab3(Engine *E, int magdealias)
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4<false>, nblk(E->n / 4), TPB, a);
     else
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3, nblk(E->n), TPB, a);
-    return phys_rotate_hist(E);
+    return folded ? VEC_OK : phys_rotate_hist(E);
 }
 
 // ---- dealias of r,t,u,v,w (every 10 steps) -----------------------------------------
