@@ -180,3 +180,77 @@ def test_ran0_sequence():
         s = (A * s) % M
         vals.append(2.0 * (s * (1.0 / M) - 0.5) * 0.5)
     assert np.array_equal(t[0].ravel(), np.array(vals) + 1.0)
+
+
+STATE_DOTS = (("r", "rdot"), ("t", "tdot"), ("u", "udot"), ("v", "vdot"), ("w", "wdot"),
+              ("pol", "poldot"), ("tor", "tordot"))
+
+
+@pytest.mark.parametrize("start,order", [("euler", 0), ("ab2", 1), ("ab3", 2)])
+def test_ab3_integrates_polynomials_exactly(start, order):
+    """Variable-step Adams-Bashforth (src/main.F90:381-403) against exact integrals.
+
+    The coefficients are the integrals over [t_n, t_n + dt] of the Lagrange
+    basis through the RHS times t_n, t_n - dt1 and t_n - dt2 (dt2 = t_n -
+    t_{n-2}). So one step of the full scheme integrates a right-hand side
+    that is quadratic in time exactly, for any step sizes. The start-up
+    steps are exact for linear (AB2, dt2 = 0) and constant (Euler) ones.
+    Also pinned: the history shift (:448-461) and the dt1/dt2 and start-flag
+    updates (:488-489).
+    """
+    nx, ny, nz = 8, 6, 6
+    o, _ = _oracle(nx, ny, nz)
+    rng = np.random.default_rng(11 + order)
+    dt, dt1, dt2 = 0.0173, 0.0211, 0.0211 + 0.0128
+    first, second = {"euler": (1, 0), "ab2": (0, 1), "ab3": (0, 0)}[start]
+    s = o.scalars()
+    s.dt, s.dt1, s.dt2, s.first, s.second = dt, dt1, dt2, first, second
+    o.set_scalars(s)
+
+    def poly(shape):
+        c = [rng.uniform(-1.0, 1.0, shape) for _ in range(3)]
+        for m in range(order + 1, 3):
+            c[m] = np.zeros(shape)
+        g = lambda t: c[0] + c[1] * t + c[2] * t * t                        # noqa: E731
+        integral = c[0] * dt + c[1] * dt ** 2 / 2.0 + c[2] * dt ** 3 / 3.0   # over [0, dt]
+        return g, integral
+
+    # histories sampled at t_n = 0, -dt1, -dt2; slots the scheme does not use
+    # hold unrelated values
+    times = {3: 0.0, 2: -dt1 if order >= 1 else None, 1: -dt2 if order >= 2 else None}
+    shape = (nz, ny, nx)
+    expect, hist = {}, {}
+    for name, dot in STATE_DOTS:
+        y0 = rng.uniform(0.9, 1.1, shape)   # r stays above the 0.05 floor
+        g, integral = poly(shape)
+        o.set(name, y0)
+        for slot, t in times.items():
+            h = g(t) if t is not None else rng.uniform(-1.0, 1.0, shape)
+            o.set(f"{dot}{slot}", h)
+            hist[(dot, slot)] = h
+        expect[name] = y0 + integral
+    for name in ("bxbar", "bybar"):
+        y0 = rng.uniform(-1.0, 1.0, nz)
+        g, integral = poly(nz)
+        o.set_mean(name, y0)
+        for slot, t in times.items():
+            h = g(t) if t is not None else rng.uniform(-1.0, 1.0, nz)
+            o.set_mean(f"{name}dot{slot}", h)
+            hist[(name + "dot", slot)] = h
+        expect[name] = y0 + integral
+
+    o.ab3_update()
+
+    for name, dot in STATE_DOTS:
+        np.testing.assert_allclose(o.get(name), expect[name], rtol=0, atol=1e-14, err_msg=name)
+        # the shift: oldest <- middle <- newest
+        assert np.array_equal(o.get(f"{dot}1"), hist[(dot, 2)])
+        assert np.array_equal(o.get(f"{dot}2"), hist[(dot, 3)])
+    for name in ("bxbar", "bybar"):
+        np.testing.assert_allclose(o.get_mean(name), expect[name], rtol=0, atol=1e-14, err_msg=name)
+        assert np.array_equal(o.get_mean(f"{name}dot1"), hist[(name + "dot", 2)])
+        assert np.array_equal(o.get_mean(f"{name}dot2"), hist[(name + "dot", 3)])
+    s = o.scalars()
+    prev_dt1 = {"euler": 0.0, "ab2": dt1, "ab3": dt1}[start]
+    assert (s.first, s.second) == {"euler": (0, 1), "ab2": (0, 0), "ab3": (0, 0)}[start]
+    assert s.dt1 == dt and s.dt2 == dt + prev_dt1
