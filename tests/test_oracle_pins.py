@@ -254,3 +254,84 @@ def test_ab3_integrates_polynomials_exactly(start, order):
     prev_dt1 = {"euler": 0.0, "ab2": dt1, "ab3": dt1}[start]
     assert (s.first, s.second) == {"euler": (0, 1), "ab2": (0, 0), "ab3": (0, 0)}[start]
     assert s.dt1 == dt and s.dt2 == dt + prev_dt1
+
+
+@pytest.mark.parametrize("radbc,constflux", [(0, 0), (1, 1)])
+def test_boundary_meets_its_conditions_through_the_stencils(radbc, constflux):
+    """boundary (src/dbydz.F90:3686-4197) against the conditions it imposes,
+    measured with the independently restated wall rows of d1bydz (flag 5,
+    src/dbydz.F90:927 and :626: 2h(-11 f0 + 18 f1 - 9 f2 + 2 f3)):
+
+    * stress-free walls: du/dz = dv/dz = 0, and w = 0;
+    * bottom: T = 1, or with radbc the radiative condition dT/dz = theta T^4;
+    * top: T = 1 + theta, or with constflux the flux condition dT/dz = theta.
+    """
+    nx, ny, nz = 6, 4, 9
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.radbc, p.constflux = radbc, constflux
+    o = O.Oracle(p)
+    rng = np.random.default_rng(3 + radbc)
+    shape = (nz, ny, nx)
+    for name in ("u", "v", "w"):
+        o.set(name, rng.uniform(-1.0, 1.0, shape))
+    zc = np.linspace(0.0, 1.0, nz)[:, None, None]
+    o.set("t", 1.0 + p.theta * zc + 0.05 * rng.uniform(-1.0, 1.0, shape))   # near the polytrope
+    o.boundary()
+    tol = 1e-12
+    for name in ("u", "v"):
+        d = o.d1bydz(o.get(name), 5)
+        assert np.abs(d[0]).max() < tol and np.abs(d[-1]).max() < tol, name
+    w = o.get("w")
+    assert not w[0].any() and not w[-1].any()
+    t = o.get("t")
+    dt = o.d1bydz(t, 5)
+    if radbc:
+        np.testing.assert_allclose(dt[0], p.theta * t[0] ** 4, rtol=1e-11, atol=0)
+    else:
+        assert np.all(t[0] == 1.0)
+    if constflux:
+        np.testing.assert_allclose(dt[-1], p.theta, rtol=1e-11, atol=0)
+    else:
+        assert np.all(t[-1] == 1.0 + p.theta)
+
+
+@pytest.mark.parametrize("perfect", [0, 1])
+def test_mag_boundary_meets_its_conditions_through_the_stencils(perfect):
+    """mag_boundary (src/dbydz.F90:4205-4791) against the conditions it
+    imposes, measured with the flag-5 wall rows of d1bydz and d1bydz1d:
+
+    * vertical field (:4663-4780): tor = 0, bxbar = bybar = 0 and
+      d(pol)/dz = 0 at both walls;
+    * perfect conductor (:4407-4560): pol = 0 and d(tor)/dz = d(bxbar)/dz =
+      d(bybar)/dz = 0 at both walls.
+    """
+    nx, ny, nz = 6, 4, 9
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.perfect = perfect
+    o = O.Oracle(p)
+    rng = np.random.default_rng(5 + perfect)
+    shape = (nz, ny, nx)
+    for name in ("pol", "tor"):
+        o.set(name, rng.uniform(-1.0, 1.0, shape))
+    for name in ("bxbar", "bybar"):
+        o.set_mean(name, rng.uniform(-1.0, 1.0, nz))
+    o.mag_boundary()
+    tol = 1e-12
+    pol, tor = o.get("pol"), o.get("tor")
+    means = [o.get_mean(n) for n in ("bxbar", "bybar")]
+
+    def walls_zero_slope(d):
+        return np.abs(d[0]).max() < tol and np.abs(d[-1]).max() < tol
+
+    if perfect:
+        assert not pol[0].any() and not pol[-1].any()
+        assert walls_zero_slope(o.d1bydz(tor, 5))
+        for m in means:
+            assert walls_zero_slope(o.d1bydz1d(m, 5))
+    else:
+        assert not tor[0].any() and not tor[-1].any()
+        for m in means:
+            assert m[0] == 0.0 and m[-1] == 0.0
+        assert walls_zero_slope(o.d1bydz(pol, 5))
