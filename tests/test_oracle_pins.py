@@ -335,3 +335,47 @@ def test_mag_boundary_meets_its_conditions_through_the_stencils(perfect):
         for m in means:
             assert m[0] == 0.0 and m[-1] == 0.0
         assert walls_zero_slope(o.d1bydz(pol, 5))
+
+
+def _static_polytrope(nz, cm, nx=8, ny=8):
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.noise_amp, p.cm, p.kappa_uniform = 0.0, cm, 1
+    o = O.Oracle(p)
+    o.static()
+    o.bandj()
+    return o
+
+
+def test_static_polytrope_is_a_discrete_equilibrium():
+    """With polytropic index m = 1 the static state (src/initial.F90:25-86)
+    has T = 1 + theta z, rho = T and p = rho T = T^2: polynomials of degree
+    <= 2 in z, on which every z stencil is exact, with a uniform vertical
+    field and uniform kappa. Hydrostatic balance (src/hydro_deriv.f90) and
+    the induction equation (src/magnetic.f90:285-487) then hold exactly in
+    discrete form: every right-hand side vanishes."""
+    o = _static_polytrope(17, 1.0)
+    o.hydro_deriv()
+    o.mag_deriv()
+    for d in ("rdot", "tdot", "udot", "vdot", "wdot", "poldot", "tordot"):
+        assert np.abs(o.get(f"{d}3")).max() < 1e-12, d
+    for m in ("bxbardot3", "bybardot3"):
+        assert np.abs(o.get_mean(m)).max() < 1e-12, m
+
+
+def test_hydrostatic_residual_converges_at_stencil_order():
+    """For m = 1.5, p = T^2.5 is no polynomial, and the hydrostatic residual
+    in dw/dt is the stencils' truncation error: fourth order at fixed
+    interior heights (src/dbydz.F90:371) and third order on the rows next
+    to the walls (:776, :1053)."""
+    res = {}
+    for nz in (33, 65, 129):
+        o = _static_polytrope(nz, 1.5)
+        o.hydro_deriv()
+        w = o.get("wdot3")[:, 0, 0]
+        res[nz] = (np.array([w[(nz - 1) // 4], w[(nz - 1) // 2], w[3 * (nz - 1) // 4]]), w[nz - 2])
+    for a, b in ((33, 65), (65, 129)):
+        interior = np.abs(res[a][0] / res[b][0])
+        assert np.all((interior > 15.0) & (interior < 17.5)), (a, b, interior)
+    wall = abs(res[65][1] / res[129][1])
+    assert 7.0 < wall < 9.5, wall
