@@ -379,3 +379,53 @@ def test_hydrostatic_residual_converges_at_stencil_order():
         assert np.all((interior > 15.0) & (interior < 17.5)), (a, b, interior)
     wall = abs(res[65][1] / res[129][1])
     assert 7.0 < wall < 9.5, wall
+
+
+@pytest.mark.parametrize("eta_contrast", [1.0, 20.0])
+def test_induction_diffusion_known_answer(eta_contrast):
+    """mag_deriv (src/magnetic.f90:285-487) with u = 0: the EMF vanishes and
+    the induction equation is pure diffusion. For one horizontal Fourier mode
+    with a cubic z profile f, every z stencil is exact, so with eta(z) =
+    zeta ck (1 + (c - 1) z) (c = eta contrast; c = 1 is the reference):
+
+        poldot = eta (-k^2 f + f'')
+        tordot = eta (-k^2 f + f'') + eta' f'
+        bxbardot = eta f'' + eta' f'   (the horizontal mean, k = 0)
+
+    with k = 2 pi i / xmax or 2 pi j / ymax computed here, independently of
+    the oracle's wavenumber tables; every other mode stays zero."""
+    nx, ny, nz = 16, 12, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.eta_contrast = eta_contrast
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    for name in ("u", "v", "w", "bx", "by", "bz"):
+        o.set(name, np.zeros(shape))
+    z = np.linspace(0.0, 1.0, nz)
+    f = 0.3 + 0.7 * z - 1.1 * z ** 2 + 0.9 * z ** 3
+    f1 = 0.7 - 2.2 * z + 2.7 * z ** 2
+    f2 = -2.2 + 5.4 * z
+    i, j = 3, 2
+    pol, tor = np.zeros(shape), np.zeros(shape)
+    pol[:, 0, i] = f   # x mode i (real part of the halfcomplex pair), y mode 0
+    tor[:, j, 0] = f   # y mode j, x mode 0
+    o.set("pol", pol)
+    o.set("tor", tor)
+    o.set_mean("bxbar", f)
+    o.set_mean("bybar", np.zeros(nz))
+    o.bzbar = 0.0
+    o.mag_deriv()
+    zck = p.zeta * p.ck
+    eta = zck * (1.0 + (eta_contrast - 1.0) * z)
+    deta = zck * (eta_contrast - 1.0)
+    kx, ky = 2 * np.pi * i / p.xmax, 2 * np.pi * j / p.ymax
+    pd, td = o.get("poldot3"), o.get("tordot3")
+    tol = 1e-13 * max(1.0, eta_contrast)
+    np.testing.assert_allclose(pd[:, 0, i], eta * (-kx * kx * f + f2), rtol=0, atol=tol)
+    np.testing.assert_allclose(td[:, j, 0], eta * (-ky * ky * f + f2) + deta * f1, rtol=0, atol=tol)
+    pd[:, 0, i] = 0.0
+    td[:, j, 0] = 0.0
+    assert not pd.any() and not td.any()
+    np.testing.assert_allclose(o.get_mean("bxbardot3"), eta * f2 + deta * f1, rtol=0, atol=tol)
+    assert not o.get_mean("bybardot3").any()
