@@ -429,3 +429,44 @@ def test_induction_diffusion_known_answer(eta_contrast):
     assert not pd.any() and not td.any()
     np.testing.assert_allclose(o.get_mean("bxbardot3"), eta * f2 + deta * f1, rtol=0, atol=tol)
     assert not o.get_mean("bybardot3").any()
+
+
+def test_viscous_shear_flow_known_answer():
+    """hydro_deriv (src/hydro_deriv.f90:5-505) on a plane shear flow u = U(z)
+    (cubic), v = w = 0, uniform rho = T = 1, no field, no rotation: div u = 0
+    and p is uniform, so with the nondimensional numbers sigma ck (viscosity)
+    and sigma ck (gamma - 1) (viscous heating), and gravity theta (m + 1):
+
+        udot = sigma ck U''                  (every row: the stencils are exact)
+        tdot = sigma ck (gamma - 1) U'^2     (interior; 0 on the fixed-T walls)
+        wdot = theta (m + 1)                 (interior; 0 on the walls)
+        rdot = vdot = 0
+    """
+    nx, ny, nz = 8, 6, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.kappa_uniform = 1
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    z = np.linspace(0.0, 1.0, nz)[:, None, None]
+    U = 0.2 + 0.5 * z - 0.8 * z ** 2 + 0.6 * z ** 3
+    U1 = 0.5 - 1.6 * z + 1.8 * z ** 2
+    U2 = -1.6 + 3.6 * z
+    for name in ("v", "w", "bx", "by", "bz", "jsq", "pol", "tor"):
+        o.set(name, np.zeros(shape))
+    o.set("u", U * np.ones(shape))
+    o.set("r", np.ones(shape))
+    o.set("t", np.ones(shape))
+    o.bzbar = 0.0
+    o.hydro_deriv()
+    sck = p.sigma * p.ck
+    one = np.ones(shape)
+    np.testing.assert_allclose(o.get("udot3"), sck * U2 * one, rtol=0, atol=1e-13)
+    heat = sck * (p.gamma - 1.0) * U1 ** 2 * one
+    heat[0] = heat[-1] = 0.0
+    np.testing.assert_allclose(o.get("tdot3"), heat, rtol=0, atol=1e-13)
+    grav = p.theta * (p.cm + 1.0) * one
+    grav[0] = grav[-1] = 0.0
+    np.testing.assert_allclose(o.get("wdot3"), grav, rtol=0, atol=1e-12)
+    assert np.abs(o.get("rdot3")).max() == 0.0
+    assert np.abs(o.get("vdot3")).max() < 1e-14
