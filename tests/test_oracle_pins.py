@@ -470,3 +470,44 @@ def test_viscous_shear_flow_known_answer():
     np.testing.assert_allclose(o.get("wdot3"), grav, rtol=0, atol=1e-12)
     assert np.abs(o.get("rdot3")).max() == 0.0
     assert np.abs(o.get("vdot3")).max() < 1e-14
+
+
+def test_lorentz_force_and_ohmic_heating_known_answer():
+    """hydro_deriv's Lorentz force, the divergence of the Maxwell stress
+    F (B_i B_j - |B|^2 delta_ij / 2) (src/hydro_deriv.f90:139-261), and
+    ohmic heating, for B = (beta(z), 0, bz0) with beta quadratic, u = 0,
+    rho = T = 1 and J = (0, beta', 0):
+
+        udot = F bz0 beta'                       (every row)
+        wdot = theta (m + 1) - F beta beta'      (interior rows, where the
+               quartic beta^2 is differentiated exactly; 0 on the walls)
+        tdot = F zeta ck (gamma - 1) |J|^2       (every row)
+    """
+    nx, ny, nz = 8, 6, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.kappa_uniform = 1
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    one = np.ones(shape)
+    z = np.linspace(0.0, 1.0, nz)[:, None, None]
+    beta = 0.4 - 0.3 * z + 0.5 * z ** 2
+    beta1 = -0.3 + 1.0 * z
+    bz0 = 0.7
+    for name in ("u", "v", "w", "by", "pol", "tor"):
+        o.set(name, np.zeros(shape))
+    o.set("bx", beta * one)
+    o.set("bz", bz0 * one)
+    o.set("jsq", beta1 ** 2 * one)
+    o.set("r", one)
+    o.set("t", one)
+    o.hydro_deriv()
+    F = p.f
+    np.testing.assert_allclose(o.get("udot3"), F * bz0 * beta1 * one, rtol=0, atol=1e-13)
+    wd = o.get("wdot3")
+    expect = (p.theta * (p.cm + 1.0) - F * beta * beta1) * one
+    np.testing.assert_allclose(wd[2:-2], expect[2:-2], rtol=0, atol=1e-12)
+    assert not wd[0].any() and not wd[-1].any()
+    heat = p.f * p.zeta * p.ck * (p.gamma - 1.0) * beta1 ** 2 * one
+    np.testing.assert_allclose(o.get("tdot3"), heat, rtol=0, atol=1e-13)
+    assert np.abs(o.get("vdot3")).max() < 1e-14 and not o.get("rdot3").any()
