@@ -511,3 +511,37 @@ def test_lorentz_force_and_ohmic_heating_known_answer():
     heat = p.f * p.zeta * p.ck * (p.gamma - 1.0) * beta1 ** 2 * one
     np.testing.assert_allclose(o.get("tdot3"), heat, rtol=0, atol=1e-13)
     assert np.abs(o.get("vdot3")).max() < 1e-14 and not o.get("rdot3").any()
+
+
+def test_thermal_conduction_known_answer():
+    """hydro_deriv's conduction with the reference's kappa(z) =
+    (tanh(10 (z - 1/2)) + 1) / 2 (src/trans_params.f90:15-69), for a cubic
+    T(z), rho = 1, u = 0, no field:
+
+        tdot = gamma ck (kappa T'' + kappa' T')   (rows inside the walls)
+        wdot = theta (m + 1) - T'                 (p = rho T; 0 on the walls)
+    """
+    nx, ny, nz = 8, 6, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.kappa_uniform = 0
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    one = np.ones(shape)
+    z = np.linspace(0.0, 1.0, nz)[:, None, None]
+    T = 1.0 + p.theta * z + 0.3 * z * (1.0 - z) + 0.2 * z ** 3
+    T1 = p.theta + 0.3 - 0.6 * z + 0.6 * z ** 2
+    T2 = -0.6 + 1.2 * z
+    for name in ("u", "v", "w", "bx", "by", "bz", "jsq", "pol", "tor"):
+        o.set(name, np.zeros(shape))
+    o.set("r", one)
+    o.set("t", T * one)
+    o.hydro_deriv()
+    kappa = 0.5 * (np.tanh(10.0 * (z - 0.5)) + 1.0)
+    dkappa = 5.0 / np.cosh(10.0 * (z - 0.5)) ** 2
+    cond = p.gamma * p.ck * (kappa * T2 + dkappa * T1) * one
+    np.testing.assert_allclose(o.get("tdot3")[1:-1], cond[1:-1], rtol=0, atol=1e-12)
+    wd = o.get("wdot3")
+    np.testing.assert_allclose(wd[1:-1], ((p.theta * (p.cm + 1.0) - T1) * one)[1:-1], rtol=0, atol=1e-12)
+    assert not wd[0].any() and not wd[-1].any()
+    assert not o.get("udot3").any() and not o.get("rdot3").any()
