@@ -545,3 +545,43 @@ def test_thermal_conduction_known_answer():
     np.testing.assert_allclose(wd[1:-1], ((p.theta * (p.cm + 1.0) - T1) * one)[1:-1], rtol=0, atol=1e-12)
     assert not wd[0].any() and not wd[-1].any()
     assert not o.get("udot3").any() and not o.get("rdot3").any()
+
+
+def test_horizontal_advection_and_pressure_known_answer():
+    """hydro_deriv with a horizontal density wave rho = 1 + a cos(kx) +
+    b sin(ly) carried by a uniform flow (U0, V0, 0) at uniform T = 1. The
+    spectral x and y derivatives are exact for resolved modes, with k and l
+    computed here, and div u = 0:
+
+        rdot = -(U0 rho_x + V0 rho_y)
+        udot = -rho_x / rho,  vdot = -rho_y / rho   (p = rho T)
+        tdot = 0,  wdot = theta (m + 1) inside the walls, 0 on them
+    """
+    nx, ny, nz = 16, 12, 9
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.kappa_uniform = 1
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    one = np.ones(shape)
+    x = (np.arange(nx) * p.xmax / nx)[None, None, :]
+    y = (np.arange(ny) * p.ymax / ny)[None, :, None]
+    k, l, a, b = 2 * np.pi * 3 / p.xmax, 2 * np.pi * 2 / p.ymax, 0.2, 0.1
+    rho = (1.0 + a * np.cos(k * x) + b * np.sin(l * y)) * one
+    rx = -a * k * np.sin(k * x) * one
+    ry = b * l * np.cos(l * y) * one
+    U0, V0 = 0.3, -0.2
+    for name in ("w", "bx", "by", "bz", "jsq", "pol", "tor"):
+        o.set(name, np.zeros(shape))
+    o.set("u", U0 * one)
+    o.set("v", V0 * one)
+    o.set("r", rho)
+    o.set("t", one)
+    o.hydro_deriv()
+    np.testing.assert_allclose(o.get("rdot3"), -U0 * rx - V0 * ry, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(o.get("udot3"), -rx / rho, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(o.get("vdot3"), -ry / rho, rtol=0, atol=1e-13)
+    assert np.abs(o.get("tdot3")).max() < 1e-13
+    wd = o.get("wdot3")
+    np.testing.assert_allclose(wd[1:-1], p.theta * (p.cm + 1.0), rtol=0, atol=1e-12)
+    assert not wd[0].any() and not wd[-1].any()
