@@ -585,3 +585,39 @@ def test_horizontal_advection_and_pressure_known_answer():
     wd = o.get("wdot3")
     np.testing.assert_allclose(wd[1:-1], p.theta * (p.cm + 1.0), rtol=0, atol=1e-12)
     assert not wd[0].any() and not wd[-1].any()
+
+
+@pytest.mark.parametrize("W0", [0.4, -0.4])
+def test_vertical_upwind_advection_known_answer(W0):
+    """hydro_deriv with a uniform vertical flow W0 through a cubic density
+    profile at T = 1 (div u = 0). The upwind z stencils (src/dbydz.F90:485,
+    :532, :579; the side follows the sign of w) are exact for cubics:
+
+        rdot = -W0 rho'              (every row inside the walls)
+        wdot = -rho'/rho + theta (m + 1)
+        tdot = 0
+
+    The w equation is checked away from the walls. Near them its viscous
+    term differentiates w with flag 1, which assumes w = 0 on the wall, and
+    a uniform W0 does not meet that.
+    """
+    nx, ny, nz = 8, 6, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.kappa_uniform = 1
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    one = np.ones(shape)
+    z = np.linspace(0.0, 1.0, nz)[:, None, None]
+    rho = 1.0 + 0.5 * z - 0.3 * z ** 2 + 0.4 * z ** 3
+    rho1 = 0.5 - 0.6 * z + 1.2 * z ** 2
+    for name in ("u", "v", "bx", "by", "bz", "jsq", "pol", "tor"):
+        o.set(name, np.zeros(shape))
+    o.set("w", W0 * one)
+    o.set("r", rho * one)
+    o.set("t", one)
+    o.hydro_deriv()
+    np.testing.assert_allclose(o.get("rdot3")[1:-1], (-W0 * rho1 * one)[1:-1], rtol=0, atol=1e-13)
+    wexp = (-rho1 / rho + p.theta * (p.cm + 1.0)) * one
+    np.testing.assert_allclose(o.get("wdot3")[3:-3], wexp[3:-3], rtol=0, atol=1e-12)
+    assert np.abs(o.get("tdot3")[1:-1]).max() < 1e-13
