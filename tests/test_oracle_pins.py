@@ -621,3 +621,36 @@ def test_vertical_upwind_advection_known_answer(W0):
     wexp = (-rho1 / rho + p.theta * (p.cm + 1.0)) * one
     np.testing.assert_allclose(o.get("wdot3")[3:-3], wexp[3:-3], rtol=0, atol=1e-12)
     assert np.abs(o.get("tdot3")[1:-1]).max() < 1e-13
+
+
+@pytest.mark.parametrize("cm,kappa_uniform", [(1.0, 1), (1.5, 1), (1.0, 0)])
+def test_diagnostics_known_answers(cm, kappa_uniform):
+    """diag (src/utils.F90:22-371, src/dbydz.F90:4796-4925) on states with
+    known values:
+
+    * the conductive static polytrope has Nusselt number 1 (the flux ratio
+      it is normalised by), no kinetic energy, T in [1, 1 + theta] and rho
+      in [1, (1 + theta)^m];
+    * a uniform flow (U0, V0, 0) at rho = 1 has kinetic energy
+      (U0^2 + V0^2) / 2 integrated over the xmax x ymax x 1 box, and
+      horizontal means U0, V0.
+    """
+    p = default_params()
+    p.nx, p.ny, p.nz = 8, 8, 33
+    p.noise_amp, p.cm, p.kappa_uniform = 0.0, cm, kappa_uniform
+    o = O.Oracle(p)
+    o.static()
+    o.bandj()
+    st, d = o.diag()
+    assert st == 0
+    assert abs(d["nusselt"] - 1.0) < 1e-12 and d["kenergy"] == 0.0
+    assert d["tmin"] == 1.0 and abs(d["tmax"] - (1.0 + p.theta)) < 1e-12
+    assert d["rmin"] == 1.0 and abs(d["rmax"] - (1.0 + p.theta) ** cm) < 1e-12 * (1.0 + p.theta) ** cm
+    shape = (p.nz, p.ny, p.nx)
+    U0, V0 = 0.3, -0.4
+    o.set("r", np.ones(shape))
+    o.set("u", U0 * np.ones(shape))
+    o.set("v", V0 * np.ones(shape))
+    st, d = o.diag()
+    assert abs(d["kenergy"] - 0.5 * (U0 ** 2 + V0 ** 2) * p.xmax * p.ymax) < 1e-13
+    assert abs(d["ubar"] - U0) < 1e-14 and abs(d["vbar"] - V0) < 1e-14
