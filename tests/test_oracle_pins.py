@@ -689,3 +689,64 @@ def test_bandj_field_is_solenoidal():
     bmax = max(np.abs(o.get(n)).max() for n in ("bx", "by", "bz"))
     assert bmax > 10.0
     assert max(abs(d["divbmax"]), abs(d["divbmin"])) < 1e-13 * bmax
+
+
+def test_bandj_single_mode_known_answer():
+    """bandj (src/magnetic.f90:492-664): B = curl curl (pol z) + curl (tor z)
+    + means, i.e. bx = d2pol/dxdz + dtor/dy, by = d2pol/dydz - dtor/dx,
+    bz = -lap_h pol. For one horizontal mode with a cubic z profile, the
+    real-space potential is A(z) cos(kx) (its spectral inverse), and k is
+    computed independently of the oracle's tables."""
+    nx, ny, nz = 16, 12, 11
+    p = default_params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    o = O.Oracle(p)
+    shape = (nz, ny, nx)
+    zc = np.linspace(0.0, 1.0, nz)
+    P = 0.3 + 0.7 * zc - 1.1 * zc ** 2 + 0.9 * zc ** 3
+    x = (np.arange(nx) * p.xmax / nx)[None, None, :]
+    y = (np.arange(ny) * p.ymax / ny)[None, :, None]
+    i, j = 3, 2
+    k, l = 2 * np.pi * i / p.xmax, 2 * np.pi * j / p.ymax
+    o.set_mean("bxbar", np.zeros(nz))
+    o.set_mean("bybar", np.zeros(nz))
+    o.bzbar = 0.0
+    zero = np.zeros(shape)
+
+    def run(pol, tor):
+        o.set("pol", pol)
+        o.set("tor", tor)
+        o.bandj()
+        return o.get("bx"), o.get("by"), o.get("bz")
+
+    def mode(jj, ii):
+        a = np.zeros(shape)
+        a[:, jj, ii] = P
+        real = o.inversefft(a)
+        return real, real[:, 0:1, 0:1]   # A(z) at x = y = 0
+
+    tol = 1e-15
+    # poloidal, x mode i: pol = A cos(kx)
+    pol = np.zeros(shape)
+    pol[:, 0, i] = P
+    pr, A = mode(0, i)
+    assert np.abs(pr - A * np.cos(k * x)).max() < tol
+    dA = o.d1bydz(A * np.ones(shape), 5)[:, 0:1, 0:1]   # A is cubic: exact
+    bx, by, bz = run(pol, zero)
+    np.testing.assert_allclose(bz, k * k * pr, rtol=0, atol=tol)
+    np.testing.assert_allclose(bx, -k * dA * np.sin(k * x) * np.ones(shape), rtol=0, atol=10 * tol)
+    assert not by.any()
+    # toroidal, y mode j: tor = A cos(ly) gives bx = dtor/dy, by = bz = 0
+    tr, A = mode(j, 0)
+    tor = np.zeros(shape)
+    tor[:, j, 0] = P
+    bx, by, bz = run(zero, tor)
+    np.testing.assert_allclose(bx, -l * A * np.sin(l * y) * np.ones(shape), rtol=0, atol=tol)
+    assert not by.any() and not bz.any()
+    # toroidal, x mode i: by = -dtor/dx
+    tr, A = mode(0, i)
+    tor = np.zeros(shape)
+    tor[:, 0, i] = P
+    bx, by, bz = run(zero, tor)
+    np.testing.assert_allclose(by, k * A * np.sin(k * x) * np.ones(shape), rtol=0, atol=tol)
+    assert not bx.any() and not bz.any()
