@@ -8,6 +8,16 @@
   ~0 error except for the top third of modes, which dealias removes.
 * z stencils (src/dbydz.F90:366-1558): interior rows exact for quartics,
   boundary rows exact for cubics, with the documented flag semantics.
+* The physics, against known answers built from first principles on states
+  where the stencils are exact:
+  - the AB3 update's polynomial exactness;
+  - the boundary conditions, through the d1bydz wall rows;
+  - the static polytrope as a discrete equilibrium, and the convergence
+    order of its residual;
+  - each term of hydro_deriv and mag_deriv on a shear flow, a field, a
+    temperature profile, and horizontal and vertical advection;
+  - bandj's field construction and its zero divergence;
+  - the diagnostics.
 """
 import numpy as np
 import pytest
