@@ -17,6 +17,7 @@
   - each term of hydro_deriv and mag_deriv on a shear flow, a field, a
     temperature profile, and horizontal and vertical advection;
   - bandj's field construction and its zero divergence;
+  - magdealias as the 2/3 rule;
   - the diagnostics.
 """
 import numpy as np
@@ -760,3 +761,51 @@ def test_bandj_single_mode_known_answer():
     bx, by, bz = run(zero, tor)
     np.testing.assert_allclose(by, k * A * np.sin(k * x) * np.ones(shape), rtol=0, atol=tol)
     assert not bx.any() and not bz.any()
+
+
+@pytest.mark.parametrize("nx,ny", [(30, 24), (32, 26), (48, 36)])
+def test_magdealias_is_the_two_thirds_rule(nx, ny):
+    """magdealias (src/magnetic.f90:666-717) on the spectral potentials
+    keeps exactly the modes with 3|kx| < nx and 3|ky| < ny: the 2/3 rule,
+    under which the product of two kept modes aliases only onto removed
+    ones. Checked two ways:
+
+    * on random fields, against a numpy FFT low-pass with that mask;
+    * dealiasing the grid product of two kept-band fields gives the
+      truncated exact product, computed on a grid that holds it unaliased.
+    """
+    nz = 6
+    o, _ = _oracle(nx, ny, nz)
+    rng = np.random.default_rng(nx + ny)
+    kx = np.abs(np.fft.fftfreq(nx, 1.0 / nx))[None, None, :]
+    ky = np.abs(np.fft.fftfreq(ny, 1.0 / ny))[None, :, None]
+    keep = (3 * kx < nx) & (3 * ky < ny)
+
+    def oracle_dealias(f):
+        o.set("pol", o.forwardfft(f))
+        o.set("tor", np.zeros_like(f))
+        o.magdealias()
+        return o.inversefft(o.get("pol"))
+
+    def lowpass(f):
+        return np.fft.ifft2(np.fft.fft2(f, axes=(1, 2)) * keep, axes=(1, 2)).real
+
+    f = rng.standard_normal((nz, ny, nx))
+    assert np.abs(oracle_dealias(f) - lowpass(f)).max() < 1e-12
+    # aliasing: a, b band-limited to the kept modes; their exact product has
+    # modes up to twice as high, held without aliasing on a 2x finer grid
+    a, b = lowpass(rng.standard_normal((nz, ny, nx))), lowpass(rng.standard_normal((nz, ny, nx)))
+
+    def fine(g):   # exact trigonometric interpolation onto the 2x grid
+        G = np.fft.fft2(g, axes=(1, 2))
+        H = np.zeros((nz, 2 * ny, 2 * nx), complex)
+        iy = np.fft.fftfreq(ny, 1.0 / ny).astype(int)
+        ix = np.fft.fftfreq(nx, 1.0 / nx).astype(int)
+        H[:, iy[:, None] % (2 * ny), ix[None, :] % (2 * nx)] = G
+        return np.fft.ifft2(H, axes=(1, 2)).real * 4.0
+
+    P = np.fft.fft2(fine(a) * fine(b), axes=(1, 2)) / 4.0
+    iy = np.fft.fftfreq(ny, 1.0 / ny).astype(int)
+    ix = np.fft.fftfreq(nx, 1.0 / nx).astype(int)
+    exact_kept = np.fft.ifft2(P[:, iy[:, None] % (2 * ny), ix[None, :] % (2 * nx)] * keep, axes=(1, 2)).real
+    assert np.abs(oracle_dealias(a * b) - exact_kept).max() < 1e-12
