@@ -16,7 +16,8 @@
     order of its residual;
   - each term of hydro_deriv and mag_deriv on a shear flow, a field, a
     temperature profile, and horizontal and vertical advection;
-  - bandj's field construction and its zero divergence;
+  - bandj's field construction and its zero divergence, and mag_init as
+    its inverse;
   - magdealias as the 2/3 rule;
   - the diagnostics.
 """
@@ -809,3 +810,50 @@ def test_magdealias_is_the_two_thirds_rule(nx, ny):
     ix = np.fft.fftfreq(nx, 1.0 / nx).astype(int)
     exact_kept = np.fft.ifft2(P[:, iy[:, None] % (2 * ny), ix[None, :] % (2 * nx)] * keep, axes=(1, 2)).real
     assert np.abs(oracle_dealias(a * b) - exact_kept).max() < 1e-12
+
+
+def test_mag_init_inverts_bandj():
+    """mag_init (src/magnetic.f90:5-279) recovers the potentials from B:
+    pol from bz = -lap_h pol, tor from the vertical current, and the means
+    from the horizontal averages. bandj (src/magnetic.f90:492-664) builds B
+    from them. Starting from random potentials inside the 2/3 band (mag_init
+    truncates B's spectra) without a horizontal mean mode, bandj then
+    mag_init returns them, the means, bzbar and |J|^2 to rounding. Wall
+    planes are excluded, since mag_init ends with mag_boundary."""
+    nx, ny, nz = 16, 12, 11
+    o, _ = _oracle(nx, ny, nz)
+    rng = np.random.default_rng(2)
+    shape = (nz, ny, nx)
+    ix = np.array([i if i <= nx // 2 else nx - i for i in range(nx)])
+    iy = np.array([j if j <= ny // 2 else ny - j for j in range(ny)])
+
+    def in_band(a):
+        a = a.copy()
+        a[:, :, 3 * ix >= nx] = 0.0
+        a[:, 3 * iy >= ny, :] = 0.0
+        a[:, 0, 0] = 0.0
+        return a
+
+    pol, tor = in_band(rng.standard_normal(shape)), in_band(rng.standard_normal(shape))
+    bxbar, bybar, bzbar = rng.standard_normal(nz), rng.standard_normal(nz), 0.7
+    o.set("pol", pol)
+    o.set("tor", tor)
+    o.set_mean("bxbar", bxbar)
+    o.set_mean("bybar", bybar)
+    o.bzbar = bzbar
+    o.bandj()
+    jsq = o.get("jsq")
+    zero = np.zeros(shape)
+    o.set("pol", zero)
+    o.set("tor", zero)
+    o.set_mean("bxbar", np.zeros(nz))
+    o.set_mean("bybar", np.zeros(nz))
+    o.bzbar = 0.0
+    o.mag_init()
+    tol = 1e-13
+    assert np.abs(o.get("pol")[1:-1] - pol[1:-1]).max() < tol * np.abs(pol).max()
+    assert np.abs(o.get("tor")[1:-1] - tor[1:-1]).max() < tol * np.abs(tor).max() * 10
+    assert np.abs(o.get_mean("bxbar")[1:-1] - bxbar[1:-1]).max() < tol
+    assert np.abs(o.get_mean("bybar")[1:-1] - bybar[1:-1]).max() < tol
+    assert abs(o.bzbar - bzbar) < tol
+    assert np.abs(o.get("jsq")[1:-1] - jsq[1:-1]).max() < tol * np.abs(jsq).max()
