@@ -857,3 +857,29 @@ def test_mag_init_inverts_bandj():
     assert np.abs(o.get_mean("bybar")[1:-1] - bybar[1:-1]).max() < tol
     assert abs(o.bzbar - bzbar) < tol
     assert np.abs(o.get("jsq")[1:-1] - jsq[1:-1]).max() < tol * np.abs(jsq).max()
+
+
+def test_global_averages_remove_mean_momentum():
+    """GlobalAverages (src/utils.F90:22-139): ubar, vbar are the density-
+    weighted means int(rho u) / int(rho), trapezoidal in z (half weight on
+    the wall planes), and the diagnostics step subtracts them from u and v.
+    Afterwards int(rho u) = int(rho v) = 0, so a second call reports zero."""
+    nx, ny, nz = 8, 6, 9
+    o, _ = _oracle(nx, ny, nz)
+    rng = np.random.default_rng(8)
+    shape = (nz, ny, nx)
+    r = rng.uniform(0.5, 2.0, shape)
+    u, v = rng.standard_normal(shape) + 0.3, rng.standard_normal(shape) - 0.2
+    for name, a in (("r", r), ("u", u), ("v", v), ("w", rng.standard_normal(shape)),
+                    ("t", np.ones(shape)), ("bx", np.zeros(shape)), ("by", np.zeros(shape)),
+                    ("bz", np.zeros(shape))):
+        o.set(name, a)
+    wz = np.ones(nz)
+    wz[0] = wz[-1] = 0.5
+    mean = lambda a: np.sum(wz[:, None, None] * r * a) / np.sum(wz[:, None, None] * r)   # noqa: E731
+    st, d = o.diag()
+    assert abs(d["ubar"] - mean(u)) < 1e-14 and abs(d["vbar"] - mean(v)) < 1e-14
+    np.testing.assert_allclose(o.get("u"), u - d["ubar"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(o.get("v"), v - d["vbar"], rtol=0, atol=1e-15)
+    st, d = o.diag()
+    assert abs(d["ubar"]) < 1e-15 and abs(d["vbar"]) < 1e-15
