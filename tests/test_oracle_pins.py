@@ -19,7 +19,8 @@
   - bandj's field construction and its zero divergence, and mag_init as
     its inverse;
   - magdealias as the 2/3 rule;
-  - the diagnostics.
+  - the diagnostics;
+  - the whole step loop, which keeps the conductive polytrope fixed.
 """
 import numpy as np
 import pytest
@@ -883,3 +884,30 @@ def test_global_averages_remove_mean_momentum():
     np.testing.assert_allclose(o.get("v"), v - d["vbar"], rtol=0, atol=1e-15)
     st, d = o.diag()
     assert abs(d["ubar"]) < 1e-15 and abs(d["vbar"]) < 1e-15
+
+
+@pytest.mark.parametrize("perfect,radbc,constflux", [(0, 0, 0), (1, 0, 0), (0, 1, 1)])
+def test_static_polytrope_is_a_fixed_point_of_the_step(perfect, radbc, constflux):
+    """The whole step loop (src/main.F90:340-747: RHS, AB3, dealias, bandj,
+    boundaries, diagnostics, calcdt) keeps the m = 1 conductive polytrope
+    with a uniform field unchanged. Every RHS is zero, the boundary
+    conditions hold for a linear T (radbc: T = 1 is the root of the
+    radiative condition; constflux: the top flux is theta), and the uniform
+    field is its own potential decomposition. Time advances by the step
+    count times dt, across the 10-step dealias and calcdt cadence and the
+    diagnostics every 5 steps."""
+    p = default_params()
+    p.nx, p.ny, p.nz = 8, 8, 17
+    p.noise_amp, p.cm, p.kappa_uniform = 0.0, 1.0, 1
+    p.perfect, p.radbc, p.constflux, p.ndu06 = perfect, radbc, constflux, 5
+    o = O.Oracle(p)
+    o.static()
+    o.mag_init()
+    dt = o.calcdt()
+    s0 = o.state()
+    assert o.step(25) == 0
+    s1 = o.state()
+    for name in s0:
+        assert np.abs(s1[name] - s0[name]).max() < 1e-12, name
+    sc = o.scalars()
+    assert sc.iter == 25 and abs(sc.ttime - 25 * dt) < 1e-15
