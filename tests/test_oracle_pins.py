@@ -951,3 +951,40 @@ def test_step_commutes_with_horizontal_symmetries(sym):
     for n in fields:
         scale = max(1.0, np.abs(a[n]).max())
         assert np.abs(act(n, a[n]) - b[n]).max() < 1e-14 * scale * 10, n
+
+
+def test_magnetic_step_commutes_with_horizontal_shifts():
+    """The MHD step loop (mag_init's seed field, induction, bandj, the
+    mean-field equations) commutes with a horizontal grid shift. The
+    spectral potentials are shifted through the inverse and forward
+    transforms. 12 steps agree to rounding, B measured against its
+    largest component."""
+    shift = (2, 3)
+    real = ("r", "t", "u", "v", "w", "bx", "by", "bz", "jsq")
+
+    def run(shifted):
+        p = default_params()
+        p.nx, p.ny, p.nz = 16, 12, 13
+        p.noise_amp, p.dynamo = 0.1, 1
+        o = O.Oracle(p)
+        o.static()
+        o.mag_init()
+        if shifted:
+            for n in real:
+                o.set(n, np.roll(o.get(n), shift, axis=(1, 2)))
+            for n in ("pol", "tor"):
+                o.set(n, o.forwardfft(np.roll(o.inversefft(o.get(n)), shift, axis=(1, 2))))
+        o.calcdt()
+        assert o.step(12) == 0
+        out = {n: o.get(n) for n in real}
+        out["pol"], out["tor"] = o.inversefft(o.get("pol")), o.inversefft(o.get("tor"))
+        return out, o.get_mean("bxbar"), o.get_mean("bybar")
+
+    a, axb, ayb = run(False)
+    b, bxb, byb = run(True)
+    bscale = max(np.abs(a[n]).max() for n in ("bx", "by", "bz"))
+    for n in a:
+        scale = bscale if n in ("bx", "by", "bz") else np.abs(a[n]).max()
+        assert np.abs(np.roll(a[n], shift, axis=(1, 2)) - b[n]).max() <= 1e-12 * scale, n
+    for m, mm in ((axb, bxb), (ayb, byb)):
+        assert np.abs(m - mm).max() <= 1e-12 * np.abs(m).max()
