@@ -1,6 +1,7 @@
 """Host-side logic of the library, run without a GPU: exported symbols, the
-INPUT parser (src/initial.F90:94-201) and the NetCDF snapshot codec
-(src/netcdf.F90 layout) against scipy's independent NetCDF reader."""
+Fortran / C / Python bindings against each other, the INPUT parser
+(src/initial.F90:94-201) and the NetCDF snapshot codec (src/netcdf.F90
+layout) against scipy's independent NetCDF reader."""
 import os
 import re
 
@@ -132,3 +133,59 @@ def test_reads_reference_restart():
         assert d["iteration"] == int(f.variables["iteration"][0])
         assert d["time"] == float(f.variables["time"][0])
         assert d["ck"] == float(f.ck) and d["f"] == float(f.f)
+
+
+def _c_struct_members(hdr, name):
+    """(type, member) pairs of `typedef struct name { ... }` in order."""
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        ctype, rest = decl.split(None, 1)
+        out += [(ctype, m.strip()) for m in rest.split(",")]
+    return out
+
+
+def _f_type_members(src, name):
+    body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type %s" % (name, name), src, re.S).group(1)
+    out = []
+    for line in body.splitlines():
+        m = re.match(r"\s*(real\(c_double\)|integer\(c_int32_t\))\s*::\s*(.*)", line)
+        if m:
+            ftype = {"real(c_double)": "double", "integer(c_int32_t)": "int32_t"}[m.group(1)]
+            out += [(ftype, v.strip()) for v in m.group(2).split(",")]
+    return out
+
+
+def test_fortran_c_and_python_bindings_agree():
+    """The drop-in boundary three ways: the Fortran module
+    (include/vec_mod.f90), the C header (include/vec.h) and the Python
+    ctypes structures must lay out vec_params, vec_scalars and vec_diag_out
+    identically, member by member. The field ids must match. Every function
+    the Fortran module binds must be declared in the header and exported by
+    the library."""
+    import ctypes as C
+    from fug30v0kxc_gb300 import params as P
+    hdr = open(os.path.join(ROOT, "include", "vec.h")).read()
+    fsrc = open(os.path.join(ROOT, "include", "vec_mod.f90")).read()
+    py = {"vec_params": P.VecParams, "vec_scalars": P.VecScalars, "vec_diag_out": P.VecDiag}
+    pytype = {C.c_double: "double", C.c_int32: "int32_t"}
+    for name, cls in py.items():
+        c = _c_struct_members(hdr, name)
+        f = _f_type_members(fsrc, name)
+        p = [(pytype[t], n) for n, t in cls._fields_]
+        assert c == f, (name, c, f)
+        assert c == p, (name, c, p)
+    fids = dict((k, int(v)) for k, v in re.findall(r"(VEC_F_[A-Z]+) = (\d+)", fsrc))
+    assert fids and all(getattr(P, k[4:]) == v for k, v in fids.items() if hasattr(P, k[4:]))
+    assert [fids[f"VEC_F_{n.upper()}"] for n in ("r", "t", "u", "v", "w", "bx", "by", "bz", "jsq", "pol", "tor")] \
+        == list(range(11))
+    names = re.findall(r"bind\(C, name='(vec_\w+)'\)", fsrc)
+    assert len(names) >= 40
+    L = lib.load()
+    for n in names:
+        assert re.search(r"\b%s\s*\(" % n, hdr), n
+        assert hasattr(L, n), n
