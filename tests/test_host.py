@@ -189,3 +189,12 @@ def test_fortran_c_and_python_bindings_agree():
     for n in names:
         assert re.search(r"\b%s\s*\(" % n, hdr), n
         assert hasattr(L, n), n
+    # argument counts of each bound function against its C prototype
+    hdr_nc = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    funcs = re.findall(r"function (vec_\w+)\(([^)]*)\)\s*bind\(C, name='(vec_\w+)'\)", fsrc)
+    assert len(funcs) == len(names)
+    for _, fargs, cname in funcs:
+        fa = [a for a in fargs.replace("&", "").split(",") if a.strip()]
+        proto = re.search(r"\b%s\s*\(([^)]*)\)\s*;" % cname, hdr_nc, re.S).group(1)
+        ca = [a for a in proto.split(",") if a.strip() and a.strip() != "void"]
+        assert len(fa) == len(ca), (cname, len(fa), len(ca))
