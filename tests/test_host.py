@@ -24,6 +24,13 @@ def test_library_exports_every_header_symbol():
     for n in sorted(names):
         assert hasattr(L, n), n
         assert n in lib.SIGNATURES, f"{n} has no ctypes signature"
+    # every ctypes signature takes as many arguments as its C prototype
+    hdr_nc = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    for n, (_, args) in lib.SIGNATURES.items():
+        proto = re.search(r"\b%s\s*\(([^)]*)\)\s*;" % n, hdr_nc, re.S)
+        assert proto, f"{n} is not declared in vec.h"
+        ca = [a for a in proto.group(1).split(",") if a.strip() and a.strip() != "void"]
+        assert len(ca) == len(args), (n, len(args), len(ca))
 
 
 INPUT_TEXT = """data file for parallel magnetoconvection program
