@@ -334,6 +334,83 @@ def net_line(args, ws):
             "gpu_launches": launches}
 
 
+def accuracy_line(args, ws):
+    """The split form's accuracy at 256^2x129 (eta contrast 20) against the
+    FP64 form, the drop-in whose every kernel is parity-checked against the
+    oracle: both start from the same seeded static state and run the time
+    loop with diagnostics every --acc-every steps (GlobalAverages, nusselt,
+    checkdivb at their reference cadence, src/main.F90:552-647).
+
+    Reported: per-field relative L2 of the split state against the FP64
+    state after 100 steps (r and T as deviations from the static polytrope),
+    and the time averages over the second half of the run of the top
+    Nusselt number (the fixed-flux bottom makes the reference's bottom one
+    identically 1), the kinetic energy, the magnetic energy and the energy
+    of the field perturbation, with their relative differences."""
+    import numpy as np
+    from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT, config1
+    from fug30v0kxc_gb300.solver import P3D
+    total, every = args.acc_steps, args.acc_every
+    runs = {}
+    for name, prec in (("split", VEC_PREC_SPLIT), ("fp64", VEC_PREC_FP64)):
+        p = config1(precision=prec)
+        p.ndu06 = every
+        g = P3D(p)
+        g.start()
+        t0 = time.perf_counter()
+        assert g.step(100) == 0
+        z = np.arange(p.nz) / (p.nz - 1)
+        bg = (1.0 + p.theta * z)[:, None, None]
+        s100 = {n: g.get(n) - (bg ** p.cm if n == "r" else bg if n == "t" else 0.0)
+                for n in ("r", "t", "u", "v", "w", "pol", "tor")}
+        rows = []
+        done = 100
+        while done < total:
+            n = every - done % every
+            st = g.step(n)
+            assert st == 0, f"{name}: step status {st} at {done + n}"
+            done += n
+            d = g.last_diag()
+            bx, by, bz = g.get("bx"), g.get("by"), g.get("bz")
+            e = (bx * bx + by * by + (bz - g.bzbar) ** 2).sum(axis=(1, 2))
+            e[0] *= 0.5
+            e[-1] *= 0.5
+            mep = p.f * 0.5 * e.sum() * (p.xmax / p.nx) * (p.ymax / p.ny) / (p.nz - 1)
+            rows.append((done, g.scalars().ttime, g.top_nusselt(), d["kenergy"], d["menergy"], mep, d["nusselt"]))
+        g.sync()
+        runs[name] = {"s100": s100, "rows": np.array(rows), "wall_s": time.perf_counter() - t0}
+        g.close()
+    rel_l2 = {n: float(np.linalg.norm((runs["split"]["s100"][n] - runs["fp64"]["s100"][n]).ravel())
+                       / max(np.linalg.norm(runs["fp64"]["s100"][n].ravel()), 1e-300))
+              for n in runs["fp64"]["s100"]}
+    half = total // 2
+    avgs = {}
+    for name in runs:
+        r = runs[name]["rows"]
+        sel = r[r[:, 0] > half]
+        avgs[name] = {"nusselt_top": float(sel[:, 2].mean()), "kenergy": float(sel[:, 3].mean()),
+                      "menergy": float(sel[:, 4].mean()), "menergy_perturbation": float(sel[:, 5].mean()),
+                      "nusselt_bottom": float(sel[:, 6].mean()), "samples": int(len(sel)),
+                      "model_time": [float(sel[0, 1]), float(sel[-1, 1])]}
+    diffs = {k: abs(avgs["split"][k] - avgs["fp64"][k]) / max(abs(avgs["fp64"][k]), 1e-300)
+             for k in ("nusselt_top", "kenergy", "menergy", "menergy_perturbation")}
+    series = {name: [[float(x) for x in row[:6]] for row in runs[name]["rows"][:: max(1, len(runs[name]["rows"]) // 20)]]
+              for name in runs}
+    value = max(diffs.values())
+    return {"metric": "split vs FP64 at 256^2x129: max relative difference of the time-averaged top Nusselt "
+                      "number, kinetic, magnetic and perturbation magnetic energy over the second half of the run",
+            "value": value, "unit": "fraction", "n_gpus": ws, "steps": total, "warmup": 0,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 vs f64",
+            "data": "synthetic (seeded static polytrope + uniform +-1e-3 T noise)",
+            "config": {"workload": WORKLOAD + " accuracy", "nx": NX, "ny": NY, "nz": NZ, "steps": total,
+                       "diag_every": every, "average_over_steps": [half, total]},
+            "within_1pct": bool(value <= 0.01),
+            "rel_l2_after_100_steps": rel_l2, "time_averages": avgs, "relative_differences": diffs,
+            "wall_s": {k: round(v["wall_s"], 1) for k, v in runs.items()},
+            "series_columns": ["step", "time", "nusselt_top", "kenergy", "menergy", "menergy_perturbation"],
+            "series": series}
+
+
 def cpu_baseline(nsteps, precision_note=""):
     """The oracle (plain C restatement, OpenMP over planes) on the host cores."""
     from oracle import oracle as O
@@ -475,9 +552,13 @@ def main():
                     help="closure workload: DNS steps of the comparison window (0: 8000 full, 2000 small)")
     ap.add_argument("--closure-judge-every", type=int, default=2000,
                     help="closure workload: coarse steps between judged fine segments")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "large", "closure", "net"],
+    ap.add_argument("--acc-steps", type=int, default=20000, help="accuracy workload: steps of each run")
+    ap.add_argument("--acc-every", type=int, default=100, help="accuracy workload: diagnostics cadence")
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "ensemble", "large", "closure", "net", "accuracy"],
                     help="ensemble: the 48-member batched ensemble as the headline line; "
-                         "large: one 1024^2x513 instance, Ra 1e7, Q 1e4, eta contrast 50 (split)")
+                         "large: one 1024^2x513 instance, Ra 1e7, Q 1e4, eta contrast 50 (split); "
+                         "accuracy: split against FP64 at 256^2x129 over --acc-steps steps")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer measurement (very large grids)")
     ap.add_argument("--no-ensemble", action="store_true",
@@ -517,8 +598,8 @@ def main():
     torch.cuda.set_device(local)
     from fug30v0kxc_gb300.params import VEC_PREC_FP64, VEC_PREC_SPLIT
     hbm, pk = peaks()
-    if args.workload in ("closure", "net"):
-        line = closure_line(args, ws) if args.workload == "closure" else net_line(args, ws)
+    if args.workload in ("closure", "net", "accuracy"):
+        line = {"closure": closure_line, "net": net_line, "accuracy": accuracy_line}[args.workload](args, ws)
         if rank == 0:
             print(json.dumps(line), flush=True)
         if _dist["on"]:

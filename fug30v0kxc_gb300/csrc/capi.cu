@@ -397,7 +397,7 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     for (int i = 0; i < W_COUNT; i++) E.wk[i] = (char *)E.wblock + esz * n * (size_t)i;
     for (int i = 0; i < 3; i++) ALLOC(E.s64[i], sizeof(double) * n);
     E.red_blocks = 152 * 4;
-    ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 24 + 64));
+    ALLOC(E.red, sizeof(double) * ((size_t)nz * 8 + 8 + (size_t)E.red_blocks * 25 + 64));
     ALLOC(E.ds, sizeof(DevScalars));
     ALLOC(E.cdt, sizeof(float) * (4 + 3 * (size_t)cdt_chunks(E.n)));
     if ((st = cdt_init(E.cdt))) { vec_destroy(c); return st; }
@@ -457,7 +457,10 @@ extern "C" int vec_sync(vec_ctx *c)
     int err = 0;
     CUDA_TRY(cudaMemcpy(&err, c->E.dev_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
-        vec_set_error("a bounded device wait ran out (TMA tile load did not complete)");
+        // reported once: the flag is cleared, the context stays usable
+        CUDA_TRY(cudaMemset(c->E.dev_err, 0, sizeof(int)));
+        vec_set_error(err == 2 ? "a bounded device wait ran out (wait self-test)"
+                               : "a bounded device wait ran out (TMA tile load did not complete)");
         return VEC_ERR_CUDA;
     }
     return VEC_OK;
@@ -656,6 +659,10 @@ extern "C" int vec_calcdt(vec_ctx *c, double *dt)
     CUDA_TRY(cudaMemcpyAsync(E.hs, E.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E.stream));
     CUDA_TRY(cudaStreamSynchronize(E.stream));
     if (dt) *dt = E.hs->dt;
+    if (E.hs->nonfinite) {
+        vec_set_error("non-finite value in the state (calcdt)");
+        return VEC_ERR_NAN;
+    }
     return VEC_OK;
 }
 
@@ -683,6 +690,32 @@ static int line_op(vec_ctx *c, int dir, const double *fin, double *f1, int op1, 
     if ((st = stage_out(E, f1, E.s64[1], E.n))) return st;
     if (op2 != OP_NONE && (st = stage_out(E, f2, E.s64[2], E.n))) return st;
     return VEC_OK;
+}
+
+// FP32 line operators: the kernels the split form's time step runs, on
+// caller data (host or device), through the context's scratch
+extern "C" int vec_line_f32(vec_ctx *c, int dir, int op1, int op2, const float *fin, float *f1, float *f2)
+{
+    if (!c || !fin || !f1 || (dir != 0 && dir != 1)) return VEC_ERR_ARG;
+    if (op1 < OP_D1 || op1 > OP_INV || (op2 != OP_NONE && (op2 < OP_D1 || op2 > OP_D2 || op1 == OP_FWD ||
+                                                           op1 == OP_INV || !f2)))
+        return VEC_ERR_ARG;
+    Engine &E = c->E;
+    // each FP64 scratch field holds 2n floats
+    float *in = reinterpret_cast<float *>(E.s64[0]), *o1 = reinterpret_cast<float *>(E.s64[1]);
+    float *o2 = reinterpret_cast<float *>(E.s64[2]);
+    const size_t bytes = sizeof(float) * E.n;
+    CUDA_TRY(cudaMemcpyAsync(in, fin, bytes, is_device_ptr(fin) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             E.stream));
+    LineJob<float> j = ljob<float>(in, o1, op1, op2 != OP_NONE ? o2 : nullptr, op2);
+    int st = launch_lines<float>(&E, dir, &j, 1);
+    if (st) return st;
+    CUDA_TRY(cudaMemcpyAsync(f1, o1, bytes, is_device_ptr(f1) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             E.stream));
+    if (op2 != OP_NONE)
+        CUDA_TRY(cudaMemcpyAsync(f2, o2, bytes, is_device_ptr(f2) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 E.stream));
+    return vec_sync(c);
 }
 
 extern "C" int vec_nc_write(const char *path, const vec_snapshot *s, int iprec);
@@ -923,15 +956,33 @@ static int one_step(Engine &E)
     return enqueue_step(E, diag_due(E, E.nit));
 }
 
+// The non-finite check that rides on calcdt: one 4-byte read-back and a
+// stream synchronisation, after the steps of a call that ran calcdt.
+static int check_nonfinite(Engine &E)
+{
+    CUDA_TRY(cudaMemcpyAsync(&E.hs->nonfinite, &E.ds->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
+    CUDA_TRY(cudaStreamSynchronize(E.stream));
+    if (E.hs->nonfinite) {
+        vec_set_error("non-finite value in the state (calcdt of the time loop)");
+        return VEC_ERR_NAN;
+    }
+    return VEC_OK;
+}
+
 extern "C" int vec_step(vec_ctx *c, int nsteps)
 {
     if (!c || nsteps < 0) return VEC_ERR_ARG;
+    bool cdt = false;
     for (int s = 0; s < nsteps; s++) {
+        cdt = cdt || (c->E.nit + 1) % 10 == 0;
         int st = one_step(c->E);
         if (st) { c->E.prof_flush(); return st; }
     }
-    if (c->E.prof_on) return c->E.prof_flush();
-    return VEC_OK;
+    if (c->E.prof_on) {
+        int st = c->E.prof_flush();
+        if (st) return st;
+    }
+    return cdt ? check_nonfinite(c->E) : VEC_OK;
 }
 
 extern "C" int vec_last_diag(vec_ctx *c, vec_diag_out *out)

@@ -1110,7 +1110,12 @@ extern "C" int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, 
         }
         if (pending && sc.ttime >= t_check) {
             int divb = 0;
-            if ((st = diag(coarse, &dc, &nutc, &divb))) return st;
+            st = diag(coarse, &dc, &nutc, &divb);
+            if (st == VEC_ERR_NAN) {   // the coarse state is no longer finite
+                rep->blowup = 1;
+                return fall_back(step);
+            }
+            if (st) return st;
             const double e0 = fmax(rel(dc.nusselt, dfine.nusselt), rel(nutc, nutf));
             const double e1 = rel(dc.kenergy, dfine.kenergy);
             const double e2 = mag_on(engine_of(coarse)) ? rel(dc.menergy, dfine.menergy) : 0.0;
@@ -1133,11 +1138,21 @@ extern "C" int vec_closure_run(vec_closure *cl, vec_ctx *coarse, vec_ctx *fine, 
             t_check = sf.ttime;
             pending = 1;
         }
-        if ((st = vec_closure_step(cl, coarse, 1))) return st;
+        st = vec_closure_step(cl, coarse, 1);
+        if (st == VEC_ERR_NAN) {   // the time loop's non-finite check
+            rep->blowup = 1;
+            return fall_back(step + 1);
+        }
+        if (st) return st;
         step += 1;
         rep->coarse_steps += 1;
         int divb = 0;
-        if (diag_every > 0 && step % diag_every == 0 && (st = record(coarse, &divb))) return st;
+        st = diag_every > 0 && step % diag_every == 0 ? record(coarse, &divb) : VEC_OK;
+        if (st == VEC_ERR_NAN) {
+            rep->blowup = 1;
+            return fall_back(step);
+        }
+        if (st) return st;
         if (divb) {
             rep->divb_fail = 1;
             return fall_back(step);

@@ -87,6 +87,9 @@ struct DevScalars {
     // reductions
     unsigned long long velmxx, velmxz, denmn;  // order-preserving keys of the reductions
     double res[64];                            // diagnostics results
+    // the last calcdt met a non-finite value (NaN or infinity) in the state
+    // or in the CFL expression; the time loop reports it as VEC_ERR_NAN
+    int nonfinite, pad_nf;
 };
 
 // AB3 coefficients of src/main.F90:381-403 from the step sizes (read-only)

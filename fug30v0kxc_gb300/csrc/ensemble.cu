@@ -132,9 +132,11 @@ extern "C" int vec_ensemble_step(vec_ens *e, int nsteps)
     const int nm = (int)e->m.size();
     int st0 = members_to_root(e);
     if (st0) return st0;
+    bool cdt = false;
     for (int s = 0; s < nsteps; s++) {
         // all members advance together, so they share nit
         const int nit = engine_of(e->m[0]).nit + 1;
+        cdt = cdt || nit % 10 == 0;
         bool eager = false;
         for (auto c : e->m) {
             Engine &E = engine_of(c);
@@ -181,7 +183,23 @@ extern "C" int vec_ensemble_step(vec_ens *e, int nsteps)
         CUDA_TRY(cudaGraphLaunch(e->g[v], e->root));
     }
     // whatever the caller does next on a member's stream follows the steps
-    return root_to_members(e);
+    int st = root_to_members(e);
+    if (st || !cdt) return st;
+    // the non-finite check of the calcdt reductions: one 4-byte read-back
+    // per member, then one wait per member stream
+    for (auto c : e->m) {
+        Engine &E = engine_of(c);
+        CUDA_TRY(cudaMemcpyAsync(&E.hs->nonfinite, &E.ds->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
+    }
+    for (int i = 0; i < nm; i++) {
+        Engine &E = engine_of(e->m[i]);
+        CUDA_TRY(cudaStreamSynchronize(E.stream));
+        if (E.hs->nonfinite) {
+            vec_set_error("ensemble member %d: non-finite value in the state (calcdt of the time loop)", i);
+            return VEC_ERR_NAN;
+        }
+    }
+    return VEC_OK;
 }
 
 extern "C" int vec_ensemble_sync(vec_ens *e)
@@ -289,5 +307,15 @@ extern "C" int vec_tunables(vec_ctx *c, int *kc, int *s)
     Engine &E = engine_of(c);
     if (kc) *kc = E.kc_pass2;
     if (s) *s = E.ct_s;
+    return VEC_OK;
+}
+
+extern "C" int vec_set_tunables(vec_ctx *c, int kc, int s)
+{
+    if (!c || (kc != 8 && kc != 16 && kc != 32) || (s != 0 && s != 4 && s != 8)) return VEC_ERR_ARG;
+    Engine &E = engine_of(c);
+    E.kc_pass2 = kc;
+    E.ct_s = s;
+    E.drop_graphs();   // captured steps hold the old launch shapes
     return VEC_OK;
 }

@@ -170,10 +170,11 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
 }
 // bounded wait: returns false (and the caller reports an error) if the
 // barrier phase does not complete within the iteration limit
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+#define MBAR_POLLS (1LL << 24)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long polls = MBAR_POLLS)
 {
     const unsigned a = smem_u32(bar);
-    for (long it = 0; it < (1L << 24); it++) {
+    for (long long it = 0; it < polls; it++) {
         unsigned ok;
         asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                      : "=r"(ok) : "r"(a), "r"(parity) : "memory");
@@ -286,19 +287,29 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     for (int t = blockIdx.x; t < total; t += gridDim.x, it++) {
         R *cur = (it & 1) ? tile1 : tile0;
         R *nxt = (it & 1) ? tile0 : tile1;
+        bool issued_next = false;
         if (t + (int)gridDim.x < total) {
             if (WS && it >= 1 && tid == 0) {
                 // every warp has read buffer nxt (its use in iteration it - 1)
                 if (!mbar_wait(&bar[2 + ((it + 1) & 1)], ((it - 1) >> 1) & 1)) {
+                    // report, then let this tile's copy (still in flight)
+                    // land before the CTA's shared memory is released
                     atomicExch(err, 1);
+                    mbar_wait(&bar[it & 1], (it >> 1) & 1);
                     return;
                 }
             }
             if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(t + gridDim.x, nxt, &bar[(it + 1) & 1]);
+            issued_next = true;
         }
         if (!mbar_wait(&bar[it & 1], (it >> 1) & 1)) {
-            if (tid == 0) atomicExch(err, 1);
+            if (tid == 0) {
+                // report, then wait (bounded) for the copies this CTA issued
+                atomicExch(err, 1);
+                mbar_wait(&bar[it & 1], (it >> 1) & 1);
+                if (issued_next) mbar_wait(&bar[(it + 1) & 1], ((it + 1) >> 1) & 1);
+            }
             return;
         }
         const int job = t / (nz * tpp);
@@ -470,6 +481,28 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             sync();
         }
     }
+}
+
+// Self-test of the bounded-wait error path: one thread waits on an mbarrier
+// that nothing arrives on, gives up after `polls` polls and raises the
+// context's error flag exactly as the line kernel does when a tile load does
+// not complete.  No copy is in flight, so nothing has to be drained.
+__global__ void k_wait_selftest(long long polls, int *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait(&bar, 0, polls)) atomicExch(err, 2);
+}
+
+extern "C" int vec_selftest_wait(vec_ctx *c, long long polls)
+{
+    if (!c || polls < 1 || polls > MBAR_POLLS) return VEC_ERR_ARG;
+    Engine &E = engine_of(c);
+    k_wait_selftest<<<1, 32, 0, E.stream>>>(polls, E.dev_err);
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
 }
 
 // ---- host side ------------------------------------------------------------------------

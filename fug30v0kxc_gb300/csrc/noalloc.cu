@@ -113,7 +113,13 @@ __global__ void k_noalloc_final(const double *scratch, int nblocks, NoallocLimit
 
 // Looks up the device address of the scratch array for the current device.
 // The first call on each device does this; it must not be the first thing
-// the process does inside a stream capture.
+// the process does inside a stream capture.  With CUDA's lazy module loading
+// (the default since CUDA 12.2) this lookup is also what loads this file's
+// module onto the device, and with it the 1.5 MiB array: the first call on a
+// device therefore needs that much free device memory, and callers whose
+// pool later takes the whole device make it at set-up, before the pool
+// reserves its memory (or run with CUDA_MODULE_LOADING=EAGER, which loads
+// every module when the library's first CUDA call creates the context).
 static int noalloc_scratch(double **out)
 {
     int dev = -1;
@@ -136,14 +142,18 @@ static int noalloc_scratch(double **out)
     return VEC_OK;
 }
 
-static bool noalloc_is_device(const void *p)
+// 1: memory of device dev (device or managed), 0: host memory, -1: memory
+// of another device (a kernel on dev would read or write a peer's memory)
+static int noalloc_where(const void *p, int dev)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeDevice) return a.device == dev ? 1 : -1;
+    if (a.type == cudaMemoryTypeManaged) return 1;
+    return 0;
 }
 
 extern "C" int vec_calcdt_noalloc(const vec_params *p, const double *u, const double *v, const double *w,
@@ -167,6 +177,19 @@ extern "C" int vec_calcdt_noalloc(const vec_params *p, const double *u, const do
     double *scratch = nullptr;
     int st = noalloc_scratch(&scratch);
     if (st) return st;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    const double *fields[8] = { u, v, w, r, t, bx, by, bz };
+    for (int i = 0; i < 8; i++)
+        if (noalloc_where(fields[i], dev) != 1) {
+            vec_set_error("vec_calcdt_noalloc: field %d is not device memory of the current device %d", i, dev);
+            return VEC_ERR_ARG;
+        }
+    const int out_where = noalloc_where(dt_out, dev);
+    if (out_where < 0) {
+        vec_set_error("vec_calcdt_noalloc: dt_out is device memory of another device than the current one (%d)", dev);
+        return VEC_ERR_ARG;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     // constants of src/constants.f90:62-107 (only those calcdt reads)
     NoallocLimits L;
@@ -187,7 +210,7 @@ extern "C" int vec_calcdt_noalloc(const vec_params *p, const double *u, const do
     }
     const int nblocks = (int)((n + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK);
     k_noalloc_partials<<<nblocks, 256, 0, s>>>(u, v, w, r, t, bx, by, bz, n, sqrt(p->gamma), p->f, scratch);
-    const bool dev_out = noalloc_is_device(dt_out);
+    const bool dev_out = out_where == 1;
     double *res = dev_out ? dt_out : scratch + 3 * (size_t)NOALLOC_MAX_BLOCKS;
     k_noalloc_final<<<1, 1024, 0, s>>>(scratch, nblocks, L, res);
     cudaError_t e = cudaGetLastError();

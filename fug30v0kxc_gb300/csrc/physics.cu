@@ -682,6 +682,7 @@ __device__ __forceinline__ void cdt_reset_keys(unsigned *gkey)
     gkey[0] = 0u;              // below every float's key
     gkey[1] = 0u;
     gkey[2] = 0xffffffffu;     // above every float's key
+    gkey[3] = 0u;              // no non-finite value seen
 }
 __global__ void k_cdt_init(unsigned *gkey) {
     PDL_WAIT(); cdt_reset_keys(gkey); }
@@ -740,14 +741,22 @@ __global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
     const size_t i0 = (size_t)blockIdx.x * CDT_CHUNK;
     const size_t i1 = i0 + CDT_CHUNK < a.n ? i0 + CDT_CHUNK : a.n;
     float mx = -INFINITY, mz = -INFINITY, mn = INFINITY;
+    // A NaN or infinity in u, v, w, T, B makes the speed estimates non-finite,
+    // and one in rho its own estimate (a negative T or rho gives a NaN square
+    // root, as in the FP64 expression); fmaxf / fminf would skip NaNs, so they
+    // are counted separately.
+    int bad = 0;
     for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const CdtEst e = cdt_estimate(a, i);
         mx = fmaxf(mx, e.xx);
         mz = fmaxf(mz, e.xz);
         mn = fminf(mn, e.r);
+        bad |= !(isfinite(e.xx) && isfinite(e.xz) && isfinite(e.r));
     }
+    bad = __syncthreads_or(bad);
     block_reduce3(mx, mz, mn, sh);
     if (threadIdx.x == 0) {
+        if (bad) atomicOr(&a.gkey[3], 1u);
         a.chunk[blockIdx.x] = mx;
         a.chunk[a.nchunks + blockIdx.x] = mz;
         a.chunk[2 * a.nchunks + blockIdx.x] = mn;
@@ -818,6 +827,7 @@ __global__ void k_calcdt_fin(DevScalars *ds, unsigned *gkey, double dd, double d
         m = fmin(m, 0.2 * dz * dz / eta_max);
     }
     ds->dt = sf * m;
+    ds->nonfinite = gkey[3] != 0u;
     ds->res[60] = velmxx; ds->res[61] = velmxz; ds->res[62] = denmn;
     ds->velmxx = OKEY_NEG_HUGE; ds->velmxz = OKEY_NEG_HUGE; ds->denmn = OKEY_POS_HUGE;
     cdt_reset_keys(gkey);
@@ -912,6 +922,7 @@ __global__ void k_minmax(const double *r, const double *t, const double *u, cons
     double mn[NMM], mx[NMM];
     for (int m = 0; m < NMM; m++) { mn[m] = 1.0e300; mx[m] = -1.0e300; }
     const size_t n = np * nz;
+    int bad = 0;    // a NaN or infinity among the state values or div B (fmin / fmax skip NaNs)
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         int k = (int)(i / np);
         size_t q = i - (size_t)k * np;
@@ -924,7 +935,12 @@ __global__ void k_minmax(const double *r, const double *t, const double *u, cons
         vals[10] = (uu * uu + vv * vv + ww * ww);
         vals[11] = dxbx[i] + dyby[i] + zd1(bz + q, np, k, nz, 5, ho12);
         for (int m = 0; m < NMM; m++) { mn[m] = fmin(mn[m], vals[m]); mx[m] = fmax(mx[m], vals[m]); }
+        bool fin = isfinite(vals[11]);
+#pragma unroll
+        for (int m = 0; m < 8; m++) fin = fin && isfinite(vals[m]);
+        bad |= !fin;
     }
+    bad = __syncthreads_or(bad);
     for (int m = 0; m < NMM; m++)
         for (int o = 16; o > 0; o >>= 1) {
             mn[m] = fmin(mn[m], __shfl_xor_sync(0xffffffffu, mn[m], o));
@@ -942,6 +958,8 @@ __global__ void k_minmax(const double *r, const double *t, const double *u, cons
         out[(size_t)blockIdx.x * 2 * NMM + m] = a;
         out[(size_t)blockIdx.x * 2 * NMM + NMM + m] = b;
     }
+    // one flag per CTA after the min/max block
+    if (threadIdx.x == 0) out[(size_t)gridDim.x * 2 * NMM + blockIdx.x] = bad ? 1.0 : 0.0;
 }
 
 __global__ void k_nusselt_sum(const double *t, size_t np, int nz, double dz, double *out)
@@ -981,7 +999,7 @@ int phys_diag(Engine *E, vec_diag_out *out)
     KLAUNCH(E, "minmax", k_minmax, blocks, 256, E->r, E->t, E->u, E->v, E->w, E->bx, E->by, E->bz, E->s64[0],
             E->s64[1], E->np, E->nz, c.ho12, mm);
     CUDA_TRY(cudaMemcpyAsync(E->hs, E->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, E->stream));
-    std::vector<double> h((size_t)blocks * 2 * NMM + 8);
+    std::vector<double> h((size_t)blocks * (2 * NMM + 1) + 8);
     CUDA_TRY(cudaMemcpyAsync(h.data(), nus, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, E->stream));
     CUDA_TRY(cudaStreamSynchronize(E->stream));
     vec_diag_out d;
@@ -1012,6 +1030,11 @@ int phys_diag(Engine *E, vec_diag_out *out)
     if (out) *out = d;
     E->last_diag = d;
     E->have_diag = 1;
+    for (int b = 0; b < blocks; b++)
+        if (h[8 + (size_t)blocks * 2 * NMM + b] != 0.0) {
+            vec_set_error("non-finite value in the state or in div B (diagnostics)");
+            return VEC_ERR_NAN;
+        }
     double divbtest = fmax(fabs(d.divbmax), fabs(d.divbmin));
     if (divbtest > 0.01) return VEC_ERR_DIVB;
     return VEC_OK;

@@ -5,8 +5,9 @@
  * Reads INPUT (src/initial.F90:94-201), starts from the static polytrope
  * (nframe 0) or restart.nc (nframe 1: parameters from the file; nframe 2:
  * parameters from INPUT), runs ntotal iterations of the time loop on the
- * GPU, prints the ndu06 diagnostics of src/main.F90:552-647 and writes the
- * T16_NNN.nc snapshots of src/main.F90:689-740.
+ * GPU, prints the ndu06 diagnostics of src/main.F90:552-647 (every value
+ * with 17 significant digits, as Fortran list-directed output prints a
+ * double) and writes the T16_NNN.nc snapshots of src/main.F90:689-740.
  *
  * Options not in INPUT (the reference hard-codes them, src/main.F90:108-116):
  *   --constflux --radbc --perfect --kinematic --dynamo --no-dealias
@@ -107,19 +108,19 @@ int main(int argc, char **argv)
             vec_diag_out d;
             CHECK(vec_get_scalars(ctx, &s));
             CHECK(vec_last_diag(ctx, &d));
-            printf("\n NIT= %d TTIME %.10e\n", nit, s.ttime);
-            printf(" ubar= %.8e vbar= %.8e\n", d.ubar, d.vbar);
-            printf(" divbmin= %.8e divbmax= %.8e\n", d.divbmin, d.divbmax);
-            printf(" alfvenmin= %.8e alfvenmax= %.8e\n", d.alfvenmin, d.alfvenmax);
-            printf(" machmin= %.8e machmax= %.8e\n", d.machmin, d.machmax);
-            printf(" rmsmin= %.8e rmsmax= %.8e\n", d.rmsmin, d.rmsmax);
-            printf(" rmin= %.8e rmax= %.8e\n tmin= %.8e tmax= %.8e\n", d.rmin, d.rmax, d.tmin, d.tmax);
-            printf(" umin= %.8e umax= %.8e\n vmin= %.8e vmax= %.8e\n", d.umin, d.umax, d.vmin, d.vmax);
-            printf(" wmin= %.8e wmax= %.8e\n", d.wmin, d.wmax);
-            printf(" bxmin= %.8e bxmax= %.8e\n bymin= %.8e bymax= %.8e\n", d.bxmin, d.bxmax, d.bymin, d.bymax);
-            printf(" bzmin= %.8e bzmax= %.8e\n\n", d.bzmin, d.bzmax);
-            printf(" magenergy= %.10e\n kinenergy= %.10e\n Nusselt= %.10e\n", d.menergy, d.kenergy, d.nusselt);
-            if (nit % 10 == 0) printf(" New value of dt %.10e\n", s.dt);
+            printf("\n NIT= %d TTIME %.16e\n", nit, s.ttime);
+            printf(" ubar= %.16e vbar= %.16e\n", d.ubar, d.vbar);
+            printf(" divbmin= %.16e divbmax= %.16e\n", d.divbmin, d.divbmax);
+            printf(" alfvenmin= %.16e alfvenmax= %.16e\n", d.alfvenmin, d.alfvenmax);
+            printf(" machmin= %.16e machmax= %.16e\n", d.machmin, d.machmax);
+            printf(" rmsmin= %.16e rmsmax= %.16e\n", d.rmsmin, d.rmsmax);
+            printf(" rmin= %.16e rmax= %.16e\n tmin= %.16e tmax= %.16e\n", d.rmin, d.rmax, d.tmin, d.tmax);
+            printf(" umin= %.16e umax= %.16e\n vmin= %.16e vmax= %.16e\n", d.umin, d.umax, d.vmin, d.vmax);
+            printf(" wmin= %.16e wmax= %.16e\n", d.wmin, d.wmax);
+            printf(" bxmin= %.16e bxmax= %.16e\n bymin= %.16e bymax= %.16e\n", d.bxmin, d.bxmax, d.bymin, d.bymax);
+            printf(" bzmin= %.16e bzmax= %.16e\n\n", d.bzmin, d.bzmax);
+            printf(" magenergy= %.16e\n kinenergy= %.16e\n Nusselt= %.16e\n", d.menergy, d.kenergy, d.nusselt);
+            if (nit % 10 == 0) printf(" New value of dt %.16e\n", s.dt);
         }
         if (p.ndu16 > 0 && nit % p.ndu16 == 0) {
             /* src/main.F90:695-740: float by default, double at the end and

@@ -144,6 +144,18 @@ class P3D:
         self._chk(self.L.vec_dealias(self.h, z.ctypes.data), "dealias")
         return z
 
+    # FP32 line kernels of the split form (VEC_OP_*: 1 d1, 2 d2, 3 dealias, 4 forward, 5 inverse)
+    def line_f32(self, direction, op1, f, op2=0):
+        f = np.ascontiguousarray(f, dtype=np.float32).reshape(self.shape)
+        a = np.empty_like(f)
+        b = np.empty_like(f) if op2 else None
+        self._chk(self.L.vec_line_f32(self.h, direction, op1, op2, f.ctypes.data, a.ctypes.data,
+                                      b.ctypes.data if op2 else None), "line_f32")
+        return (a, b) if op2 else a
+
+    def set_tunables(self, kc=16, s=0):
+        self._chk(self.L.vec_set_tunables(self.h, kc, s), "set_tunables")
+
     # -- src/dbydz.F90 ---------------------------------------------------------------
     def _oz(self, fn, f, flag, shape, name):
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(shape)
@@ -221,6 +233,11 @@ class P3D:
 
     def use_graphs(self, on=True):
         self._chk(self.L.vec_use_graphs(self.h, 1 if on else 0), "use_graphs")
+
+    def top_nusselt(self):
+        v = C.c_double()
+        self._chk(self.L.vec_top_nusselt(self.h, C.byref(v)), "top_nusselt")
+        return v.value
 
     def tunables(self):
         kc, s = C.c_int(), C.c_int()

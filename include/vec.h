@@ -144,7 +144,9 @@ int vec_set_scalars(vec_ctx *ctx, const vec_scalars *s);
 int vec_static(vec_ctx *ctx);
 /* B (real space) -> pol, tor, means, jsq; src/magnetic.f90:5-279 */
 int vec_mag_init(vec_ctx *ctx);
-/* CFL + diffusive time step, src/utils.F90:144-244; also stored as ctx dt */
+/* CFL + diffusive time step, src/utils.F90:144-244; also stored as ctx dt.
+ * VEC_ERR_NAN (dt still written) if a term of the CFL expression is not
+ * finite. */
 int vec_calcdt(vec_ctx *ctx, double *dt);
 
 /* ---- horizontal spectral operators, src/fft.F90:255-799 ---------------- */
@@ -165,6 +167,24 @@ int vec_d2bydz(vec_ctx *ctx, const double *fin, double *fout, int dflag);
 int vec_d1bydz1d(vec_ctx *ctx, const double *fin, double *fout, int dflag);
 int vec_d2bydz1d(vec_ctx *ctx, const double *fin, double *fout, int dflag);
 
+/* ---- FP32 forms of the horizontal operators ------------------------------
+ * The line kernels the split form's time step runs (FP32 data, FP32
+ * twiddles and multipliers), on caller data: dir 0 transforms along x
+ * (d1bydx, d2bydx, ... of src/fft.F90:255-489), dir 1 along y (:329-581).
+ * op1: VEC_OP_D1, VEC_OP_D2, VEC_OP_DEALIAS (one direction of
+ * src/fft.F90:586-682), VEC_OP_FWD (r2hc), VEC_OP_INV (hc2r divided by n);
+ * op2 (a second output from the same forward transform, as d2bydx's f1out /
+ * f2out pair): VEC_OP_NONE, VEC_OP_D1 or VEC_OP_D2, with op1 D1, D2 or
+ * DEALIAS.  Arrays are (nx,ny,nz) floats, host or device; any context
+ * precision. */
+#define VEC_OP_NONE         0
+#define VEC_OP_D1           1
+#define VEC_OP_D2           2
+#define VEC_OP_DEALIAS      3
+#define VEC_OP_FWD          4
+#define VEC_OP_INV          5
+int vec_line_f32(vec_ctx *ctx, int dir, int op1, int op2, const float *fin, float *f1out, float *f2out);
+
 /* ---- physics on the context's state ------------------------------------ */
 int vec_hydro_deriv(vec_ctx *ctx);   /* src/hydro_deriv.f90:5-505 -> slot 3 */
 int vec_mag_deriv(vec_ctx *ctx);     /* src/magnetic.f90:285-487 -> slot 3  */
@@ -177,13 +197,21 @@ int vec_mag_boundary(vec_ctx *ctx);  /* src/dbydz.F90:4205-4791             */
 int vec_ab3_update(vec_ctx *ctx);
 /* GlobalAverages (which removes the mean horizontal momentum from u,v),
  * nusselt, checkdivb, sminmax: src/utils.F90:22-371, src/dbydz.F90:4796-4925,
- * src/main.F90:552-647.  Returns VEC_ERR_DIVB when |div B| > 0.01. */
+ * src/main.F90:552-647.  Returns VEC_ERR_NAN when r, T, u, v, w, B or div B
+ * holds a NaN or an infinity (out is still written), else VEC_ERR_DIVB when
+ * |div B| > 0.01. */
 int vec_diag(vec_ctx *ctx, vec_diag_out *out);
 
 /* ---- the time loop ----------------------------------------------------- */
 /* nsteps iterations of src/main.F90:340-747 (no printing, no snapshots):
  * diagnostics every ndu06 steps, calcdt every 10, dealias every 10.
- * Returns VEC_ERR_DIVB / VEC_ERR_NAN if a check fails. */
+ * Returns VEC_ERR_DIVB if the div B check of a diagnostics step fails
+ * (src/main.F90:583-590).  Returns VEC_ERR_NAN if the state holds a NaN or
+ * an infinity: the diagnostics check r, T, u, v, w, B and div B, and calcdt
+ * checks the terms of its CFL expression (a negative T or rho counts, as
+ * its square root is not finite).  The calcdt check is read back once, at
+ * the end of a call whose steps ran calcdt; the steps of that call have
+ * then all been executed. */
 int vec_step(vec_ctx *ctx, int nsteps);
 /* Steps without diagnostics run as replays of a captured CUDA graph of one
  * step (two variants: plain, and the tenth step with dealias and calcdt);
@@ -226,14 +254,21 @@ int vec_read_restart(vec_ctx *ctx, const char *path);
 /* No counterpart in the reference.  calcdt (src/utils.F90:144-244) for
  * callers that cannot allocate device memory: programs whose device memory
  * is all handed out by their own arena or pool, and which therefore cannot
- * create a vec_ctx (vec_create allocates).  The caller passes device
- * pointers to the eight fields (nx*ny*nz doubles each, sizes taken from p)
- * and dt_out (device or host).  No memory is allocated: the reduction's
- * scratch is a fixed 1.5 MiB __device__ array inside the library, held by
- * every GPU that loads it until the process exits.  The first call on a
- * device looks up that array's address, so make the first call before any
- * stream capture.  Grids above 2^27 points return VEC_ERR_SIZE.  All calls
- * on a device share the scratch: calls that overlap on the GPU race. */
+ * create a vec_ctx (vec_create allocates).  The caller passes pointers to
+ * the eight fields (nx*ny*nz doubles each, sizes taken from p) in memory of
+ * the current device, and dt_out (device memory of the current device, or
+ * host memory); other pointers return VEC_ERR_ARG.  No memory is allocated
+ * by a call: the reduction's scratch is a fixed 1.5 MiB __device__ array
+ * inside the library, held until the process exits by every GPU that has
+ * loaded it.  The first call on a device looks up that array's address;
+ * with CUDA's lazy module loading (the default) that is also when the
+ * array is placed on the device, so make the first call on each device at
+ * set-up, before any stream capture and before a pool reserves the whole
+ * device (or set CUDA_MODULE_LOADING=EAGER).  A host dt_out makes the call
+ * synchronise the stream and read the result back, which cannot be
+ * captured in a CUDA graph; a device dt_out keeps the call asynchronous.
+ * Grids above 2^27 points return VEC_ERR_SIZE.  All calls on a device share
+ * the scratch: calls that overlap on the GPU race. */
 int vec_calcdt_noalloc(const vec_params *p, const double *u, const double *v, const double *w,
                        const double *r, const double *t, const double *bx, const double *by,
                        const double *bz, double *dt_out, void *stream);
@@ -258,6 +293,8 @@ int vec_ensemble_sync(vec_ens *ens);
 int vec_ensemble_tune(vec_ens *ens, int steps, const char *cache);
 /* the tile shapes in use by a context */
 int vec_tunables(vec_ctx *ctx, int *kc, int *s);
+/* sets them: kc in {8, 16, 32}; s in {0 (the kernel's default), 4, 8} */
+int vec_set_tunables(vec_ctx *ctx, int kc, int s);
 
 /* ---- learned closure: the network ---------------------------------------
  * No reference counterpart (an addition to the solver).  Four 3x3x3
@@ -385,6 +422,13 @@ int vec_profile_get(vec_ctx *ctx, int i, char *name, int *launches, double *ms, 
 int vec_profile_reset(vec_ctx *ctx);
 /* kernels launched by this context since creation */
 long long vec_launch_count(vec_ctx *ctx);
+/* Self-test of the bounded-wait error path: launches, on the context's
+ * stream, one kernel that waits on a shared-memory barrier nothing arrives
+ * on, gives up after `polls` polls (1 .. 2^24, the line kernels' limit) and
+ * raises the context's error flag, as a line kernel does when a tile copy
+ * does not complete.  The next vec_sync returns VEC_ERR_CUDA once and clears
+ * the flag; the context stays usable. */
+int vec_selftest_wait(vec_ctx *ctx, long long polls);
 
 #ifdef __cplusplus
 }

@@ -15,7 +15,7 @@ module vec_mod
   use iso_c_binding
   implicit none
 
-  integer(c_int), parameter :: VEC_OK = 0, VEC_ERR_DIVB = -12, VEC_ERR_FLAG = -7
+  integer(c_int), parameter :: VEC_OK = 0, VEC_ERR_DIVB = -12, VEC_ERR_FLAG = -7, VEC_ERR_NAN = -20
   integer(c_int), parameter :: VEC_PREC_FP64 = 0, VEC_PREC_SPLIT = 1
   integer(c_int), parameter :: VEC_F_R = 0, VEC_F_T = 1, VEC_F_U = 2, VEC_F_V = 3, &
                                VEC_F_W = 4, VEC_F_BX = 5, VEC_F_BY = 6, VEC_F_BZ = 7, &

@@ -49,3 +49,27 @@ def rel_err(a, b):
     b = np.asarray(b, dtype=np.float64)
     scale = max(np.abs(b).max(), 1e-300)
     return float(np.abs(a - b).max() / scale)
+
+
+def top_nusselt(p, t):
+    """Nusselt number at the fixed-temperature top plane: the formula of
+    src/dbydz.F90:4877-4925 with its one-sided derivative mirrored to the
+    top, (-11 T1 + 18 T2 - 9 T3 + 2 T4) / (6 dz) averaged over the plane.
+    With the fixed-flux bottom of these configurations the reference's own
+    (bottom) Nusselt number is identically one, so this is the live one."""
+    dz = 1.0 / (p.nz - 1)
+    tz = (-11.0 * t[0] + 18.0 * t[1] - 9.0 * t[2] + 2.0 * t[3]) / (6.0 * dz)
+    nusstmp = p.theta * (p.cm + 1.0) * (1.0 - 1.0 / p.gamma)
+    return (float(tz.mean()) - nusstmp) / (p.theta - nusstmp)
+
+
+def perturbation_menergy(p, bx, by, bz, bzbar):
+    """Magnetic energy of the field perturbation: the diagnostic's
+    F * (1/2) int |B|^2 (trapezium in z, src/utils.F90:22-139) with the
+    uniform seed field bzbar taken out of bz before squaring, so that the
+    small perturbation energy is not a difference of two large numbers."""
+    e = (bx * bx + by * by + (bz - bzbar) ** 2).sum(axis=(1, 2))
+    wz = np.ones(p.nz)
+    wz[0] = wz[-1] = 0.5
+    dxdydz = (p.xmax / p.nx) * (p.ymax / p.ny) / (p.nz - 1)
+    return float(p.f * 0.5 * (wz * e).sum() * dxdydz)

@@ -2,9 +2,11 @@
 
 Single RHS evaluations agree with the FP64 oracle to FP32 accuracy relative
 to each array's scale (tolerance 2e-5).  Over 100 steps the per-field
-relative L2 error stays below 1e-4, and the Nusselt number and the kinetic /
-magnetic energies track the FP64 oracle within 1 % (the target stated for
-the split form), sampled along the run.
+relative L2 error stays below 1e-4, and the top Nusselt number, the kinetic
+energy and the magnetic energy of the field perturbation track the FP64
+oracle within 1 % (the target stated for the split form), sampled along the
+run.  (With the fixed-flux bottom the reference's bottom Nusselt number is
+identically one; the uniform seed field dominates the total magnetic energy.)
 """
 import numpy as np
 import pytest
@@ -12,7 +14,7 @@ import pytest
 from oracle import oracle as O
 from fug30v0kxc_gb300.params import VEC_PREC_SPLIT, convection_params
 from fug30v0kxc_gb300.solver import P3D
-from tests.helpers import rel_err, smooth_state
+from tests.helpers import perturbation_menergy, rel_err, smooth_state, top_nusselt
 
 pytestmark = pytest.mark.gpu
 
@@ -65,9 +67,10 @@ def test_split_100_steps_vs_fp64_oracle():
     for _ in range(10):
         assert g.step(10) == 0 and o.step(10) == 0
         dg, do = g.last_diag(), o.last_diag()
-        nus.append((dg["nusselt"], do["nusselt"]))
+        nus.append((g.top_nusselt(), top_nusselt(p, o.get("t"))))
         kes.append((dg["kenergy"], do["kenergy"]))
-        mes.append((dg["menergy"], do["menergy"]))
+        mes.append((perturbation_menergy(p, g.get("bx"), g.get("by"), g.get("bz"), g.bzbar),
+                    perturbation_menergy(p, o.get("bx"), o.get("by"), o.get("bz"), o.bzbar)))
     errs = {}
     for n in ("r", "t", "u", "v", "w", "pol", "tor"):
         a, b = g.get(n), o.get(n)
@@ -87,7 +90,7 @@ def test_split_100_steps_vs_fp64_oracle():
             assert e < 5e-2, (n, e, errs)
         else:
             assert e < 1e-4, (n, e, errs)
-    for name, series in (("nusselt", nus), ("kenergy", kes), ("menergy", mes)):
+    for name, series in (("nusselt_top", nus), ("kenergy", kes), ("menergy_pert", mes)):
         a = np.mean([x for x, _ in series])
         b = np.mean([y for _, y in series])
         assert abs(a - b) <= 0.01 * abs(b), (name, a, b)

@@ -13,7 +13,11 @@ from fug30v0kxc_gb300.params import ck_from_rayleigh
 from fug30v0kxc_gb300.solver import SNAP_ATTRS, SNAP_FIELDS, nc_read, nc_write, read_input
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_BIN = "/root/reference/VarElecCond/bin"
+# the reference's VarElecCond directory, when it is mounted (tests that read
+# its files directly skip without it; its INPUT files are also committed as
+# a fixture by tests/golden/make_fixtures.py)
+REF_DIR = os.environ.get("VEC_REFERENCE_DIR", "")
+REF_BIN = os.path.join(REF_DIR, "bin") if REF_DIR else ""
 
 
 def test_library_exports_every_header_symbol():
@@ -85,11 +89,21 @@ def test_input_ck_f_and_errors(tmp_path):
         read_input(str(tmp_path / "missing"))
 
 
-@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference inputs not mounted")
-def test_reference_input_files():
-    for sub in ("INPUT", "originalINPUT", "test1/INPUT"):
-        p = read_input(os.path.join(REF_BIN, sub))
-        assert p.nx > 0 and p.ck > 0
+def test_reference_input_files(tmp_path):
+    """The reference's own parameter files (bin/INPUT, bin/originalINPUT,
+    bin/test1/INPUT, kept as a fixture) through the INPUT reader."""
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "reference_inputs.json")) as f:
+        texts = json.load(f)
+    assert sorted(texts) == ["INPUT", "originalINPUT", "test1/INPUT"]
+    for sub, text in texts.items():
+        path = tmp_path / sub.replace("/", "_")
+        path.write_text(text)
+        p = read_input(str(path))
+        assert p.nx > 0 and p.ny > 0 and p.nz > 0 and p.ck > 0, sub
+    # bin/INPUT: flag 2 (Ra / Q), converted as src/initial.F90:186-199 does
+    p = read_input(str(tmp_path / "INPUT"))
+    assert p.rayl > 0 and abs(p.f - p.chand * p.zeta * p.sigma * p.ck * p.ck) <= 1e-12 * abs(p.f)
 
 
 def _snapshot(nx=12, ny=10, nz=7, seed=0):
@@ -129,7 +143,7 @@ def test_snapshot_roundtrip_and_scipy(tmp_path, iprec, fmt):
             assert getattr(f, a) == float(i) + 0.5
 
 
-@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference inputs not mounted")
+@pytest.mark.skipif(not REF_BIN or not os.path.exists(REF_BIN), reason="set VEC_REFERENCE_DIR to the reference")
 def test_reads_reference_restart():
     from scipy.io import netcdf_file
     path = os.path.join(REF_BIN, "restart.nc")
