@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libvec_gpu.so")
-SOURCES = ["capi.cu", "lines.cu", "lines_ct.cu", "physics.cu", "split.cu", "noalloc.cu", "ensemble.cu", "closure_net.cu", "closure.cu", "netcdf_io.cpp"]
+SOURCES = ["capi.cu", "lines.cu", "lines_ct.cu", "physics.cu", "split.cu", "noalloc.cu", "ensemble.cu", "closure_net.cu", "closure.cu", "peaks.cu", "netcdf_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

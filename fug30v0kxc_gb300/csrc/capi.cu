@@ -271,6 +271,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         E.vec4 = !(v4 && v4[0] == '0');
         const char *hc = getenv("VEC_HW_CVT");
         E.int_cvt = !(hc && hc[0] == '1');
+        const char *zp = getenv("VEC_ZPENCIL");
+        E.zpencil = !(zp && zp[0] == '0');
     }
     set_consts(E);
     int st;

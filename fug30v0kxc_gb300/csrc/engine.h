@@ -106,12 +106,13 @@ struct Engine {
     double *corr_bx = nullptr, *corr_by = nullptr;
     int corr_on = 0;
     // tunables (the ensemble autotuner sets them per grid)
-    int kc_pass2 = 16;          // planes per thread in the z-marching hydro kernel
+    int kc_pass2 = 16;          // planes per z chunk of hydro pass 2 (z-pencil or z-marching kernel)
     int ct_s = 0;               // sequences per line tile (0: default for the size)
     bool ct_warp = true;        // x-line tiles synchronised per warp (VEC_CT_WARP=0: per CTA)
     bool prof_kinds = false;    // VEC_PROF_KINDS=1: line launches profiled per job kind
     bool pdl = true;            // programmatic dependent launches (VEC_PDL=0: ordinary launches)
     bool vec4 = true;           // four-point (16-byte) forms of the split pointwise kernels (VEC_VEC4=0: one point)
+    bool zpencil = true;        // split pass 2 with TMA-staged z-pencils (VEC_ZPENCIL=0: per-plane form)
     bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
                                 // (VEC_HW_CVT=1: hardware conversions; the same bits)
 

@@ -9,8 +9,8 @@
 // runs small members concurrently.  Steps with diagnostics (a host read-back)
 // run without the graph.
 //
-// The autotuner picks, per distinct grid, the planes per thread of the
-// z-marching hydro kernel and the sequences per tile of the line kernels by
+// The autotuner picks, per distinct grid, the planes per z chunk of hydro
+// pass 2 and the sequences per tile of the line kernels by
 // timing a scratch context of that grid; results can be cached in a text
 // file (one line per grid: nx ny nz precision kc s).
 #include <stdio.h>
@@ -269,11 +269,23 @@ extern "C" int vec_ensemble_tune(vec_ens *e, int steps, const char *cache)
         const Entry *hit = nullptr;
         for (auto &t : tab) if (same(t.k, k)) { hit = &t; break; }
         if (!hit) {
+            // planes per z chunk of hydro pass 2 (the z-pencil kernel's
+            // chunk, or the z-marching kernel's where nx % 4 != 0)
             const int kcs[3] = { 8, 16, 32 };
-            // sequences per tile: the CT kernel's default or 8; the generic
-            // kernel's default or 4 / 8
-            const bool pow2 = (E.nx & (E.nx - 1)) == 0 && (E.ny & (E.ny - 1)) == 0;
-            std::vector<int> ss = pow2 ? std::vector<int>{ 0, 8 } : std::vector<int>{ 0, 4, 8 };
+            // sequences per tile: the register-FFT kernel's default, or its
+            // alternative (8 for n <= 256, 4 for n >= 768); the generic
+            // kernel's default, 4 or 8
+            auto ct_len = [](int n) {
+                return n == 64 || n == 96 || n == 128 || n == 192 || n == 256 || n == 384 || n == 512 || n == 768 ||
+                       n == 1024;
+            };
+            std::vector<int> ss = { 0 };
+            if (ct_len(E.nx) && ct_len(E.ny)) {
+                if (E.nx <= 256 || E.ny <= 256) ss.push_back(8);
+                if (E.nx >= 768 || E.ny >= 768) ss.push_back(4);
+            } else {
+                ss = { 0, 4, 8 };
+            }
             Entry best = { k, 16, 0 };
             float best_ms = 1e30f;
             for (int kc : kcs)

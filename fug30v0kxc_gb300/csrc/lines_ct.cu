@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "tma.cuh"
 
 template <typename R> struct JobPackCT { LineJob<R> j[MAX_JOBS]; };
 // one TMA descriptor per job input (y lines: 3-D view nx x ny x nz)
@@ -142,47 +143,13 @@ template <bool INV> struct RDft<6, INV> { template <typename C> static __device_
 template <bool INV> struct RDft<12, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<4, 3, INV>(v); } };
 template <bool INV> struct RDft<24, INV> { template <typename C> static __device__ __forceinline__ void run(C *v) { reg_ct<8, 3, INV>(v); } };
 
-// ---- TMA / mbarrier helpers ------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void tma_load(void *dst, const void *src, unsigned bytes, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
-}
+// ---- TMA helpers (tma.cuh) and the 3-D tiled load of the y tiles -------------------
 // 3-D tiled TMA load of one box (c0 innermost) into shared memory
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar)
 {
     asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
                  ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar)) : "memory");
 }
-// bounded wait: returns false (and the caller reports an error) if the
-// barrier phase does not complete within the iteration limit
-#define MBAR_POLLS (1LL << 24)
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long polls = MBAR_POLLS)
-{
-    const unsigned a = smem_u32(bar);
-    for (long long it = 0; it < polls; it++) {
-        unsigned ok;
-        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-                     : "=r"(ok) : "r"(a), "r"(parity) : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
 // rows per TMA box of a y tile: TMA boxes are at most 256 rows, and the box
 // must divide the line length
 __host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
@@ -196,8 +163,26 @@ __host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 
 // through their tiles independently; an "empty" mbarrier per tile buffer
 // (one arrival per warp once it has read the tile) tells the thread that
 // issues the TMA copies when a buffer may be refilled.
+// dynamic shared memory of one CTA: two tile buffers, the exchange rows,
+// the twiddle table(s) and the three multiplier tables
+template <typename R, int N1, int N2, int S>
+__host__ __device__ constexpr size_t ct_smem_bytes()
+{
+    constexpr int N = N1 * N2, NP = N1 > N2 ? N1 : N2;
+    constexpr int LDS = ((NP * (NP + 1)) / 16) * 16 + 17;
+    return 2 * (size_t)(2 * S * N) * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * (size_t)N) * 2 * sizeof(R)
+           + 3 * (size_t)N * sizeof(R);
+}
+// two CTAs per SM where their shared memory fits (227 KB per SM), else one
+// CTA with the whole register file
+template <typename R, int N1, int N2, int S>
+__host__ __device__ constexpr int ct_min_blocks()
+{
+    return (S * (N1 > N2 ? N1 : N2) <= 256 && 2 * ct_smem_bytes<R, N1, N2, S>() <= 232448) ? 2 : 1;
+}
+
 template <typename R, int DIR, int N1, int N2, int S, bool WSYNC>
-__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (S * (N1 > N2 ? N1 : N2) <= 256) ? 2 : 1)
+__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (ct_min_blocks<R, N1, N2, S>()))
 line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R> tb, int nx, int ny, int nz,
         int tpp, int total, int *err)
 {
@@ -586,8 +571,10 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     constexpr int LX = NP + 1;
     constexpr int LDS = ((NP * LX) / 16) * 16 + 17;
     static bool attr_set = false;
-    const size_t smem = 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C)
-                        + 3 * (size_t)N * sizeof(R);
+    const size_t smem = ct_smem_bytes<R, N1, N2, S>();
+    static_assert(ct_smem_bytes<R, N1, N2, S>() == 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C) + 3 * (size_t)N * sizeof(R),
+                  "shared memory layout");
+    static_assert(ct_smem_bytes<R, N1, N2, S>() + 128 <= 232448, "tile does not fit one SM's shared memory");
     if (!attr_set) {
         CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S, WSYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
@@ -641,10 +628,14 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
     switch (n) {
     case 64: case 96: case 128: case 192: case 256: S = F ? 16 : 8; break;
     case 384: case 512: S = F ? 8 : 4; break;
-    case 768: case 1024: S = F ? 4 : 2; break;
+    // (n >= 768, FP32: 8 sequences make the y tiles' rows 64 bytes wide and
+    // give 8 warps per SM; with 4 the 1024-point passes ran at 1.7-1.8 TB/s,
+    // with 8 at 3.2-3.4 TB/s, measured at 1024^2 x 17)
+    case 768: case 1024: S = F ? 8 : 2; break;
     default: return 0;
     }
-    if (F && n <= 256 && E->ct_s == 8) S = 8;   // autotuned alternative
+    if (F && n <= 256 && E->ct_s == 8) S = 8;    // autotuned alternatives
+    if (F && n >= 768 && E->ct_s == 4) S = 4;
     if (L % (2 * S) != 0) return 0;
     if ((E->nx * (int)sizeof(R)) % 16 != 0) return 0;
     for (int j = 0; j < njobs; j++) {
@@ -675,9 +666,9 @@ int launch_lines_ct(Engine *E, int dir, const LineJob<R> *jobs, int njobs)
         if constexpr (F) {
             CT_CASE(64, 8, 8, 16) CT_CASE(128, 16, 8, 16) CT_CASE(256, 16, 16, 16)
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
-            CT_CASE(512, 32, 16, 8) CT_CASE(1024, 32, 32, 4)
+            CT_CASE(512, 32, 16, 8) CT_CASE(1024, 32, 32, 4) CT_CASE(1024, 32, 32, 8)
             CT_CASE(96, 8, 12, 16) CT_CASE(192, 16, 12, 16) CT_CASE(96, 8, 12, 8) CT_CASE(192, 16, 12, 8)
-            CT_CASE(384, 16, 24, 8) CT_CASE(768, 32, 24, 4)
+            CT_CASE(384, 16, 24, 8) CT_CASE(768, 32, 24, 4) CT_CASE(768, 32, 24, 8)
         } else {
             CT_CASE(64, 8, 8, 8) CT_CASE(128, 16, 8, 8) CT_CASE(256, 16, 16, 8)
             CT_CASE(512, 32, 16, 4) CT_CASE(1024, 32, 32, 2)

@@ -31,6 +31,7 @@
 #include "engine.h"
 #include "fpconv.cuh"
 #include "magkern.cuh"
+#include "tma.cuh"
 #include "zstencil.cuh"
 
 #define TPB 256
@@ -293,14 +294,15 @@ __host__ __device__ __forceinline__ V4 operator/(V4 a, V4 b) { return V4(a.x / b
 
 // one point (T = float, idx a point index) or four (T = V4, idx a 4-vector
 // index) of the terms without second-level derivatives
+// (tp, u0, v0, w0: t', u, v, w at the point)
 template <typename T>
-__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z)
+__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z,
+                                                  const T tp, const T u0, const T v0, const T w0)
 {
     const int nz = a.nz;
     const float *pc = a.pc;
     const T rho0 = T(pc[PC_RHO0 * nz + k]), t0 = T(pc[PC_T0 * nz + k]);
-    const T rp = ldv<T>(a.r, idx), tp = ldv<T>(a.t, idx), u0 = ldv<T>(a.u, idx), v0 = ldv<T>(a.v, idx);
-    const T w0 = ldv<T>(a.w, idx);
+    const T rp = ldv<T>(a.r, idx);
     const T rr = rho0 + rp, tt = t0 + tp;
     const T bx = ldv<T>(a.bx, idx), by = ldv<T>(a.by, idx), bzp = ldv<T>(a.bz, idx), bz = T(a.bzbar) + bzp;
     const T rx = ldv<T>(a.rx, idx), ry = ldv<T>(a.ry, idx);
@@ -359,6 +361,11 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     stv(a.g, idx, T(a.f) * bz * bx);
     stv(a.hh, idx, T(a.f) * bz * by);
 }
+template <typename T>
+__device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z)
+{
+    split_pass2_point<T>(a, idx, k, z, ldv<T>(a.t, idx), ldv<T>(a.u, idx), ldv<T>(a.v, idx), ldv<T>(a.w, idx));
+}
 
 // two consecutive x points per thread, one plane per CTA row (grid
 // (np/2/256, nz)); the z neighbours come through L1/L2.  (Three CTAs per
@@ -382,6 +389,102 @@ __global__ void __launch_bounds__(256, 3) k_split_pass2_v2(SplitHydroArgs a)
     z.uzu = zd1up(u2, np2, k, nz, 2, h, w0); z.vzu = zd1up(v2, np2, k, nz, 2, h, w0);
     z.uzz = zd2(u2, np2, k, nz, 3, s); z.vzz = zd2(v2, np2, k, nz, 3, s);
     split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z);
+}
+
+// Pass 2 with TMA-staged z-pencils.  A CTA owns ZT_TILE consecutive points
+// of the plane (two per thread) and a chunk of planes [k0, k1) and marches
+// down in z.  The planes of t', u, v, w that the z stencils read sit in a
+// ring of ZT_SLOTS shared-memory slots (a slot = the tile of the four fields
+// on one plane), filled by bulk copies (cp.async.bulk + mbarrier) one plane
+// ahead of the row being computed.  Row k reads planes k-3..k+3 (0..5 and
+// nz-6..nz-1 next to the walls), so every plane comes from DRAM/L2 once per
+// chunk instead of once per stencil tap.  The other inputs of the point are
+// read directly.  Same arithmetic as k_split_pass2_v2, value for value.
+#define ZT_TILE 512
+#define ZT_SLOTS 8
+struct ZRing2 {
+    const V2 *base;     // slot 0 of one field, this thread's point pair
+    __device__ __forceinline__ V2 operator()(int kk) const
+    {
+        return base[(size_t)(kk & (ZT_SLOTS - 1)) * (4 * ZT_TILE / 2)];
+    }
+};
+
+__global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(SplitHydroArgs a, int kc, int *err)
+{
+    PDL_WAIT();
+    extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE]
+    __shared__ __align__(8) uint64_t full[ZT_SLOTS];
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const size_t p0 = (size_t)blockIdx.x * ZT_TILE;
+    const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
+    const int tid = threadIdx.x;
+    auto lo_of = [&](int k) { return max(0, k >= nz - 2 ? min(k - 3, nz - 6) : k - 3); };
+    auto hi_of = [&](int k) { return min(nz - 1, k <= 1 ? max(k + 3, 5) : k + 3); };
+    const int kbase = lo_of(k0), kcap = hi_of(k1 - 1);
+    auto parity = [&](int kk) { return (unsigned)(((kk - kbase) >> 3) & 1); };
+    auto issue = [&](int kk) {   // one thread: plane kk of the four fields into slot kk mod 8
+        uint64_t *b = &full[kk & (ZT_SLOTS - 1)];
+        float *dst = zring + (size_t)(kk & (ZT_SLOTS - 1)) * 4 * ZT_TILE;
+        const size_t off = (size_t)kk * np + p0;
+        mbar_expect_tx(b, 4 * ZT_TILE * (unsigned)sizeof(float));
+        tma_load(dst, a.t + off, ZT_TILE * sizeof(float), b);
+        tma_load(dst + ZT_TILE, a.u + off, ZT_TILE * sizeof(float), b);
+        tma_load(dst + 2 * ZT_TILE, a.v + off, ZT_TILE * sizeof(float), b);
+        tma_load(dst + 3 * ZT_TILE, a.w + off, ZT_TILE * sizeof(float), b);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < ZT_SLOTS; s++) mbar_init(&full[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    int khi = min(kcap, hi_of(k0) + 1);   // highest plane issued (one plane of lookahead)
+    if (tid == 0)
+        for (int kk = kbase; kk <= khi; kk++) issue(kk);
+    int kw = kbase - 1;                   // highest plane this thread has waited for
+    bool ok = true;
+    const ZRing2 Rt{ reinterpret_cast<const V2 *>(zring) + tid };
+    const ZRing2 Ru{ reinterpret_cast<const V2 *>(zring + ZT_TILE) + tid };
+    const ZRing2 Rv{ reinterpret_cast<const V2 *>(zring + 2 * ZT_TILE) + tid };
+    const ZRing2 Rw{ reinterpret_cast<const V2 *>(zring + 3 * ZT_TILE) + tid };
+    const V2 h(a.ho12), sc(a.sc1);
+    const size_t np2 = np / 2, q2 = p0 / 2 + tid;
+    for (int k = k0; k < k1; k++) {
+        if (k > k0) {
+            // every thread is done with row k - 1: the slot of plane k - 4 is free
+            if (!__syncthreads_and(ok)) {
+                if (tid == 0) {
+                    // report, then let the copies in flight land before the CTA exits
+                    atomicExch(err, 1);
+                    for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++)
+                        mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+                }
+                return;
+            }
+            const int want = min(kcap, hi_of(k) + 1);
+            if (tid == 0 && want > khi) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                for (int kk = khi + 1; kk <= want; kk++) issue(kk);
+            }
+            khi = max(khi, want);
+        }
+        for (int kk = kw + 1; kk <= hi_of(k) && ok; kk++) ok = mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+        kw = max(kw, hi_of(k));
+        if (!ok) continue;
+        const V2 w0 = Rw(k);
+        ZDer<V2> z;
+        z.tzu = zd1upa(Rt, k, nz, 5, h, w0); z.tzp = zd1a(Rt, k, nz, 5, h); z.tzz = zd2a(Rt, k, nz, 0, sc);
+        z.wzu = zd1upa(Rw, k, nz, 1, h, w0); z.wz = zd1a(Rw, k, nz, 1, h);
+        z.uzu = zd1upa(Ru, k, nz, 2, h, w0); z.vzu = zd1upa(Rv, k, nz, 2, h, w0);
+        z.uzz = zd2a(Ru, k, nz, 3, sc); z.vzz = zd2a(Rv, k, nz, 3, sc);
+        split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0);
+    }
+    if (!__syncthreads_and(ok) && tid == 0) {
+        atomicExch(err, 1);
+        for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++) mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+    }
 }
 
 // z-marching: one thread per (i,j) column and chunk of kc planes, with
@@ -591,7 +694,22 @@ int split_hydro(Engine *E)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
-    if (E->nx % 4 == 0 && E->vec4) {
+    if (E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6) {
+        static bool attr = false;
+        const size_t smem = (size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float);
+        if (!attr) {
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr = true;
+        }
+        // chunks of about kc_pass2 planes (tunable), balanced over nz
+        const int kt = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
+        const int nch = (E->nz + kt - 1) / kt, kc = (E->nz + nch - 1) / nch;
+        E->prof_begin("hydro_pass2_f32", FB(E, 39, 4));
+        CUDA_TRY(launch_k(*E, k_split_pass2_zt, dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
+                          dim3(ZT_TILE / 2), smem, a, kc, E->dev_err));
+        E->prof_end();
+        CUDA_TRY(cudaGetLastError());
+    } else if (E->nx % 4 == 0 && E->vec4) {
         KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v2,
                  dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB, a);
     } else {

@@ -11,13 +11,18 @@
 //         k=nz-2 d2lastdz_up :1271, k=nz-1 d2lastdz(flag) :1180
 #pragma once
 
-template <typename R>
-__host__ __device__ __forceinline__ R zld(const R *f, size_t np, int k) { return f[(size_t)k * np]; }
+// A column of planes: F(k) = f[k np].  The stencils below take any accessor
+// F(k) -> value of plane k (a column in global memory, or a ring of planes
+// in shared memory); the pointer forms wrap a column.
+template <typename R> struct ZCol {
+    const R *f;
+    size_t np;
+    __host__ __device__ __forceinline__ R operator()(int k) const { return f[(size_t)k * np]; }
+};
 
-template <typename R>
-__host__ __device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R h)
+template <typename R, typename A>
+__host__ __device__ __forceinline__ R zd1a(const A &F, int k, int nz, int fl, R h)
 {
-#define F(kk) zld(f, np, kk)
     if (k == 0) {
         if (fl == 1) return h * ((R)14 * F(0) + (R)36 * F(1) - (R)18 * F(2) + (R)4 * F(3));
         if (fl == 5) return h * ((R)-22 * F(0) + (R)36 * F(1) - (R)18 * F(2) + (R)4 * F(3));
@@ -31,14 +36,12 @@ __host__ __device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, 
         return (R)0;
     }
     return h * (F(k - 2) - (R)8 * F(k - 1) + (R)8 * F(k + 1) - F(k + 2));
-#undef F
 }
 
-template <typename R>
-__host__ __device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl, R h, R wv)
+template <typename R, typename A>
+__host__ __device__ __forceinline__ R zd1upa(const A &F, int k, int nz, int fl, R h, R wv)
 {
-#define F(kk) zld(f, np, kk)
-    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k <= 1 || k >= nz - 2) return zd1a(F, k, nz, fl, h);
     if (k == 2) {
         if (wv >= (R)0) return h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3));
         return h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1));
@@ -51,13 +54,11 @@ __host__ __device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz
     if (wv >= (R)0)
         return h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1));
     return h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1));
-#undef F
 }
 
-template <typename R>
-__host__ __device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, int fl, R s)
+template <typename R, typename A>
+__host__ __device__ __forceinline__ R zd2a(const A &F, int k, int nz, int fl, R s)
 {
-#define F(kk) zld(f, np, kk)
     if (k == 0) {
         if (fl == 3)
             return s * ((R)45 * F(0) - (R)154 * F(1) + (R)214 * F(2) - (R)156 * F(3) + (R)61 * F(4) - (R)10 * F(5));
@@ -73,8 +74,17 @@ __host__ __device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, 
         return (R)0;
     }
     return s * (-F(k - 2) + (R)16 * F(k - 1) - (R)30 * F(k) + (R)16 * F(k + 1) - F(k + 2));
-#undef F
 }
+
+template <typename R>
+__host__ __device__ __forceinline__ R zd1(const R *f, size_t np, int k, int nz, int fl, R h)
+{ return zd1a(ZCol<R>{ f, np }, k, nz, fl, h); }
+template <typename R>
+__host__ __device__ __forceinline__ R zd1up(const R *f, size_t np, int k, int nz, int fl, R h, R wv)
+{ return zd1upa(ZCol<R>{ f, np }, k, nz, fl, h, wv); }
+template <typename R>
+__host__ __device__ __forceinline__ R zd2(const R *f, size_t np, int k, int nz, int fl, R s)
+{ return zd2a(ZCol<R>{ f, np }, k, nz, fl, s); }
 
 // spectral d/dx of a 2-D halfcomplex plane at (i,j): index shuffle of
 // src/fft.F90:292-302 (the reference's "+ik" on the x halfcomplex index).
@@ -135,11 +145,11 @@ __host__ __device__ __forceinline__ V4 upsel(V4 w, V4 p, V4 m)
 // zd1up for four points: both one-sided stencils of each row, chosen per
 // component by the sign of w (the same formulas and operation order as the
 // scalar zd1up)
-__host__ __device__ __forceinline__ V4 zd1up(const V4 *f, size_t np, int k, int nz, int fl, V4 h, V4 wv)
+template <typename A>
+__host__ __device__ __forceinline__ V4 zd1upa(const A &F, int k, int nz, int fl, V4 h, V4 wv)
 {
     typedef V4 R;
-#define F(kk) zld(f, np, kk)
-    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k <= 1 || k >= nz - 2) return zd1a(F, k, nz, fl, h);
     if (k == 2)
         return upsel(wv, h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3)),
                      h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1)));
@@ -148,8 +158,9 @@ __host__ __device__ __forceinline__ V4 zd1up(const V4 *f, size_t np, int k, int 
                      h * ((R)-2 * F(nz - 1) + (R)12 * F(nz - 2) - (R)6 * F(nz - 3) - (R)4 * F(nz - 4)));
     return upsel(wv, h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1)),
                  h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1)));
-#undef F
 }
+__host__ __device__ __forceinline__ V4 zd1up(const V4 *f, size_t np, int k, int nz, int fl, V4 h, V4 wv)
+{ return zd1upa(ZCol<V4>{ f, np }, k, nz, fl, h, wv); }
 
 // Two consecutive x points (8-byte loads), the same operators as V4
 struct __align__(8) V2 {
@@ -167,11 +178,11 @@ __host__ __device__ __forceinline__ V2 upsel(V2 w, V2 p, V2 m)
 {
     return V2(w.x >= 0.0f ? p.x : m.x, w.y >= 0.0f ? p.y : m.y);
 }
-__host__ __device__ __forceinline__ V2 zd1up(const V2 *f, size_t np, int k, int nz, int fl, V2 h, V2 wv)
+template <typename A>
+__host__ __device__ __forceinline__ V2 zd1upa(const A &F, int k, int nz, int fl, V2 h, V2 wv)
 {
     typedef V2 R;
-#define F(kk) zld(f, np, kk)
-    if (k <= 1 || k >= nz - 2) return zd1(f, np, k, nz, fl, h);
+    if (k <= 1 || k >= nz - 2) return zd1a(F, k, nz, fl, h);
     if (k == 2)
         return upsel(wv, h * ((R)2 * F(0) - (R)12 * F(1) + (R)6 * F(2) + (R)4 * F(3)),
                      h * (F(5) - (R)6 * F(4) + (R)18 * F(3) - (R)10 * F(2) - (R)3 * F(1)));
@@ -180,8 +191,9 @@ __host__ __device__ __forceinline__ V2 zd1up(const V2 *f, size_t np, int k, int 
                      h * ((R)-2 * F(nz - 1) + (R)12 * F(nz - 2) - (R)6 * F(nz - 3) - (R)4 * F(nz - 4)));
     return upsel(wv, h * (-F(k - 3) + (R)6 * F(k - 2) - (R)18 * F(k - 1) + (R)10 * F(k) + (R)3 * F(k + 1)),
                  h * (F(k + 3) - (R)6 * F(k + 2) + (R)18 * F(k + 1) - (R)10 * F(k) - (R)3 * F(k - 1)));
-#undef F
 }
+__host__ __device__ __forceinline__ V2 zd1up(const V2 *f, size_t np, int k, int nz, int fl, V2 h, V2 wv)
+{ return zd1upa(ZCol<V2>{ f, np }, k, nz, fl, h, wv); }
 
 // Interior rows (3 <= k <= nz-4) from a register window v[d] = f(k-3+d):
 // the same formulas and operation order as zd1 / zd1up / zd2.

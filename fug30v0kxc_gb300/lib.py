@@ -74,6 +74,7 @@ SIGNATURES = {
     "vec_set_tunables": (C.c_int, [_vp, C.c_int, C.c_int]),
     "vec_line_f32": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
     "vec_selftest_wait": (C.c_int, [_vp, C.c_longlong]),
+    "vec_measure_fp64": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "vec_net_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_vp)]),
     "vec_net_destroy": (C.c_int, [_vp]),
     "vec_net_nparams": (C.c_longlong, [_vp]),

@@ -293,7 +293,9 @@ int vec_ensemble_sync(vec_ens *ens);
 int vec_ensemble_tune(vec_ens *ens, int steps, const char *cache);
 /* the tile shapes in use by a context */
 int vec_tunables(vec_ctx *ctx, int *kc, int *s);
-/* sets them: kc in {8, 16, 32}; s in {0 (the kernel's default), 4, 8} */
+/* sets them: kc in {8, 16, 32}; s in {0 (the kernel's default), 4, 8}
+ * (FP32 register-FFT lines: 8 selects 8 sequences per tile for n <= 256,
+ * 4 selects 4 for n >= 768; the generic kernel takes 4 or 8) */
 int vec_set_tunables(vec_ctx *ctx, int kc, int s);
 
 /* ---- learned closure: the network ---------------------------------------
@@ -422,6 +424,10 @@ int vec_profile_get(vec_ctx *ctx, int i, char *name, int *launches, double *ms, 
 int vec_profile_reset(vec_ctx *ctx);
 /* kernels launched by this context since creation */
 long long vec_launch_count(vec_ctx *ctx);
+/* FP64 fused multiply-add throughput of the current device in TFLOP/s (a
+ * timed microbenchmark, the best of reps launches): the roofline of the
+ * plain FP64 form, whose kernels are bound by the FP64 pipe */
+int vec_measure_fp64(int reps, double *tflops);
 /* Self-test of the bounded-wait error path: launches, on the context's
  * stream, one kernel that waits on a shared-memory barrier nothing arrives
  * on, gives up after `polls` polls (1 .. 2^24, the line kernels' limit) and

@@ -5,7 +5,8 @@ transforms (src/fft.F90:255-799) through the FP32 instances of the line
 kernels: the TMA-fed register FFT for n = 2^a and 3*2^a (64..1024, two tile
 shapes for n <= 256: 16 and 8 sequences per tile) and the generic Stockham
 kernel for the other lengths.  vec_line_f32 runs exactly those kernels on
-caller data.  Every instance is compared on seeded random data with the
+caller data (two tile shapes for n >= 768 too: 8 and 4 sequences).  Every
+instance is compared on seeded random data with the
 oracle's FP64 operators; a wrong twiddle, multiplier or index gives O(1)
 errors, FP32 rounding gives ~1e-7.
 
@@ -56,14 +57,14 @@ def _check_direction(g, o, direction, f):
     return errs
 
 
-CASES = [(n, 0) for n in LENGTHS] + [(n, 8) for n in LENGTHS if n <= 256]
+CASES = [(n, 0) for n in LENGTHS] + [(n, 8) for n in LENGTHS if n <= 256] + [(n, 4) for n in LENGTHS if n >= 768]
 
 
 @pytest.mark.parametrize("n,tile", CASES)
 def test_f32_line_kernels_match_fp64_oracle(n, tile):
     """x lines of length n on an (n, 64, 6) grid and y lines of length n on
-    a (64, n, 6) grid; tile 8 selects the 8-sequence tile where the kernel
-    has one (n <= 256), else the kernel's own shape."""
+    a (64, n, 6) grid; tile 8 selects the 8-sequence tile for n <= 256 and
+    tile 4 the 4-sequence tile for n >= 768; 0 is the kernel's default."""
     rng = np.random.default_rng(n + tile)
     for direction, (nx, ny) in ((0, (n, 64)), (1, (64, n))):
         g, o = _pair(nx, ny)

@@ -97,7 +97,8 @@ def test_split_100_steps_vs_fp64_oracle():
 
 
 @pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17)])
-@pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6)])
+@pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6),
+                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6)])
 def test_split_variants_agree(grid, var, values, tol, monkeypatch):
     """Two implementations of the same arithmetic after twelve steps (Euler,
     AB2, AB3, a dealias step and a calcdt at step 10).
@@ -108,6 +109,11 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
       the one-point forms.  The compiler contracts multiply-adds within one
       expression, not across the vector type's operator functions, so
       single roundings differ; tolerance 1e-6 relative L2 per field.
+    * VEC_ZPENCIL: hydro pass 2 with its z-stencil planes staged through a
+      shared-memory ring by bulk copies, against the per-plane form that
+      reads them from global memory: the same formulas on the same values,
+      but the two kernels are compiled separately and the compiler may fuse
+      different multiply-adds; tolerance 1e-6 relative L2 per field.
     """
     states = []
     for val in values:
@@ -129,3 +135,29 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
         else:
             e = rel_l2(states[1][n], states[0][n])
             assert e <= tol, (n, e)
+
+
+@pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17), (128, 32, 40)])
+def test_zpencil_pass2_matches_per_plane_form(grid, monkeypatch):
+    """One hydro_deriv with pass 2 fed by the shared-memory z ring against
+    the per-plane form, every RHS at every plane (the wall rows read planes
+    0..5 and nz-6..nz-1; several z chunks per column): largest difference
+    below 1e-6 of the array's largest value (single roundings only)."""
+    out = []
+    for val in ("0", "1"):
+        monkeypatch.setenv("VEC_ZPENCIL", val)
+        p = convection_params(*grid, eta_contrast=20.0, precision=VEC_PREC_SPLIT)
+        g = P3D(p)
+        for n, a in smooth_state(p, seed=9).items():
+            g.set(n, a)
+        g.mag_init()
+        g.hydro_deriv()
+        out.append({n: g.get(n) for n in ("rdot3", "tdot3", "udot3", "vdot3", "wdot3")})
+        g.close()
+    for n in out[0]:
+        e = rel_err(out[1][n], out[0][n])
+        assert e < 1e-6, (n, e)
+        # per plane: no row of the ring form is off
+        for k in range(grid[2]):
+            scale = max(np.abs(out[0][n]).max(), 1e-30)
+            assert np.abs(out[1][n][k] - out[0][n][k]).max() / scale < 1e-6, (n, k)
