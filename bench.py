@@ -287,7 +287,8 @@ def closure_line(args, ws):
                     "upsampled, spun up)",
             "config": {"workload": "closure %dx%dx%d DNS -> %dx%dx%d, Ra 1e6, Q 1e3, eta contrast 20"
                                    % tuple(r["fine"] + r["coarse"]), **kw},
-            "roofline": {"bound": "tensor", "kernel": "closure network training step (mma.sync BF16)",
+            "roofline": {"bound": "tensor", "kernel": "closure network training step (BF16: forward and input gradient on "
+                                   "tcgen05 at nx = 128, weight gradient on mma.sync)",
                          "achieved": round(ach, 2) if ach else None, "peak": peak, "peak_kind": pk, "unit": "TFLOP/s",
                          "frac": round(ach / peak, 4) if ach else None, "traffic": None},
             "closure": r}

@@ -887,8 +887,11 @@ static int enqueue_step(Engine &E, bool diag_now)
         if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
         CUDA_TRY(cudaStreamWaitEvent(E.stream, E.ev_join, 0));
     } else {
-        if ((st = E.split ? split_hydro(&E) : phys_hydro64(&E))) return st;
-        if (mag) st = E.split ? split_mag(&E, fold) : phys_mag64(&E);
+        // (split form, magnetic branch after the hydro one: the transforms
+        // of E = u x B ride in the hydro derivatives' line launches)
+        const bool share = E.split && mag;
+        if ((st = E.split ? split_hydro(&E, share) : phys_hydro64(&E))) return st;
+        if (mag) st = E.split ? split_mag(&E, fold, share) : phys_mag64(&E);
         else st = phys_zero_mag_rhs(&E);
         if (st) return st;
     }

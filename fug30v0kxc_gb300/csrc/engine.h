@@ -229,12 +229,14 @@ struct BoundaryMirrors {
     float *u32, *v32, *w32, *t32, *pol32, *tor32;
     const double *t0;
 };
-int split_hydro(Engine *E);
+// with_mag: E = u x B and its forward transforms ride along (the x and y
+// line launches carry them); split_mag then runs with spectra_done
+int split_hydro(Engine *E, bool with_mag = false);
 // In one time step the AB3 coefficient step can ride on the mean-field CTA
 // of split_mag's mag_div kernel (ab3_coef) and the history rotation on the
 // first kernel of split_bandj (rotate_hist); split_ab3 then runs the update
 // alone (folded).
-int split_mag(Engine *E, bool ab3_coef = false);
+int split_mag(Engine *E, bool ab3_coef = false, bool spectra_done = false);
 int split_bandj(Engine *E, bool rotate_hist = false);
 int split_refresh(Engine *E);
 int split_refresh_field(Engine *E, int field);   // one field's mirror (VEC_F_*)

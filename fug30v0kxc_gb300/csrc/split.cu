@@ -655,27 +655,50 @@ __global__ void __launch_bounds__(256, 4) k_split_pass4_v4(SplitHydro4Args a)
     reinterpret_cast<V4 *>(a.ht->p[4][2])[i4] = wfin * ri;
 }
 
-int split_hydro(Engine *E)
+// the three forward transforms of E = u x B that mag_deriv starts with;
+// with with_mag the x and y passes of the hydro derivatives carry them as
+// extra jobs, so one launch per direction serves both
+int split_emf(Engine *E);
+static void mag_fwd_jobs(Engine *E, LineJob<float> *fx, LineJob<float> *fy)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    fx[0] = ljob<float>(W[W_M1], W[W_EX], OP_FWD);
+    fx[1] = ljob<float>(W[W_M2], W[W_EY], OP_FWD);
+    fx[2] = ljob<float>(W[W_M3], W[W_EZ], OP_FWD);
+    fy[0] = ljob<float>(W[W_EX], W[W_EX], OP_FWD);
+    fy[1] = ljob<float>(W[W_EY], W[W_EY], OP_FWD);
+    fy[2] = ljob<float>(W[W_EZ], W[W_EZ], OP_FWD);
+}
+
+int split_hydro(Engine *E, bool with_mag)
 {
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
     int st;
-    LineJob<float> jx[5] = {
+    LineJob<float> fx[3], fy[3];
+    if (with_mag) {
+        if ((st = split_emf(E))) return st;
+        mag_fwd_jobs(E, fx, fy);
+    }
+    LineJob<float> jx[8] = {
         ljob<float>(E->r32, W[W_RX], OP_D1),
         ljob<float>(E->t32, W[W_TX], OP_D1, W[W_TXX], OP_D2),
         ljob<float>(E->u32, W[W_UX], OP_D1, W[W_UXX], OP_D2),
         ljob<float>(E->v32, W[W_VX], OP_D1, W[W_VXX], OP_D2),
         ljob<float>(E->w32, W[W_WX], OP_D1, W[W_WXX], OP_D2),
     };
-    if ((st = launch_lines<float>(E, 0, jx, 5))) return st;
-    LineJob<float> jy[5] = {
+    if (with_mag) for (int i = 0; i < 3; i++) jx[5 + i] = fx[i];
+    if ((st = launch_lines<float>(E, 0, jx, with_mag ? 8 : 5))) return st;
+    LineJob<float> jy[8] = {
         ljob<float>(E->r32, W[W_RY], OP_D1),
         ljob<float>(E->t32, W[W_TY], OP_D1, W[W_TYY], OP_D2),
         ljob<float>(E->u32, W[W_UY], OP_D1, W[W_UYY], OP_D2),
         ljob<float>(E->v32, W[W_VY], OP_D1, W[W_VYY], OP_D2),
         ljob<float>(E->w32, W[W_WY], OP_D1, W[W_WYY], OP_D2),
     };
-    if ((st = launch_lines<float>(E, 1, jy, 5))) return st;
+    if (with_mag) for (int i = 0; i < 3; i++) jy[5 + i] = fy[i];
+    if ((st = launch_lines<float>(E, 1, jy, with_mag ? 8 : 5))) return st;
 
     const Consts &c = E->k;
     SplitHydroArgs a;
@@ -753,25 +776,34 @@ int split_hydro(Engine *E)
 }
 
 // ---- mag_deriv ---------------------------------------------------------------
-int split_mag(Engine *E, bool ab3_coef)
+// E = u x B (real space, FP32)
+int split_emf(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    if (E->nx % 4 == 0 && E->vec4)
+        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf4, nblk(E->n / 4), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
+                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n / 4, (float)E->bzbar);
+    else
+        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf<float>, nblk(E->n), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
+                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n, (float)E->bzbar);
+    return VEC_OK;
+}
+
+int split_mag(Engine *E, bool ab3_coef, bool spectra_done)
 {
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
     int st;
     const bool v4 = E->nx % 4 == 0 && E->vec4;
     const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
-    if (v4)
-        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf4, nblk(E->n / 4), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
-                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n / 4, (float)E->bzbar);
-    else
-        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf<float>, nblk(E->n), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
-                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n, (float)E->bzbar);
-    LineJob<float> fx[3] = { ljob<float>(W[W_M1], W[W_EX], OP_FWD), ljob<float>(W[W_M2], W[W_EY], OP_FWD),
-                             ljob<float>(W[W_M3], W[W_EZ], OP_FWD) };
-    if ((st = launch_lines<float>(E, 0, fx, 3))) return st;
-    LineJob<float> fy[3] = { ljob<float>(W[W_EX], W[W_EX], OP_FWD), ljob<float>(W[W_EY], W[W_EY], OP_FWD),
-                             ljob<float>(W[W_EZ], W[W_EZ], OP_FWD) };
-    if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
+    if (!spectra_done) {
+        if ((st = split_emf(E))) return st;
+        LineJob<float> fx[3], fy[3];
+        mag_fwd_jobs(E, fx, fy);
+        if ((st = launch_lines<float>(E, 0, fx, 3))) return st;
+        if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
+    }
     const Consts &c = E->k;
     MeanArgs<float> ma;
     ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
