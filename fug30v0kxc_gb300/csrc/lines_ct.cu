@@ -163,26 +163,42 @@ __host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 
 // through their tiles independently; an "empty" mbarrier per tile buffer
 // (one arrival per warp once it has read the tile) tells the thread that
 // issues the TMA copies when a buffer may be refilled.
+// Per-sequence stride of the exchange rows, in complex elements.  A
+// shared-memory wavefront serves U = 128 / sizeof(complex) consecutive
+// elements.  x lines: the threads of a half-warp (quarter-warp in FP64)
+// belong to one or two sequences, and a stride of 1 mod 16 keeps them on
+// distinct banks.  y lines: thread tid is lane tid / S of sequence tid % S,
+// so a wavefront's threads are G = U / S lanes of U / G sequences; a
+// stride of G mod U puts them on distinct banks (exchange element
+// sidx * stride + lane * 1 or lane * (NP + 1) + const; NP + 1 is odd).
+template <typename R, int DIR, int NP, int S>
+__host__ __device__ constexpr int ct_lds()
+{
+    constexpr int U = 128 / (2 * (int)sizeof(R));
+    constexpr int G = U / S > 1 ? U / S : 1;
+    return DIR == 0 ? ((NP * (NP + 1)) / 16) * 16 + 17 : ((NP * (NP + 1)) / U) * U + U + G;
+}
+
 // dynamic shared memory of one CTA: two tile buffers, the exchange rows,
 // the twiddle table(s) and the three multiplier tables
-template <typename R, int N1, int N2, int S>
+template <typename R, int DIR, int N1, int N2, int S>
 __host__ __device__ constexpr size_t ct_smem_bytes()
 {
     constexpr int N = N1 * N2, NP = N1 > N2 ? N1 : N2;
-    constexpr int LDS = ((NP * (NP + 1)) / 16) * 16 + 17;
+    constexpr int LDS = ct_lds<R, DIR, NP, S>();
     return 2 * (size_t)(2 * S * N) * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * (size_t)N) * 2 * sizeof(R)
            + 3 * (size_t)N * sizeof(R);
 }
 // two CTAs per SM where their shared memory fits (227 KB per SM), else one
 // CTA with the whole register file
-template <typename R, int N1, int N2, int S>
+template <typename R, int DIR, int N1, int N2, int S>
 __host__ __device__ constexpr int ct_min_blocks()
 {
-    return (S * (N1 > N2 ? N1 : N2) <= 256 && 2 * ct_smem_bytes<R, N1, N2, S>() <= 232448) ? 2 : 1;
+    return (S * (N1 > N2 ? N1 : N2) <= 256 && 2 * ct_smem_bytes<R, DIR, N1, N2, S>() <= 232448) ? 2 : 1;
 }
 
 template <typename R, int DIR, int N1, int N2, int S, bool WSYNC>
-__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (ct_min_blocks<R, N1, N2, S>()))
+__global__ void __launch_bounds__(S * (N1 > N2 ? N1 : N2), (ct_min_blocks<R, DIR, N1, N2, S>()))
 line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R> tb, int nx, int ny, int nz,
         int tpp, int total, int *err)
 {
@@ -193,7 +209,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     constexpr int NT = S * NP;
     constexpr int TILE = 2 * S * N;                   // reals per tile
     constexpr int LX = (N1 > N2 ? N1 : N2) + 1;       // padded exchange row
-    constexpr int LDS = ((NP * LX) / 16) * 16 + 17;   // per-sequence exchange stride (== 1 mod 16)
+    constexpr int LDS = ct_lds<R, DIR, NP, S>();      // per-sequence exchange stride
     constexpr bool WS = WSYNC && DIR == 0 && (32 % NP == 0) && NT % 32 == 0;
 
     extern __shared__ __align__(128) unsigned char smem[];
@@ -569,12 +585,13 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     constexpr int NP = N1 > N2 ? N1 : N2;
     constexpr int TILE = 2 * S * N;
     constexpr int LX = NP + 1;
-    constexpr int LDS = ((NP * LX) / 16) * 16 + 17;
+    constexpr int LDS = ct_lds<R, DIR, NP, S>();
     static bool attr_set = false;
-    const size_t smem = ct_smem_bytes<R, N1, N2, S>();
-    static_assert(ct_smem_bytes<R, N1, N2, S>() == 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C) + 3 * (size_t)N * sizeof(R),
+    const size_t smem = ct_smem_bytes<R, DIR, N1, N2, S>();
+    static_assert(ct_smem_bytes<R, DIR, N1, N2, S>() == 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C) + 3 * (size_t)N * sizeof(R),
                   "shared memory layout");
-    static_assert(ct_smem_bytes<R, N1, N2, S>() + 128 <= 232448, "tile does not fit one SM's shared memory");
+    static_assert(ct_smem_bytes<R, DIR, N1, N2, S>() + 128 <= 232448, "tile does not fit one SM's shared memory");
+    static_assert(LDS >= NP * LX && LDS >= N + N / 32 + 1, "exchange rows");
     if (!attr_set) {
         CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S, WSYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
