@@ -911,6 +911,56 @@ static int enqueue_step(Engine &E, bool diag_now)
     return VEC_OK;
 }
 
+// Whether a and b can step as members of one batch (one launch per kernel):
+// split form, the same grid, box, tile choices and kernel forms, the
+// four-point and z-pencil kernels, no closure correction, and the magnetic
+// branch (if any) after the hydro one.
+bool engine_batchable(const Engine &a, const Engine &b)
+{
+    auto ok = [](const Engine &e) {
+        return e.split && !e.corr_on && !e.prof_on && !(mag_on(e) && e.par_mag) && e.nx % 4 == 0 && e.vec4 &&
+               e.zpencil && e.np % 512 == 0 && e.nz >= 6;
+    };
+    return ok(a) && ok(b) && a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.p.xmax == b.p.xmax &&
+           a.p.ymax == b.p.ymax && a.kc_pass2 == b.kc_pass2 && a.ct_s == b.ct_s && a.pdl == b.pdl &&
+           a.int_cvt == b.int_cvt && a.generic_lines == b.generic_lines && a.ct_warp == b.ct_warp &&
+           a.p.dalias == b.p.dalias && a.nit == b.nit;
+}
+
+// The device work of one time step (no diagnostics) of a batch of members
+// that engine_batchable pairs, each kernel one launch over all of them; the
+// same stages in the same order as enqueue_step, per member: members with a
+// magnetic branch take the folded path (coefficients in mag_div, history
+// rotation in bandj), the others zero their magnetic RHS.  Host counters are
+// advanced by the caller.
+int engine_enqueue_step_batch(Engine *const *Es, int nE)
+{
+    if (nE < 1 || nE > BATCH_MAX) return VEC_ERR_ARG;
+    Engine *mag[BATCH_MAX], *off[BATCH_MAX];
+    bool wm[BATCH_MAX], folded[BATCH_MAX];
+    int mdeal[BATCH_MAX];
+    int nm = 0, no = 0, st;
+    for (int i = 0; i < nE; i++) {
+        const bool m = mag_on(*Es[i]) != 0;
+        wm[i] = m;
+        folded[i] = m;
+        mdeal[i] = Es[i]->p.dalias && m;
+        if (m) mag[nm++] = Es[i];
+        else off[no++] = Es[i];
+    }
+    if ((st = split_hydro_m(Es, nE, wm))) return st;
+    if (nm && (st = split_mag_m(mag, nm, true, true))) return st;
+    if (no && (st = phys_zero_mag_rhs_m(off, no))) return st;
+    if ((st = split_ab3_m(Es, nE, mdeal, folded))) return st;
+    const int nit = Es[0]->nit;
+    if (Es[0]->p.dalias && nit % 10 == 0 && (st = split_dealias_m(Es, nE))) return st;
+    if (nm && (st = split_bandj_m(mag, nm, true))) return st;
+    if (nm && (st = phys_boundaries_m(mag, nm))) return st;
+    if (no && (st = phys_boundary_m(off, no))) return st;
+    if (nit % 10 == 0 && (st = split_calcdt_m(Es, nE))) return st;
+    return VEC_OK;
+}
+
 static bool diag_due(const Engine &E, int nit)
 {
     return E.p.diag_cadence && E.p.ndu06 > 0 && (nit % E.p.ndu06 == 0);

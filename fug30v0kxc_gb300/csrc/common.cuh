@@ -45,7 +45,7 @@ struct LineJob {
     double addc;
 };
 
-#define MAX_JOBS 16
+#define MAX_JOBS 64   // line jobs per launch (an ensemble batch carries 5-8 per member)
 
 // spectral tables of one direction (device pointers)
 template <typename R>
@@ -135,6 +135,14 @@ struct HistTable {
     void *p[7][3];          // r, t, u, v, w, pol, tor
     double *bx[3], *by[3];  // bxbardot, bybardot
 };
+
+// The arguments of one kernel for each member of a batch: equally sized
+// contexts (one grid size of an ensemble) whose step runs as one launch per
+// kernel, blockIdx.z picking the member.  A single context is a batch of
+// one (NB = 1, member index 0).
+#define BATCH_MAX 16
+template <typename A, int NB> struct Batch { A a[NB]; };
+#define BATCH_MEMBER(bt, NB) ((bt).a[(NB) > 1 ? blockIdx.z : 0])
 
 // First statement of the step's kernels: with programmatic dependent launch
 // a kernel may be started while its predecessor in the stream still runs,

@@ -159,6 +159,38 @@ inline cudaError_t launch_k(const Engine &E, void (*kern)(KArgs...), dim3 grid, 
     return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
+// One kernel over the members of a batch of equally sized contexts (see
+// Batch): make(E) builds a member's arguments; a batch of one launches the
+// NB = 1 instance, a larger one the BATCH_MAX instance with one grid layer
+// (blockIdx.z) per member.  The launch runs on (and is counted and profiled
+// by) the first member; bytes are per member.
+template <typename A, typename F>
+inline int launch_members(Engine *const *Es, int nE, const char *name, double bytes, dim3 grid, dim3 block,
+                          size_t smem, void (*k1)(Batch<A, 1>), void (*kb)(Batch<A, BATCH_MAX>), F make)
+{
+    Engine *E = Es[0];
+    if (nE < 1 || nE > BATCH_MAX) return VEC_ERR_ARG;
+    E->prof_begin(name, bytes * nE);
+    cudaError_t e;
+    if (nE == 1) {
+        Batch<A, 1> b;
+        b.a[0] = make(Es[0]);
+        e = launch_k(*E, k1, grid, block, smem, b);
+    } else {
+        Batch<A, BATCH_MAX> b;
+        for (int i = 0; i < nE; i++) b.a[i] = make(Es[i]);
+        grid.z = (unsigned)nE;
+        e = launch_k(*E, kb, grid, block, smem, b);
+    }
+    E->prof_end();
+    if (e != cudaSuccess) {
+        vec_set_error("%s: launch failed: %s", name, cudaGetErrorString(e));
+        return VEC_ERR_CUDA;
+    }
+    CUDA_TRY(cudaGetLastError());
+    return VEC_OK;
+}
+
 template <typename R> inline HTab<R> htab(const Engine &E);
 // one CTA row of 256 threads per plane (the spectral kernels of magkern.cuh)
 inline dim3 plane_grid(const Engine &E) { return dim3((unsigned)((E.np + 255) / 256), (unsigned)E.nz); }
@@ -246,3 +278,25 @@ int split_sync_b64(Engine *E);
 int split_ab3(Engine *E, int magdealias, bool folded = false);
 int split_dealias(Engine *E);
 int split_calcdt(Engine *E);
+
+// The same stages for a batch of equally sized split-form contexts (one grid
+// of an ensemble): one launch per kernel covers every member (Batch,
+// launch_members); line jobs of all members share the line launches.
+int phys_zero_mag_rhs_m(Engine *const *Es, int nE);
+int phys_boundary_m(Engine *const *Es, int nE);
+int phys_boundaries_m(Engine *const *Es, int nE);
+int phys_rotate_hist_m(Engine *const *Es, int nE);
+int phys_ab3_coef_m(Engine *const *Es, int nE);
+int phys_calcdt_m(Engine *const *Es, int nE);
+int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag);
+int split_emf_m(Engine *const *Es, int nE);
+int split_mag_m(Engine *const *Es, int nE, bool ab3_coef, bool spectra_done);
+int split_bandj_m(Engine *const *Es, int nE, bool rotate_hist);
+int split_ab3_m(Engine *const *Es, int nE, const int *magdealias, const bool *folded);
+int split_dealias_m(Engine *const *Es, int nE);
+int split_sync_b64_m(Engine *const *Es, int nE);
+int split_calcdt_m(Engine *const *Es, int nE);
+// capi.cu: one graph step of a batch (no diagnostics, no profiling), and
+// whether two contexts can share a batch
+int engine_enqueue_step_batch(Engine *const *Es, int nE);
+bool engine_batchable(const Engine &a, const Engine &b);

@@ -3,11 +3,15 @@
 //
 // Every member is a full context (its own arrays and stream).  One ensemble
 // step is captured once per step variant (plain, or the tenth step with
-// dealias and calcdt): the root stream forks to every member stream through
-// an event, each member enqueues its own time step, and the root joins them
-// again, so the graph holds one independent branch per member and the GPU
-// runs small members concurrently.  Steps with diagnostics (a host read-back)
-// run without the graph.
+// dealias and calcdt).  Members of one grid (and the same kernel forms and
+// tile choices) form batches of up to BATCH_MAX: every kernel of the step is
+// one launch over all members of a batch (blockIdx.z picks the member, the
+// line kernels take all members' jobs), so the ensemble step is a few
+// launches per grid rather than per member.  The root stream forks to each
+// batch (and each member that fits no batch) through an event and joins them
+// again, so the graph holds one branch per batch and the GPU runs them
+// concurrently.  Steps with diagnostics (a host read-back) run without the
+// graph, member by member.
 //
 // The autotuner picks, per distinct grid, the planes per z chunk of hydro
 // pass 2 and the sequences per tile of the line kernels by
@@ -149,20 +153,42 @@ extern "C" int vec_ensemble_step(vec_ens *e, int nsteps)
         }
         const int v = nit % 10 == 0 ? 1 : 0;
         if (!e->g[v]) {
+            // members that can share launches form batches of up to
+            // BATCH_MAX (one grid, one launch per kernel for all of them);
+            // each batch, and each other member, is one branch of the graph
+            std::vector<std::vector<int>> groups;
+            for (int i = 0; i < nm; i++) {
+                Engine &E = engine_of(e->m[i]);
+                bool placed = false;
+                for (auto &g : groups) {
+                    Engine &L = engine_of(e->m[g[0]]);
+                    if ((int)g.size() < BATCH_MAX && engine_batchable(L, E)) { g.push_back(i); placed = true; break; }
+                }
+                if (!placed) groups.push_back(std::vector<int>{ i });
+            }
             CUDA_TRY(cudaStreamBeginCapture(e->root, cudaStreamCaptureModeThreadLocal));
             int st = VEC_OK;
             if (cudaEventRecord(e->ev_root, e->root) != cudaSuccess) st = VEC_ERR_CUDA;
-            for (int i = 0; i < nm && !st; i++) {
-                Engine &E = engine_of(e->m[i]);
-                if (cudaStreamWaitEvent(E.stream, e->ev_root, 0) != cudaSuccess) { st = VEC_ERR_CUDA; break; }
-                E.nit += 1;
-                E.iter += 1;
-                const long long l0 = E.launches;
-                st = engine_enqueue_step(E, false);
-                e->b32_after[v][i] = E.b32_auth;
-                e->launches[v][i] = E.launches - l0;
-                if (!st && cudaEventRecord(e->ev[i], E.stream) != cudaSuccess) st = VEC_ERR_CUDA;
-                if (!st && cudaStreamWaitEvent(e->root, e->ev[i], 0) != cudaSuccess) st = VEC_ERR_CUDA;
+            for (size_t gi = 0; gi < groups.size() && !st; gi++) {
+                const std::vector<int> &g = groups[gi];
+                Engine &L = engine_of(e->m[g[0]]);
+                if (cudaStreamWaitEvent(L.stream, e->ev_root, 0) != cudaSuccess) { st = VEC_ERR_CUDA; break; }
+                Engine *Es[BATCH_MAX];
+                long long l0[BATCH_MAX];
+                for (size_t q = 0; q < g.size(); q++) {
+                    Engine &E = engine_of(e->m[g[q]]);
+                    E.nit += 1;
+                    E.iter += 1;
+                    l0[q] = E.launches;
+                    Es[q] = &E;
+                }
+                st = g.size() == 1 ? engine_enqueue_step(L, false) : engine_enqueue_step_batch(Es, (int)g.size());
+                for (size_t q = 0; q < g.size(); q++) {
+                    e->b32_after[v][g[q]] = Es[q]->b32_auth;
+                    e->launches[v][g[q]] = Es[q]->launches - l0[q];
+                }
+                if (!st && cudaEventRecord(e->ev[g[0]], L.stream) != cudaSuccess) st = VEC_ERR_CUDA;
+                if (!st && cudaStreamWaitEvent(e->root, e->ev[g[0]], 0) != cudaSuccess) st = VEC_ERR_CUDA;
             }
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(e->root, &g);

@@ -255,10 +255,21 @@ __device__ __forceinline__ V4 sdy4(const float *plane, int i0, int j, int nx, in
     return 2 * j < ny ? -v : v;
 }
 
-static __global__ void k_emf4(const float *u, const float *v, const float *w, const float *bx, const float *by,
-                              const float *bz, float *e1, float *e2, float *e3, size_t n4, float bzoff)
+struct Emf4Args {
+    const float *u, *v, *w, *bx, *by, *bz;
+    float *e1, *e2, *e3;
+    size_t n4;
+    float bzoff;
+};
+template <int NB>
+static __global__ void k_emf4(const __grid_constant__ Batch<Emf4Args, NB> bt)
 {
     PDL_WAIT();
+    const Emf4Args &A = BATCH_MEMBER(bt, NB);
+    const float *u = A.u, *v = A.v, *w = A.w, *bx = A.bx, *by = A.by, *bz = A.bz;
+    float *e1 = A.e1, *e2 = A.e2, *e3 = A.e3;
+    const size_t n4 = A.n4;
+    const float bzoff = A.bzoff;
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n4) return;
     const V4 U = ld4(u, i), Vv = ld4(v, i), W = ld4(w, i), BX = ld4(bx, i), BY = ld4(by, i);
@@ -273,10 +284,23 @@ static __global__ void k_emf4(const float *u, const float *v, const float *w, co
 // two; the row is dispatched first, so that the CTA's serial FP64 work is
 // not the grid's tail.  No plane of this kernel, and none of k_mag_final4
 // that follows it, reads ds, bxbar, bybar or the bx/by histories.)
-static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, int nx, int ny, HTab<float> h,
-                                  MeanArgs<float> ma)
+struct MagDiv4Args {
+    const float *ex, *ey;
+    float *w1;
+    int nx, ny;
+    HTab<float> h;
+    MeanArgs<float> ma;
+};
+template <int NB>
+static __global__ void k_mag_div4(const __grid_constant__ Batch<MagDiv4Args, NB> bt)
 {
     PDL_WAIT();
+    const MagDiv4Args &A = BATCH_MEMBER(bt, NB);
+    const float *ex = A.ex, *ey = A.ey;
+    float *w1 = A.w1;
+    const int nx = A.nx, ny = A.ny;
+    const HTab<float> &h = A.h;
+    const MeanArgs<float> &ma = A.ma;
     if (blockIdx.y == 0) {
         if (blockIdx.x == 0) {
             mean_rhs_block(ma);
@@ -297,9 +321,11 @@ static __global__ void k_mag_div4(const float *ex, const float *ey, float *w1, i
 }
 
 // (four CTAs per SM: 3.4 TB/s against 2.1 at the compiler's own 90 registers)
-static __global__ void __launch_bounds__(256, 4) k_mag_final4(MagArgs<float> a)
+template <int NB>
+static __global__ void __launch_bounds__(256, 4) k_mag_final4(const __grid_constant__ Batch<MagArgs<float>, NB> bt)
 {
     PDL_WAIT();
+    const MagArgs<float> &a = BATCH_MEMBER(bt, NB);
     const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -333,9 +359,11 @@ static __global__ void __launch_bounds__(256, 4) k_mag_final4(MagArgs<float> a)
     }
 }
 
-static __global__ void k_bandj_spec4(BandjArgs<float> a)
+template <int NB>
+static __global__ void k_bandj_spec4(const __grid_constant__ Batch<BandjArgs<float>, NB> bt)
 {
     PDL_WAIT();
+    const BandjArgs<float> &a = BATCH_MEMBER(bt, NB);
     const unsigned np = (unsigned)a.nx * a.ny, np4 = np / 4;
     const unsigned q4 = blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -379,10 +407,23 @@ static __global__ void k_bandj_spec4(BandjArgs<float> a)
     st4(a.dxbz, i4, V4(dx[0], dx[1], dx[2], dx[3]));
 }
 
-static __global__ void k_jsq4(const float *jz, const float *dybz, const float *dxbz, const float *bx, const float *by,
-                              float *jsq, size_t np, int nz, float h)
+struct Jsq4Args {
+    const float *jz, *dybz, *dxbz, *bx, *by;
+    float *jsq;
+    size_t np;
+    int nz;
+    float h;
+};
+template <int NB>
+static __global__ void k_jsq4(const __grid_constant__ Batch<Jsq4Args, NB> bt)
 {
     PDL_WAIT();
+    const Jsq4Args &A = BATCH_MEMBER(bt, NB);
+    const float *jz = A.jz, *dybz = A.dybz, *dxbz = A.dxbz, *bx = A.bx, *by = A.by;
+    float *jsq = A.jsq;
+    const size_t np = A.np;
+    const int nz = A.nz;
+    const float h = A.h;
     const size_t np4 = np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -417,10 +458,18 @@ static __global__ void k_truncate(R *a, R *b, int nx, int ny, int nz, int cx, in
 }
 
 // zero the newest magnetic RHS slots (F = 0, src/main.F90:355-376)
-template <typename R>
-static __global__ void k_zero_mag_rhs(const HistTable *ht, size_t n, int nz)
+struct ZeroMagArgs {
+    const HistTable *ht;
+    size_t n;
+    int nz;
+};
+template <typename R, int NB>
+static __global__ void k_zero_mag_rhs(const __grid_constant__ Batch<ZeroMagArgs, NB> bt)
 {
     PDL_WAIT();
+    const HistTable *ht = BATCH_MEMBER(bt, NB).ht;
+    const size_t n = BATCH_MEMBER(bt, NB).n;
+    const int nz = BATCH_MEMBER(bt, NB).nz;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) { ((R *)ht->p[5][2])[i] = (R)0; ((R *)ht->p[6][2])[i] = (R)0; }
     if (i < (size_t)nz) { ht->bx[2][i] = 0.0; ht->by[2][i] = 0.0; }
@@ -440,8 +489,9 @@ __device__ __forceinline__ void rotate_hist_table(HistTable *ht)
     ht->bx[0] = ht->bx[1]; ht->bx[1] = ht->bx[2]; ht->bx[2] = x;
     ht->by[0] = ht->by[1]; ht->by[1] = ht->by[2]; ht->by[2] = y;
 }
-static __global__ void k_rotate_hist(HistTable *ht)
+template <int NB>
+static __global__ void k_rotate_hist(const __grid_constant__ Batch<HistTable *, NB> bt)
 {
     PDL_WAIT();
-    if (threadIdx.x == 0) rotate_hist_table(ht);
+    if (threadIdx.x == 0) rotate_hist_table(BATCH_MEMBER(bt, NB));
 }

@@ -335,15 +335,18 @@ int phys_mag64(Engine *E)
     return VEC_OK;
 }
 
-int phys_zero_mag_rhs(Engine *E)
+int phys_zero_mag_rhs_m(Engine *const *Es, int nE)
 {
+    Engine *E = Es[0];
     size_t cnt = E->n > (size_t)E->nz ? E->n : (size_t)E->nz;
+    auto mk = [](Engine *e) { return ZeroMagArgs{ e->ht, e->n, e->nz }; };
     if (E->split)
-        KLAUNCH(E, "zero_mag_rhs", k_zero_mag_rhs<float>, nblk(cnt), TPB, E->ht, E->n, E->nz);
-    else
-        KLAUNCH(E, "zero_mag_rhs", k_zero_mag_rhs<double>, nblk(cnt), TPB, E->ht, E->n, E->nz);
-    return VEC_OK;
+        return launch_members<ZeroMagArgs>(Es, nE, "zero_mag_rhs", 0.0, dim3(nblk(cnt)), dim3(TPB), 0,
+                                           k_zero_mag_rhs<float, 1>, k_zero_mag_rhs<float, BATCH_MAX>, mk);
+    return launch_members<ZeroMagArgs>(Es, nE, "zero_mag_rhs", 0.0, dim3(nblk(cnt)), dim3(TPB), 0,
+                                       k_zero_mag_rhs<double, 1>, k_zero_mag_rhs<double, BATCH_MAX>, mk);
 }
+int phys_zero_mag_rhs(Engine *E) { return phys_zero_mag_rhs_m(&E, 1); }
 
 // ============================================================================
 // bandj: src/magnetic.f90:492-664
@@ -432,25 +435,45 @@ __device__ __forceinline__ void boundary_column(double *u, double *v, double *w,
 #undef P
 }
 
-__global__ void k_boundary(double *u, double *v, double *w, double *t, size_t np, int nz, double theta,
-                           double dz, int radbc, int constflux, BoundaryMirrors mb)
-{
-    PDL_WAIT();
-    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < np) boundary_column(u, v, w, t, np, nz, theta, dz, radbc, constflux, mb, q);
-}
+// arguments of k_boundary / k_boundaries
+struct BndArgs {
+    double *u, *v, *w, *t, *pol, *tor, *bxb, *byb;
+    size_t np;
+    int nz;
+    double theta, dz;
+    int radbc, constflux, perfect;
+    BoundaryMirrors mb;
+};
 
-int phys_boundary(Engine *E)
+static BndArgs bnd_args(Engine *E)
 {
+    BndArgs a;
     BoundaryMirrors mb = {};
     if (E->split) {
         mb.u32 = E->u32; mb.v32 = E->v32; mb.w32 = E->w32; mb.t32 = E->t32; mb.t0 = split_bg_t0(E);
         mb.pol32 = E->pol32; mb.tor32 = E->tor32;
     }
-    KLAUNCH(E, "boundary_f64", k_boundary, nblk(E->np), TPB, E->u, E->v, E->w, E->t, E->np, E->nz, E->p.theta,
-            E->k.dz, E->p.radbc, E->p.constflux, mb);
-    return VEC_OK;
+    a.u = E->u; a.v = E->v; a.w = E->w; a.t = E->t; a.pol = E->pol; a.tor = E->tor; a.bxb = E->bxbar; a.byb = E->bybar;
+    a.np = E->np; a.nz = E->nz; a.theta = E->p.theta; a.dz = E->k.dz;
+    a.radbc = E->p.radbc; a.constflux = E->p.constflux; a.perfect = E->p.perfect; a.mb = mb;
+    return a;
 }
+
+template <int NB>
+__global__ void k_boundary(const __grid_constant__ Batch<BndArgs, NB> bt)
+{
+    PDL_WAIT();
+    const BndArgs &a = BATCH_MEMBER(bt, NB);
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < a.np) boundary_column(a.u, a.v, a.w, a.t, a.np, a.nz, a.theta, a.dz, a.radbc, a.constflux, a.mb, q);
+}
+
+int phys_boundary_m(Engine *const *Es, int nE)
+{
+    return launch_members<BndArgs>(Es, nE, "boundary_f64", 0.0, dim3(nblk(Es[0]->np)), dim3(TPB), 0, k_boundary<1>,
+                                   k_boundary<BATCH_MAX>, bnd_args);
+}
+int phys_boundary(Engine *E) { return phys_boundary_m(&E, 1); }
 
 __device__ __forceinline__ void mag_boundary_column(double *pol, double *tor, double *bxb, double *byb, size_t np,
                                                     int nz, int perfect, const BoundaryMirrors &mb, size_t q)
@@ -496,27 +519,22 @@ __global__ void k_mag_boundary(double *pol, double *tor, double *bxb, double *by
 }
 
 // boundary and mag_boundary of one step in one launch (disjoint fields)
-__global__ void k_boundaries(double *u, double *v, double *w, double *t, double *pol, double *tor, double *bxb,
-                             double *byb, size_t np, int nz, double theta, double dz, int radbc, int constflux,
-                             int perfect, BoundaryMirrors mb)
+template <int NB>
+__global__ void k_boundaries(const __grid_constant__ Batch<BndArgs, NB> bt)
 {
     PDL_WAIT();
+    const BndArgs &a = BATCH_MEMBER(bt, NB);
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < np) boundary_column(u, v, w, t, np, nz, theta, dz, radbc, constflux, mb, q);
-    mag_boundary_column(pol, tor, bxb, byb, np, nz, perfect, mb, q);
+    if (q < a.np) boundary_column(a.u, a.v, a.w, a.t, a.np, a.nz, a.theta, a.dz, a.radbc, a.constflux, a.mb, q);
+    mag_boundary_column(a.pol, a.tor, a.bxb, a.byb, a.np, a.nz, a.perfect, a.mb, q);
 }
 
-int phys_boundaries(Engine *E)
+int phys_boundaries_m(Engine *const *Es, int nE)
 {
-    BoundaryMirrors mb = {};
-    if (E->split) {
-        mb.u32 = E->u32; mb.v32 = E->v32; mb.w32 = E->w32; mb.t32 = E->t32; mb.t0 = split_bg_t0(E);
-        mb.pol32 = E->pol32; mb.tor32 = E->tor32;
-    }
-    KLAUNCH(E, "boundaries", k_boundaries, nblk(E->np), TPB, E->u, E->v, E->w, E->t, E->pol, E->tor, E->bxbar,
-            E->bybar, E->np, E->nz, E->p.theta, E->k.dz, E->p.radbc, E->p.constflux, E->p.perfect, mb);
-    return VEC_OK;
+    return launch_members<BndArgs>(Es, nE, "boundaries", 0.0, dim3(nblk(Es[0]->np)), dim3(TPB), 0, k_boundaries<1>,
+                                   k_boundaries<BATCH_MAX>, bnd_args);
 }
+int phys_boundaries(Engine *E) { return phys_boundaries_m(&E, 1); }
 
 int phys_mag_boundary(Engine *E)
 {
@@ -532,10 +550,18 @@ int phys_mag_boundary(Engine *E)
 // ============================================================================
 // coefficients (:381-403), dt1/dt2 (:488-489), ttime (:345) and the 1-D mean
 // update (:469-476) on one CTA
-__global__ void k_ab3_coef(DevScalars *ds, double *bxbar, double *bybar, const HistTable *ht, int nz, int do_means)
+struct CoefArgs {
+    DevScalars *ds;
+    double *bxbar, *bybar;
+    const HistTable *ht;
+    int nz, do_means;
+};
+template <int NB>
+__global__ void k_ab3_coef(const __grid_constant__ Batch<CoefArgs, NB> bt)
 {
     PDL_WAIT();
-    ab3_coef_block(ds, bxbar, bybar, ht, nz, do_means);
+    const CoefArgs &a = BATCH_MEMBER(bt, NB);
+    ab3_coef_block(a.ds, a.bxbar, a.bybar, a.ht, a.nz, a.do_means);
 }
 
 struct Ab3Args {
@@ -579,11 +605,12 @@ __global__ void k_ab3_update(Ab3Args a)
 #undef H
 }
 
-int phys_rotate_hist(Engine *E)
+int phys_rotate_hist_m(Engine *const *Es, int nE)
 {
-    KLAUNCH(E, "rotate_hist", k_rotate_hist, 1, 32, E->ht);
-    return VEC_OK;
+    return launch_members<HistTable *>(Es, nE, "rotate_hist", 0.0, dim3(1), dim3(32), 0, k_rotate_hist<1>,
+                                       k_rotate_hist<BATCH_MAX>, [](Engine *e) { return e->ht; });
 }
+int phys_rotate_hist(Engine *E) { return phys_rotate_hist_m(&E, 1); }
 
 int hist_table_host(Engine *E, HistTable *h)
 {
@@ -592,11 +619,13 @@ int hist_table_host(Engine *E, HistTable *h)
     return VEC_OK;
 }
 
-int phys_ab3_coef(Engine *E)
+int phys_ab3_coef_m(Engine *const *Es, int nE)
 {
-    KLAUNCH(E, "ab3_coef", k_ab3_coef, 1, 256, E->ds, E->bxbar, E->bybar, E->ht, E->nz, 1);
-    return VEC_OK;
+    return launch_members<CoefArgs>(Es, nE, "ab3_coef", 0.0, dim3(1), dim3(256), 0, k_ab3_coef<1>,
+                                    k_ab3_coef<BATCH_MAX>,
+                                    [](Engine *e) { return CoefArgs{ e->ds, e->bxbar, e->bybar, e->ht, e->nz, 1 }; });
 }
+int phys_ab3_coef(Engine *E) { return phys_ab3_coef_m(&E, 1); }
 
 int phys_ab3(Engine *E, int magdealias)
 {
@@ -734,9 +763,12 @@ __device__ __forceinline__ void block_reduce3(float &mx, float &mz, float &mn, f
     }
 }
 
-__global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
+template <int NB>
+__global__ void __launch_bounds__(256) k_calcdt_est(const __grid_constant__ Batch<CdtArgs, NB> bt)
 {
     PDL_WAIT();
+    const CdtArgs &a = BATCH_MEMBER(bt, NB);
+    if ((int)blockIdx.x >= a.nchunks) return;
     __shared__ float sh[96];
     const size_t i0 = (size_t)blockIdx.x * CDT_CHUNK;
     const size_t i1 = i0 + CDT_CHUNK < a.n ? i0 + CDT_CHUNK : a.n;
@@ -766,9 +798,12 @@ __global__ void __launch_bounds__(256) k_calcdt_est(CdtArgs a)
     }
 }
 
-__global__ void __launch_bounds__(256) k_calcdt_exact(CdtArgs a)
+template <int NB>
+__global__ void __launch_bounds__(256) k_calcdt_exact(const __grid_constant__ Batch<CdtArgs, NB> bt)
 {
     PDL_WAIT();
+    const CdtArgs &a = BATCH_MEMBER(bt, NB);
+    if ((int)blockIdx.x >= a.nchunks) return;
     const float gx = okey32_dec(a.gkey[0]), gz = okey32_dec(a.gkey[1]), gr = okey32_dec(a.gkey[2]);
     // thresholds a relative margin below (above) the estimates; scaling
     // keeps infinite estimates infinite
@@ -808,11 +843,23 @@ __global__ void __launch_bounds__(256) k_calcdt_exact(CdtArgs a)
     }
 }
 
-__global__ void k_calcdt_fin(DevScalars *ds, unsigned *gkey, double dd, double dz, double dtvisc0x,
-                             double dtvisc0z, double dtdiff0x, double dtdiff0z, double sf, int var_eta,
-                             double eta_max)
+struct CdtFinArgs {
+    DevScalars *ds;
+    unsigned *gkey;
+    double dd, dz, dtvisc0x, dtvisc0z, dtdiff0x, dtdiff0z, sf;
+    int var_eta;
+    double eta_max;
+};
+template <int NB>
+__global__ void k_calcdt_fin(const __grid_constant__ Batch<CdtFinArgs, NB> bt)
 {
     PDL_WAIT();
+    const CdtFinArgs &A = BATCH_MEMBER(bt, NB);
+    DevScalars *ds = A.ds;
+    unsigned *gkey = A.gkey;
+    const double dd = A.dd, dz = A.dz, dtvisc0x = A.dtvisc0x, dtvisc0z = A.dtvisc0z, dtdiff0x = A.dtdiff0x;
+    const double dtdiff0z = A.dtdiff0z, sf = A.sf, eta_max = A.eta_max;
+    const int var_eta = A.var_eta;
     double velmxx = okey_dec(ds->velmxx);
     double velmxz = okey_dec(ds->velmxz);
     double denmn = okey_dec(ds->denmn);
@@ -835,7 +882,7 @@ __global__ void k_calcdt_fin(DevScalars *ds, unsigned *gkey, double dd, double d
 
 int cdt_chunks(size_t n) { return (int)((n + CDT_CHUNK - 1) / CDT_CHUNK); }
 
-int phys_calcdt(Engine *E)
+static CdtArgs cdt_args(Engine *E)
 {
     CdtArgs a;
     a.u = E->u; a.v = E->v; a.w = E->w; a.r = E->r; a.t = E->t; a.bx = E->bx; a.by = E->by; a.bz = E->bz;
@@ -844,13 +891,29 @@ int phys_calcdt(Engine *E)
     a.gkey = reinterpret_cast<unsigned *>(E->cdt);
     a.chunk = E->cdt + 4;
     a.ds = E->ds;
-    KLAUNCHB(E, "calcdt_est_f64", FB(E, 8, 8), k_calcdt_est, (unsigned)a.nchunks, 256, a);
-    KLAUNCH(E, "calcdt_exact", k_calcdt_exact, (unsigned)a.nchunks, 256, a);
-    const Consts &c = E->k;
-    KLAUNCH(E, "calcdt_fin", k_calcdt_fin, 1, 1, E->ds, a.gkey, c.dd, c.dz, c.dtvisc0x, c.dtvisc0z, c.dtdiff0x,
-            c.dtdiff0z, c.sf, c.var_eta, c.eta_max);
-    return VEC_OK;
+    return a;
 }
+
+int phys_calcdt_m(Engine *const *Es, int nE)
+{
+    Engine *E = Es[0];
+    const unsigned nch = (unsigned)cdt_chunks(E->n);
+    int st;
+    if ((st = launch_members<CdtArgs>(Es, nE, "calcdt_est_f64", FB(E, 8, 8), dim3(nch), dim3(256), 0,
+                                      k_calcdt_est<1>, k_calcdt_est<BATCH_MAX>, cdt_args)))
+        return st;
+    if ((st = launch_members<CdtArgs>(Es, nE, "calcdt_exact", 0.0, dim3(nch), dim3(256), 0, k_calcdt_exact<1>,
+                                      k_calcdt_exact<BATCH_MAX>, cdt_args)))
+        return st;
+    return launch_members<CdtFinArgs>(Es, nE, "calcdt_fin", 0.0, dim3(1), dim3(1), 0, k_calcdt_fin<1>,
+                                      k_calcdt_fin<BATCH_MAX>, [](Engine *e) {
+                                          const Consts &c = e->k;
+                                          return CdtFinArgs{ e->ds, reinterpret_cast<unsigned *>(e->cdt), c.dd, c.dz,
+                                                             c.dtvisc0x, c.dtvisc0z, c.dtdiff0x, c.dtdiff0z, c.sf,
+                                                             c.var_eta, c.eta_max };
+                                      });
+}
+int phys_calcdt(Engine *E) { return phys_calcdt_m(&E, 1); }
 
 // ============================================================================
 // diagnostics: GlobalAverages (src/utils.F90:22-139), nusselt

@@ -203,10 +203,21 @@ static int mirror(Engine *E, int mask, int k0, int k1)
     return VEC_OK;
 }
 
-__global__ void k_b64(const float *bx32, const float *by32, const float *bz32, const float *jsq32, double *bx,
-                      double *by, double *bz, double *jsq, double bzbar, size_t n)
+struct B64Args {
+    const float *bx32, *by32, *bz32, *jsq32;
+    double *bx, *by, *bz, *jsq;
+    double bzbar;
+    size_t n;
+};
+template <int NB>
+__global__ void k_b64(const __grid_constant__ Batch<B64Args, NB> bt)
 {
     PDL_WAIT();
+    const B64Args &A = BATCH_MEMBER(bt, NB);
+    const float *bx32 = A.bx32, *by32 = A.by32, *bz32 = A.bz32, *jsq32 = A.jsq32;
+    double *bx = A.bx, *by = A.by, *bz = A.bz, *jsq = A.jsq;
+    const double bzbar = A.bzbar;
+    const size_t n = A.n;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     // (conversions on the integer pipe, the same bits as the casts)
@@ -217,13 +228,22 @@ __global__ void k_b64(const float *bx32, const float *by32, const float *bz32, c
 }
 
 // FP64 B and jsq from the FP32 ones when the FP32 copy is the newer one
+// (every member of the batch, which all have it newer)
+int split_sync_b64_m(Engine *const *Es, int nE)
+{
+    int st = launch_members<B64Args>(Es, nE, "b_to_f64", FB(Es[0], 4, 12), dim3(nblk(Es[0]->n)), dim3(TPB), 0,
+                                     k_b64<1>, k_b64<BATCH_MAX>, [](Engine *e) {
+                                         return B64Args{ e->bx32, e->by32, e->bz32, e->jsq32, e->bx, e->by, e->bz,
+                                                         e->jsq, e->bzbar, e->n };
+                                     });
+    if (st) return st;
+    for (int i = 0; i < nE; i++) Es[i]->b32_auth = 0;
+    return VEC_OK;
+}
 int split_sync_b64(Engine *E)
 {
     if (!E->b32_auth) return VEC_OK;
-    KLAUNCHB(E, "b_to_f64", FB(E, 4, 12), k_b64, nblk(E->n), TPB, E->bx32, E->by32, E->bz32, E->jsq32, E->bx,
-             E->by, E->bz, E->jsq, E->bzbar, E->n);
-    E->b32_auth = 0;
-    return VEC_OK;
+    return split_sync_b64_m(&E, 1);
 }
 
 // all FP32 mirrors from the FP64 state (after the state was set from outside)
@@ -273,6 +293,8 @@ struct SplitHydroArgs {
     int var_eta;
     size_t np;
     int nz;
+    int kc;                 // z-pencil kernel: planes per chunk
+    int *err;               // z-pencil kernel: the bounded waits' error flag
 };
 
 // the FP32 counterpart of k_hydro_pass2 (src/hydro_deriv.f90 terms without
@@ -410,9 +432,13 @@ struct ZRing2 {
     }
 };
 
-__global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(SplitHydroArgs a, int kc, int *err)
+template <int NB>
+__global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
 {
     PDL_WAIT();
+    const SplitHydroArgs &a = BATCH_MEMBER(bt, NB);
+    const int kc = a.kc;
+    int *err = a.err;
     extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE]
     __shared__ __align__(8) uint64_t full[ZT_SLOTS];
     const int nz = a.nz;
@@ -599,9 +625,11 @@ __global__ void k_split_pass4(SplitHydro4Args a)
 // loads and stores, four times fewer memory instructions in flight per point
 // (four CTAs per SM: 64 registers with a few spilled values; 5.3 TB/s
 // against 4.2 at the compiler's own 94 registers)
-__global__ void __launch_bounds__(256, 4) k_split_pass4_v4(SplitHydro4Args a)
+template <int NB>
+__global__ void __launch_bounds__(256, 4) k_split_pass4_v4(const __grid_constant__ Batch<SplitHydro4Args, NB> bt)
 {
     PDL_WAIT();
+    const SplitHydro4Args &a = BATCH_MEMBER(bt, NB);
     const size_t np4 = a.np / 4;
     const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q4 >= np4) return;
@@ -658,7 +686,7 @@ __global__ void __launch_bounds__(256, 4) k_split_pass4_v4(SplitHydro4Args a)
 // the three forward transforms of E = u x B that mag_deriv starts with;
 // with with_mag the x and y passes of the hydro derivatives carry them as
 // extra jobs, so one launch per direction serves both
-int split_emf(Engine *E);
+int split_emf_m(Engine *const *Es, int nE);
 static void mag_fwd_jobs(Engine *E, LineJob<float> *fx, LineJob<float> *fy)
 {
     float *W[W_COUNT];
@@ -671,35 +699,10 @@ static void mag_fwd_jobs(Engine *E, LineJob<float> *fx, LineJob<float> *fy)
     fy[2] = ljob<float>(W[W_EZ], W[W_EZ], OP_FWD);
 }
 
-int split_hydro(Engine *E, bool with_mag)
+static SplitHydroArgs hydro_args(Engine *E)
 {
     float *W[W_COUNT];
     for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
-    int st;
-    LineJob<float> fx[3], fy[3];
-    if (with_mag) {
-        if ((st = split_emf(E))) return st;
-        mag_fwd_jobs(E, fx, fy);
-    }
-    LineJob<float> jx[8] = {
-        ljob<float>(E->r32, W[W_RX], OP_D1),
-        ljob<float>(E->t32, W[W_TX], OP_D1, W[W_TXX], OP_D2),
-        ljob<float>(E->u32, W[W_UX], OP_D1, W[W_UXX], OP_D2),
-        ljob<float>(E->v32, W[W_VX], OP_D1, W[W_VXX], OP_D2),
-        ljob<float>(E->w32, W[W_WX], OP_D1, W[W_WXX], OP_D2),
-    };
-    if (with_mag) for (int i = 0; i < 3; i++) jx[5 + i] = fx[i];
-    if ((st = launch_lines<float>(E, 0, jx, with_mag ? 8 : 5))) return st;
-    LineJob<float> jy[8] = {
-        ljob<float>(E->r32, W[W_RY], OP_D1),
-        ljob<float>(E->t32, W[W_TY], OP_D1, W[W_TYY], OP_D2),
-        ljob<float>(E->u32, W[W_UY], OP_D1, W[W_UYY], OP_D2),
-        ljob<float>(E->v32, W[W_VY], OP_D1, W[W_VYY], OP_D2),
-        ljob<float>(E->w32, W[W_WY], OP_D1, W[W_WYY], OP_D2),
-    };
-    if (with_mag) for (int i = 0; i < 3; i++) jy[5 + i] = fy[i];
-    if ((st = launch_lines<float>(E, 1, jy, with_mag ? 8 : 5))) return st;
-
     const Consts &c = E->k;
     SplitHydroArgs a;
     a.r = E->r32; a.t = E->t32; a.u = E->u32; a.v = E->v32; a.w = E->w32;
@@ -717,121 +720,216 @@ int split_hydro(Engine *E, bool with_mag)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
+    // chunks of about kc_pass2 planes (tunable), balanced over nz
+    const int kt = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
+    const int nch = (E->nz + kt - 1) / kt;
+    a.kc = (E->nz + nch - 1) / nch;
+    a.err = E->dev_err;
+    return a;
+}
+
+// the second-level horizontal derivatives of pass 4 (the first-level
+// derivative arrays, free once pass 2 has run)
+#define DXU W_TXX
+#define DXV W_UXX
+#define DXW W_VXX
+#define DYU W_TYY
+#define DYV W_UYY
+#define DYW W_VYY
+
+static SplitHydro4Args hydro4_args(Engine *E)
+{
+    float *W[W_COUNT];
+    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    SplitHydro4Args b;
+    b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
+    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres; b.pc = E->pcf;
+    b.dxu = W[DXU]; b.dyu = W[DYU]; b.dxv = W[DXV]; b.dyv = W[DYV]; b.dxw = W[DXW]; b.dyw = W[DYW];
+    b.ht = E->ht;
+    b.ho12 = (float)E->k.ho12; b.np = E->np; b.nz = E->nz;
+    return b;
+}
+
+// True when the members' step can run as one launch per kernel: the
+// four-point and z-pencil forms (a batch of one takes any form)
+static bool batch_forms(Engine *const *Es, int nE)
+{
+    for (int i = 0; i < nE; i++) {
+        const Engine *E = Es[i];
+        if (!(E->nx % 4 == 0 && E->vec4 && E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6)) return nE == 1;
+    }
+    return true;
+}
+
+// hydro_deriv of the members (equally sized; one launch per kernel for all
+// of them).  with_mag[i]: E = u x B of member i and its forward transforms
+// ride in the line launches.
+int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
+{
+    Engine *E = Es[0];
+    if (!batch_forms(Es, nE)) return VEC_ERR_ARG;
+    int st;
+    Engine *mag[BATCH_MAX];
+    int nm = 0;
+    for (int i = 0; i < nE; i++)
+        if (with_mag[i]) mag[nm++] = Es[i];
+    if (nm && (st = split_emf_m(mag, nm))) return st;
+    std::vector<LineJob<float>> jx, jy, kx, ky;
+    for (int i = 0; i < nE; i++) {
+        Engine *M = Es[i];
+        float *W[W_COUNT];
+        for (int q = 0; q < W_COUNT; q++) W[q] = M->W<float>(q);
+        jx.push_back(ljob<float>(M->r32, W[W_RX], OP_D1));
+        jx.push_back(ljob<float>(M->t32, W[W_TX], OP_D1, W[W_TXX], OP_D2));
+        jx.push_back(ljob<float>(M->u32, W[W_UX], OP_D1, W[W_UXX], OP_D2));
+        jx.push_back(ljob<float>(M->v32, W[W_VX], OP_D1, W[W_VXX], OP_D2));
+        jx.push_back(ljob<float>(M->w32, W[W_WX], OP_D1, W[W_WXX], OP_D2));
+        jy.push_back(ljob<float>(M->r32, W[W_RY], OP_D1));
+        jy.push_back(ljob<float>(M->t32, W[W_TY], OP_D1, W[W_TYY], OP_D2));
+        jy.push_back(ljob<float>(M->u32, W[W_UY], OP_D1, W[W_UYY], OP_D2));
+        jy.push_back(ljob<float>(M->v32, W[W_VY], OP_D1, W[W_VYY], OP_D2));
+        jy.push_back(ljob<float>(M->w32, W[W_WY], OP_D1, W[W_WYY], OP_D2));
+        if (with_mag[i]) {
+            LineJob<float> fx[3], fy[3];
+            mag_fwd_jobs(M, fx, fy);
+            for (int q = 0; q < 3; q++) { jx.push_back(fx[q]); jy.push_back(fy[q]); }
+        }
+        // the second-level fluxes' derivatives (after pass 2)
+        kx.push_back(ljob<float>(W[W_P1], W[DXU], OP_D1));
+        kx.push_back(ljob<float>(W[W_Q], W[DXV], OP_D1));
+        kx.push_back(ljob<float>(W[W_G], W[DXW], OP_D1));
+        ky.push_back(ljob<float>(W[W_P2], W[DYV], OP_D1));
+        ky.push_back(ljob<float>(W[W_Q], W[DYU], OP_D1));
+        ky.push_back(ljob<float>(W[W_H], W[DYW], OP_D1));
+    }
+    if ((st = launch_lines<float>(E, 0, jx.data(), (int)jx.size()))) return st;
+    if ((st = launch_lines<float>(E, 1, jy.data(), (int)jy.size()))) return st;
+
     if (E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6) {
         static bool attr = false;
         const size_t smem = (size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float);
         if (!attr) {
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
             attr = true;
         }
-        // chunks of about kc_pass2 planes (tunable), balanced over nz
-        const int kt = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
-        const int nch = (E->nz + kt - 1) / kt, kc = (E->nz + nch - 1) / nch;
-        E->prof_begin("hydro_pass2_f32", FB(E, 39, 4));
-        CUDA_TRY(launch_k(*E, k_split_pass2_zt, dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
-                          dim3(ZT_TILE / 2), smem, a, kc, E->dev_err));
-        E->prof_end();
-        CUDA_TRY(cudaGetLastError());
+        const int kc = hydro_args(E).kc;
+        if ((st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4),
+                                                 dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
+                                                 dim3(ZT_TILE / 2), smem, k_split_pass2_zt<1>,
+                                                 k_split_pass2_zt<BATCH_MAX>, hydro_args)))
+            return st;
     } else if (E->nx % 4 == 0 && E->vec4) {
+        const SplitHydroArgs a = hydro_args(E);
         KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v2,
                  dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB, a);
     } else {
-        const int kc = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
-        dim3 g2(nblk(E->np), (unsigned)((E->nz + kc - 1) / kc));
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, kc);
+        const SplitHydroArgs a = hydro_args(E);
+        dim3 g2(nblk(E->np), (unsigned)((E->nz + a.kc - 1) / a.kc));
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, a.kc);
     }
 
-    // The second-level horizontal derivatives go to separate arrays (the
-    // first-level derivative arrays, free once pass 2 has run) and pass 4
-    // adds them: a line pass that accumulates into its output reads each
-    // output element before writing it, and that dependent read made those
-    // two launches the slowest line passes of the step.
-    float *dxu = W[W_TXX], *dxv = W[W_UXX], *dxw = W[W_VXX];
-    float *dyu = W[W_TYY], *dyv = W[W_UYY], *dyw = W[W_VYY];
-    LineJob<float> kx[3] = {
-        ljob<float>(W[W_P1], dxu, OP_D1),
-        ljob<float>(W[W_Q], dxv, OP_D1),
-        ljob<float>(W[W_G], dxw, OP_D1),
-    };
-    if ((st = launch_lines<float>(E, 0, kx, 3))) return st;
-    LineJob<float> ky[3] = {
-        ljob<float>(W[W_P2], dyv, OP_D1),
-        ljob<float>(W[W_Q], dyu, OP_D1),
-        ljob<float>(W[W_H], dyw, OP_D1),
-    };
-    if ((st = launch_lines<float>(E, 1, ky, 3))) return st;
+    // The second-level horizontal derivatives go to separate arrays and
+    // pass 4 adds them: a line pass that accumulates into its output reads
+    // each output element before writing it, and that dependent read made
+    // those two launches the slowest line passes of the step.
+    if ((st = launch_lines<float>(E, 0, kx.data(), (int)kx.size()))) return st;
+    if ((st = launch_lines<float>(E, 1, ky.data(), (int)ky.size()))) return st;
 
-    SplitHydro4Args b;
-    b.r = E->r32; b.t = E->t32; b.w = E->w32; b.p3 = W[W_P3]; b.p4 = W[W_P4]; b.g = W[W_G]; b.hh = W[W_H];
-    b.racc = W[W_RACC]; b.uacc = W[W_UACC]; b.vacc = W[W_VACC]; b.wacc = W[W_WACC]; b.bg = E->hres; b.pc = E->pcf;
-    b.dxu = dxu; b.dyu = dyu; b.dxv = dxv; b.dyv = dyv; b.dxw = dxw; b.dyw = dyw;
-    b.ht = E->ht;
-    b.ho12 = (float)c.ho12; b.np = E->np; b.nz = E->nz;
-    if (E->nx % 4 == 0 && E->vec4)
-        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 21, 4), k_split_pass4_v4,
-                 dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), TPB, b);
-    else
+    if (E->nx % 4 == 0 && E->vec4) {
+        if ((st = launch_members<SplitHydro4Args>(Es, nE, "hydro_pass4_f32", FB(E, 21, 4),
+                                                  dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), dim3(TPB), 0,
+                                                  k_split_pass4_v4<1>, k_split_pass4_v4<BATCH_MAX>, hydro4_args)))
+            return st;
+    } else {
+        const SplitHydro4Args b = hydro4_args(E);
         KLAUNCHB(E, "hydro_pass4_f32", FB(E, 21, 4), k_split_pass4, plane_grid(*E), TPB, b);
+    }
     return VEC_OK;
 }
+int split_hydro(Engine *E, bool with_mag) { return split_hydro_m(&E, 1, &with_mag); }
 
 // ---- mag_deriv ---------------------------------------------------------------
 // E = u x B (real space, FP32)
-int split_emf(Engine *E)
+int split_emf_m(Engine *const *Es, int nE)
 {
-    float *W[W_COUNT];
-    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    Engine *E = Es[0];
+    auto mk = [](Engine *e) {
+        float *W1 = e->W<float>(W_M1), *W2 = e->W<float>(W_M2), *W3 = e->W<float>(W_M3);
+        return Emf4Args{ e->u32, e->v32, e->w32, e->bx32, e->by32, e->bz32, W1, W2, W3, e->n / 4, (float)e->bzbar };
+    };
     if (E->nx % 4 == 0 && E->vec4)
-        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf4, nblk(E->n / 4), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
-                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n / 4, (float)E->bzbar);
-    else
-        KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf<float>, nblk(E->n), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
-                 E->bz32, W[W_M1], W[W_M2], W[W_M3], E->n, (float)E->bzbar);
+        return launch_members<Emf4Args>(Es, nE, "emf_f32", FB(E, 9, 4), dim3(nblk(E->n / 4)), dim3(TPB), 0,
+                                        k_emf4<1>, k_emf4<BATCH_MAX>, mk);
+    if (nE != 1) return VEC_ERR_ARG;
+    KLAUNCHB(E, "emf_f32", FB(E, 9, 4), k_emf<float>, nblk(E->n), TPB, E->u32, E->v32, E->w32, E->bx32, E->by32,
+             E->bz32, E->W<float>(W_M1), E->W<float>(W_M2), E->W<float>(W_M3), E->n, (float)E->bzbar);
     return VEC_OK;
 }
+int split_emf(Engine *E) { return split_emf_m(&E, 1); }
 
-int split_mag(Engine *E, bool ab3_coef, bool spectra_done)
+static MeanArgs<float> mean_args(Engine *E, bool ab3_coef)
 {
-    float *W[W_COUNT];
-    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
-    int st;
-    const bool v4 = E->nx % 4 == 0 && E->vec4;
-    const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
-    if (!spectra_done) {
-        if ((st = split_emf(E))) return st;
-        LineJob<float> fx[3], fy[3];
-        mag_fwd_jobs(E, fx, fy);
-        if ((st = launch_lines<float>(E, 0, fx, 3))) return st;
-        if ((st = launch_lines<float>(E, 1, fy, 3))) return st;
-    }
     const Consts &c = E->k;
+    const bool v4 = E->nx % 4 == 0 && E->vec4;
     MeanArgs<float> ma;
-    ma.ex = W[W_EX]; ma.ey = W[W_EY]; ma.bxbar = E->bxbar; ma.bybar = E->bybar; ma.eta = E->eta; ma.deta = E->deta;
+    ma.ex = E->W<float>(W_EX); ma.ey = E->W<float>(W_EY); ma.bxbar = E->bxbar; ma.bybar = E->bybar;
+    ma.eta = E->eta; ma.deta = E->deta;
     ma.ht = E->ht; ma.scratch = E->w1d; ma.np = E->np; ma.nz = E->nz;
     ma.xn = c.xn; ma.zck = c.zck; ma.ho12 = c.ho12; ma.sc1 = c.sc1; ma.var_eta = c.var_eta;
     ma.ds = v4 && ab3_coef ? E->ds : nullptr; ma.bxm = E->bxbar; ma.bym = E->bybar;
-    if (v4) {
-        KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div4, dim3(g4.x, g4.y + 1), TPB, W[W_EX], W[W_EY], W[W_M4],
-                 E->nx, E->ny, E->hf, ma);
-    } else {
-        KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, ma);
-        KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, plane_grid(*E), TPB, W[W_EX], W[W_EY], W[W_M4],
-                 E->nx, E->ny, E->hf);
-    }
+    return ma;
+}
+
+static MagArgs<float> mag_args(Engine *E)
+{
+    const Consts &c = E->k;
     MagArgs<float> a;
-    a.ex = W[W_EX]; a.ey = W[W_EY]; a.ez = W[W_EZ]; a.w1 = W[W_M4]; a.pol = E->pol32; a.tor = E->tor32;
+    a.ex = E->W<float>(W_EX); a.ey = E->W<float>(W_EY); a.ez = E->W<float>(W_EZ); a.w1 = E->W<float>(W_M4);
+    a.pol = E->pol32; a.tor = E->tor32;
     a.eta = E->pcf + PC_ETA * E->nz; a.deta = E->pcf + PC_DETA * E->nz; a.h = E->hf;
     a.ht = E->ht;
     a.zck = (float)c.zck; a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.var_eta = c.var_eta;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    if (v4) {
-        KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final4, g4, TPB, a);
-    } else {
-        KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, plane_grid(*E), TPB, a);
-        if (ab3_coef) return phys_ab3_coef(E);
+    return a;
+}
+
+int split_mag_m(Engine *const *Es, int nE, bool ab3_coef, bool spectra_done)
+{
+    Engine *E = Es[0];
+    int st;
+    const bool v4 = E->nx % 4 == 0 && E->vec4;
+    if (!v4 && nE != 1) return VEC_ERR_ARG;
+    const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
+    if (!spectra_done) {
+        if ((st = split_emf_m(Es, nE))) return st;
+        std::vector<LineJob<float>> fx(3 * nE), fy(3 * nE);
+        for (int i = 0; i < nE; i++) mag_fwd_jobs(Es[i], &fx[3 * i], &fy[3 * i]);
+        if ((st = launch_lines<float>(E, 0, fx.data(), 3 * nE))) return st;
+        if ((st = launch_lines<float>(E, 1, fy.data(), 3 * nE))) return st;
     }
+    if (v4) {
+        if ((st = launch_members<MagDiv4Args>(Es, nE, "mag_div_f32", FB(E, 3, 4), dim3(g4.x, g4.y + 1), dim3(TPB), 0,
+                                              k_mag_div4<1>, k_mag_div4<BATCH_MAX>, [ab3_coef](Engine *e) {
+                                                  return MagDiv4Args{ e->W<float>(W_EX), e->W<float>(W_EY),
+                                                                      e->W<float>(W_M4), e->nx, e->ny, e->hf,
+                                                                      mean_args(e, ab3_coef) };
+                                              })))
+            return st;
+        return launch_members<MagArgs<float>>(Es, nE, "mag_final_f32", FB(E, 8, 4), g4, dim3(TPB), 0,
+                                              k_mag_final4<1>, k_mag_final4<BATCH_MAX>, mag_args);
+    }
+    const MeanArgs<float> ma = mean_args(E, ab3_coef);
+    KLAUNCHB(E, "mean_rhs", 0, k_mean_rhs<float>, 1, 256, ma);
+    KLAUNCHB(E, "mag_div_f32", FB(E, 3, 4), k_mag_div<float>, plane_grid(*E), TPB, E->W<float>(W_EX),
+             E->W<float>(W_EY), E->W<float>(W_M4), E->nx, E->ny, E->hf);
+    const MagArgs<float> a = mag_args(E);
+    KLAUNCHB(E, "mag_final_f32", FB(E, 8, 4), k_mag_final<float>, plane_grid(*E), TPB, a);
+    if (ab3_coef) return phys_ab3_coef(E);
     return VEC_OK;
 }
+int split_mag(Engine *E, bool ab3_coef, bool spectra_done) { return split_mag_m(&E, 1, ab3_coef, spectra_done); }
 
 // ---- bandj --------------------------------------------------------------------
 // z-marching, grid (np/256, nz/kc)
@@ -854,10 +952,26 @@ __global__ void __launch_bounds__(256) k_d1z_f(const float *in, float *out, int 
 // with rot set, an extra first CTA row (blockIdx.y == 0) rotates the history
 // table: the first kernel after the AB3 update, and none of its planes reads
 // the table
-__global__ void __launch_bounds__(256) k_d1z4(const float *in, float *out, int fl, size_t np, int nz, float h,
-                                              HistTable *rot)
+struct D1z4Args {
+    const float *in;
+    float *out;
+    int fl;
+    size_t np;
+    int nz;
+    float h;
+    HistTable *rot;
+};
+template <int NB>
+__global__ void __launch_bounds__(256) k_d1z4(const __grid_constant__ Batch<D1z4Args, NB> bt)
 {
     PDL_WAIT();
+    const D1z4Args &A = BATCH_MEMBER(bt, NB);
+    const float *in = A.in;
+    float *out = A.out;
+    const int fl = A.fl, nz = A.nz;
+    const size_t np = A.np;
+    const float h = A.h;
+    HistTable *rot = A.rot;
     if (rot && blockIdx.y == 0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) rotate_hist_table(rot);
         return;
@@ -869,46 +983,82 @@ __global__ void __launch_bounds__(256) k_d1z4(const float *in, float *out, int f
     reinterpret_cast<V4 *>(out)[(size_t)k * np4 + q4] = zd1(reinterpret_cast<const V4 *>(in) + q4, np4, k, nz, fl, V4(h));
 }
 
-int split_bandj(Engine *E, bool rotate_hist)
+// bandj of the members (equally sized; one launch per kernel for all)
+int split_bandj_m(Engine *const *Es, int nE, bool rotate_hist)
 {
-    float *W[W_COUNT];
-    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    Engine *E = Es[0];
     int st;
     const bool v4 = E->nx % 4 == 0 && E->vec4;
+    if (!v4 && nE != 1) return VEC_ERR_ARG;
     const dim3 g4((unsigned)nblk(E->np / 4), (unsigned)E->nz);
     if (!v4 && rotate_hist && (st = phys_rotate_hist(E))) return st;
-    if (v4)
-        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z4, dim3(g4.x, g4.y + (rotate_hist ? 1 : 0)), TPB, E->pol32,
-                 W[W_M1], 5, E->np, E->nz, (float)E->k.ho12, rotate_hist ? E->ht : nullptr);
-    else
-        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, W[W_M1], 5, E->np,
-                 E->nz, (float)E->k.ho12, ZCHUNK);
-    BandjArgs<float> a;
-    a.dzs = W[W_M1]; a.pol = E->pol32; a.tor = E->tor32; a.h = E->hf;
-    a.bxh = W[W_EX]; a.byh = W[W_EY]; a.bzh = W[W_EZ]; a.dybz = W[W_M2]; a.dxbz = W[W_M3]; a.jzh = W[W_M4];
-    a.nx = E->nx; a.ny = E->ny; a.nz = E->nz;
-    if (v4) KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec4, g4, TPB, a);
-    else KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, plane_grid(*E), TPB, a);
-    LineJob<float> ix[6] = { ljob<float>(W[W_EX], W[W_EX], OP_INV), ljob<float>(W[W_EY], W[W_EY], OP_INV),
-                             ljob<float>(W[W_EZ], W[W_EZ], OP_INV), ljob<float>(W[W_M2], W[W_M2], OP_INV),
-                             ljob<float>(W[W_M3], W[W_M3], OP_INV), ljob<float>(W[W_M4], W[W_M4], OP_INV) };
-    if ((st = launch_lines<float>(E, 0, ix, 6))) return st;
-    // bz32 keeps bz - bzbar: no constant added
-    LineJob<float> iy[6] = { ljob<float>(W[W_EX], E->bx32, OP_INV), ljob<float>(W[W_EY], E->by32, OP_INV),
-                             ljob<float>(W[W_EZ], E->bz32, OP_INV), ljob<float>(W[W_M2], W[W_M2], OP_INV),
-                             ljob<float>(W[W_M3], W[W_M3], OP_INV), ljob<float>(W[W_M4], W[W_M4], OP_INV) };
-    iy[0].addk = E->bxbar;
-    iy[1].addk = E->bybar;
-    if ((st = launch_lines<float>(E, 1, iy, 6))) return st;
-    if (v4)
-        KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq4, g4, TPB, W[W_M4], W[W_M2], W[W_M3], E->bx32, E->by32, E->jsq32,
-                 E->np, E->nz, (float)E->k.ho12);
-    else
-        KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq<float>, plane_grid(*E), TPB, W[W_M4], W[W_M2], W[W_M3],
-                 E->bx32, E->by32, E->jsq32, E->np, E->nz, (float)E->k.ho12);
-    E->b32_auth = 1;
+    if (v4) {
+        if ((st = launch_members<D1z4Args>(Es, nE, "d1bydz_f32", FB(E, 2, 4), dim3(g4.x, g4.y + (rotate_hist ? 1 : 0)),
+                                           dim3(TPB), 0, k_d1z4<1>, k_d1z4<BATCH_MAX>, [rotate_hist](Engine *e) {
+                                               return D1z4Args{ e->pol32, e->W<float>(W_M1), 5, e->np, e->nz,
+                                                                (float)e->k.ho12, rotate_hist ? e->ht : nullptr };
+                                           })))
+            return st;
+    } else {
+        KLAUNCHB(E, "d1bydz_f32", FB(E, 2, 4), k_d1z_f, zmarch_grid(E->np, E->nz), TPB, E->pol32, E->W<float>(W_M1),
+                 5, E->np, E->nz, (float)E->k.ho12, ZCHUNK);
+    }
+    auto bj = [](Engine *e) {
+        BandjArgs<float> a;
+        a.dzs = e->W<float>(W_M1); a.pol = e->pol32; a.tor = e->tor32; a.h = e->hf;
+        a.bxh = e->W<float>(W_EX); a.byh = e->W<float>(W_EY); a.bzh = e->W<float>(W_EZ);
+        a.dybz = e->W<float>(W_M2); a.dxbz = e->W<float>(W_M3); a.jzh = e->W<float>(W_M4);
+        a.nx = e->nx; a.ny = e->ny; a.nz = e->nz;
+        return a;
+    };
+    if (v4) {
+        if ((st = launch_members<BandjArgs<float>>(Es, nE, "bandj_spec_f32", FB(E, 9, 4), g4, dim3(TPB), 0,
+                                                   k_bandj_spec4<1>, k_bandj_spec4<BATCH_MAX>, bj)))
+            return st;
+    } else {
+        const BandjArgs<float> a = bj(E);
+        KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, plane_grid(*E), TPB, a);
+    }
+    std::vector<LineJob<float>> ix, iy;
+    for (int i = 0; i < nE; i++) {
+        Engine *M = Es[i];
+        float *W[W_COUNT];
+        for (int q = 0; q < W_COUNT; q++) W[q] = M->W<float>(q);
+        ix.push_back(ljob<float>(W[W_EX], W[W_EX], OP_INV));
+        ix.push_back(ljob<float>(W[W_EY], W[W_EY], OP_INV));
+        ix.push_back(ljob<float>(W[W_EZ], W[W_EZ], OP_INV));
+        ix.push_back(ljob<float>(W[W_M2], W[W_M2], OP_INV));
+        ix.push_back(ljob<float>(W[W_M3], W[W_M3], OP_INV));
+        ix.push_back(ljob<float>(W[W_M4], W[W_M4], OP_INV));
+        // bz32 keeps bz - bzbar: no constant added
+        LineJob<float> jbx = ljob<float>(W[W_EX], M->bx32, OP_INV), jby = ljob<float>(W[W_EY], M->by32, OP_INV);
+        jbx.addk = M->bxbar;
+        jby.addk = M->bybar;
+        iy.push_back(jbx);
+        iy.push_back(jby);
+        iy.push_back(ljob<float>(W[W_EZ], M->bz32, OP_INV));
+        iy.push_back(ljob<float>(W[W_M2], W[W_M2], OP_INV));
+        iy.push_back(ljob<float>(W[W_M3], W[W_M3], OP_INV));
+        iy.push_back(ljob<float>(W[W_M4], W[W_M4], OP_INV));
+    }
+    if ((st = launch_lines<float>(E, 0, ix.data(), (int)ix.size()))) return st;
+    if ((st = launch_lines<float>(E, 1, iy.data(), (int)iy.size()))) return st;
+    if (v4) {
+        if ((st = launch_members<Jsq4Args>(Es, nE, "jsq_f32", FB(E, 6, 4), g4, dim3(TPB), 0, k_jsq4<1>,
+                                           k_jsq4<BATCH_MAX>, [](Engine *e) {
+                                               return Jsq4Args{ e->W<float>(W_M4), e->W<float>(W_M2),
+                                                                e->W<float>(W_M3), e->bx32, e->by32, e->jsq32, e->np,
+                                                                e->nz, (float)e->k.ho12 };
+                                           })))
+            return st;
+    } else {
+        KLAUNCHB(E, "jsq_f32", FB(E, 6, 4), k_jsq<float>, plane_grid(*E), TPB, E->W<float>(W_M4), E->W<float>(W_M2),
+                 E->W<float>(W_M3), E->bx32, E->by32, E->jsq32, E->np, E->nz, (float)E->k.ho12);
+    }
+    for (int i = 0; i < nE; i++) Es[i]->b32_auth = 1;
     return VEC_OK;
 }
+int split_bandj(Engine *E, bool rotate_hist) { return split_bandj_m(&E, 1, rotate_hist); }
 
 // ---- AB3 update in FP64 with FP32 histories ------------------------------------------
 struct SplitAb3Args {
@@ -969,10 +1119,11 @@ __global__ void k_split_ab3(SplitAb3Args a)
 // leaving the FP64 pipe only the additions; same bits as the casts.
 // (no launch bound: the compiler's 78 registers at three CTAs per SM beat
 // four CTAs at 64 registers, 6.0 against 5.8 TB/s)
-template <bool ICVT>
-__global__ void k_split_ab3_v4(SplitAb3Args a)
+template <bool ICVT, int NB>
+__global__ void k_split_ab3_v4(const __grid_constant__ Batch<SplitAb3Args, NB> bt)
 {
     PDL_WAIT();
+    const SplitAb3Args &a = BATCH_MEMBER(bt, NB);
     const size_t np = (size_t)a.nx * a.ny;
     const size_t i4 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (i4 >= np * a.nz) return;
@@ -1037,10 +1188,8 @@ __global__ void k_split_ab3_v4(SplitAb3Args a)
     }
 }
 
-int split_ab3(Engine *E, int magdealias, bool folded)
+static SplitAb3Args ab3_args(Engine *E, int magdealias)
 {
-    int st;
-    if (!folded && (st = phys_ab3_coef(E))) return st;
     SplitAb3Args a;
     double *xs[7] = { E->u, E->v, E->w, E->r, E->t, E->pol, E->tor };
     float *ms[7] = { E->u32, E->v32, E->w32, E->r32, E->t32, E->pol32, E->tor32 };
@@ -1055,16 +1204,45 @@ int split_ab3(Engine *E, int magdealias, bool folded)
     a.ds = E->ds;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
+    return a;
+}
+
+// AB3 update of the members (equally sized): magdealias[i] as in split_ab3;
+// members not folded[i] get the coefficient step before and the history
+// rotation after the update
+int split_ab3_m(Engine *const *Es, int nE, const int *magdealias, const bool *folded)
+{
+    Engine *E = Es[0];
+    int st;
+    Engine *unf[BATCH_MAX];
+    int nu = 0;
+    int md[BATCH_MAX];
+    for (int i = 0; i < nE; i++) {
+        if (!folded[i]) unf[nu++] = Es[i];
+        md[i] = magdealias[i];
+    }
+    if (nu && (st = phys_ab3_coef_m(unf, nu))) return st;
     // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B
     const double bytes = (double)E->n * (14 * 8 + 21 * 4 + 7 * 4);
-    if (E->nx % 4 == 0 && E->int_cvt)
-        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4<true>, nblk(E->n / 4), TPB, a);
-    else if (E->nx % 4 == 0)
-        KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3_v4<false>, nblk(E->n / 4), TPB, a);
-    else
+    if (E->nx % 4 == 0) {
+        // (the members' magdealias flags, in member order)
+        int i = 0;
+        auto mk = [&i, md](Engine *e) { return ab3_args(e, md[i++]); };
+        st = E->int_cvt ? launch_members<SplitAb3Args>(Es, nE, "ab3_update_split", bytes, dim3(nblk(E->n / 4)),
+                                                       dim3(TPB), 0, k_split_ab3_v4<true, 1>,
+                                                       k_split_ab3_v4<true, BATCH_MAX>, mk)
+                        : launch_members<SplitAb3Args>(Es, nE, "ab3_update_split", bytes, dim3(nblk(E->n / 4)),
+                                                       dim3(TPB), 0, k_split_ab3_v4<false, 1>,
+                                                       k_split_ab3_v4<false, BATCH_MAX>, mk);
+        if (st) return st;
+    } else {
+        if (nE != 1) return VEC_ERR_ARG;
+        const SplitAb3Args a = ab3_args(E, md[0]);
         KLAUNCHB(E, "ab3_update_split", bytes, k_split_ab3, nblk(E->n), TPB, a);
-    return folded ? VEC_OK : phys_rotate_hist(E);
+    }
+    return nu ? phys_rotate_hist_m(unf, nu) : VEC_OK;
 }
+int split_ab3(Engine *E, int magdealias, bool folded) { return split_ab3_m(&E, 1, &magdealias, &folded); }
 
 // ---- dealias of r,t,u,v,w (every 10 steps) -----------------------------------------
 // The background is horizontally uniform, so the 2/3 truncation only touches
@@ -1080,9 +1258,11 @@ struct DealiasArgs {
 
 // grid (np/256, nz); float <-> double conversions on the integer pipe (the
 // same bits as the casts; the FP64 pipe keeps only the subtractions)
-__global__ void k_split_dealias_apply(DealiasArgs a)
+template <int NB>
+__global__ void k_split_dealias_apply(const __grid_constant__ Batch<DealiasArgs, NB> bt)
 {
     PDL_WAIT();
+    const DealiasArgs &a = BATCH_MEMBER(bt, NB);
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.np) return;
     const int k = blockIdx.y;
@@ -1096,26 +1276,37 @@ __global__ void k_split_dealias_apply(DealiasArgs a)
     }
 }
 
-int split_dealias(Engine *E)
+static DealiasArgs dealias_args(Engine *E)
 {
-    float *W[W_COUNT];
-    for (int i = 0; i < W_COUNT; i++) W[i] = E->W<float>(i);
+    DealiasArgs a;
     float *ms[5] = { E->r32, E->t32, E->u32, E->v32, E->w32 };
     double *xs[5] = { E->r, E->t, E->u, E->v, E->w };
-    float *tmp[5] = { W[W_RX], W[W_TX], W[W_UX], W[W_VX], W[W_WX] };
-    LineJob<float> jx[5], jy[5];
-    for (int i = 0; i < 5; i++) {
-        jx[i] = ljob<float>(ms[i], tmp[i], OP_DEALIAS);
-        jy[i] = ljob<float>(tmp[i], tmp[i], OP_DEALIAS);
+    const int tmp[5] = { W_RX, W_TX, W_UX, W_VX, W_WX };
+    for (int i = 0; i < 5; i++) { a.x[i] = xs[i]; a.m[i] = ms[i]; a.d[i] = E->W<float>(tmp[i]); }
+    a.bg = E->hres; a.np = E->np; a.nz = E->nz;
+    return a;
+}
+
+// dealias of r, t, u, v, w of the members (equally sized)
+int split_dealias_m(Engine *const *Es, int nE)
+{
+    Engine *E = Es[0];
+    std::vector<LineJob<float>> jx, jy;
+    for (int m = 0; m < nE; m++) {
+        const DealiasArgs a = dealias_args(Es[m]);
+        for (int i = 0; i < 5; i++) {
+            jx.push_back(ljob<float>(a.m[i], (float *)a.d[i], OP_DEALIAS));
+            jy.push_back(ljob<float>(a.d[i], (float *)a.d[i], OP_DEALIAS));
+        }
     }
     int st;
-    if ((st = launch_lines<float>(E, 0, jx, 5)) || (st = launch_lines<float>(E, 1, jy, 5))) return st;
-    DealiasArgs a;
-    for (int i = 0; i < 5; i++) { a.x[i] = xs[i]; a.m[i] = ms[i]; a.d[i] = tmp[i]; }
-    a.bg = E->hres; a.np = E->np; a.nz = E->nz;
-    KLAUNCHB(E, "dealias_apply_split", FB(E, 5, 24), k_split_dealias_apply, plane_grid(*E), TPB, a);
-    return VEC_OK;
+    if ((st = launch_lines<float>(E, 0, jx.data(), (int)jx.size())) ||
+        (st = launch_lines<float>(E, 1, jy.data(), (int)jy.size())))
+        return st;
+    return launch_members<DealiasArgs>(Es, nE, "dealias_apply_split", FB(E, 5, 24), plane_grid(*E), dim3(TPB), 0,
+                                       k_split_dealias_apply<1>, k_split_dealias_apply<BATCH_MAX>, dealias_args);
 }
+int split_dealias(Engine *E) { return split_dealias_m(&E, 1); }
 
 // ---- calcdt on the FP64 state with the FP32 field ---------------------------------------
 int split_calcdt(Engine *E)
@@ -1123,4 +1314,16 @@ int split_calcdt(Engine *E)
     int st = split_sync_b64(E);
     if (st) return st;
     return phys_calcdt(E);
+}
+
+// calcdt of the members (equally sized)
+int split_calcdt_m(Engine *const *Es, int nE)
+{
+    Engine *sync[BATCH_MAX];
+    int ns = 0;
+    for (int i = 0; i < nE; i++)
+        if (Es[i]->b32_auth) sync[ns++] = Es[i];
+    int st;
+    if (ns && (st = split_sync_b64_m(sync, ns))) return st;
+    return phys_calcdt_m(Es, nE);
 }

@@ -389,10 +389,12 @@ int vec_closure_infer(vec_closure *cl, vec_ctx *coarse);
 /* nsteps steps, the correction recomputed before each */
 int vec_closure_step(vec_closure *cl, vec_ctx *coarse, int nsteps);
 /* judged run to time t_end: every `every` coarse steps a plain fine segment
- * of nfine steps from the upsampled coarse state; if the Nusselt numbers
- * (bottom and top), kinetic or magnetic energy of the coarse run at the
- * segment's end time differ by more than tol (relative), or the coarse
- * state fails the div B check of src/main.F90:583-590, or the coarse run
+ * of nfine steps from the upsampled coarse state; if the change over the
+ * segment of the Nusselt numbers (bottom and top), kinetic or magnetic
+ * energy in the coarse run differs from their change in the fine run by
+ * more than tol of the fine value (the drift; the offset between the coarse
+ * state and the filtered upsampled one at the segment start is not drift),
+ * or the coarse state fails the div B check of src/main.F90:583-590, or the coarse run
  * stops advancing (non-finite time or step, or a step below 1e-3 of its
  * first), the run continues on the fine solver from the last state it holds
  * -- the upsampled start of the run, then the end of the last judged

@@ -12,7 +12,13 @@
   of the coarse RHS on held-out pairs (mse with the closure < 0.5 x mse of
   the plain coarse RHS);
 * the judged run falls back to the fine solver when the tolerance is
-  unattainable and never when it is loose.
+  unattainable and never when it is loose;
+* a posteriori, at small scale (a 256^2 x 129 DNS at Ra 1e6, Q 1e3, eta
+  contrast 20, filtered to 64^2 x 33): over an 8000-step DNS window the
+  judged closure run keeps the time averages of the top Nusselt number and
+  the kinetic and magnetic energies within 3 % of the filtered DNS, at less
+  than half the error of the plain coarse run, more than 10 times faster
+  than the DNS and without falling back.
 """
 import numpy as np
 import pytest
@@ -160,3 +166,15 @@ def test_top_nusselt_of_conductive_state():
     z = np.arange(9) / 8.0
     g.set("t", np.broadcast_to((1.0 + p.theta * z)[:, None, None], g.shape).copy())
     assert abs(top_nusselt(g) - 1.0) < 1e-12
+
+
+def test_closure_beats_plain_coarse_a_posteriori():
+    from fug30v0kxc_gb300.closure import run_workload
+    r = run_workload(nxf=256, nyf=256, nzf=129, pre_time=1.5, spinup=1000, pairs=200, pair_every=4, iters=500,
+                     window=8000, diag_every=50, judge_every=100, nfine=50)
+    print("closure a-posteriori:", {k: r[k] for k in ("closure", "plain", "judge", "speedup_vs_dns")})
+    assert r["dns_blowup"] == 0 and r["judge"]["judges"] >= 1
+    assert r["judge"]["fallback_step"] == -1
+    assert r["closure"]["max_err"] < 0.03
+    assert r["closure"]["max_err"] < 0.5 * r["plain"]["max_err"]
+    assert r["speedup_vs_dns"] > 10
