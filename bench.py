@@ -262,7 +262,7 @@ def closure_line(args, ws):
     from fug30v0kxc_gb300.closure import run_workload
     if args.closure_scale == "full":
         kw = dict(nxf=512, nyf=512, nzf=257, pre_time=args.closure_pre_time, spinup=2000, pairs=2000,
-                  pair_every=4, iters=2000, window=8000, diag_every=100, judge_every=args.closure_judge_every,
+                  pair_every=4, iters=2000, window=40000, diag_every=100, judge_every=args.closure_judge_every,
                   nfine=50)
     else:
         kw = dict(nxf=256, nyf=256, nzf=129, pre_time=args.closure_pre_time, spinup=1000, pairs=200, pair_every=4,
@@ -560,7 +560,8 @@ def main():
     ap.add_argument("--closure-pre-time", type=float, default=1.5,
                     help="closure workload: model time the coarse solver develops convection before the DNS")
     ap.add_argument("--closure-window", type=int, default=0,
-                    help="closure workload: DNS steps of the comparison window (0: 8000 full, 2000 small)")
+                    help="closure workload: DNS steps of the comparison window (0: 40000 full, which holds the "
+                         "judge after 2000 coarse steps; 2000 small)")
     ap.add_argument("--closure-judge-every", type=int, default=2000,
                     help="closure workload: coarse steps between judged fine segments")
     ap.add_argument("--acc-steps", type=int, default=20000, help="accuracy workload: steps of each run")
