@@ -273,6 +273,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         E.int_cvt = !(hc && hc[0] == '1');
         const char *zp = getenv("VEC_ZPENCIL");
         E.zpencil = !(zp && zp[0] == '0');
+        const char *ps = getenv("VEC_P2STAGE");
+        E.p2_stage = ps && ps[0] == '1';
     }
     set_consts(E);
     int st;
@@ -333,25 +335,30 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
     {
         // the wavenumber tables per precision; kh2 = akx2[i] + aky2[j] per plane point
         std::vector<double> kh2(E.np);
-        std::vector<float> kx1f(E.nx), ky1f(E.ny), kh2f(E.np);
+        std::vector<float> kx1f(E.nx), ky1f(E.ny), kh2f(E.np), kh2if(E.np);
         for (int j = 0; j < E.ny; j++)
             for (int i = 0; i < E.nx; i++) {
-                kh2[(size_t)j * E.nx + i] = akx2[i] + aky2[j];
-                kh2f[(size_t)j * E.nx + i] = (float)kh2[(size_t)j * E.nx + i];
+                const size_t q = (size_t)j * E.nx + i;
+                kh2[q] = akx2[i] + aky2[j];
+                kh2f[q] = (float)kh2[q];
+                kh2if[q] = q == 0 ? 0.0f : (float)(1.0 / kh2[q]);
             }
         for (int i = 0; i < E.nx; i++) kx1f[i] = (float)akx1[i];
         for (int j = 0; j < E.ny; j++) ky1f[j] = (float)aky1[j];
-        float *fx = nullptr, *fy = nullptr, *fk = nullptr;
+        float *fx = nullptr, *fy = nullptr, *fk = nullptr, *fki = nullptr;
         double *dk = nullptr;
         ALLOC(fx, sizeof(float) * E.nx); E.hf.kx1 = fx;
         ALLOC(fy, sizeof(float) * E.ny); E.hf.ky1 = fy;
         ALLOC(fk, sizeof(float) * E.np); E.hf.kh2 = fk;
+        ALLOC(fki, sizeof(float) * E.np); E.hf.kh2inv = fki;
+        E.hd.kh2inv = nullptr;
         ALLOC(dk, sizeof(double) * E.np); E.hd.kh2 = dk;
         E.hd.kx1 = E.akx1;
         E.hd.ky1 = E.aky1;
         if (cudaMemcpy(fx, kx1f.data(), sizeof(float) * E.nx, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(fy, ky1f.data(), sizeof(float) * E.ny, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(fk, kh2f.data(), sizeof(float) * E.np, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(fki, kh2if.data(), sizeof(float) * E.np, cudaMemcpyHostToDevice) != cudaSuccess ||
             upload(dk, kh2)) {
             vec_destroy(c);
             return VEC_ERR_CUDA;
@@ -428,7 +435,7 @@ extern "C" int vec_destroy(vec_ctx *c)
                      E.r32, E.t32, E.u32, E.v32, E.w32, E.bx32, E.by32, E.bz32, E.jsq32, E.pol32, E.tor32,
                      E.rho0, E.t0, E.hres, E.corr, E.corr_bx };
     for (void *q : ptrs) if (q) cudaFree(q);
-    const void *tabs[] = { E.hf.kx1, E.hf.ky1, E.hf.kh2, E.hd.kh2, E.pcf };
+    const void *tabs[] = { E.hf.kx1, E.hf.ky1, E.hf.kh2, E.hf.kh2inv, E.hd.kh2, E.pcf };
     for (const void *q : tabs) if (q) cudaFree((void *)q);
     for (int f = 0; f < 7; f++) for (int s = 0; s < 3; s++) if (E.hbuf[f][s]) cudaFree(E.hbuf[f][s]);
     for (int s = 0; s < 3; s++) { if (E.bxd_buf[s]) cudaFree(E.bxd_buf[s]); if (E.byd_buf[s]) cudaFree(E.byd_buf[s]); }
@@ -924,6 +931,7 @@ bool engine_batchable(const Engine &a, const Engine &b)
     return ok(a) && ok(b) && a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.p.xmax == b.p.xmax &&
            a.p.ymax == b.p.ymax && a.kc_pass2 == b.kc_pass2 && a.ct_s == b.ct_s && a.pdl == b.pdl &&
            a.int_cvt == b.int_cvt && a.generic_lines == b.generic_lines && a.ct_warp == b.ct_warp &&
+           a.p2_stage == b.p2_stage &&
            a.p.dalias == b.p.dalias && a.nit == b.nit;
 }
 

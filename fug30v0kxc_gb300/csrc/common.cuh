@@ -61,6 +61,7 @@ struct LineTables {
 template <typename R>
 struct HTab {
     const R *kx1, *ky1, *kh2;
+    const R *kh2inv;        // 1 / kh2 (0 at the mean, kh2 = 0), rounded once from FP64; FP32 only
 };
 
 // ---- per-context derived constants: src/constants.f90:56-109 -----------

@@ -338,11 +338,11 @@ static __global__ void __launch_bounds__(256, 4) k_mag_final4(const __grid_const
     const V4 *polc = reinterpret_cast<const V4 *>(a.pol) + q4, *torc = reinterpret_cast<const V4 *>(a.tor) + q4;
     const V4 w3a = zd1(w1c, (size_t)np4, k, a.nz, 5, V4(a.ho12));
     const V4 kk = ld4(a.h.kh2, q4);
-    V4 w2, w3;
-    w2.x = q == 0 ? 0.0f : w2a.x / kk.x; w3.x = q == 0 ? 0.0f : w3a.x / kk.x;
-    w2.y = w2a.y / kk.y; w3.y = w3a.y / kk.y;
-    w2.z = w2a.z / kk.z; w3.z = w3a.z / kk.z;
-    w2.w = w2a.w / kk.w; w3.w = w3a.w / kk.w;
+    // the inverse horizontal Laplacian as a product with the reciprocal
+    // table (rounded once from FP64; zero for the mean) instead of eight
+    // divisions per four points
+    const V4 ki = ld4(a.h.kh2inv, q4);
+    const V4 w2 = w2a * ki, w3 = w3a * ki;
     const V4 d2p = zd2(polc, (size_t)np4, k, a.nz, 3, V4(a.sc1));
     const V4 d2t = zd2(torc, (size_t)np4, k, a.nz, 3, V4(a.sc1));
     float *poldot = (float *)a.ht->p[5][2], *tordot = (float *)a.ht->p[6][2];

@@ -314,24 +314,48 @@ __device__ __forceinline__ void stv(float *p, size_t i, V4 v) { reinterpret_cast
 __device__ __forceinline__ float upsel(float w, float p, float m) { return w >= 0.0f ? p : m; }
 __host__ __device__ __forceinline__ V4 operator/(V4 a, V4 b) { return V4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
 
+// the point inputs of pass 2 besides t', u, v, w (which the z stencils read)
+enum P2Field {
+    P2_R, P2_BX, P2_BY, P2_BZ, P2_JSQ, P2_RX, P2_RY, P2_TX, P2_TXX, P2_TY, P2_TYY, P2_UX, P2_UXX, P2_UY, P2_UYY,
+    P2_VX, P2_VXX, P2_VY, P2_VYY, P2_WX, P2_WXX, P2_WY, P2_WYY, P2_COUNT
+};
+__device__ __forceinline__ const float *p2_src(const SplitHydroArgs &a, int f)
+{
+    switch (f) {
+    case P2_R: return a.r; case P2_BX: return a.bx; case P2_BY: return a.by; case P2_BZ: return a.bz;
+    case P2_JSQ: return a.jsq; case P2_RX: return a.rx; case P2_RY: return a.ry; case P2_TX: return a.tx;
+    case P2_TXX: return a.txx; case P2_TY: return a.ty; case P2_TYY: return a.tyy; case P2_UX: return a.ux;
+    case P2_UXX: return a.uxx; case P2_UY: return a.uy; case P2_UYY: return a.uyy; case P2_VX: return a.vx;
+    case P2_VXX: return a.vxx; case P2_VY: return a.vy; case P2_VYY: return a.vyy; case P2_WX: return a.wx;
+    case P2_WXX: return a.wxx; case P2_WY: return a.wy; default: return a.wyy;
+    }
+}
+// the point inputs read from global memory
+template <typename T> struct P2Global {
+    const SplitHydroArgs &a;
+    size_t idx;
+    __device__ __forceinline__ T operator()(int f) const { return ldv<T>(p2_src(a, f), idx); }
+};
+
 // one point (T = float, idx a point index) or four (T = V4, idx a 4-vector
 // index) of the terms without second-level derivatives
 // (tp, u0, v0, w0: t', u, v, w at the point)
-template <typename T>
+// (L(f): point input f of P2Field)
+template <typename T, typename L>
 __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z,
-                                                  const T tp, const T u0, const T v0, const T w0)
+                                                  const T tp, const T u0, const T v0, const T w0, const L &ld)
 {
     const int nz = a.nz;
     const float *pc = a.pc;
     const T rho0 = T(pc[PC_RHO0 * nz + k]), t0 = T(pc[PC_T0 * nz + k]);
-    const T rp = ldv<T>(a.r, idx);
+    const T rp = ld(P2_R);
     const T rr = rho0 + rp, tt = t0 + tp;
-    const T bx = ldv<T>(a.bx, idx), by = ldv<T>(a.by, idx), bzp = ldv<T>(a.bz, idx), bz = T(a.bzbar) + bzp;
-    const T rx = ldv<T>(a.rx, idx), ry = ldv<T>(a.ry, idx);
-    const T tx = ldv<T>(a.tx, idx), txx = ldv<T>(a.txx, idx), ty = ldv<T>(a.ty, idx), tyy = ldv<T>(a.tyy, idx);
-    const T ux = ldv<T>(a.ux, idx), uxx = ldv<T>(a.uxx, idx), uy = ldv<T>(a.uy, idx), uyy = ldv<T>(a.uyy, idx);
-    const T vx = ldv<T>(a.vx, idx), vxx = ldv<T>(a.vxx, idx), vy = ldv<T>(a.vy, idx), vyy = ldv<T>(a.vyy, idx);
-    const T wx = ldv<T>(a.wx, idx), wxx = ldv<T>(a.wxx, idx), wy = ldv<T>(a.wy, idx), wyy = ldv<T>(a.wyy, idx);
+    const T bx = ld(P2_BX), by = ld(P2_BY), bzp = ld(P2_BZ), bz = T(a.bzbar) + bzp;
+    const T rx = ld(P2_RX), ry = ld(P2_RY);
+    const T tx = ld(P2_TX), txx = ld(P2_TXX), ty = ld(P2_TY), tyy = ld(P2_TYY);
+    const T ux = ld(P2_UX), uxx = ld(P2_UXX), uy = ld(P2_UY), uyy = ld(P2_UYY);
+    const T vx = ld(P2_VX), vxx = ld(P2_VXX), vy = ld(P2_VY), vyy = ld(P2_VYY);
+    const T wx = ld(P2_WX), wxx = ld(P2_WXX), wy = ld(P2_WY), wyy = ld(P2_WYY);
 
     const T tzu = z.tzu + upsel(w0, T(pc[PC_T0ZU_P * nz + k]), T(pc[PC_T0ZU_M * nz + k]));
     const T tzp = z.tzp;
@@ -347,7 +371,7 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     T td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
            + T(a.gck) * T(pc[PC_KAPPA * nz + k]) * (txx + tyy + tzz)
            + T(a.gck) * T(pc[PC_DKAPPA * nz + k]) * tzu
-           + T(a.fzckg) * ohm * ldv<T>(a.jsq, idx);
+           + T(a.fzckg) * ohm * ld(P2_JSQ);
     td = td - T(a.gm1) * tt * divu * rr + T(2.0f) * T(a.sckg) * (ux * ux + vy * vy + wz * wz - third * divu * divu);
     td = td + T(a.sckg) * (uy + vx) * (uy + vx);
     td = td + T(a.sckg) * (wx + uzu) * (wx + uzu);
@@ -386,7 +410,8 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
 template <typename T>
 __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z)
 {
-    split_pass2_point<T>(a, idx, k, z, ldv<T>(a.t, idx), ldv<T>(a.u, idx), ldv<T>(a.v, idx), ldv<T>(a.w, idx));
+    split_pass2_point<T>(a, idx, k, z, ldv<T>(a.t, idx), ldv<T>(a.u, idx), ldv<T>(a.v, idx), ldv<T>(a.w, idx),
+                         P2Global<T>{ a, idx });
 }
 
 // two consecutive x points per thread, one plane per CTA row (grid
@@ -432,15 +457,33 @@ struct ZRing2 {
     }
 };
 
-template <int NB>
-__global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
+// the point inputs staged in shared memory (PS): stage s of [2][P2_COUNT][ZT_TILE]
+struct P2Smem {
+    const float *base;   // this plane's stage
+    int tid;
+    __device__ __forceinline__ V2 operator()(int f) const
+    {
+        return reinterpret_cast<const V2 *>(base + (size_t)f * ZT_TILE)[tid];
+    }
+};
+#define ZT_SMEM_RING ((size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float))
+#define ZT_SMEM_PTS ((size_t)2 * P2_COUNT * ZT_TILE * sizeof(float))
+
+// PS: the 23 other inputs of each plane are bulk-copied into a two-stage
+// buffer too, one plane ahead, so that no thread waits on a global load
+// (one CTA per SM: 156 KB of shared memory)
+template <int NB, bool PS>
+__global__ void __launch_bounds__(ZT_TILE / 2, PS ? 1 : 3)
+k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
 {
     PDL_WAIT();
     const SplitHydroArgs &a = BATCH_MEMBER(bt, NB);
     const int kc = a.kc;
     int *err = a.err;
-    extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE]
+    extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE], then (PS) the point stages
+    float *pts = zring + (size_t)ZT_SLOTS * 4 * ZT_TILE;
     __shared__ __align__(8) uint64_t full[ZT_SLOTS];
+    __shared__ __align__(8) uint64_t pfull[2];
     const int nz = a.nz;
     const size_t np = a.np;
     const size_t p0 = (size_t)blockIdx.x * ZT_TILE;
@@ -460,17 +503,42 @@ __global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_
         tma_load(dst + 2 * ZT_TILE, a.v + off, ZT_TILE * sizeof(float), b);
         tma_load(dst + 3 * ZT_TILE, a.w + off, ZT_TILE * sizeof(float), b);
     };
+    // (PS) the point inputs of plane kk into stage (kk - k0) mod 2
+    auto issue_pts = [&](int kk) {
+        const int sg = (kk - k0) & 1;
+        uint64_t *b = &pfull[sg];
+        float *dst = pts + (size_t)sg * P2_COUNT * ZT_TILE;
+        const size_t off = (size_t)kk * np + p0;
+        mbar_expect_tx(b, P2_COUNT * ZT_TILE * (unsigned)sizeof(float));
+#pragma unroll 1
+        for (int f = 0; f < P2_COUNT; f++) tma_load(dst + (size_t)f * ZT_TILE, p2_src(a, f) + off, ZT_TILE * sizeof(float), b);
+    };
+    auto pparity = [&](int kk) { return (unsigned)(((kk - k0) >> 1) & 1); };
     if (tid == 0) {
         for (int s = 0; s < ZT_SLOTS; s++) mbar_init(&full[s], 1);
+        mbar_init(&pfull[0], 1);
+        mbar_init(&pfull[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
     int khi = min(kcap, hi_of(k0) + 1);   // highest plane issued (one plane of lookahead)
-    if (tid == 0)
+    int phi = PS ? min(k1 - 1, k0 + 1) : k0 - 1;   // highest plane whose point inputs were issued
+    if (tid == 0) {
         for (int kk = kbase; kk <= khi; kk++) issue(kk);
+        if (PS)
+            for (int kk = k0; kk <= phi; kk++) issue_pts(kk);
+    }
     int kw = kbase - 1;                   // highest plane this thread has waited for
+    int pw = k0 - 1;                      // (PS) the same for the point inputs
     bool ok = true;
+    // after a failed wait: wait (bounded) for every copy still in flight
+    auto drain = [&]() {
+        for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++)
+            mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+        if (PS)
+            for (int kk = max(pw + 1, phi - 1); kk <= phi; kk++) mbar_wait(&pfull[(kk - k0) & 1], pparity(kk));
+    };
     const ZRing2 Rt{ reinterpret_cast<const V2 *>(zring) + tid };
     const ZRing2 Ru{ reinterpret_cast<const V2 *>(zring + ZT_TILE) + tid };
     const ZRing2 Rv{ reinterpret_cast<const V2 *>(zring + 2 * ZT_TILE) + tid };
@@ -484,20 +552,27 @@ __global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_
                 if (tid == 0) {
                     // report, then let the copies in flight land before the CTA exits
                     atomicExch(err, 1);
-                    for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++)
-                        mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+                    drain();
                 }
                 return;
             }
             const int want = min(kcap, hi_of(k) + 1);
-            if (tid == 0 && want > khi) {
+            const bool next_pts = PS && k + 1 < k1;
+            if (tid == 0 && (want > khi || next_pts)) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 for (int kk = khi + 1; kk <= want; kk++) issue(kk);
+                // the stage of plane k - 1 is free again
+                if (next_pts) issue_pts(k + 1);
             }
             khi = max(khi, want);
+            if (next_pts) phi = k + 1;
         }
         for (int kk = kw + 1; kk <= hi_of(k) && ok; kk++) ok = mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
         kw = max(kw, hi_of(k));
+        if (PS && ok) {
+            ok = mbar_wait(&pfull[(k - k0) & 1], pparity(k));
+            pw = k;
+        }
         if (!ok) continue;
         const V2 w0 = Rw(k);
         ZDer<V2> z;
@@ -505,11 +580,16 @@ __global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_
         z.wzu = zd1upa(Rw, k, nz, 1, h, w0); z.wz = zd1a(Rw, k, nz, 1, h);
         z.uzu = zd1upa(Ru, k, nz, 2, h, w0); z.vzu = zd1upa(Rv, k, nz, 2, h, w0);
         z.uzz = zd2a(Ru, k, nz, 3, sc); z.vzz = zd2a(Rv, k, nz, 3, sc);
-        split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0);
+        if constexpr (PS)
+            split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0,
+                                  P2Smem{ pts + (size_t)((k - k0) & 1) * P2_COUNT * ZT_TILE, tid });
+        else
+            split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0,
+                                  P2Global<V2>{ a, (size_t)k * np2 + q2 });
     }
     if (!__syncthreads_and(ok) && tid == 0) {
         atomicExch(err, 1);
-        for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++) mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+        drain();
     }
 }
 
@@ -807,19 +887,27 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
 
     if (E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6) {
         static bool attr = false;
-        const size_t smem = (size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float);
         if (!attr) {
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)ZT_SMEM_RING));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX, false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZT_SMEM_RING));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(ZT_SMEM_RING + ZT_SMEM_PTS)));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX, true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ZT_SMEM_RING + ZT_SMEM_PTS)));
             attr = true;
         }
         const int kc = hydro_args(E).kc;
-        if ((st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4),
-                                                 dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
-                                                 dim3(ZT_TILE / 2), smem, k_split_pass2_zt<1>,
-                                                 k_split_pass2_zt<BATCH_MAX>, hydro_args)))
-            return st;
+        const dim3 grid((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc));
+        st = E->p2_stage ? launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4), grid,
+                                                          dim3(ZT_TILE / 2), ZT_SMEM_RING + ZT_SMEM_PTS,
+                                                          k_split_pass2_zt<1, true>,
+                                                          k_split_pass2_zt<BATCH_MAX, true>, hydro_args)
+                         : launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4), grid,
+                                                          dim3(ZT_TILE / 2), ZT_SMEM_RING, k_split_pass2_zt<1, false>,
+                                                          k_split_pass2_zt<BATCH_MAX, false>, hydro_args);
+        if (st) return st;
     } else if (E->nx % 4 == 0 && E->vec4) {
         const SplitHydroArgs a = hydro_args(E);
         KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v2,
