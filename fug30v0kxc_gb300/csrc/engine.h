@@ -113,7 +113,6 @@ struct Engine {
     bool pdl = true;            // programmatic dependent launches (VEC_PDL=0: ordinary launches)
     bool vec4 = true;           // four-point (16-byte) forms of the split pointwise kernels (VEC_VEC4=0: one point)
     bool zpencil = true;        // split pass 2 with TMA-staged z-pencils (VEC_ZPENCIL=0: per-plane form)
-    bool p2_stage = false;      // ... and its other point inputs staged too (VEC_P2STAGE=1)
     bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
                                 // (VEC_HW_CVT=1: hardware conversions; the same bits)
 

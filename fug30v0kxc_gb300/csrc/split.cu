@@ -457,33 +457,15 @@ struct ZRing2 {
     }
 };
 
-// the point inputs staged in shared memory (PS): stage s of [2][P2_COUNT][ZT_TILE]
-struct P2Smem {
-    const float *base;   // this plane's stage
-    int tid;
-    __device__ __forceinline__ V2 operator()(int f) const
-    {
-        return reinterpret_cast<const V2 *>(base + (size_t)f * ZT_TILE)[tid];
-    }
-};
-#define ZT_SMEM_RING ((size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float))
-#define ZT_SMEM_PTS ((size_t)2 * P2_COUNT * ZT_TILE * sizeof(float))
-
-// PS: the 23 other inputs of each plane are bulk-copied into a two-stage
-// buffer too, one plane ahead, so that no thread waits on a global load
-// (one CTA per SM: 156 KB of shared memory)
-template <int NB, bool PS>
-__global__ void __launch_bounds__(ZT_TILE / 2, PS ? 1 : 3)
-k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
+template <int NB>
+__global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
 {
     PDL_WAIT();
     const SplitHydroArgs &a = BATCH_MEMBER(bt, NB);
     const int kc = a.kc;
     int *err = a.err;
-    extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE], then (PS) the point stages
-    float *pts = zring + (size_t)ZT_SLOTS * 4 * ZT_TILE;
+    extern __shared__ __align__(128) float zring[];   // [slot][t', u, v, w][ZT_TILE]
     __shared__ __align__(8) uint64_t full[ZT_SLOTS];
-    __shared__ __align__(8) uint64_t pfull[2];
     const int nz = a.nz;
     const size_t np = a.np;
     const size_t p0 = (size_t)blockIdx.x * ZT_TILE;
@@ -503,41 +485,21 @@ k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
         tma_load(dst + 2 * ZT_TILE, a.v + off, ZT_TILE * sizeof(float), b);
         tma_load(dst + 3 * ZT_TILE, a.w + off, ZT_TILE * sizeof(float), b);
     };
-    // (PS) the point inputs of plane kk into stage (kk - k0) mod 2
-    auto issue_pts = [&](int kk) {
-        const int sg = (kk - k0) & 1;
-        uint64_t *b = &pfull[sg];
-        float *dst = pts + (size_t)sg * P2_COUNT * ZT_TILE;
-        const size_t off = (size_t)kk * np + p0;
-        mbar_expect_tx(b, P2_COUNT * ZT_TILE * (unsigned)sizeof(float));
-#pragma unroll 1
-        for (int f = 0; f < P2_COUNT; f++) tma_load(dst + (size_t)f * ZT_TILE, p2_src(a, f) + off, ZT_TILE * sizeof(float), b);
-    };
-    auto pparity = [&](int kk) { return (unsigned)(((kk - k0) >> 1) & 1); };
     if (tid == 0) {
         for (int s = 0; s < ZT_SLOTS; s++) mbar_init(&full[s], 1);
-        mbar_init(&pfull[0], 1);
-        mbar_init(&pfull[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
     int khi = min(kcap, hi_of(k0) + 1);   // highest plane issued (one plane of lookahead)
-    int phi = PS ? min(k1 - 1, k0 + 1) : k0 - 1;   // highest plane whose point inputs were issued
-    if (tid == 0) {
+    if (tid == 0)
         for (int kk = kbase; kk <= khi; kk++) issue(kk);
-        if (PS)
-            for (int kk = k0; kk <= phi; kk++) issue_pts(kk);
-    }
     int kw = kbase - 1;                   // highest plane this thread has waited for
-    int pw = k0 - 1;                      // (PS) the same for the point inputs
     bool ok = true;
     // after a failed wait: wait (bounded) for every copy still in flight
     auto drain = [&]() {
         for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++)
             mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
-        if (PS)
-            for (int kk = max(pw + 1, phi - 1); kk <= phi; kk++) mbar_wait(&pfull[(kk - k0) & 1], pparity(kk));
     };
     const ZRing2 Rt{ reinterpret_cast<const V2 *>(zring) + tid };
     const ZRing2 Ru{ reinterpret_cast<const V2 *>(zring + ZT_TILE) + tid };
@@ -557,22 +519,14 @@ k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
                 return;
             }
             const int want = min(kcap, hi_of(k) + 1);
-            const bool next_pts = PS && k + 1 < k1;
-            if (tid == 0 && (want > khi || next_pts)) {
+            if (tid == 0 && want > khi) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 for (int kk = khi + 1; kk <= want; kk++) issue(kk);
-                // the stage of plane k - 1 is free again
-                if (next_pts) issue_pts(k + 1);
             }
             khi = max(khi, want);
-            if (next_pts) phi = k + 1;
         }
         for (int kk = kw + 1; kk <= hi_of(k) && ok; kk++) ok = mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
         kw = max(kw, hi_of(k));
-        if (PS && ok) {
-            ok = mbar_wait(&pfull[(k - k0) & 1], pparity(k));
-            pw = k;
-        }
         if (!ok) continue;
         const V2 w0 = Rw(k);
         ZDer<V2> z;
@@ -580,12 +534,8 @@ k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
         z.wzu = zd1upa(Rw, k, nz, 1, h, w0); z.wz = zd1a(Rw, k, nz, 1, h);
         z.uzu = zd1upa(Ru, k, nz, 2, h, w0); z.vzu = zd1upa(Rv, k, nz, 2, h, w0);
         z.uzz = zd2a(Ru, k, nz, 3, sc); z.vzz = zd2a(Rv, k, nz, 3, sc);
-        if constexpr (PS)
-            split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0,
-                                  P2Smem{ pts + (size_t)((k - k0) & 1) * P2_COUNT * ZT_TILE, tid });
-        else
-            split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0,
-                                  P2Global<V2>{ a, (size_t)k * np2 + q2 });
+        split_pass2_point<V2>(a, (size_t)k * np2 + q2, k, z, Rt(k), Ru(k), Rv(k), w0,
+                              P2Global<V2>{ a, (size_t)k * np2 + q2 });
     }
     if (!__syncthreads_and(ok) && tid == 0) {
         atomicExch(err, 1);
@@ -887,26 +837,18 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
 
     if (E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6) {
         static bool attr = false;
+        const size_t smem = (size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float);
         if (!attr) {
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)ZT_SMEM_RING));
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX, false>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZT_SMEM_RING));
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(ZT_SMEM_RING + ZT_SMEM_PTS)));
-            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX, true>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ZT_SMEM_RING + ZT_SMEM_PTS)));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass2_zt<BATCH_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
             attr = true;
         }
         const int kc = hydro_args(E).kc;
-        const dim3 grid((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc));
-        st = E->p2_stage ? launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4), grid,
-                                                          dim3(ZT_TILE / 2), ZT_SMEM_RING + ZT_SMEM_PTS,
-                                                          k_split_pass2_zt<1, true>,
-                                                          k_split_pass2_zt<BATCH_MAX, true>, hydro_args)
-                         : launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4), grid,
-                                                          dim3(ZT_TILE / 2), ZT_SMEM_RING, k_split_pass2_zt<1, false>,
-                                                          k_split_pass2_zt<BATCH_MAX, false>, hydro_args);
+        st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4),
+                                            dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
+                                            dim3(ZT_TILE / 2), smem, k_split_pass2_zt<1>, k_split_pass2_zt<BATCH_MAX>,
+                                            hydro_args);
         if (st) return st;
     } else if (E->nx % 4 == 0 && E->vec4) {
         const SplitHydroArgs a = hydro_args(E);

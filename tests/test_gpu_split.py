@@ -98,7 +98,7 @@ def test_split_100_steps_vs_fp64_oracle():
 
 @pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17)])
 @pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6),
-                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6), ("VEC_P2STAGE", ("0", "1"), 1e-6)])
+                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6)])
 def test_split_variants_agree(grid, var, values, tol, monkeypatch):
     """Two implementations of the same arithmetic after twelve steps (Euler,
     AB2, AB3, a dealias step and a calcdt at step 10).
@@ -114,9 +114,6 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
       reads them from global memory: the same formulas on the same values,
       but the two kernels are compiled separately and the compiler may fuse
       different multiply-adds; tolerance 1e-6 relative L2 per field.
-    * VEC_P2STAGE: the z-pencil pass 2 with its other point inputs staged in
-      shared memory too, against the one that reads them directly; same
-      tolerance.
     """
     states = []
     for val in values:
