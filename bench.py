@@ -461,12 +461,15 @@ def dominant_roofline(prof, hbm_peak, peak_kind):
             "alg_bytes_per_launch": per_launch}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of the split step at
-# 256x256x129, from the ncu capture summarised in
-# profiles/dram_traffic_split_256x256x129.md (other workloads: null)
-TRAFFIC_256x256x129 = {"line_x_f32": 267.1e6, "line_y_f32": 259.1e6, "hydro_pass2_f32": 1349.5e6,
-                       "ab3_update_split": 1835.3e6, "hydro_pass4_f32": 695.7e6, "mag_final_f32": 249.3e6,
-                       "bandj_spec_f32": 246.9e6, "emf_f32": 254.9e6, "jsq_f32": 187.4e6, "d1bydz_f32": 34.2e6}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the split step's
+# kernels, from one-kernel ncu captures at 256x256x65 scaled by the points to
+# 256x256x129 (profiles/dram_traffic_split_256x256x65.md; the line kernels'
+# figures are the mean over a step's three launches); other workloads: null
+_SCALE_129_65 = 129.0 / 65.0
+TRAFFIC_256x256x129 = {k: v * _SCALE_129_65 for k, v in {
+    "ab3_update_split": 900.9e6, "hydro_pass2_f32": 667.2e6, "hydro_pass4_f32": 344.8e6,
+    "mag_final_f32": 119.5e6, "line_x_f32": (294.2e6 + 55.6e6 + 145.5e6) / 3,
+    "line_y_f32": (279.2e6 + 53.3e6 + 139.6e6) / 3}.items()}
 TRAFFIC = {}
 # operation count of one grid-point-step at n = 256 (formula: ~72 real
 # transform passes x 2.5 log2 n, ~200 for the z stencils, ~300 pointwise,
