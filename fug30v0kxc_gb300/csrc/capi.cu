@@ -938,9 +938,28 @@ bool engine_batchable(const Engine &a, const Engine &b)
 // magnetic branch take the folded path (coefficients in mag_div, history
 // rotation in bandj), the others zero their magnetic RHS.  Host counters are
 // advanced by the caller.
+static int enqueue_step_batch_body(Engine *const *Es, int nE);
+
 int engine_enqueue_step_batch(Engine *const *Es, int nE)
 {
     if (nE < 1 || nE > BATCH_MAX) return VEC_ERR_ARG;
+    // A batched kernel launches on the stream of the first member of the
+    // list it is given, and the magnetic and non-magnetic sub-batches below
+    // start with other members than the batch.  All of them must land on
+    // the first member's stream: under stream capture a launch on any other
+    // stream would run once, at capture time, and be missing from the graph.
+    cudaStream_t own[BATCH_MAX];
+    for (int i = 0; i < nE; i++) {
+        own[i] = Es[i]->stream;
+        Es[i]->stream = Es[0]->stream;
+    }
+    const int st = enqueue_step_batch_body(Es, nE);
+    for (int i = 0; i < nE; i++) Es[i]->stream = own[i];
+    return st;
+}
+
+static int enqueue_step_batch_body(Engine *const *Es, int nE)
+{
     Engine *mag[BATCH_MAX], *off[BATCH_MAX];
     bool wm[BATCH_MAX], folded[BATCH_MAX];
     int mdeal[BATCH_MAX];

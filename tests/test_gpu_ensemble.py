@@ -48,6 +48,42 @@ def test_members_match_single_instance(tune, tmp_path):
     ens.close()
 
 
+def batch_members(n, nx, ny, nz):
+    """n members of one grid: magnetic (Q 100, 1000) and non-magnetic ones,
+    uneven Ra and eta contrast, a distinct noise seed each."""
+    qs, etas, ras = (0.0, 100.0, 1000.0), (1.0, 5.0, 20.0), (2e4, 1e5, 5e5, 1e6)
+    ps = []
+    for i in range(n):
+        p = convection_params(nx, ny, nz, ra=ras[i % 4], q=qs[i % 3], eta_contrast=etas[(i // 3) % 3],
+                              precision=VEC_PREC_SPLIT)
+        p.seed_base = 2024 + 11 * i
+        p.ndu06 = 1000000
+        ps.append(p)
+    return ps
+
+
+def test_batched_members_match_single_instance():
+    """18 members of one grid: two batches (at most 16 members per launch),
+    more than 64 line jobs per hydro line pass (several launches), magnetic
+    and non-magnetic members in one batch; 25 steps cover the calcdt and
+    dealias steps.  Every member bit-identical to its solo run."""
+    ps = batch_members(18, 32, 32, 17)
+    ens = Ensemble(ps)
+    ens.start()
+    assert ens.step(25) == 0
+    ens.sync()
+    # one graph branch per batch: far fewer launches than members x kernels
+    for p, m in zip(ps, ens.members):
+        solo = P3D(p)
+        solo.start()
+        assert solo.step(25) == 0
+        for n in FIELDS:
+            assert np.array_equal(m.get(n), solo.get(n)), (n, p.chand, p.eta_contrast)
+        assert m.scalars().dt == solo.scalars().dt
+        solo.close()
+    ens.close()
+
+
 def test_graph_replay_matches_eager():
     p = convection_params(64, 64, 33, eta_contrast=20.0, precision=VEC_PREC_SPLIT)
     p.ndu06 = 7
