@@ -31,7 +31,8 @@ enum LineOp {
     OP_D2 = 2,       // second derivative (-k^2), Nyquist kept: src/fft.F90:442-454
     OP_DEALIAS = 3,  // 2/3-rule truncation: src/fft.F90:618-626
     OP_FWD = 4,      // real -> halfcomplex, unnormalised (rfftw forward)
-    OP_INV = 5,      // halfcomplex -> real, divided by n (rfftw backward / n)
+    OP_INV = 5,      // halfcomplex -> real, divided by n (rfftw backward / n); op2
+                     // OP_D1 adds the derivative of that inverse as a second output
 };
 
 template <typename R>

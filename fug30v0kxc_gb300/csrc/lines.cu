@@ -216,8 +216,20 @@ line_kernel(JobPack<R> jobs, LinePlan pl, LineTables<R> tb, int nx, int ny, int 
             C z; z.x = ar - bi; z.y = ai + br;
             A[s * ld + k] = z;
         }
+        // op2 OP_D1: also the derivative of the inverse, B <- m1 * Z
+        const bool two = op2 == OP_D1;
+        if (two) {
+            __syncthreads();
+            for (int idx = tid; idx < P * n; idx += nt) {
+                const int s = idx / n, k = idx - s * n;
+                const C z = A[s * ld + k];
+                const R m = tb.m1[k];
+                C y; y.x = -m * z.y; y.y = m * z.x;
+                B[s * ld + k] = y;
+            }
+        }
         __syncthreads();
-        fft_run<true>(A, P, ld, pl, tw);
+        fft_run<true>(A, two ? 2 * P : P, ld, pl, tw);
         const R sc = (R)1 / (R)n;
         for (int idx = tid; idx < 2 * P * n; idx += nt) {
             int l, e;
@@ -233,6 +245,12 @@ line_kernel(JobPack<R> jobs, LinePlan pl, LineTables<R> tb, int nx, int ny, int 
             if (jb.addk) res = res + (R)jb.addk[plane];
             if (jb.addc != 0.0) res = res + (R)jb.addc;
             *o = res;
+            if (two) {
+                const C y = B[(l >> 1) * ld + e];
+                R *o2 = jb.out2 + pbase + LOFF(gl, e);
+                const R r2 = jb.alpha2 * ((l & 1) ? y.y : y.x);
+                *o2 = jb.acc2 ? *o2 + r2 : r2;
+            }
         }
         return;
     }

@@ -422,8 +422,10 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             continue;
         }
 
-        // one or two outputs: Y = m(X), inverse transform, store
-        const int nout = (op2 != OP_NONE && op1 != OP_INV) ? 2 : 1;
+        // one or two outputs: Y = m(X), inverse transform, store (a
+        // halfcomplex input takes a second output only for OP_D1: the
+        // derivative of its inverse)
+        const int nout = (op2 != OP_NONE && (op1 != OP_INV || op2 == OP_D1)) ? 2 : 1;
         for (int o = 0; o < nout; o++) {
             const int op = o == 0 ? op1 : op2;
             R *out = o == 0 ? jb.out1 : jb.out2;

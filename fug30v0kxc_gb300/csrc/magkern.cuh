@@ -178,6 +178,8 @@ static __global__ void k_bandj_spec(BandjArgs<R> a)
     const R kk = a.h.kh2[q];
     a.bzh[idx] = (R)-1 * pp[q] * kk;
     a.jzh[idx] = (R)-1 * tp[q] * kk;
+    // (dybz null: the line transforms take the derivatives of bz instead)
+    if (!a.dybz) return;
     // d/dy and d/dx of ez = -pol*(akx2+aky2), evaluated at the mirrored index
     R dy = (R)0, dx = (R)0;
     if (!(j == 0 || 2 * j == a.ny)) {
@@ -376,6 +378,8 @@ static __global__ void k_bandj_spec4(const __grid_constant__ Batch<BandjArgs<flo
     const V4 kk = ld4(a.h.kh2, q4);
     st4(a.bzh, i4, V4(-1.0f) * ld4(pp, q4) * kk);
     st4(a.jzh, i4, V4(-1.0f) * ld4(tp, q4) * kk);
+    // (dybz null: the line transforms take the derivatives of bz instead)
+    if (!a.dybz) return;
     // d/dy of ez = -pol*(akx2+aky2) at the mirrored row
     V4 dy(0.0f);
     if (!(j == 0 || 2 * j == a.ny)) {

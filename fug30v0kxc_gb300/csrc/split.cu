@@ -281,6 +281,9 @@ int split_refresh_planes(Engine *E, int mask)
 int split_refresh_uv(Engine *E) { return mirror(E, MIR_UV, 0, E->nz); }
 
 // ---- hydro_deriv ------------------------------------------------------------
+// a context with a magnetic field (its induction equation is stepped)
+static inline int split_mag_on(const Engine &E) { return E.p.f != 0.0 || E.p.kinematic; }
+
 struct SplitHydroArgs {
     const float *r, *t, *u, *v, *w, *bx, *by, *bz, *jsq;
     const float *rx, *tx, *txx, *ux, *uxx, *vx, *vxx, *wx, *wxx;
@@ -291,6 +294,8 @@ struct SplitHydroArgs {
     float *p1, *p2, *q, *g, *hh, *p3, *p4;
     float gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, ho12, sc1, bzbar;
     int var_eta;
+    int mag;                // 0: no magnetic field (Q = 0): B, J^2 and the Lorentz
+                            // fluxes q, g, h are zero, neither read nor written
     size_t np;
     int nz;
     int kc;                 // z-pencil kernel: planes per chunk
@@ -350,7 +355,10 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     const T rho0 = T(pc[PC_RHO0 * nz + k]), t0 = T(pc[PC_T0 * nz + k]);
     const T rp = ld(P2_R);
     const T rr = rho0 + rp, tt = t0 + tp;
-    const T bx = ld(P2_BX), by = ld(P2_BY), bzp = ld(P2_BZ), bz = T(a.bzbar) + bzp;
+    // (without a magnetic field the B mirrors hold zeros: the same values)
+    const bool mg = a.mag != 0;
+    const T bx = mg ? ld(P2_BX) : T(0.0f), by = mg ? ld(P2_BY) : T(0.0f), bzp = mg ? ld(P2_BZ) : T(0.0f);
+    const T bz = T(a.bzbar) + bzp;
     const T rx = ld(P2_RX), ry = ld(P2_RY);
     const T tx = ld(P2_TX), txx = ld(P2_TXX), ty = ld(P2_TY), tyy = ld(P2_TYY);
     const T ux = ld(P2_UX), uxx = ld(P2_UXX), uy = ld(P2_UY), uyy = ld(P2_UYY);
@@ -371,7 +379,7 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     T td = -rr * (u0 * tx + v0 * ty + w0 * tzu)
            + T(a.gck) * T(pc[PC_KAPPA * nz + k]) * (txx + tyy + tzz)
            + T(a.gck) * T(pc[PC_DKAPPA * nz + k]) * tzu
-           + T(a.fzckg) * ohm * ld(P2_JSQ);
+           + T(a.fzckg) * ohm * (mg ? ld(P2_JSQ) : T(0.0f));
     td = td - T(a.gm1) * tt * divu * rr + T(2.0f) * T(a.sckg) * (ux * ux + vy * vy + wz * wz - third * divu * divu);
     td = td + T(a.sckg) * (uy + vx) * (uy + vx);
     td = td + T(a.sckg) * (wx + uzu) * (wx + uzu);
@@ -403,9 +411,11 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
     stv(a.p2, idx, dv + temp2 - temp1 - temp3);
     stv(a.p3, idx, T(a.scko3) * ux + T(a.scko3) * vy + temp3 - temp1 - temp2);
     stv(a.p4, idx, T(4.0f) * T(a.scko3) * wz);
-    stv(a.q, idx, T(a.f) * by * bx);
-    stv(a.g, idx, T(a.f) * bz * bx);
-    stv(a.hh, idx, T(a.f) * bz * by);
+    if (mg) {
+        stv(a.q, idx, T(a.f) * by * bx);
+        stv(a.g, idx, T(a.f) * bz * bx);
+        stv(a.hh, idx, T(a.f) * bz * by);
+    }
 }
 template <typename T>
 __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_t idx, int k, const ZDer<T> &z)
@@ -603,6 +613,7 @@ struct SplitHydro4Args {
     const float *pc;
     const HistTable *ht;    // rdot, udot, vdot, wdot = newest slots
     float ho12;
+    int mag;                // 0: g, h and the derivatives of q, g, h are zero (not read)
     size_t np;
     int nz;
 };
@@ -624,12 +635,14 @@ __global__ void k_split_pass4(SplitHydro4Args a)
     const float rp = a.r[idx], tp = a.t[idx], w0 = a.w[idx];
     const float rr = rho0 + rp, tt = t0 + tp;
     // (sums in the order of the reference's accumulation: x, then y, then z)
-    const float wacc = (a.wacc[idx] + a.dxw[idx]) + a.dyw[idx];
-    const float uacc = (a.uacc[idx] + a.dxu[idx]) + a.dyu[idx];
-    const float vacc = (a.vacc[idx] + a.dxv[idx]) + a.dyv[idx];
+    // (without a magnetic field q, g and h are zero: their terms are left out)
+    const bool mg = a.mag != 0;
+    const float wacc = mg ? (a.wacc[idx] + a.dxw[idx]) + a.dyw[idx] : a.wacc[idx];
+    const float uacc = mg ? (a.uacc[idx] + a.dxu[idx]) + a.dyu[idx] : a.uacc[idx] + a.dxu[idx];
+    const float vacc = mg ? (a.vacc[idx] + a.dxv[idx]) + a.dyv[idx] : a.vacc[idx] + a.dyv[idx];
     float wd = wacc + zd1(a.p3 + q, np, k, nz, 2, h) + zd1(a.p4 + q, np, k, nz, 5, h);
-    const float ud = uacc + zd1(a.g + q, np, k, nz, 5, h);
-    const float vd = vacc + zd1(a.hh + q, np, k, nz, 5, h);
+    const float ud = mg ? uacc + zd1(a.g + q, np, k, nz, 5, h) : uacc;
+    const float vd = mg ? vacc + zd1(a.hh + q, np, k, nz, 5, h) : vacc;
     float rdot, wfin;
     if (k == 0 || k == nz - 1) {
         // src/hydro_deriv.f90:455-470: d(rho)/dz chosen so that dw/dt = 0
@@ -676,12 +689,14 @@ __global__ void __launch_bounds__(256, 4) k_split_pass4_v4(const __grid_constant
     const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
     const V4 rp = ld(a.r, i4), tp = ld(a.t, i4), w0 = ld(a.w, i4);
     const V4 rr = V4(rho0) + rp, tt = V4(t0) + tp;
-    const V4 wacc = (ld(a.wacc, i4) + ld(a.dxw, i4)) + ld(a.dyw, i4);
-    const V4 uacc = (ld(a.uacc, i4) + ld(a.dxu, i4)) + ld(a.dyu, i4);
-    const V4 vacc = (ld(a.vacc, i4) + ld(a.dxv, i4)) + ld(a.dyv, i4);
+    // (without a magnetic field q, g and h are zero: their terms are left out)
+    const bool mg = a.mag != 0;
+    const V4 wacc = mg ? (ld(a.wacc, i4) + ld(a.dxw, i4)) + ld(a.dyw, i4) : ld(a.wacc, i4);
+    const V4 uacc = mg ? (ld(a.uacc, i4) + ld(a.dxu, i4)) + ld(a.dyu, i4) : ld(a.uacc, i4) + ld(a.dxu, i4);
+    const V4 vacc = mg ? (ld(a.vacc, i4) + ld(a.dxv, i4)) + ld(a.dyv, i4) : ld(a.vacc, i4) + ld(a.dyv, i4);
     V4 wd = wacc + zd1(p3, np4, k, nz, 2, h) + zd1(p4, np4, k, nz, 5, h);
-    const V4 ud = uacc + zd1(g, np4, k, nz, 5, h);
-    const V4 vd = vacc + zd1(hh, np4, k, nz, 5, h);
+    const V4 ud = mg ? uacc + zd1(g, np4, k, nz, 5, h) : uacc;
+    const V4 vd = mg ? vacc + zd1(hh, np4, k, nz, 5, h) : vacc;
     const V4 racc = ld(a.racc, i4);
     V4 rdot, wfin;
     if (k == 0 || k == nz - 1) {
@@ -750,6 +765,7 @@ static SplitHydroArgs hydro_args(Engine *E)
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
     a.ho12 = (float)c.ho12; a.sc1 = (float)c.sc1; a.bzbar = (float)E->bzbar;
     a.var_eta = c.var_eta; a.np = E->np; a.nz = E->nz;
+    a.mag = split_mag_on(*E);
     // chunks of about kc_pass2 planes (tunable), balanced over nz
     const int kt = E->kc_pass2 > 0 ? E->kc_pass2 : 16;
     const int nch = (E->nz + kt - 1) / kt;
@@ -777,6 +793,7 @@ static SplitHydro4Args hydro4_args(Engine *E)
     b.dxu = W[DXU]; b.dyu = W[DYU]; b.dxv = W[DXV]; b.dyv = W[DYV]; b.dxw = W[DXW]; b.dyw = W[DYW];
     b.ht = E->ht;
     b.ho12 = (float)E->k.ho12; b.np = E->np; b.nz = E->nz;
+    b.mag = split_mag_on(*E);
     return b;
 }
 
@@ -824,13 +841,16 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
             mag_fwd_jobs(M, fx, fy);
             for (int q = 0; q < 3; q++) { jx.push_back(fx[q]); jy.push_back(fy[q]); }
         }
-        // the second-level fluxes' derivatives (after pass 2)
+        // the second-level fluxes' derivatives (after pass 2); the Lorentz
+        // fluxes q, g, h only with a magnetic field
         kx.push_back(ljob<float>(W[W_P1], W[DXU], OP_D1));
-        kx.push_back(ljob<float>(W[W_Q], W[DXV], OP_D1));
-        kx.push_back(ljob<float>(W[W_G], W[DXW], OP_D1));
         ky.push_back(ljob<float>(W[W_P2], W[DYV], OP_D1));
-        ky.push_back(ljob<float>(W[W_Q], W[DYU], OP_D1));
-        ky.push_back(ljob<float>(W[W_H], W[DYW], OP_D1));
+        if (split_mag_on(*M)) {
+            kx.push_back(ljob<float>(W[W_Q], W[DXV], OP_D1));
+            kx.push_back(ljob<float>(W[W_G], W[DXW], OP_D1));
+            ky.push_back(ljob<float>(W[W_Q], W[DYU], OP_D1));
+            ky.push_back(ljob<float>(W[W_H], W[DYW], OP_D1));
+        }
     }
     if ((st = launch_lines<float>(E, 0, jx.data(), (int)jx.size()))) return st;
     if ((st = launch_lines<float>(E, 1, jy.data(), (int)jy.size()))) return st;
@@ -845,19 +865,19 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
             attr = true;
         }
         const int kc = hydro_args(E).kc;
-        st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, 39, 4),
+        st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4),
                                             dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
                                             dim3(ZT_TILE / 2), smem, k_split_pass2_zt<1>, k_split_pass2_zt<BATCH_MAX>,
                                             hydro_args);
         if (st) return st;
     } else if (E->nx % 4 == 0 && E->vec4) {
         const SplitHydroArgs a = hydro_args(E);
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2_v2,
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4), k_split_pass2_v2,
                  dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB, a);
     } else {
         const SplitHydroArgs a = hydro_args(E);
         dim3 g2(nblk(E->np), (unsigned)((E->nz + a.kc - 1) / a.kc));
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, 39, 4), k_split_pass2, g2, TPB, a, a.kc);
+        KLAUNCHB(E, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4), k_split_pass2, g2, TPB, a, a.kc);
     }
 
     // The second-level horizontal derivatives go to separate arrays and
@@ -868,13 +888,13 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
     if ((st = launch_lines<float>(E, 1, ky.data(), (int)ky.size()))) return st;
 
     if (E->nx % 4 == 0 && E->vec4) {
-        if ((st = launch_members<SplitHydro4Args>(Es, nE, "hydro_pass4_f32", FB(E, 21, 4),
+        if ((st = launch_members<SplitHydro4Args>(Es, nE, "hydro_pass4_f32", FB(E, split_mag_on(*E) ? 21 : 15, 4),
                                                   dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), dim3(TPB), 0,
                                                   k_split_pass4_v4<1>, k_split_pass4_v4<BATCH_MAX>, hydro4_args)))
             return st;
     } else {
         const SplitHydro4Args b = hydro4_args(E);
-        KLAUNCHB(E, "hydro_pass4_f32", FB(E, 21, 4), k_split_pass4, plane_grid(*E), TPB, b);
+        KLAUNCHB(E, "hydro_pass4_f32", FB(E, split_mag_on(*E) ? 21 : 15, 4), k_split_pass4, plane_grid(*E), TPB, b);
     }
     return VEC_OK;
 }
@@ -1037,28 +1057,28 @@ int split_bandj_m(Engine *const *Es, int nE, bool rotate_hist)
         BandjArgs<float> a;
         a.dzs = e->W<float>(W_M1); a.pol = e->pol32; a.tor = e->tor32; a.h = e->hf;
         a.bxh = e->W<float>(W_EX); a.byh = e->W<float>(W_EY); a.bzh = e->W<float>(W_EZ);
-        a.dybz = e->W<float>(W_M2); a.dxbz = e->W<float>(W_M3); a.jzh = e->W<float>(W_M4);
+        a.dybz = nullptr; a.dxbz = nullptr; a.jzh = e->W<float>(W_M4);   // d(bz)/dx, dy: below
         a.nx = e->nx; a.ny = e->ny; a.nz = e->nz;
         return a;
     };
     if (v4) {
-        if ((st = launch_members<BandjArgs<float>>(Es, nE, "bandj_spec_f32", FB(E, 9, 4), g4, dim3(TPB), 0,
+        if ((st = launch_members<BandjArgs<float>>(Es, nE, "bandj_spec_f32", FB(E, 7, 4), g4, dim3(TPB), 0,
                                                    k_bandj_spec4<1>, k_bandj_spec4<BATCH_MAX>, bj)))
             return st;
     } else {
         const BandjArgs<float> a = bj(E);
-        KLAUNCHB(E, "bandj_spec_f32", FB(E, 9, 4), k_bandj_spec<float>, plane_grid(*E), TPB, a);
+        KLAUNCHB(E, "bandj_spec_f32", FB(E, 7, 4), k_bandj_spec<float>, plane_grid(*E), TPB, a);
     }
     std::vector<LineJob<float>> ix, iy;
     for (int i = 0; i < nE; i++) {
         Engine *M = Es[i];
         float *W[W_COUNT];
         for (int q = 0; q < W_COUNT; q++) W[q] = M->W<float>(q);
+        // the x inverse of bz's spectrum also gives that of d(bz)/dx (into
+        // M3); the y inverse of the former gives bz and d(bz)/dy (into M2)
         ix.push_back(ljob<float>(W[W_EX], W[W_EX], OP_INV));
         ix.push_back(ljob<float>(W[W_EY], W[W_EY], OP_INV));
-        ix.push_back(ljob<float>(W[W_EZ], W[W_EZ], OP_INV));
-        ix.push_back(ljob<float>(W[W_M2], W[W_M2], OP_INV));
-        ix.push_back(ljob<float>(W[W_M3], W[W_M3], OP_INV));
+        ix.push_back(ljob<float>(W[W_EZ], W[W_EZ], OP_INV, W[W_M3], OP_D1));
         ix.push_back(ljob<float>(W[W_M4], W[W_M4], OP_INV));
         // bz32 keeps bz - bzbar: no constant added
         LineJob<float> jbx = ljob<float>(W[W_EX], M->bx32, OP_INV), jby = ljob<float>(W[W_EY], M->by32, OP_INV);
@@ -1066,8 +1086,7 @@ int split_bandj_m(Engine *const *Es, int nE, bool rotate_hist)
         jby.addk = M->bybar;
         iy.push_back(jbx);
         iy.push_back(jby);
-        iy.push_back(ljob<float>(W[W_EZ], M->bz32, OP_INV));
-        iy.push_back(ljob<float>(W[W_M2], W[W_M2], OP_INV));
+        iy.push_back(ljob<float>(W[W_EZ], M->bz32, OP_INV, W[W_M2], OP_D1));
         iy.push_back(ljob<float>(W[W_M3], W[W_M3], OP_INV));
         iy.push_back(ljob<float>(W[W_M4], W[W_M4], OP_INV));
     }
@@ -1099,6 +1118,8 @@ struct SplitAb3Args {
     const double *bg;
     const DevScalars *ds;
     int nx, ny, nz, cx, cy, magdealias;
+    int nf;                // 7, or 5 without a magnetic field: pol and tor
+                           // (zero right-hand side) are left as they are
 };
 
 // src/main.F90:413-462 with FP64 accumulation; order u,v,w,r,t,pol,tor
@@ -1126,21 +1147,26 @@ __global__ void k_split_ab3(SplitAb3Args a)
         int j = (int)(q / a.nx), i = (int)(q - (size_t)j * a.nx);
         trunc = truncated(i, j, a.nx, a.ny, a.cx, a.cy);
     }
+    const int nf = a.nf;
 #pragma unroll
     for (int f = 5; f < 7; f++) {
+        if (f >= nf) break;
         double v = a.x[f][idx] + (double)(c0 * H(f, 2)[idx] + c1 * H(f, 1)[idx] + c2 * H(f, 0)[idx]);
         xs[f] = trunc ? 0.0 : v;
     }
 #undef H
 #pragma unroll
-    for (int f = 0; f < 7; f++) a.x[f][idx] = xs[f];
+    for (int f = 0; f < 7; f++)
+        if (f < nf) a.x[f][idx] = xs[f];
     a.m[0][idx] = (float)xs[0];
     a.m[1][idx] = (float)xs[1];
     a.m[2][idx] = (float)xs[2];
     a.m[3][idx] = (float)(xs[3] - a.bg[BG_RHO0 * a.nz + k]);
     a.m[4][idx] = (float)(xs[4] - a.bg[BG_T0 * a.nz + k]);
-    a.m[5][idx] = (float)xs[5];
-    a.m[6][idx] = (float)xs[6];
+    if (nf == 7) {
+        a.m[5][idx] = (float)xs[5];
+        a.m[6][idx] = (float)xs[6];
+    }
 }
 
 // four consecutive points per thread (x fastest, nx % 4 == 0): 16-byte
@@ -1162,8 +1188,10 @@ __global__ void k_split_ab3_v4(const __grid_constant__ Batch<SplitAb3Args, NB> b
     // the histories); only the accumulation into the state is FP64
     const float c0 = (float)a.ds->c0, c1 = (float)a.ds->c1, c2 = (float)a.ds->c2;
     double xs[7][4];
+    const int nf = a.nf;
 #pragma unroll
     for (int f = 0; f < 7; f++) {
+        if (f >= nf) break;
         const double2 s01 = *reinterpret_cast<const double2 *>(a.x[f] + i4);
         const double2 s23 = *reinterpret_cast<const double2 *>(a.x[f] + i4 + 2);
         const float *const *hp = (const float *const *)a.ht->p[a.hmap[f]];
@@ -1203,6 +1231,7 @@ __global__ void k_split_ab3_v4(const __grid_constant__ Batch<SplitAb3Args, NB> b
     const double rb = a.bg[BG_RHO0 * a.nz + k], tb = a.bg[BG_T0 * a.nz + k];
 #pragma unroll
     for (int f = 0; f < 7; f++) {
+        if (f >= nf) break;
         *reinterpret_cast<double2 *>(a.x[f] + i4) = make_double2(xs[f][0], xs[f][1]);
         *reinterpret_cast<double2 *>(a.x[f] + i4 + 2) = make_double2(xs[f][2], xs[f][3]);
         float4 m;
@@ -1234,6 +1263,7 @@ static SplitAb3Args ab3_args(Engine *E, int magdealias)
     a.ds = E->ds;
     a.nx = E->nx; a.ny = E->ny; a.nz = E->nz; a.cx = E->k.icutoffx; a.cy = E->k.icutoffy;
     a.magdealias = magdealias;
+    a.nf = split_mag_on(*E) ? 7 : 5;
     return a;
 }
 
@@ -1252,8 +1282,9 @@ int split_ab3_m(Engine *const *Es, int nE, const int *magdealias, const bool *fo
         md[i] = magdealias[i];
     }
     if (nu && (st = phys_ab3_coef_m(unf, nu))) return st;
-    // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B
-    const double bytes = (double)E->n * (14 * 8 + 21 * 4 + 7 * 4);
+    // state 14 x 8 B, histories 21 x 4 B, mirrors 7 x 4 B (without a
+    // magnetic field 10 x 8, 15 x 4 and 5 x 4 B)
+    const double bytes = (double)E->n * (split_mag_on(*E) ? 14 * 8 + 21 * 4 + 7 * 4 : 10 * 8 + 15 * 4 + 5 * 4);
     if (E->nx % 4 == 0) {
         // (the members' magdealias flags, in member order)
         int i = 0;
