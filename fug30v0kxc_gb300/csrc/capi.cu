@@ -273,6 +273,8 @@ extern "C" int vec_create(const vec_params *p, vec_ctx **out)
         E.int_cvt = !(hc && hc[0] == '1');
         const char *zp = getenv("VEC_ZPENCIL");
         E.zpencil = !(zp && zp[0] == '0');
+        const char *z4 = getenv("VEC_ZPENCIL4");
+        E.zpencil4 = z4 && (z4[0] == '0' || z4[0] == '1') ? z4[0] - '0' : -1;
     }
     set_consts(E);
     int st;
@@ -929,6 +931,7 @@ bool engine_batchable(const Engine &a, const Engine &b)
     return ok(a) && ok(b) && a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.p.xmax == b.p.xmax &&
            a.p.ymax == b.p.ymax && a.kc_pass2 == b.kc_pass2 && a.ct_s == b.ct_s && a.pdl == b.pdl &&
            a.int_cvt == b.int_cvt && a.generic_lines == b.generic_lines && a.ct_warp == b.ct_warp &&
+           a.zpencil4 == b.zpencil4 &&
            a.p.dalias == b.p.dalias && a.nit == b.nit;
 }
 

@@ -113,6 +113,9 @@ struct Engine {
     bool pdl = true;            // programmatic dependent launches (VEC_PDL=0: ordinary launches)
     bool vec4 = true;           // four-point (16-byte) forms of the split pointwise kernels (VEC_VEC4=0: one point)
     bool zpencil = true;        // split pass 2 with TMA-staged z-pencils (VEC_ZPENCIL=0: per-plane form)
+    int zpencil4 = -1;          // the same for pass 4: 1 on, 0 off (four points per thread, per
+                                // plane), -1 from np >= 1024^2 on, where its z window of five
+                                // fields no longer stays in L2 (VEC_ZPENCIL4)
     bool int_cvt = true;        // FP32/FP64 conversions of the split AB3 update on the integer pipe
                                 // (VEC_HW_CVT=1: hardware conversions; the same bits)
 

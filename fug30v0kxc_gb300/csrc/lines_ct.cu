@@ -163,20 +163,24 @@ __host__ __device__ constexpr int ybox_rows(int n) { return n <= 256 ? n : (n % 
 // through their tiles independently; an "empty" mbarrier per tile buffer
 // (one arrival per warp once it has read the tile) tells the thread that
 // issues the TMA copies when a buffer may be refilled.
-// Per-sequence stride of the exchange rows, in complex elements.  A
-// shared-memory wavefront serves U = 128 / sizeof(complex) consecutive
-// elements.  x lines: the threads of a half-warp (quarter-warp in FP64)
-// belong to one or two sequences, and a stride of 1 mod 16 keeps them on
-// distinct banks.  y lines: thread tid is lane tid / S of sequence tid % S,
-// so a wavefront's threads are G = U / S lanes of U / G sequences; a
-// stride of G mod U puts them on distinct banks (exchange element
-// sidx * stride + lane * 1 or lane * (NP + 1) + const; NP + 1 is odd).
-template <typename R, int DIR, int NP, int S>
+// Per-sequence stride of the exchange rows, in complex elements.  The
+// forward exchange holds N1 rows of N2 + 1, the inverse one N2 rows of
+// N1 + 1, the spectra's separation N + N/32 padded elements: the stride
+// covers the largest.  A shared-memory wavefront serves U = 128 /
+// sizeof(complex) consecutive elements.  x lines: the threads of a
+// half-warp (quarter-warp in FP64) belong to one or two sequences, and a
+// stride of 1 mod 16 keeps them on distinct banks.  y lines: thread tid is
+// lane tid / S of sequence tid % S, so a wavefront's threads are G = U / S
+// lanes of U / G sequences; a stride of G mod U puts them on distinct banks
+// (exchange element sidx * stride + lane * 1 or lane * (odd row) + const).
+template <typename R, int DIR, int N1, int N2, int S>
 __host__ __device__ constexpr int ct_lds()
 {
     constexpr int U = 128 / (2 * (int)sizeof(R));
     constexpr int G = U / S > 1 ? U / S : 1;
-    return DIR == 0 ? ((NP * (NP + 1)) / 16) * 16 + 17 : ((NP * (NP + 1)) / U) * U + U + G;
+    constexpr int MF = N1 * (N2 + 1), MI = N2 * (N1 + 1), MS = N1 * N2 + (N1 * N2) / 32 + 1;
+    constexpr int M = MF > MI ? (MF > MS ? MF : MS) : (MI > MS ? MI : MS);
+    return DIR == 0 ? ((M + 15) / 16) * 16 + 1 : ((M + U - 1) / U) * U + G;
 }
 
 // dynamic shared memory of one CTA: two tile buffers, the exchange rows,
@@ -184,8 +188,8 @@ __host__ __device__ constexpr int ct_lds()
 template <typename R, int DIR, int N1, int N2, int S>
 __host__ __device__ constexpr size_t ct_smem_bytes()
 {
-    constexpr int N = N1 * N2, NP = N1 > N2 ? N1 : N2;
-    constexpr int LDS = ct_lds<R, DIR, NP, S>();
+    constexpr int N = N1 * N2;
+    constexpr int LDS = ct_lds<R, DIR, N1, N2, S>();
     return 2 * (size_t)(2 * S * N) * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * (size_t)N) * 2 * sizeof(R)
            + 3 * (size_t)N * sizeof(R);
 }
@@ -208,8 +212,9 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     constexpr int NP = N1 > N2 ? N1 : N2;
     constexpr int NT = S * NP;
     constexpr int TILE = 2 * S * N;                   // reals per tile
-    constexpr int LX = (N1 > N2 ? N1 : N2) + 1;       // padded exchange row
-    constexpr int LDS = ct_lds<R, DIR, NP, S>();      // per-sequence exchange stride
+    constexpr int LXF = N2 + 1;                       // padded exchange rows: forward,
+    constexpr int LXI = N1 + 1;                       // inverse
+    constexpr int LDS = ct_lds<R, DIR, N1, N2, S>();  // per-sequence exchange stride
     constexpr bool WS = WSYNC && DIR == 0 && (32 % NP == 0) && NT % 32 == 0;
 
     extern __shared__ __align__(128) unsigned char smem[];
@@ -359,14 +364,14 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
                     C w = TW2 ? twf[k1 * N2 + lane] : twf[modn<N>(lane * k1)];
-                    ex_s[k1 * LX + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
+                    ex_s[k1 * LXF + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
                 }
             }
             sync();
             // second level: thread k1 = lane, N2-point DFT over m2
             if (lane < N1) {
 #pragma unroll
-                for (int m2 = 0; m2 < N2; m2++) X[m2] = ex_s[lane * LX + m2];
+                for (int m2 = 0; m2 < N2; m2++) X[m2] = ex_s[lane * LXF + m2];
                 RDft<N2, false>::run(X);
             }
             sync();
@@ -448,7 +453,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 for (int m2 = 0; m2 < N2; m2++) {
                     C w = TW2 ? twi[m2 * N1 + lane] : twf[modn<N>(m2 * lane)];
                     w.y = -w.y;
-                    ex_s[m2 * LX + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
+                    ex_s[m2 * LXI + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
                 }
             }
             sync();
@@ -456,7 +461,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
             if (lane < N2) {
                 C a[N1];
 #pragma unroll
-                for (int k1 = 0; k1 < N1; k1++) a[k1] = ex_s[lane * LX + k1];
+                for (int k1 = 0; k1 < N1; k1++) a[k1] = ex_s[lane * LXI + k1];
                 RDft<N1, true>::run(a);
                 const R sc = op == OP_INV ? (R)1 / (R)N : (R)1;
                 const int la = l0 + 2 * sidx;
@@ -586,14 +591,13 @@ static int run_ct(Engine *E, const LineJob<R> *jobs, int nj, const char *name)
     constexpr int N = N1 * N2;
     constexpr int NP = N1 > N2 ? N1 : N2;
     constexpr int TILE = 2 * S * N;
-    constexpr int LX = NP + 1;
-    constexpr int LDS = ct_lds<R, DIR, NP, S>();
+    constexpr int LDS = ct_lds<R, DIR, N1, N2, S>();
     static bool attr_set = false;
     const size_t smem = ct_smem_bytes<R, DIR, N1, N2, S>();
     static_assert(ct_smem_bytes<R, DIR, N1, N2, S>() == 2 * TILE * sizeof(R) + ((size_t)S * LDS + (sizeof(R) == 4 ? 2 : 1) * N) * sizeof(C) + 3 * (size_t)N * sizeof(R),
                   "shared memory layout");
     static_assert(ct_smem_bytes<R, DIR, N1, N2, S>() + 128 <= 232448, "tile does not fit one SM's shared memory");
-    static_assert(LDS >= NP * LX && LDS >= N + N / 32 + 1, "exchange rows");
+    static_assert(LDS >= N1 * (N2 + 1) && LDS >= N2 * (N1 + 1) && LDS >= N + N / 32 + 1, "exchange rows");
     if (!attr_set) {
         CUDA_TRY(cudaFuncSetAttribute(line_ct<R, DIR, N1, N2, S, WSYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));

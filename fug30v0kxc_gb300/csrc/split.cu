@@ -459,13 +459,18 @@ __global__ void __launch_bounds__(256, 3) k_split_pass2_v2(SplitHydroArgs a)
 // read directly.  Same arithmetic as k_split_pass2_v2, value for value.
 #define ZT_TILE 512
 #define ZT_SLOTS 8
-struct ZRing2 {
+// one field of a ring whose slots hold NF fields' tiles
+template <int NF> struct ZRingF {
     const V2 *base;     // slot 0 of one field, this thread's point pair
     __device__ __forceinline__ V2 operator()(int kk) const
     {
-        return base[(size_t)(kk & (ZT_SLOTS - 1)) * (4 * ZT_TILE / 2)];
+        return base[(size_t)(kk & (ZT_SLOTS - 1)) * (NF * ZT_TILE / 2)];
     }
 };
+using ZRing2 = ZRingF<4>;
+// the z window of plane k's stencils (d1, d1up, d2 with their wall rows)
+__device__ __forceinline__ int zt_lo(int k, int nz) { return max(0, k >= nz - 2 ? min(k - 3, nz - 6) : k - 3); }
+__device__ __forceinline__ int zt_hi(int k, int nz) { return min(nz - 1, k <= 1 ? max(k + 3, 5) : k + 3); }
 
 template <int NB>
 __global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_constant__ Batch<SplitHydroArgs, NB> bt)
@@ -481,8 +486,8 @@ __global__ void __launch_bounds__(ZT_TILE / 2, 3) k_split_pass2_zt(const __grid_
     const size_t p0 = (size_t)blockIdx.x * ZT_TILE;
     const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
     const int tid = threadIdx.x;
-    auto lo_of = [&](int k) { return max(0, k >= nz - 2 ? min(k - 3, nz - 6) : k - 3); };
-    auto hi_of = [&](int k) { return min(nz - 1, k <= 1 ? max(k + 3, 5) : k + 3); };
+    auto lo_of = [&](int k) { return zt_lo(k, nz); };
+    auto hi_of = [&](int k) { return zt_hi(k, nz); };
     const int kbase = lo_of(k0), kcap = hi_of(k1 - 1);
     auto parity = [&](int kk) { return (unsigned)(((kk - kbase) >> 3) & 1); };
     auto issue = [&](int kk) {   // one thread: plane kk of the four fields into slot kk mod 8
@@ -616,6 +621,8 @@ struct SplitHydro4Args {
     int mag;                // 0: g, h and the derivatives of q, g, h are zero (not read)
     size_t np;
     int nz;
+    int kc;                 // z-pencil kernel: planes per chunk
+    int *err;               // z-pencil kernel: the bounded waits' error flag
 };
 
 // one thread per point, grid (np/256, nz): k = blockIdx.y
@@ -728,6 +735,136 @@ __global__ void __launch_bounds__(256, 4) k_split_pass4_v4(const __grid_constant
     reinterpret_cast<V4 *>(a.ht->p[4][2])[i4] = wfin * ri;
 }
 
+// Pass 4 with TMA-staged z-pencils: the planes of the fields its z stencils
+// read -- p3, p4, r' and (with a magnetic field) g, h -- in an eight-slot
+// shared-memory ring filled by bulk copies one plane ahead, as in
+// k_split_pass2_zt; a CTA owns ZT_TILE consecutive points of a chunk of
+// about kc planes, two points per thread; the other inputs are read
+// directly.  Same arithmetic as k_split_pass4_v4, value for value.
+#define Z4_FIELDS 5
+template <int NB>
+__global__ void __launch_bounds__(ZT_TILE / 2, 2) k_split_pass4_zt(const __grid_constant__ Batch<SplitHydro4Args, NB> bt)
+{
+    PDL_WAIT();
+    const SplitHydro4Args &a = BATCH_MEMBER(bt, NB);
+    const int kc = a.kc;
+    int *err = a.err;
+    extern __shared__ __align__(128) float zring[];   // [slot][p3, p4, r', g, h][ZT_TILE]
+    __shared__ __align__(8) uint64_t full[ZT_SLOTS];
+    const int nz = a.nz;
+    const size_t np = a.np;
+    const size_t p0 = (size_t)blockIdx.x * ZT_TILE;
+    const int k0 = blockIdx.y * kc, k1 = min(nz, k0 + kc);
+    const int tid = threadIdx.x;
+    const bool mg = a.mag != 0;
+    const int nf = mg ? 5 : 3;   // (g and h are zero without a magnetic field)
+    const int kbase = zt_lo(k0, nz), kcap = zt_hi(k1 - 1, nz);
+    auto parity = [&](int kk) { return (unsigned)(((kk - kbase) >> 3) & 1); };
+    auto issue = [&](int kk) {   // one thread: plane kk of the ring's fields into slot kk mod 8
+        uint64_t *b = &full[kk & (ZT_SLOTS - 1)];
+        float *dst = zring + (size_t)(kk & (ZT_SLOTS - 1)) * Z4_FIELDS * ZT_TILE;
+        const size_t off = (size_t)kk * np + p0;
+        mbar_expect_tx(b, (unsigned)nf * ZT_TILE * (unsigned)sizeof(float));
+        tma_load(dst, a.p3 + off, ZT_TILE * sizeof(float), b);
+        tma_load(dst + ZT_TILE, a.p4 + off, ZT_TILE * sizeof(float), b);
+        tma_load(dst + 2 * ZT_TILE, a.r + off, ZT_TILE * sizeof(float), b);
+        if (mg) {
+            tma_load(dst + 3 * ZT_TILE, a.g + off, ZT_TILE * sizeof(float), b);
+            tma_load(dst + 4 * ZT_TILE, a.hh + off, ZT_TILE * sizeof(float), b);
+        }
+    };
+    if (tid == 0) {
+        for (int s = 0; s < ZT_SLOTS; s++) mbar_init(&full[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    int khi = min(kcap, zt_hi(k0, nz) + 1);   // highest plane issued (one plane of lookahead)
+    if (tid == 0)
+        for (int kk = kbase; kk <= khi; kk++) issue(kk);
+    int kw = kbase - 1;                       // highest plane this thread has waited for
+    bool ok = true;
+    // after a failed wait: wait (bounded) for every copy still in flight
+    auto drain = [&]() {
+        for (int kk = max(kw + 1, khi - ZT_SLOTS + 1); kk <= khi; kk++)
+            mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+    };
+    const V2 *zr = reinterpret_cast<const V2 *>(zring) + tid;
+    const ZRingF<Z4_FIELDS> Rp3{ zr }, Rp4{ zr + ZT_TILE / 2 }, Rr{ zr + ZT_TILE }, Rg{ zr + 3 * ZT_TILE / 2 },
+        Rh{ zr + 2 * ZT_TILE };
+    const V2 h(a.ho12);
+    const double *bg = a.bg;
+    const float *pc = a.pc;
+    const size_t np2 = np / 2, q2 = p0 / 2 + tid;
+    for (int k = k0; k < k1; k++) {
+        if (k > k0) {
+            // every thread is done with row k - 1: the slot of plane k - 4 is free
+            if (!__syncthreads_and(ok)) {
+                if (tid == 0) {
+                    // report, then let the copies in flight land before the CTA exits
+                    atomicExch(err, 1);
+                    drain();
+                }
+                return;
+            }
+            const int want = min(kcap, zt_hi(k, nz) + 1);
+            if (tid == 0 && want > khi) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                for (int kk = khi + 1; kk <= want; kk++) issue(kk);
+            }
+            khi = max(khi, want);
+        }
+        for (int kk = kw + 1; kk <= zt_hi(k, nz) && ok; kk++) ok = mbar_wait(&full[kk & (ZT_SLOTS - 1)], parity(kk));
+        kw = max(kw, zt_hi(k, nz));
+        if (!ok) continue;
+        const size_t i2 = (size_t)k * np2 + q2;
+        const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
+        const V2 rp = Rr(k), tp = ldv<V2>(a.t, i2), w0 = ldv<V2>(a.w, i2);
+        const V2 rr = V2(rho0) + rp, tt = V2(t0) + tp;
+        const V2 wacc = mg ? (ldv<V2>(a.wacc, i2) + ldv<V2>(a.dxw, i2)) + ldv<V2>(a.dyw, i2) : ldv<V2>(a.wacc, i2);
+        const V2 uacc = mg ? (ldv<V2>(a.uacc, i2) + ldv<V2>(a.dxu, i2)) + ldv<V2>(a.dyu, i2)
+                           : ldv<V2>(a.uacc, i2) + ldv<V2>(a.dxu, i2);
+        const V2 vacc = mg ? (ldv<V2>(a.vacc, i2) + ldv<V2>(a.dxv, i2)) + ldv<V2>(a.dyv, i2)
+                           : ldv<V2>(a.vacc, i2) + ldv<V2>(a.dyv, i2);
+        V2 wd = wacc + zd1a(Rp3, k, nz, 2, h) + zd1a(Rp4, k, nz, 5, h);
+        const V2 ud = mg ? uacc + zd1a(Rg, k, nz, 5, h) : uacc;
+        const V2 vd = mg ? vacc + zd1a(Rh, k, nz, 5, h) : vacc;
+        const V2 racc = ldv<V2>(a.racc, i2);
+        V2 rdot, wfin;
+        if (k == 0 || k == nz - 1) {
+            // src/hydro_deriv.f90:455-470: d(rho)/dz chosen so that dw/dt = 0
+            const double A = bg[BG_A * nz + k];
+            const float wdv[2] = { wd.x, wd.y }, ttv[2] = { tt.x, tt.y };
+            const float w0v[2] = { w0.x, w0.y }, rav[2] = { racc.x, racc.y };
+            float rd[2], wf[2];
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const double wdn = (double)wdv[c] + A;
+                const double rz = wdn / (double)ttv[c];
+                rd[c] = rav[c] - w0v[c] * (float)rz;
+                wf[c] = (float)(wdn - (double)ttv[c] * rz);
+            }
+            rdot = V2(rd[0], rd[1]);
+            wfin = V2(wf[0], wf[1]);
+        } else {
+            const V2 up(pc[PC_RHO0ZU_P * nz + k]), um(pc[PC_RHO0ZU_M * nz + k]);
+            const V2 rzu = zd1upa(Rr, k, nz, 0, h, w0) + upsel(w0, up, um);
+            const V2 rzp = zd1a(Rr, k, nz, 0, h);
+            rdot = racc - w0 * rzu;
+            wfin = wd + V2(pc[PC_AB * nz + k]) - V2(t0) * rzp - tp * V2(pc[PC_RHO0Z0 * nz + k]) - tp * rzp;
+        }
+        const V2 ri(1.0f / rr.x, 1.0f / rr.y);
+        stv((float *)a.ht->p[0][2], i2, rdot);
+        stv((float *)a.ht->p[2][2], i2, ud * ri);
+        stv((float *)a.ht->p[3][2], i2, vd * ri);
+        stv((float *)a.ht->p[4][2], i2, wfin * ri);
+    }
+    if (!__syncthreads_and(ok) && tid == 0) {
+        atomicExch(err, 1);
+        drain();
+    }
+}
+
 // the three forward transforms of E = u x B that mag_deriv starts with;
 // with with_mag the x and y passes of the hydro derivatives carry them as
 // extra jobs, so one launch per direction serves both
@@ -794,6 +931,8 @@ static SplitHydro4Args hydro4_args(Engine *E)
     b.ht = E->ht;
     b.ho12 = (float)E->k.ho12; b.np = E->np; b.nz = E->nz;
     b.mag = split_mag_on(*E);
+    b.kc = hydro_args(E).kc;
+    b.err = E->dev_err;
     return b;
 }
 
@@ -887,7 +1026,26 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
     if ((st = launch_lines<float>(E, 0, kx.data(), (int)kx.size()))) return st;
     if ((st = launch_lines<float>(E, 1, ky.data(), (int)ky.size()))) return st;
 
-    if (E->nx % 4 == 0 && E->vec4) {
+    // (the z-pencil form pays where the per-plane form's z neighbours fall
+    // out of L2: 4.8 against 3.9 TB/s at 1024^2 x 513; at 512^2 x 257 and
+    // below its two CTAs per SM lose to four: 4.6 against 5.6 TB/s)
+    const bool zt4 = E->zpencil4 == 1 || (E->zpencil4 < 0 && E->np >= (size_t)1024 * 1024);
+    if (E->nx % 4 == 0 && E->vec4 && E->zpencil && zt4 && E->np % ZT_TILE == 0 && E->nz >= 6) {
+        static bool attr4 = false;
+        const size_t smem = (size_t)ZT_SLOTS * Z4_FIELDS * ZT_TILE * sizeof(float);
+        if (!attr4) {
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass4_zt<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(k_split_pass4_zt<BATCH_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+            attr4 = true;
+        }
+        const int kc = hydro4_args(E).kc;
+        if ((st = launch_members<SplitHydro4Args>(Es, nE, "hydro_pass4_f32", FB(E, split_mag_on(*E) ? 21 : 15, 4),
+                                                  dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
+                                                  dim3(ZT_TILE / 2), smem, k_split_pass4_zt<1>,
+                                                  k_split_pass4_zt<BATCH_MAX>, hydro4_args)))
+            return st;
+    } else if (E->nx % 4 == 0 && E->vec4) {
         if ((st = launch_members<SplitHydro4Args>(Es, nE, "hydro_pass4_f32", FB(E, split_mag_on(*E) ? 21 : 15, 4),
                                                   dim3((unsigned)nblk(E->np / 4), (unsigned)E->nz), dim3(TPB), 0,
                                                   k_split_pass4_v4<1>, k_split_pass4_v4<BATCH_MAX>, hydro4_args)))

@@ -98,7 +98,7 @@ def test_split_100_steps_vs_fp64_oracle():
 
 @pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17)])
 @pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6),
-                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6)])
+                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6), ("VEC_ZPENCIL4", ("0", "1"), 1e-6)])
 def test_split_variants_agree(grid, var, values, tol, monkeypatch):
     """Two implementations of the same arithmetic after twelve steps (Euler,
     AB2, AB3, a dealias step and a calcdt at step 10).
@@ -109,11 +109,12 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
       the one-point forms.  The compiler contracts multiply-adds within one
       expression, not across the vector type's operator functions, so
       single roundings differ; tolerance 1e-6 relative L2 per field.
-    * VEC_ZPENCIL: hydro pass 2 with its z-stencil planes staged through a
-      shared-memory ring by bulk copies, against the per-plane form that
-      reads them from global memory: the same formulas on the same values,
-      but the two kernels are compiled separately and the compiler may fuse
-      different multiply-adds; tolerance 1e-6 relative L2 per field.
+    * VEC_ZPENCIL: hydro passes 2 and 4 with their z-stencil planes staged
+      through shared-memory rings by bulk copies, against the per-plane
+      forms that read them from global memory: the same formulas on the
+      same values, but the kernels are compiled separately and the compiler
+      may fuse different multiply-adds; tolerance 1e-6 relative L2 per
+      field.  VEC_ZPENCIL4: the same for pass 4 alone.
     """
     states = []
     for val in values:
@@ -137,16 +138,20 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
             assert e <= tol, (n, e)
 
 
-@pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17), (128, 32, 40)])
-def test_zpencil_pass2_matches_per_plane_form(grid, monkeypatch):
-    """One hydro_deriv with pass 2 fed by the shared-memory z ring against
-    the per-plane form, every RHS at every plane (the wall rows read planes
-    0..5 and nz-6..nz-1; several z chunks per column): largest difference
-    below 1e-6 of the array's largest value (single roundings only)."""
+@pytest.mark.parametrize("var", ["VEC_ZPENCIL", "VEC_ZPENCIL4"])
+@pytest.mark.parametrize("grid,q", [((64, 64, 33), 100.0), ((96, 48, 17), 100.0), ((128, 32, 40), 100.0),
+                                    ((64, 64, 33), 0.0)])
+def test_zpencil_passes_match_per_plane_form(grid, q, var, monkeypatch):
+    """One hydro_deriv with passes 2 and 4 (VEC_ZPENCIL) or pass 4 alone
+    (VEC_ZPENCIL4) fed by the shared-memory z rings against the per-plane
+    forms, every RHS at every plane (the wall rows read planes 0..5 and
+    nz-6..nz-1; several z chunks per column; Q = 0 leaves g and h out of
+    pass 4's ring): largest difference below 1e-6 of the array's largest
+    value (single roundings only)."""
     out = []
     for val in ("0", "1"):
-        monkeypatch.setenv("VEC_ZPENCIL", val)
-        p = convection_params(*grid, eta_contrast=20.0, precision=VEC_PREC_SPLIT)
+        monkeypatch.setenv(var, val)
+        p = convection_params(*grid, q=q, eta_contrast=20.0, precision=VEC_PREC_SPLIT)
         g = P3D(p)
         for n, a in smooth_state(p, seed=9).items():
             g.set(n, a)
