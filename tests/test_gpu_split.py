@@ -19,8 +19,8 @@ from tests.helpers import perturbation_menergy, rel_err, smooth_state, top_nusse
 pytestmark = pytest.mark.gpu
 
 
-def _pair(nx, ny, nz, eta, seed=0, **kw):
-    p = convection_params(nx, ny, nz, eta_contrast=eta, precision=VEC_PREC_SPLIT)
+def _pair(nx, ny, nz, eta, seed=0, q=100.0, **kw):
+    p = convection_params(nx, ny, nz, q=q, eta_contrast=eta, precision=VEC_PREC_SPLIT)
     for k, v in kw.items():
         setattr(p, k, v)
     p.ndu06 = 10
@@ -55,6 +55,38 @@ def test_split_rhs(eta, grid):
         assert e < 2e-5, (n, e)
     bz_g, bz_o = g.get("bz") - o.bzbar, o.get("bz") - o.bzbar
     assert rel_err(bz_g, bz_o) < 2e-5
+
+
+def test_split_rhs_without_magnetic_field():
+    """Q = 0: the split kernels leave out B, J^2 and the Lorentz fluxes (zero
+    for f = 0); hydro_deriv still matches the FP64 oracle, which keeps
+    them, at FP32 accuracy."""
+    g, o, p = _pair(64, 64, 33, 5.0, q=0.0)
+    assert p.f == 0.0
+    g.hydro_deriv(); o.hydro_deriv()
+    for n in ("rdot3", "tdot3", "udot3", "vdot3", "wdot3"):
+        e = rel_err(g.get(n), o.get(n))
+        assert e < 2e-5, (n, e)
+
+
+def test_split_30_steps_without_magnetic_field_vs_fp64_oracle():
+    """Q = 0, seeded static start, 30 steps (three calcdt and dealias
+    steps): relative L2 of r, t (deviations from the polytrope), u, v, w
+    against the FP64 oracle below 1e-4."""
+    p = convection_params(64, 64, 33, q=0.0, eta_contrast=5.0, precision=VEC_PREC_SPLIT)
+    p.ndu06 = 10
+    g, o = P3D(p), O.Oracle(p)
+    g.start(); o.start()
+    assert g.step(30) == 0 and o.step(30) == 0
+    z = np.arange(p.nz) / (p.nz - 1)
+    t0 = (1.0 + p.theta * z)[:, None, None]
+    for n in ("r", "t", "u", "v", "w"):
+        a, b = g.get(n), o.get(n)
+        if n in ("r", "t"):
+            bgd = t0 ** p.cm if n == "r" else t0
+            a, b = a - bgd, b - bgd
+        e = rel_l2(a, b)
+        assert e < 1e-4, (n, e)
 
 
 def test_split_100_steps_vs_fp64_oracle():
