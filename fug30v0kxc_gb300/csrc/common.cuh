@@ -46,7 +46,10 @@ struct LineJob {
     double addc;
 };
 
-#define MAX_JOBS 64   // line jobs per launch (an ensemble batch carries 5-8 per member)
+// line jobs per launch: a batch of 16 members carries up to 96 (five hydro
+// jobs, and the Lorentz fluxes' and E's transforms, per member); the job
+// and tensor-map packs then take 24 KB of the 32 KB kernel parameter space
+#define MAX_JOBS 128
 
 // spectral tables of one direction (device pointers)
 template <typename R>

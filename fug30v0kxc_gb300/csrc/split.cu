@@ -292,6 +292,7 @@ struct SplitHydroArgs {
     const HistTable *ht;    // tdot = newest slot of t
     float *racc, *uacc, *vacc, *wacc;
     float *p1, *p2, *q, *g, *hh, *p3, *p4;
+    float *e1, *e2, *e3;    // E = u x B (the emf of mag_deriv) when not null
     float gck, fzckg, gm1, sckg, fo2, scko3, f, thmplus1, cor, cpsi, spsi, sck, ho12, sc1, bzbar;
     int var_eta;
     int mag;                // 0: no magnetic field (Q = 0): B, J^2 and the Lorentz
@@ -415,6 +416,12 @@ __device__ __forceinline__ void split_pass2_point(const SplitHydroArgs &a, size_
         stv(a.q, idx, T(a.f) * by * bx);
         stv(a.g, idx, T(a.f) * bz * bx);
         stv(a.hh, idx, T(a.f) * bz * by);
+        // E = u x B from the same values (src/magnetic.f90 mag_deriv's emf)
+        if (a.e1) {
+            stv(a.e1, idx, v0 * bz - w0 * by);
+            stv(a.e2, idx, w0 * bx - u0 * bz);
+            stv(a.e3, idx, u0 * by - v0 * bx);
+        }
     }
 }
 template <typename T>
@@ -897,6 +904,7 @@ static SplitHydroArgs hydro_args(Engine *E)
     a.racc = W[W_RACC]; a.ht = E->ht;
     a.uacc = W[W_UACC]; a.vacc = W[W_VACC]; a.wacc = W[W_WACC];
     a.p1 = W[W_P1]; a.p2 = W[W_P2]; a.q = W[W_Q]; a.g = W[W_G]; a.hh = W[W_H]; a.p3 = W[W_P3]; a.p4 = W[W_P4];
+    a.e1 = a.e2 = a.e3 = nullptr;
     a.gck = (float)c.gck; a.fzckg = (float)c.fzckg; a.gm1 = (float)c.gm1; a.sckg = (float)c.sckg;
     a.fo2 = (float)c.fo2; a.scko3 = (float)c.scko3; a.f = (float)c.f; a.thmplus1 = (float)c.thmplus1;
     a.cor = (float)c.cor; a.cpsi = (float)c.cpsi; a.spsi = (float)c.spsi; a.sck = (float)c.sck;
@@ -955,11 +963,6 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
     Engine *E = Es[0];
     if (!batch_forms(Es, nE)) return VEC_ERR_ARG;
     int st;
-    Engine *mag[BATCH_MAX];
-    int nm = 0;
-    for (int i = 0; i < nE; i++)
-        if (with_mag[i]) mag[nm++] = Es[i];
-    if (nm && (st = split_emf_m(mag, nm))) return st;
     std::vector<LineJob<float>> jx, jy, kx, ky;
     for (int i = 0; i < nE; i++) {
         Engine *M = Es[i];
@@ -975,11 +978,6 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
         jy.push_back(ljob<float>(M->u32, W[W_UY], OP_D1, W[W_UYY], OP_D2));
         jy.push_back(ljob<float>(M->v32, W[W_VY], OP_D1, W[W_VYY], OP_D2));
         jy.push_back(ljob<float>(M->w32, W[W_WY], OP_D1, W[W_WYY], OP_D2));
-        if (with_mag[i]) {
-            LineJob<float> fx[3], fy[3];
-            mag_fwd_jobs(M, fx, fy);
-            for (int q = 0; q < 3; q++) { jx.push_back(fx[q]); jy.push_back(fy[q]); }
-        }
         // the second-level fluxes' derivatives (after pass 2); the Lorentz
         // fluxes q, g, h only with a magnetic field
         kx.push_back(ljob<float>(W[W_P1], W[DXU], OP_D1));
@@ -990,10 +988,30 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
             ky.push_back(ljob<float>(W[W_Q], W[DYU], OP_D1));
             ky.push_back(ljob<float>(W[W_H], W[DYW], OP_D1));
         }
+        // with_mag: pass 2 writes E = u x B, and its forward transforms ride
+        // in the second-level line launches
+        if (with_mag[i]) {
+            LineJob<float> fx[3], fy[3];
+            mag_fwd_jobs(M, fx, fy);
+            for (int q = 0; q < 3; q++) { kx.push_back(fx[q]); ky.push_back(fy[q]); }
+        }
     }
     if ((st = launch_lines<float>(E, 0, jx.data(), (int)jx.size()))) return st;
     if ((st = launch_lines<float>(E, 1, jy.data(), (int)jy.size()))) return st;
 
+    // pass 2 (with E = u x B for the members whose mag branch shares the
+    // transforms: 3 fields more)
+    int im = 0;
+    auto p2args = [&im, with_mag](Engine *e) {
+        SplitHydroArgs a = hydro_args(e);
+        if (with_mag[im++]) {
+            a.e1 = e->W<float>(W_M1);
+            a.e2 = e->W<float>(W_M2);
+            a.e3 = e->W<float>(W_M3);
+        }
+        return a;
+    };
+    const double p2b = FB(E, split_mag_on(*E) ? (with_mag[0] ? 42 : 39) : 32, 4);
     if (E->zpencil && E->np % ZT_TILE == 0 && E->nz >= 6) {
         static bool attr = false;
         const size_t smem = (size_t)ZT_SLOTS * 4 * ZT_TILE * sizeof(float);
@@ -1004,19 +1022,21 @@ int split_hydro_m(Engine *const *Es, int nE, const bool *with_mag)
             attr = true;
         }
         const int kc = hydro_args(E).kc;
-        st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4),
+        st = launch_members<SplitHydroArgs>(Es, nE, "hydro_pass2_f32", p2b,
                                             dim3((unsigned)(E->np / ZT_TILE), (unsigned)((E->nz + kc - 1) / kc)),
                                             dim3(ZT_TILE / 2), smem, k_split_pass2_zt<1>, k_split_pass2_zt<BATCH_MAX>,
-                                            hydro_args);
+                                            p2args);
         if (st) return st;
     } else if (E->nx % 4 == 0 && E->vec4) {
-        const SplitHydroArgs a = hydro_args(E);
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4), k_split_pass2_v2,
-                 dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB, a);
+        if (nE != 1) return VEC_ERR_ARG;
+        const SplitHydroArgs a = p2args(E);
+        KLAUNCHB(E, "hydro_pass2_f32", p2b, k_split_pass2_v2, dim3((unsigned)nblk(E->np / 2), (unsigned)E->nz), TPB,
+                 a);
     } else {
-        const SplitHydroArgs a = hydro_args(E);
+        if (nE != 1) return VEC_ERR_ARG;
+        const SplitHydroArgs a = p2args(E);
         dim3 g2(nblk(E->np), (unsigned)((E->nz + a.kc - 1) / a.kc));
-        KLAUNCHB(E, "hydro_pass2_f32", FB(E, split_mag_on(*E) ? 39 : 32, 4), k_split_pass2, g2, TPB, a, a.kc);
+        KLAUNCHB(E, "hydro_pass2_f32", p2b, k_split_pass2, g2, TPB, a, a.kc);
     }
 
     // The second-level horizontal derivatives go to separate arrays and
