@@ -211,7 +211,9 @@ int vec_diag(vec_ctx *ctx, vec_diag_out *out);
  * checks the terms of its CFL expression (a negative T or rho counts, as
  * its square root is not finite).  The calcdt check is read back once, at
  * the end of a call whose steps ran calcdt; the steps of that call have
- * then all been executed. */
+ * then all been executed.  Without a magnetic field (f = 0 and not
+ * kinematic) the split form leaves pol and tor as they are: their
+ * right-hand side is zero, and the FP64 form's update adds exactly zero. */
 int vec_step(vec_ctx *ctx, int nsteps);
 /* Steps without diagnostics run as replays of a captured CUDA graph of one
  * step (two variants: plain, and the tenth step with dealias and calcdt);
