@@ -678,68 +678,90 @@ __global__ void k_split_pass4(SplitHydro4Args a)
     ((float *)a.ht->p[4][2])[idx] = wfin * ri;
 }
 
-// the same for four consecutive x points per thread (nx % 4 == 0): 16-byte
-// loads and stores, four times fewer memory instructions in flight per point
-// (four CTAs per SM: 64 registers with a few spilled values; 5.3 TB/s
-// against 4.2 at the compiler's own 94 registers)
-template <int NB>
-__global__ void __launch_bounds__(256, 4) k_split_pass4_v4(const __grid_constant__ Batch<SplitHydro4Args, NB> bt)
+// per-component access of the vector point types
+template <typename T> struct VecN;
+template <> struct VecN<V4> {
+    static constexpr int n = 4;
+    static __device__ __forceinline__ void get(const V4 &v, float *o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+    static __device__ __forceinline__ V4 make(const float *o) { return V4(o[0], o[1], o[2], o[3]); }
+    static __device__ __forceinline__ V4 recip(const V4 &v) { return V4(1.0f / v.x, 1.0f / v.y, 1.0f / v.z, 1.0f / v.w); }
+};
+template <> struct VecN<V2> {
+    static constexpr int n = 2;
+    static __device__ __forceinline__ void get(const V2 &v, float *o) { o[0] = v.x; o[1] = v.y; }
+    static __device__ __forceinline__ V2 make(const float *o) { return V2(o[0], o[1]); }
+    static __device__ __forceinline__ V2 recip(const V2 &v) { return V2(1.0f / v.x, 1.0f / v.y); }
+};
+
+// the same for VecN<T>::n consecutive x points per thread (nx % 4 == 0):
+// 16- or 8-byte loads and stores, grid (np/n/256, nz)
+template <typename T, int NB>
+__device__ __forceinline__ void split_pass4_vec(const Batch<SplitHydro4Args, NB> &bt)
 {
-    PDL_WAIT();
+    constexpr int NV = VecN<T>::n;
     const SplitHydro4Args &a = BATCH_MEMBER(bt, NB);
-    const size_t np4 = a.np / 4;
-    const size_t q4 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q4 >= np4) return;
+    const size_t npv = a.np / NV;
+    const size_t qv = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qv >= npv) return;
     const int nz = a.nz;
     const int k = blockIdx.y;
-    const size_t i4 = (size_t)k * np4 + q4;
-    const V4 h(a.ho12);
+    const size_t iv = (size_t)k * npv + qv;
+    const T h(a.ho12);
     const double *bg = a.bg;
     const float *pc = a.pc;
-    auto ld = [](const float *p, size_t i) { return reinterpret_cast<const V4 *>(p)[i]; };
-    const V4 *p3 = reinterpret_cast<const V4 *>(a.p3) + q4, *p4 = reinterpret_cast<const V4 *>(a.p4) + q4;
-    const V4 *g = reinterpret_cast<const V4 *>(a.g) + q4, *hh = reinterpret_cast<const V4 *>(a.hh) + q4;
-    const V4 *rr4 = reinterpret_cast<const V4 *>(a.r) + q4;
+    auto ld = [](const float *p, size_t i) { return reinterpret_cast<const T *>(p)[i]; };
+    const T *p3 = reinterpret_cast<const T *>(a.p3) + qv, *p4 = reinterpret_cast<const T *>(a.p4) + qv;
+    const T *g = reinterpret_cast<const T *>(a.g) + qv, *hh = reinterpret_cast<const T *>(a.hh) + qv;
+    const T *rrv = reinterpret_cast<const T *>(a.r) + qv;
     const float rho0 = pc[PC_RHO0 * nz + k], t0 = pc[PC_T0 * nz + k];
-    const V4 rp = ld(a.r, i4), tp = ld(a.t, i4), w0 = ld(a.w, i4);
-    const V4 rr = V4(rho0) + rp, tt = V4(t0) + tp;
+    const T rp = ld(a.r, iv), tp = ld(a.t, iv), w0 = ld(a.w, iv);
+    const T rr = T(rho0) + rp, tt = T(t0) + tp;
     // (without a magnetic field q, g and h are zero: their terms are left out)
     const bool mg = a.mag != 0;
-    const V4 wacc = mg ? (ld(a.wacc, i4) + ld(a.dxw, i4)) + ld(a.dyw, i4) : ld(a.wacc, i4);
-    const V4 uacc = mg ? (ld(a.uacc, i4) + ld(a.dxu, i4)) + ld(a.dyu, i4) : ld(a.uacc, i4) + ld(a.dxu, i4);
-    const V4 vacc = mg ? (ld(a.vacc, i4) + ld(a.dxv, i4)) + ld(a.dyv, i4) : ld(a.vacc, i4) + ld(a.dyv, i4);
-    V4 wd = wacc + zd1(p3, np4, k, nz, 2, h) + zd1(p4, np4, k, nz, 5, h);
-    const V4 ud = mg ? uacc + zd1(g, np4, k, nz, 5, h) : uacc;
-    const V4 vd = mg ? vacc + zd1(hh, np4, k, nz, 5, h) : vacc;
-    const V4 racc = ld(a.racc, i4);
-    V4 rdot, wfin;
+    const T wacc = mg ? (ld(a.wacc, iv) + ld(a.dxw, iv)) + ld(a.dyw, iv) : ld(a.wacc, iv);
+    const T uacc = mg ? (ld(a.uacc, iv) + ld(a.dxu, iv)) + ld(a.dyu, iv) : ld(a.uacc, iv) + ld(a.dxu, iv);
+    const T vacc = mg ? (ld(a.vacc, iv) + ld(a.dxv, iv)) + ld(a.dyv, iv) : ld(a.vacc, iv) + ld(a.dyv, iv);
+    T wd = wacc + zd1(p3, npv, k, nz, 2, h) + zd1(p4, npv, k, nz, 5, h);
+    const T ud = mg ? uacc + zd1(g, npv, k, nz, 5, h) : uacc;
+    const T vd = mg ? vacc + zd1(hh, npv, k, nz, 5, h) : vacc;
+    const T racc = ld(a.racc, iv);
+    T rdot, wfin;
     if (k == 0 || k == nz - 1) {
         // src/hydro_deriv.f90:455-470: d(rho)/dz chosen so that dw/dt = 0
         const double A = bg[BG_A * nz + k];
-        float rd[4], wf[4];
-        const float wdv[4] = { wd.x, wd.y, wd.z, wd.w }, ttv[4] = { tt.x, tt.y, tt.z, tt.w };
-        const float w0v[4] = { w0.x, w0.y, w0.z, w0.w }, rav[4] = { racc.x, racc.y, racc.z, racc.w };
+        float rd[NV], wf[NV], wdv[NV], ttv[NV], w0v[NV], rav[NV];
+        VecN<T>::get(wd, wdv); VecN<T>::get(tt, ttv); VecN<T>::get(w0, w0v); VecN<T>::get(racc, rav);
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < NV; c++) {
             const double wdn = (double)wdv[c] + A;
             const double rz = wdn / (double)ttv[c];
             rd[c] = rav[c] - w0v[c] * (float)rz;
             wf[c] = (float)(wdn - (double)ttv[c] * rz);
         }
-        rdot = V4(rd[0], rd[1], rd[2], rd[3]);
-        wfin = V4(wf[0], wf[1], wf[2], wf[3]);
+        rdot = VecN<T>::make(rd);
+        wfin = VecN<T>::make(wf);
     } else {
-        const V4 up(pc[PC_RHO0ZU_P * nz + k]), um(pc[PC_RHO0ZU_M * nz + k]);
-        const V4 rzu = zd1up(rr4, np4, k, nz, 0, h, w0) + upsel(w0, up, um);
-        const V4 rzp = zd1(rr4, np4, k, nz, 0, h);
+        const T up(pc[PC_RHO0ZU_P * nz + k]), um(pc[PC_RHO0ZU_M * nz + k]);
+        const T rzu = zd1up(rrv, npv, k, nz, 0, h, w0) + upsel(w0, up, um);
+        const T rzp = zd1(rrv, npv, k, nz, 0, h);
         rdot = racc - w0 * rzu;
-        wfin = wd + V4(pc[PC_AB * nz + k]) - V4(t0) * rzp - tp * V4(pc[PC_RHO0Z0 * nz + k]) - tp * rzp;
+        wfin = wd + T(pc[PC_AB * nz + k]) - T(t0) * rzp - tp * T(pc[PC_RHO0Z0 * nz + k]) - tp * rzp;
     }
-    const V4 ri(1.0f / rr.x, 1.0f / rr.y, 1.0f / rr.z, 1.0f / rr.w);
-    reinterpret_cast<V4 *>(a.ht->p[0][2])[i4] = rdot;
-    reinterpret_cast<V4 *>(a.ht->p[2][2])[i4] = ud * ri;
-    reinterpret_cast<V4 *>(a.ht->p[3][2])[i4] = vd * ri;
-    reinterpret_cast<V4 *>(a.ht->p[4][2])[i4] = wfin * ri;
+    const T ri = VecN<T>::recip(rr);
+    reinterpret_cast<T *>(a.ht->p[0][2])[iv] = rdot;
+    reinterpret_cast<T *>(a.ht->p[2][2])[iv] = ud * ri;
+    reinterpret_cast<T *>(a.ht->p[3][2])[iv] = vd * ri;
+    reinterpret_cast<T *>(a.ht->p[4][2])[iv] = wfin * ri;
+}
+
+// four points per thread, four CTAs per SM (64 registers with a few spilled
+// values; 5.3 TB/s against 4.2 at the compiler's own 94 registers, and 5.0
+// against 4.3 for two points per thread at 56 registers without spills)
+template <int NB>
+__global__ void __launch_bounds__(256, 4) k_split_pass4_v4(const __grid_constant__ Batch<SplitHydro4Args, NB> bt)
+{
+    PDL_WAIT();
+    split_pass4_vec<V4, NB>(bt);
 }
 
 // Pass 4 with TMA-staged z-pencils: the planes of the fields its z stencils
