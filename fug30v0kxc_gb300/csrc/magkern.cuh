@@ -322,7 +322,8 @@ static __global__ void k_mag_div4(const __grid_constant__ Batch<MagDiv4Args, NB>
     st4(w1 + pb, q4, sdx4(ex + pb, i0, j, nx, h.kx1) + sdy4(ey + pb, i0, j, nx, ny, h.ky1));
 }
 
-// (four CTAs per SM: 3.4 TB/s against 2.1 at the compiler's own 90 registers)
+// (four CTAs per SM: 3.4 TB/s against 2.1 at the compiler's own 90 registers
+// and 3.0 at three CTAs per SM with 80 registers and no spills)
 template <int NB>
 static __global__ void __launch_bounds__(256, 4) k_mag_final4(const __grid_constant__ Batch<MagArgs<float>, NB> bt)
 {
