@@ -706,8 +706,9 @@ static int line_op(vec_ctx *c, int dir, const double *fin, double *f1, int op1, 
 extern "C" int vec_line_f32(vec_ctx *c, int dir, int op1, int op2, const float *fin, float *f1, float *f2)
 {
     if (!c || !fin || !f1 || (dir != 0 && dir != 1)) return VEC_ERR_ARG;
+    // second outputs: D1 or D2 of a real input, D1 of an inverse
     if (op1 < OP_D1 || op1 > OP_INV || (op2 != OP_NONE && (op2 < OP_D1 || op2 > OP_D2 || op1 == OP_FWD ||
-                                                           op1 == OP_INV || !f2)))
+                                                           (op1 == OP_INV && op2 != OP_D1) || !f2)))
         return VEC_ERR_ARG;
     Engine &E = c->E;
     // each FP64 scratch field holds 2n floats

@@ -175,8 +175,9 @@ int vec_d2bydz1d(vec_ctx *ctx, const double *fin, double *fout, int dflag);
  * src/fft.F90:586-682), VEC_OP_FWD (r2hc), VEC_OP_INV (hc2r divided by n);
  * op2 (a second output from the same forward transform, as d2bydx's f1out /
  * f2out pair): VEC_OP_NONE, VEC_OP_D1 or VEC_OP_D2, with op1 D1, D2 or
- * DEALIAS.  Arrays are (nx,ny,nz) floats, host or device; any context
- * precision. */
+ * DEALIAS; or VEC_OP_D1 with op1 INV: the derivative of the inverse, from
+ * the same spectrum (how the split bandj takes d(bz)/dx and d(bz)/dy).
+ * Arrays are (nx,ny,nz) floats, host or device; any context precision. */
 #define VEC_OP_NONE         0
 #define VEC_OP_D1           1
 #define VEC_OP_D2           2

@@ -53,7 +53,16 @@ def _check_direction(g, o, direction, f):
     ref_F = o.forwardfft(f)
     errs["forward"] = rel_err(F, ref_F)
     back = g.line_f32(other, INV, g.line_f32(direction, INV, ref_F.astype(np.float32)))
-    errs["inverse"] = rel_err(back, o.inversefft(ref_F))
+    ref_back = o.inversefft(ref_F)
+    errs["inverse"] = rel_err(back, ref_back)
+    # an inverse with the derivative of the inverse as its second output
+    # (the split bandj's d(bz)/dx, d(bz)/dy): completed by the other
+    # direction's inverse, the second output is the derivative of the 2-D
+    # inverse transform
+    a, b = g.line_f32(direction, INV, ref_F.astype(np.float32), op2=D1)
+    errs["inv+d1.inv"] = rel_err(g.line_f32(other, INV, a), ref_back)
+    ref_dback = o.d1bydx(ref_back) if direction == 0 else o.d1bydy(ref_back)
+    errs["inv+d1.d1"] = rel_err(g.line_f32(other, INV, b), ref_dback)
     return errs
 
 
@@ -92,6 +101,6 @@ def test_f32_line_rejects_bad_operators():
     g, _ = _pair(64, 64)
     f = np.zeros((6, 64, 64), np.float32)
     out = np.empty_like(f)
-    for d, op1, op2 in ((2, D1, 0), (0, 0, 0), (0, 6, 0), (0, FWD, D2), (0, D1, DEALIAS)):
+    for d, op1, op2 in ((2, D1, 0), (0, 0, 0), (0, 6, 0), (0, FWD, D2), (0, D1, DEALIAS), (0, INV, D2)):
         st = g.L.vec_line_f32(g.h, d, op1, op2, f.ctypes.data, out.ctypes.data, out.ctypes.data)
         assert st == -31, (d, op1, op2, st)
