@@ -686,15 +686,9 @@ template <> struct VecN<V4> {
     static __device__ __forceinline__ V4 make(const float *o) { return V4(o[0], o[1], o[2], o[3]); }
     static __device__ __forceinline__ V4 recip(const V4 &v) { return V4(1.0f / v.x, 1.0f / v.y, 1.0f / v.z, 1.0f / v.w); }
 };
-template <> struct VecN<V2> {
-    static constexpr int n = 2;
-    static __device__ __forceinline__ void get(const V2 &v, float *o) { o[0] = v.x; o[1] = v.y; }
-    static __device__ __forceinline__ V2 make(const float *o) { return V2(o[0], o[1]); }
-    static __device__ __forceinline__ V2 recip(const V2 &v) { return V2(1.0f / v.x, 1.0f / v.y); }
-};
 
 // the same for VecN<T>::n consecutive x points per thread (nx % 4 == 0):
-// 16- or 8-byte loads and stores, grid (np/n/256, nz)
+// 16-byte loads and stores, grid (np/n/256, nz)
 template <typename T, int NB>
 __device__ __forceinline__ void split_pass4_vec(const Batch<SplitHydro4Args, NB> &bt)
 {
