@@ -64,15 +64,24 @@ def batch_members(n, nx, ny, nz):
 
 def test_batched_members_match_single_instance():
     """18 members of one grid: two batches (at most 16 members per launch),
-    more than 64 line jobs per hydro line pass (several launches), magnetic
-    and non-magnetic members in one batch; 25 steps cover the calcdt and
-    dealias steps.  Every member bit-identical to its solo run."""
+    80 jobs in a hydro line launch, magnetic and non-magnetic members in one
+    batch (the first one non-magnetic); 25 steps cover the calcdt and
+    dealias steps.  Fewer than 30 launches per batch and step; every member
+    bit-identical to its solo run."""
     ps = batch_members(18, 32, 32, 17)
     ens = Ensemble(ps)
     ens.start()
-    assert ens.step(25) == 0
+    assert ens.step(5) == 0
     ens.sync()
-    # one graph branch per batch: far fewer launches than members x kernels
+    # graph replays: one launch per kernel for each batch (two batches here),
+    # not one per member
+    l0 = sum(m.launch_count() for m in ens.members)
+    assert ens.step(10) == 0
+    ens.sync()
+    per_step = (sum(m.launch_count() for m in ens.members) - l0) / 10
+    assert per_step < 2 * 30, per_step
+    assert ens.step(10) == 0
+    ens.sync()
     for p, m in zip(ps, ens.members):
         solo = P3D(p)
         solo.start()
