@@ -130,7 +130,8 @@ def test_split_100_steps_vs_fp64_oracle():
 
 @pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17)])
 @pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6),
-                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6), ("VEC_ZPENCIL4", ("0", "1"), 1e-6)])
+                                            ("VEC_ZPENCIL", ("0", "1"), 1e-6), ("VEC_ZPENCIL4", ("0", "1"), 1e-6),
+                                            ("VEC_SERIAL_MAG", ("1", "0"), 0.0)])
 def test_split_variants_agree(grid, var, values, tol, monkeypatch):
     """Two implementations of the same arithmetic after twelve steps (Euler,
     AB2, AB3, a dealias step and a calcdt at step 10).
@@ -147,6 +148,10 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
       same values, but the kernels are compiled separately and the compiler
       may fuse different multiply-adds; tolerance 1e-6 relative L2 per
       field.  VEC_ZPENCIL4: the same for pass 4 alone.
+    * VEC_SERIAL_MAG: the magnetic branch after the hydro one (E = u x B
+      from pass 2, its transforms in the second-level line launches) against
+      the branch on a second stream beside hydro (its own emf kernel and
+      transforms): bit-identical states.
     """
     states = []
     for val in values:
