@@ -131,7 +131,8 @@ def test_split_100_steps_vs_fp64_oracle():
 @pytest.mark.parametrize("grid", [(64, 64, 33), (96, 48, 17)])
 @pytest.mark.parametrize("var,values,tol", [("VEC_HW_CVT", ("1", "0"), 0.0), ("VEC_VEC4", ("0", "1"), 1e-6),
                                             ("VEC_ZPENCIL", ("0", "1"), 1e-6), ("VEC_ZPENCIL4", ("0", "1"), 1e-6),
-                                            ("VEC_SERIAL_MAG", ("1", "0"), 0.0)])
+                                            ("VEC_SERIAL_MAG", ("1", "0"), 0.0), ("VEC_PDL", ("1", "0"), 0.0),
+                                            ("VEC_CT_WARP", ("1", "0"), 0.0)])
 def test_split_variants_agree(grid, var, values, tol, monkeypatch):
     """Two implementations of the same arithmetic after twelve steps (Euler,
     AB2, AB3, a dealias step and a calcdt at step 10).
@@ -152,6 +153,10 @@ def test_split_variants_agree(grid, var, values, tol, monkeypatch):
       from pass 2, its transforms in the second-level line launches) against
       the branch on a second stream beside hydro (its own emf kernel and
       transforms): bit-identical states.
+    * VEC_PDL, VEC_CT_WARP: programmatic dependent launches against ordinary
+      ones, warp barriers in the x line tiles against CTA-wide ones; only
+      the synchronisation differs, so the states are bit-identical (a
+      missing wait would show as a difference).
     """
     states = []
     for val in values:
