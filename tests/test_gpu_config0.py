@@ -104,3 +104,28 @@ def test_split_1000_steps_vs_oracle(oracle_run):
         b = np.mean([d[k] for d in rdiag])
         assert abs(a - b) <= 0.01 * abs(b), (k, a, b)
     g.close()
+
+
+@pytest.mark.parametrize("var,values", [("VEC_SERIAL_MAG", ("0", "1")), ("VEC_PDL", ("1", "0"))])
+def test_fp64_step_forms_bit_identical(var, values, monkeypatch):
+    """The FP64 step's magnetic branch on a second stream (its default)
+    against the serial order, and programmatic dependent launches against
+    ordinary ones: 12 steps of the config-0 physics at 64^2 x 33 give the
+    same bits."""
+    from tests.helpers import smooth_state
+    states = []
+    for val in values:
+        monkeypatch.setenv(var, val)
+        p = config0(precision=VEC_PREC_FP64)
+        p.nz = 33
+        p.ndu06 = 1000
+        g = P3D(p)
+        for n, a in smooth_state(p, seed=3).items():
+            g.set(n, a)
+        g.calcdt()
+        g.mag_init()
+        assert g.step(12) == 0
+        states.append({n: g.get(n) for n in ("r", "t", "u", "v", "w", "pol", "tor", "bx", "by", "bz")})
+        g.close()
+    for n in states[0]:
+        assert np.array_equal(states[0][n], states[1][n]), (var, n)
