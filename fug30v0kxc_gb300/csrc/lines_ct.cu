@@ -227,6 +227,7 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
     // eight-way bank conflicts).  FP64: one table of N (the second would
     // cost the second CTA per SM).
     constexpr bool TW2 = sizeof(R) == 4;
+    static_assert(!TW2 || (N1 % 4 == 0 && N2 % 4 == 0), "FP32 twiddles factor the index as 4 a + b");
     C *twf = ex + (size_t)S * LDS;                    // twf[k1 N2 + m2] (FP64: tw[e])
     C *twi = twf + N;                                 // twi[m2 N1 + k1]
     R *sm1 = reinterpret_cast<R *>(twi + (TW2 ? N : 0));   // spectral multipliers
@@ -361,9 +362,24 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 for (int m1 = 0; m1 < N1; m1++) a[m1] = tile_z(N2 * (m1 ^ sw) + lane);
                 unswap(a, N1);
                 RDft<N1, false>::run(a);
+                // FP32: W^(lane k1) = W^(lane 4 (k1 / 4)) W^(lane (k1 % 4)): 3 + N1/4 - 1
+                // table reads instead of N1 - 1, one product more per twiddle
+                C lo[4], hi[N1 / 4];
+                if constexpr (TW2) {
+#pragma unroll
+                    for (int j = 1; j < 4; j++) lo[j] = twf[j * N2 + lane];
+#pragma unroll
+                    for (int j = 1; j < N1 / 4; j++) hi[j] = twf[4 * j * N2 + lane];
+                }
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) {
-                    C w = TW2 ? twf[k1 * N2 + lane] : twf[modn<N>(lane * k1)];
+                    C w;
+                    if constexpr (TW2) {
+                        const int ja = k1 >> 2, jb = k1 & 3;
+                        w = ja == 0 ? lo[jb] : (jb == 0 ? hi[ja] : cmul_(hi[ja], lo[jb]));
+                    } else {
+                        w = twf[modn<N>(lane * k1)];
+                    }
                     ex_s[k1 * LXF + lane] = k1 == 0 ? a[k1] : cmul_(a[k1], w);
                 }
             }
@@ -449,9 +465,23 @@ line_ct(JobPackCT<R> jobs, const __grid_constant__ TmapPack tmaps, LineTables<R>
                 }
                 // inverse, first level: thread k1 = lane, N2-point DFT over k2
                 RDft<N2, true>::run(Y);
+                // (FP32: the same factorisation of W^(m2 lane), m2 = 4 (m2 / 4) + m2 % 4)
+                C lo[4], hi[N2 / 4];
+                if constexpr (TW2) {
+#pragma unroll
+                    for (int j = 1; j < 4; j++) lo[j] = twi[j * N1 + lane];
+#pragma unroll
+                    for (int j = 1; j < N2 / 4; j++) hi[j] = twi[4 * j * N1 + lane];
+                }
 #pragma unroll
                 for (int m2 = 0; m2 < N2; m2++) {
-                    C w = TW2 ? twi[m2 * N1 + lane] : twf[modn<N>(m2 * lane)];
+                    C w;
+                    if constexpr (TW2) {
+                        const int ja = m2 >> 2, jb = m2 & 3;
+                        w = ja == 0 ? lo[jb] : (jb == 0 ? hi[ja] : cmul_(hi[ja], lo[jb]));
+                    } else {
+                        w = twf[modn<N>(m2 * lane)];
+                    }
                     w.y = -w.y;
                     ex_s[m2 * LXI + lane] = m2 == 0 ? Y[m2] : cmul_(Y[m2], w);
                 }
